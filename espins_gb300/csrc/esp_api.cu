@@ -1,0 +1,811 @@
+// C ABI of libespins_gpu.so (declared in include/espins_gpu.h): the handle,
+// device memory, and the schedules of mcarlo (ESpinS src/mcarlo.F90:463-733)
+// and pt_mcarlo (src/pt.F90:504-1024) driven from the host.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/espins_gpu.h"
+#include "esp_kernels.h"
+#include "esp_tables.h"
+
+using namespace esp;
+
+struct RunState {
+    bool active = false;
+    esp_schedule s{};
+    std::vector<int32_t> levels;
+    int nlev = 0;
+    int64_t total_units = 0, units_done = 0, meas_done = 0;
+    long long const_hits = 0;
+    int64_t steps_tot[2] = {0, 0};
+    std::vector<double> e_init;
+};
+
+struct esp_handle {
+    RunState run;
+    std::string err;
+    int N = 0, R = 0, na = 0, L[3] = {0, 0, 0};
+    bool open = false;
+    cudaStream_t own = nullptr, st = nullptr;
+    int device = 0, num_sms = 0, max_blocks = 0;
+    long long launches = 0;
+    bool have_tables = false, have_temps = false;
+    int64_t next_sweep = 0, next_swap = 0;
+    // tables
+    PrepOutput prep;
+    bool hsi = false, hfld = false;
+    int32_t *d_nnb = nullptr, *d_nbr = nullptr, *d_perm = nullptr, *d_inv = nullptr;
+    float *d_J = nullptr, *d_B = nullptr, *d_Dx = nullptr, *d_Dy = nullptr, *d_Dz = nullptr, *d_mag = nullptr;
+    float4 *d_si = nullptr, *d_fld = nullptr;
+    // state
+    float *d_sx = nullptr, *d_sy = nullptr, *d_sz = nullptr;
+    int32_t *d_temp_of = nullptr, *d_repl_at = nullptr;
+    float *d_beta = nullptr;
+    double *d_inv_t = nullptr;
+    double *d_e_run = nullptr, *d_m_run = nullptr;
+    unsigned long long *d_rej = nullptr;
+    double *d_scratch = nullptr;
+    int e_blocks = 0;
+    double *d_tmp_e = nullptr, *d_tmp_m = nullptr;
+    // accumulators
+    double *d_data = nullptr, *d_lsum = nullptr, *d_bin = nullptr;
+    int32_t *d_levels = nullptr;
+    int nlev_alloc = 0;
+    unsigned long long *d_pm = nullptr;
+    long long *d_swaps = nullptr;
+    std::vector<double> tems;
+    int nf = 2;
+    double m_min = 0, m_max = 0;
+};
+
+namespace {
+
+std::string g_create_err;
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            h->err = std::string(#call) + ": " + cudaGetErrorString(e_);                           \
+            return ESP_ECUDA;                                                                      \
+        }                                                                                          \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(T **p, size_t n)
+{
+    if (n == 0) n = 1;
+    return cudaMalloc((void **)p, n * sizeof(T));
+}
+
+template <class T>
+void dfree(T *&p)
+{
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+
+void free_tables(esp_handle *h)
+{
+    dfree(h->d_nnb); dfree(h->d_nbr); dfree(h->d_perm); dfree(h->d_inv);
+    dfree(h->d_J); dfree(h->d_B); dfree(h->d_Dx); dfree(h->d_Dy); dfree(h->d_Dz); dfree(h->d_mag);
+    dfree(h->d_si); dfree(h->d_fld); dfree(h->d_scratch);
+}
+
+void free_all(esp_handle *h)
+{
+    free_tables(h);
+    dfree(h->d_sx); dfree(h->d_sy); dfree(h->d_sz);
+    dfree(h->d_temp_of); dfree(h->d_repl_at); dfree(h->d_beta); dfree(h->d_inv_t);
+    dfree(h->d_e_run); dfree(h->d_m_run); dfree(h->d_rej); dfree(h->d_tmp_e); dfree(h->d_tmp_m);
+    dfree(h->d_data); dfree(h->d_lsum); dfree(h->d_bin); dfree(h->d_levels); dfree(h->d_pm); dfree(h->d_swaps);
+}
+
+SweepArgs sweep_args(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o)
+{
+    SweepArgs a;
+    a.nnb = h->d_nnb; a.nbr = h->d_nbr; a.J = h->d_J; a.B = h->d_B;
+    a.Dx = h->d_Dx; a.Dy = h->d_Dy; a.Dz = h->d_Dz;
+    a.perm = h->d_perm; a.mag = h->d_mag; a.si = h->hsi ? h->d_si : nullptr; a.fld = h->hfld ? h->d_fld : nullptr;
+    a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz;
+    a.temp_of = h->d_temp_of; a.beta = h->d_beta;
+    a.e_run = h->d_e_run; a.m_run = h->d_m_run; a.rej = h->d_rej;
+    a.N = h->N; a.R = h->R; a.num_atoms = h->na;
+    a.off_c = h->prep.off[c]; a.n_c = h->prep.off[c + 1] - h->prep.off[c];
+    a.phase = o->phase ? 1 : 0; a.mode = o->mcarlo_mode ? 1 : 0; a.tilt = (float)o->tilt_angles_max;
+    a.key0 = (uint32_t)o->seed; a.key1 = (uint32_t)(o->seed >> 32);
+    a.sw_lo = (uint32_t)sweep; a.sw_hi = (uint32_t)((uint64_t)sweep >> 32);
+    return a;
+}
+
+EnergyArgsHost energy_args(esp_handle *h)
+{
+    EnergyArgsHost a;
+    a.nnb = h->d_nnb; a.nbr = h->d_nbr; a.J = h->d_J; a.B = h->d_B;
+    a.Dx = h->d_Dx; a.Dy = h->d_Dy; a.Dz = h->d_Dz;
+    a.perm = h->d_perm; a.si = h->hsi ? h->d_si : nullptr; a.fld = h->hfld ? h->d_fld : nullptr;
+    a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz;
+    a.scratch = h->d_scratch; a.N = h->N; a.R = h->R; a.num_atoms = h->na;
+    return a;
+}
+
+int require(esp_handle *h, bool tables, bool temps)
+{
+    if (!h) return ESP_EINVAL;
+    if (tables && !h->have_tables) { h->err = "tables not uploaded (esp_upload_tables)"; return ESP_ESTATE; }
+    if (temps && !h->have_temps) { h->err = "temperatures not set (esp_set_temperatures)"; return ESP_ESTATE; }
+    return ESP_OK;
+}
+
+int do_sweep_colour(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o)
+{
+    SweepArgs a = sweep_args(h, c, sweep, o);
+    if (a.n_c == 0) return ESP_OK;
+    CK(launch_sweep(a, h->prep.has_b, h->prep.has_d, h->max_blocks, h->st));
+    h->launches++;
+    return ESP_OK;
+}
+
+int do_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o)
+{
+    for (int64_t w = 0; w < n; ++w)
+        for (int c = 0; c < h->prep.num_colours; ++c) {
+            int rc = do_sweep_colour(h, c, first + w, o);
+            if (rc) return rc;
+        }
+    return ESP_OK;
+}
+
+// energy by replica into d_tmp_e / d_tmp_m
+int do_energy(esp_handle *h)
+{
+    CK(launch_energy(energy_args(h), h->d_tmp_e, h->d_tmp_m, h->e_blocks, h->st));
+    h->launches += 2;
+    return ESP_OK;
+}
+
+int reset_running(esp_handle *h)
+{
+    int rc = do_energy(h);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h->d_e_run, h->d_tmp_e, sizeof(double) * h->R, cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_m_run, h->d_tmp_m, sizeof(double) * 3 * h->R, cudaMemcpyDeviceToDevice, h->st));
+    return ESP_OK;
+}
+
+int identity_labels(esp_handle *h)
+{
+    std::vector<int32_t> id(h->R);
+    for (int r = 0; r < h->R; ++r) id[r] = r;
+    CK(cudaMemcpyAsync(h->d_temp_of, id.data(), sizeof(int32_t) * h->R, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_repl_at, id.data(), sizeof(int32_t) * h->R, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return ESP_OK;
+}
+
+int get_repl_at(esp_handle *h, std::vector<int32_t> &ra)
+{
+    ra.resize(h->R);
+    CK(cudaMemcpyAsync(ra.data(), h->d_repl_at, sizeof(int32_t) * h->R, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return ESP_OK;
+}
+
+int by_slot(esp_handle *h, const double *d_by_rep, int width, double *out)
+{
+    std::vector<int32_t> ra;
+    int rc = get_repl_at(h, ra);
+    if (rc) return rc;
+    std::vector<double> v((size_t)h->R * width);
+    CK(cudaMemcpyAsync(v.data(), d_by_rep, sizeof(double) * width * h->R, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    for (int t = 0; t < h->R; ++t)
+        for (int c = 0; c < width; ++c) out[(size_t)t * width + c] = v[(size_t)ra[t] * width + c];
+    return ESP_OK;
+}
+
+int measure(esp_handle *h, long long step, int nlev, bool pt_quirk, long long &const_hits)
+{
+    MeasureArgs m;
+    m.e_run = h->d_e_run; m.m_run = h->d_m_run; m.repl_at = h->d_repl_at;
+    m.data = h->d_data; m.lsum = h->d_lsum; m.binning = h->d_bin; m.levels = h->d_levels;
+    m.R = h->R; m.N = h->N; m.nlev = nlev; m.pt_quirk = pt_quirk ? 1 : 0; m.step = step;
+    CK(launch_measure(m, h->st));
+    h->launches++;
+    if (h->na == 1) {
+        // one atom per cell: |sum_cell s| = |m| for every cell, so every cell
+        // lands in the top bin of Pm_get's grid; count it without a pass.
+        const_hits++;
+    } else {
+        PmArgs p;
+        p.sx = h->d_sx; p.sy = h->d_sy; p.sz = h->d_sz; p.inv = h->d_inv; p.temp_of = h->d_temp_of;
+        p.counts = h->d_pm; p.R = h->R; p.ncell = h->N / h->na; p.num_atoms = h->na; p.nf = h->nf;
+        p.use_shared = 0; p.m_min = h->m_min; p.m_max = h->m_max;
+        CK(launch_pm(p, h->max_blocks, h->st));
+        h->launches++;
+    }
+    return ESP_OK;
+}
+
+int ensure_levels(esp_handle *h, int nlev, const int32_t *levels)
+{
+    if (nlev > h->nlev_alloc) {
+        dfree(h->d_lsum); dfree(h->d_bin); dfree(h->d_levels);
+        CK(dalloc(&h->d_lsum, (size_t)h->R * nlev * 2));
+        CK(dalloc(&h->d_bin, (size_t)h->R * nlev * 2));
+        CK(dalloc(&h->d_levels, (size_t)nlev));
+        h->nlev_alloc = nlev;
+    }
+    if (nlev > 0) {
+        CK(cudaMemcpyAsync(h->d_levels, levels, sizeof(int32_t) * nlev, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemsetAsync(h->d_lsum, 0, sizeof(double) * h->R * nlev * 2, h->st));
+        CK(cudaMemsetAsync(h->d_bin, 0, sizeof(double) * h->R * nlev * 2, h->st));
+    }
+    return ESP_OK;
+}
+
+int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Copies on the handle's stream (which may be non-blocking with respect to
+// the legacy default stream), completed before returning.
+int h2d(esp_handle *h, void *dst, const void *src, size_t bytes)
+{
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return ESP_OK;
+}
+
+int d2h(esp_handle *h, void *dst, const void *src, size_t bytes)
+{
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return ESP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int esp_create(const esp_dims *dims, esp_handle **out)
+{
+    if (!dims || !out) { g_create_err = "null argument"; return ESP_EINVAL; }
+    *out = nullptr;
+    if (dims->num_sites <= 0 || dims->num_atoms <= 0 || dims->num_replicas <= 0 ||
+        dims->supercell[0] <= 0 || dims->supercell[1] <= 0 || dims->supercell[2] <= 0) {
+        g_create_err = "dimensions must be positive";
+        return ESP_EINVAL;
+    }
+    if ((long long)dims->supercell[0] * dims->supercell[1] * dims->supercell[2] * dims->num_atoms != dims->num_sites) {
+        g_create_err = "num_sites != prod(supercell) * num_atoms";
+        return ESP_EINVAL;
+    }
+    esp_handle *h = new (std::nothrow) esp_handle();
+    if (!h) { g_create_err = "host allocation failed"; return ESP_ENOMEM; }
+    h->N = dims->num_sites; h->R = dims->num_replicas; h->na = dims->num_atoms;
+    for (int c = 0; c < 3; ++c) h->L[c] = dims->supercell[c];
+    h->open = dims->open_boundary != 0;
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        g_create_err = std::string("CUDA unavailable: ") + cudaGetErrorString(e);
+        delete h;
+        return ESP_ECUDA;
+    }
+    h->st = h->own;
+    h->max_blocks = h->num_sms * 8;
+    const size_t NR = (size_t)h->N * h->R;
+    e = cudaSuccess;
+    if (e == cudaSuccess) e = dalloc(&h->d_sx, NR);
+    if (e == cudaSuccess) e = dalloc(&h->d_sy, NR);
+    if (e == cudaSuccess) e = dalloc(&h->d_sz, NR);
+    if (e == cudaSuccess) e = dalloc(&h->d_temp_of, h->R);
+    if (e == cudaSuccess) e = dalloc(&h->d_repl_at, h->R);
+    if (e == cudaSuccess) e = dalloc(&h->d_beta, h->R);
+    if (e == cudaSuccess) e = dalloc(&h->d_inv_t, h->R);
+    if (e == cudaSuccess) e = dalloc(&h->d_e_run, h->R);
+    if (e == cudaSuccess) e = dalloc(&h->d_m_run, 3 * (size_t)h->R);
+    if (e == cudaSuccess) e = dalloc(&h->d_rej, 2 * (size_t)h->R);
+    if (e == cudaSuccess) e = dalloc(&h->d_tmp_e, h->R);
+    if (e == cudaSuccess) e = dalloc(&h->d_tmp_m, 3 * (size_t)h->R);
+    if (e == cudaSuccess) e = dalloc(&h->d_data, 6 * (size_t)h->R);
+    if (e == cudaSuccess) e = dalloc(&h->d_swaps, 2 * (size_t)h->R);
+    if (e != cudaSuccess) {
+        g_create_err = std::string("device allocation failed: ") + cudaGetErrorString(e);
+        free_all(h);
+        cudaStreamDestroy(h->own);
+        delete h;
+        return ESP_ENOMEM;
+    }
+    cudaMemset(h->d_rej, 0, sizeof(unsigned long long) * 2 * h->R);
+    cudaMemset(h->d_e_run, 0, sizeof(double) * h->R);
+    cudaMemset(h->d_m_run, 0, sizeof(double) * 3 * h->R);
+    *out = h;
+    return identity_labels(h);
+}
+
+int esp_destroy(esp_handle *h)
+{
+    if (!h) return ESP_EINVAL;
+    if (h->st) cudaStreamSynchronize(h->st);
+    free_all(h);
+    if (h->own) cudaStreamDestroy(h->own);
+    delete h;
+    return ESP_OK;
+}
+
+int esp_last_error(const esp_handle *h, char *buf, size_t len)
+{
+    if (!buf || len == 0) return ESP_EINVAL;
+    const std::string &s = h ? h->err : g_create_err;
+    std::snprintf(buf, len, "%s", s.c_str());
+    return ESP_OK;
+}
+
+int esp_set_stream(esp_handle *h, void *stream)
+{
+    if (!h) return ESP_EINVAL;
+    CK(cudaStreamSynchronize(h->st));
+    h->st = stream ? (cudaStream_t)stream : h->own;
+    return ESP_OK;
+}
+
+int esp_upload_tables(esp_handle *h, const esp_tables *t)
+{
+    if (!h || !t) return ESP_EINVAL;
+    PrepInput in;
+    in.N = h->N; in.num_atoms = h->na; in.L[0] = h->L[0]; in.L[1] = h->L[1]; in.L[2] = h->L[2];
+    in.mag = t->mag;
+    in.j_maxnb = t->j_maxnb; in.j_nn = t->j_nn; in.j_nbors = t->j_nbors; in.j_val = t->j_val;
+    in.b_maxnb = t->b_maxnb; in.b_nn = t->b_nn; in.b_nbors = t->b_nbors; in.b_val = t->b_val;
+    in.d_maxnb = t->d_maxnb; in.d_nn = t->d_nn; in.d_nbors = t->d_nbors; in.d_val = t->d_val;
+    if (in.b_nn && (!in.b_nbors || !in.b_val)) { h->err = "incomplete bij tables"; return ESP_EINVAL; }
+    if (in.d_nn && (!in.d_nbors || !in.d_val)) { h->err = "incomplete dij tables"; return ESP_EINVAL; }
+    PrepOutput prep;
+    std::string err;
+    int rc = prepare_tables(in, prep, err);
+    if (rc) { h->err = err; return rc == 2 ? ESP_ECOLOR : ESP_EINVAL; }
+    CK(cudaStreamSynchronize(h->st));
+    free_tables(h);
+    h->have_tables = false;
+    const size_t M = (size_t)prep.maxnb * h->N;
+    CK(dalloc(&h->d_nnb, h->N));
+    CK(dalloc(&h->d_nbr, M));
+    CK(dalloc(&h->d_perm, h->N));
+    CK(dalloc(&h->d_inv, h->N));
+    CK(dalloc(&h->d_J, M));
+    CK(dalloc(&h->d_mag, h->N));
+    if ((rc = h2d(h, h->d_nnb, prep.nnb.data(), sizeof(int32_t) * h->N))) return rc;
+    if ((rc = h2d(h, h->d_nbr, prep.nbr.data(), sizeof(int32_t) * M))) return rc;
+    if ((rc = h2d(h, h->d_perm, prep.perm.data(), sizeof(int32_t) * h->N))) return rc;
+    if ((rc = h2d(h, h->d_inv, prep.inv.data(), sizeof(int32_t) * h->N))) return rc;
+    if ((rc = h2d(h, h->d_J, prep.J.data(), sizeof(float) * M))) return rc;
+    if ((rc = h2d(h, h->d_mag, prep.mag.data(), sizeof(float) * h->N))) return rc;
+    if (prep.has_b) {
+        CK(dalloc(&h->d_B, M));
+        if ((rc = h2d(h, h->d_B, prep.B.data(), sizeof(float) * M))) return rc;
+    }
+    if (prep.has_d) {
+        CK(dalloc(&h->d_Dx, M)); CK(dalloc(&h->d_Dy, M)); CK(dalloc(&h->d_Dz, M));
+        if ((rc = h2d(h, h->d_Dx, prep.Dx.data(), sizeof(float) * M))) return rc;
+        if ((rc = h2d(h, h->d_Dy, prep.Dy.data(), sizeof(float) * M))) return rc;
+        if ((rc = h2d(h, h->d_Dz, prep.Dz.data(), sizeof(float) * M))) return rc;
+    }
+    h->hsi = t->si_axis != nullptr && t->si_delta != nullptr;
+    h->hfld = t->field_axis != nullptr && t->field_val != nullptr;
+    std::vector<float4> si(h->na), fl(h->na);
+    for (int a = 0; a < h->na; ++a) {
+        if (h->hsi)
+            si[a] = make_float4((float)t->si_axis[3 * a], (float)t->si_axis[3 * a + 1], (float)t->si_axis[3 * a + 2],
+                                (float)t->si_delta[a]);
+        if (h->hfld)
+            fl[a] = make_float4((float)(t->field_val[a] * t->field_axis[3 * a]),
+                                (float)(t->field_val[a] * t->field_axis[3 * a + 1]),
+                                (float)(t->field_val[a] * t->field_axis[3 * a + 2]), 0.f);
+    }
+    CK(dalloc(&h->d_si, h->na));
+    CK(dalloc(&h->d_fld, h->na));
+    if ((rc = h2d(h, h->d_si, si.data(), sizeof(float4) * h->na))) return rc;
+    if ((rc = h2d(h, h->d_fld, fl.data(), sizeof(float4) * h->na))) return rc;
+    h->e_blocks = energy_blocks(h->N, h->R, h->max_blocks);
+    CK(dalloc(&h->d_scratch, (size_t)h->e_blocks * h->R * 4));
+    // P(M) grid (mcarlo.F90:432-442)
+    double mmax = 0.0;
+    for (int a = 0; a < h->na; ++a) mmax += std::fabs(t->mag[a]);
+    h->m_max = mmax; h->m_min = -mmax;
+    h->nf = (int)std::llround((h->m_max - h->m_min) / 0.01) + 1;
+    if (h->nf == 1) h->nf = 2;
+    dfree(h->d_pm);
+    CK(dalloc(&h->d_pm, (size_t)h->R * h->nf));
+    h->prep = std::move(prep);
+    h->have_tables = true;
+    return ESP_OK;
+}
+
+int esp_set_temperatures(esp_handle *h, const double *tems)
+{
+    if (!h || !tems) return ESP_EINVAL;
+    std::vector<float> beta(h->R);
+    std::vector<double> inv(h->R);
+    for (int t = 0; t < h->R; ++t) {
+        if (!(tems[t] > 0.0)) { h->err = "temperatures must be positive"; return ESP_EINVAL; }
+        beta[t] = (float)(1.0 / tems[t]);
+        inv[t] = 1.0 / tems[t];
+    }
+    h->tems.assign(tems, tems + h->R);
+    CK(cudaMemcpyAsync(h->d_beta, beta.data(), sizeof(float) * h->R, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_inv_t, inv.data(), sizeof(double) * h->R, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->have_temps = true;
+    return identity_labels(h);
+}
+
+int esp_set_spins(esp_handle *h, const double *spins)
+{
+    int rc = require(h, true, false);
+    if (rc) return rc;
+    if (!spins) { h->err = "null spins"; return ESP_EINVAL; }
+    std::vector<int32_t> ra;
+    if ((rc = get_repl_at(h, ra))) return rc;
+    const size_t NR = (size_t)h->N * h->R;
+    std::vector<float> x(NR), y(NR), z(NR);
+    for (int t = 0; t < h->R; ++t) {
+        const int r = ra[t];
+        for (int i = 0; i < h->N; ++i) {
+            const size_t o = (size_t)h->prep.inv[i] * h->R + r;
+            const double *s = spins + 3 * ((size_t)t * h->N + i);
+            x[o] = (float)s[0]; y[o] = (float)s[1]; z[o] = (float)s[2];
+        }
+    }
+    if ((rc = h2d(h, h->d_sx, x.data(), sizeof(float) * NR))) return rc;
+    if ((rc = h2d(h, h->d_sy, y.data(), sizeof(float) * NR))) return rc;
+    if ((rc = h2d(h, h->d_sz, z.data(), sizeof(float) * NR))) return rc;
+    if ((rc = reset_running(h))) return rc;
+    CK(cudaStreamSynchronize(h->st));
+    return ESP_OK;
+}
+
+int esp_init_spins(esp_handle *h, int32_t kind, uint64_t seed)
+{
+    int rc = require(h, true, false);
+    if (rc) return rc;
+    if (kind != 0 && kind != 1) { h->err = "kind must be 0 (ferro) or 1 (rand)"; return ESP_EINVAL; }
+    CK(launch_init_spins(h->d_perm, h->d_mag, h->d_sx, h->d_sy, h->d_sz, h->N, h->R, kind, seed, h->st));
+    h->launches++;
+    if ((rc = reset_running(h))) return rc;
+    CK(cudaStreamSynchronize(h->st));
+    return ESP_OK;
+}
+
+int esp_get_spins(esp_handle *h, double *spins)
+{
+    int rc = require(h, true, false);
+    if (rc) return rc;
+    std::vector<int32_t> ra;
+    if ((rc = get_repl_at(h, ra))) return rc;
+    const size_t NR = (size_t)h->N * h->R;
+    std::vector<float> x(NR), y(NR), z(NR);
+    CK(cudaMemcpyAsync(x.data(), h->d_sx, sizeof(float) * NR, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(y.data(), h->d_sy, sizeof(float) * NR, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(z.data(), h->d_sz, sizeof(float) * NR, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    for (int t = 0; t < h->R; ++t) {
+        const int r = ra[t];
+        for (int i = 0; i < h->N; ++i) {
+            const size_t o = (size_t)h->prep.inv[i] * h->R + r;
+            double *s = spins + 3 * ((size_t)t * h->N + i);
+            s[0] = x[o]; s[1] = y[o]; s[2] = z[o];
+        }
+    }
+    return ESP_OK;
+}
+
+int esp_sweep(esp_handle *h, int64_t n, int64_t first_sweep, const esp_sweep_opts *o)
+{
+    int rc = require(h, true, true);
+    if (rc) return rc;
+    if (!o || n < 0) { h->err = "bad sweep arguments"; return ESP_EINVAL; }
+    if ((rc = do_sweeps(h, n, first_sweep, o))) return rc;
+    CK(cudaGetLastError());
+    return ESP_OK;
+}
+
+int esp_sweep_colour(esp_handle *h, int32_t colour, int64_t sweep, const esp_sweep_opts *o)
+{
+    int rc = require(h, true, true);
+    if (rc) return rc;
+    if (!o || colour < 0 || colour >= h->prep.num_colours) { h->err = "bad colour"; return ESP_EINVAL; }
+    return do_sweep_colour(h, colour, sweep, o);
+}
+
+int esp_pt_swap(esp_handle *h, int32_t start, int64_t swap_index, uint64_t seed)
+{
+    int rc = require(h, true, true);
+    if (rc) return rc;
+    if (start != 1 && start != 2) { h->err = "start must be 1 or 2"; return ESP_EINVAL; }
+    PtSwapArgs a;
+    a.repl_at = h->d_repl_at; a.temp_of = h->d_temp_of; a.e_run = h->d_e_run; a.inv_t = h->d_inv_t;
+    a.num_swaps = h->d_swaps; a.R = h->R; a.start0 = start - 1;
+    a.key0 = (uint32_t)seed; a.key1 = (uint32_t)(seed >> 32);
+    a.idx_lo = (uint32_t)swap_index; a.idx_hi = (uint32_t)((uint64_t)swap_index >> 32);
+    CK(launch_pt_swap(a, h->st));
+    h->launches++;
+    return ESP_OK;
+}
+
+int esp_energy(esp_handle *h, double *energy_out)
+{
+    int rc = require(h, true, false);
+    if (rc) return rc;
+    if ((rc = reset_running(h))) return rc;
+    if (energy_out) return by_slot(h, h->d_tmp_e, 1, energy_out);
+    CK(cudaStreamSynchronize(h->st));
+    return ESP_OK;
+}
+
+int esp_running_energy(esp_handle *h, double *out)
+{
+    int rc = require(h, true, false);
+    if (rc) return rc;
+    return by_slot(h, h->d_e_run, 1, out);
+}
+
+int esp_running_magnetization(esp_handle *h, double *out)
+{
+    int rc = require(h, true, false);
+    if (rc) return rc;
+    return by_slot(h, h->d_m_run, 3, out);
+}
+
+int esp_local_terms(esp_handle *h, double *g_out, double *q_out)
+{
+    int rc = require(h, true, false);
+    if (rc) return rc;
+    const size_t NR = (size_t)h->N * h->R;
+    float *dg = nullptr, *dq = nullptr;
+    CK(dalloc(&dg, NR * 3));
+    cudaError_t e = dalloc(&dq, NR * 6);
+    if (e != cudaSuccess) { cudaFree(dg); h->err = cudaGetErrorString(e); return ESP_ENOMEM; }
+    e = launch_local_terms(energy_args(h), dg, dq, h->st);
+    h->launches++;
+    std::vector<float> g(NR * 3), q(NR * 6);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g.data(), dg, sizeof(float) * NR * 3, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(q.data(), dq, sizeof(float) * NR * 6, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    cudaFree(dg); cudaFree(dq);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return ESP_ECUDA; }
+    std::vector<int32_t> ra;
+    if ((rc = get_repl_at(h, ra))) return rc;
+    for (int t = 0; t < h->R; ++t)
+        for (int i = 0; i < h->N; ++i) {
+            const size_t it = (size_t)h->prep.inv[i] * h->R + ra[t];
+            const size_t o = (size_t)t * h->N + i;
+            if (g_out) for (int c = 0; c < 3; ++c) g_out[3 * o + c] = g[3 * it + c];
+            if (q_out) for (int c = 0; c < 6; ++c) q_out[6 * o + c] = q[6 * it + c];
+        }
+    return ESP_OK;
+}
+
+int esp_get_colouring(esp_handle *h, int32_t *colour_out, int32_t *num_colours)
+{
+    int rc = require(h, true, false);
+    if (rc) return rc;
+    if (colour_out) for (int i = 0; i < h->N; ++i) colour_out[i] = h->prep.colour[i];
+    if (num_colours) *num_colours = h->prep.num_colours;
+    return ESP_OK;
+}
+
+int esp_get_rejected(esp_handle *h, int64_t *out)
+{
+    if (!h || !out) return ESP_EINVAL;
+    CK(cudaMemcpyAsync(out, h->d_rej, sizeof(int64_t) * 2 * h->R, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return ESP_OK;
+}
+
+int esp_get_replica_of_slot(esp_handle *h, int32_t *out)
+{
+    if (!h || !out) return ESP_EINVAL;
+    std::vector<int32_t> ra;
+    int rc = get_repl_at(h, ra);
+    if (rc) return rc;
+    std::copy(ra.begin(), ra.end(), out);
+    return ESP_OK;
+}
+
+int esp_num_freq(const esp_handle *h, int32_t *nf)
+{
+    if (!h || !nf) return ESP_EINVAL;
+    *nf = h->nf;
+    return ESP_OK;
+}
+
+int esp_launch_count(const esp_handle *h, int64_t *count)
+{
+    if (!h || !count) return ESP_EINVAL;
+    *count = h->launches;
+    return ESP_OK;
+}
+
+int esp_begin(esp_handle *h, const esp_schedule *s)
+{
+    int rc = require(h, true, true);
+    if (rc) return rc;
+    if (!s) { h->err = "null schedule"; return ESP_EINVAL; }
+    if (s->steps_mc < 1 || s->steps_warmup < 0 || s->steps_measure < 0 || (s->pt && s->pt_steps_swap < 1)) {
+        h->err = "invalid schedule";
+        return ESP_EINVAL;
+    }
+    const int R = h->R, N = h->N;
+    const int nlev = s->lbinerror ? s->num_binning_level : 0;
+    if (nlev > 0 && !s->binning_level) { h->err = "binning_level missing"; return ESP_EINVAL; }
+    for (int l = 0; l < nlev; ++l)
+        if (s->binning_level[l] <= 0 || s->binning_level[l] > 62) { h->err = "binning_level out of range"; return ESP_EINVAL; }
+    if ((rc = ensure_levels(h, nlev, s->binning_level))) return rc;
+    RunState &u = h->run;
+    u = RunState();
+    u.s = *s;
+    u.levels.assign(s->binning_level, s->binning_level + nlev);
+    u.nlev = nlev;
+    CK(cudaMemsetAsync(h->d_data, 0, sizeof(double) * 6 * R, h->st));
+    CK(cudaMemsetAsync(h->d_pm, 0, sizeof(unsigned long long) * R * h->nf, h->st));
+    CK(cudaMemsetAsync(h->d_rej, 0, sizeof(unsigned long long) * 2 * R, h->st));
+    CK(cudaMemsetAsync(h->d_swaps, 0, sizeof(long long) * 2 * R, h->st));
+    esp_sweep_opts o;
+    o.mcarlo_mode = s->mcarlo_mode; o.tilt_angles_max = s->tilt_angles_max; o.seed = s->seed; o.phase = 0;
+    u.e_init.assign(R, 0.0);
+    if (!s->pt) {
+        // mcarlo.F90:506-521: direct energy, then the warm-up sweeps
+        if ((rc = esp_energy(h, u.e_init.data()))) return rc;
+        if ((rc = do_sweeps(h, s->steps_warmup * s->steps_measure, h->next_sweep, &o))) return rc;
+        h->next_sweep += s->steps_warmup * s->steps_measure;
+        u.steps_tot[0] = s->steps_warmup * s->steps_measure * (int64_t)N;
+        u.total_units = s->steps_mc;
+    } else {
+        // pt.F90:524-735: warm-up halved into plain sweeps and swapped sweeps,
+        // both rounded up to whole swap intervals
+        const int64_t pss = s->pt_steps_swap;
+        int64_t sw = ceil_div(s->steps_warmup, 2);
+        const int64_t nsw_warm = ceil_div(sw, pss);
+        sw = nsw_warm * pss;
+        u.total_units = ceil_div(s->steps_mc, pss);
+        if ((rc = esp_energy(h, nullptr))) return rc;
+        if (sw > 0) {
+            if ((rc = do_sweeps(h, sw * s->steps_measure, h->next_sweep, &o))) return rc;
+            h->next_sweep += sw * s->steps_measure;
+            for (int64_t l = 1; l <= nsw_warm; ++l) {
+                if ((rc = do_sweeps(h, pss * s->steps_measure, h->next_sweep, &o))) return rc;
+                h->next_sweep += pss * s->steps_measure;
+                if ((rc = esp_pt_swap(h, (int)((l + 1) % 2) + 1, h->next_swap++, s->seed))) return rc;
+            }
+        }
+        u.steps_tot[0] = 2 * sw * s->steps_measure * (int64_t)N;
+        if ((rc = by_slot(h, h->d_e_run, 1, u.e_init.data()))) return rc;
+        CK(cudaMemsetAsync(h->d_swaps, 0, sizeof(long long) * 2 * R, h->st));
+    }
+    u.active = true;
+    return ESP_OK;
+}
+
+int esp_advance(esp_handle *h, int64_t n)
+{
+    int rc = require(h, true, true);
+    if (rc) return rc;
+    RunState &u = h->run;
+    if (!u.active) { h->err = "esp_begin has not been called"; return ESP_ESTATE; }
+    if (n < 0) { h->err = "negative step count"; return ESP_EINVAL; }
+    const esp_schedule &s = u.s;
+    esp_sweep_opts o;
+    o.mcarlo_mode = s.mcarlo_mode; o.tilt_angles_max = s.tilt_angles_max; o.seed = s.seed; o.phase = 1;
+    for (int64_t k = 0; k < n; ++k) {
+        if (!s.pt) {
+            // mcarlo.F90:526-590: steps_measure sweeps, then one measurement
+            if ((rc = do_sweeps(h, s.steps_measure, h->next_sweep, &o))) return rc;
+            h->next_sweep += s.steps_measure;
+            ++u.meas_done;
+            if ((rc = measure(h, u.meas_done, u.nlev, false, u.const_hits))) return rc;
+        } else {
+            // pt.F90:773-907: one swap interval, then pt_swap
+            const int64_t l = ++u.units_done;
+            for (int64_t mc = 1; mc <= s.pt_steps_swap; ++mc) {
+                if ((rc = do_sweeps(h, s.steps_measure, h->next_sweep, &o))) return rc;
+                h->next_sweep += s.steps_measure;
+                ++u.meas_done;
+                if ((rc = measure(h, u.meas_done, u.nlev, true, u.const_hits))) return rc;
+            }
+            if ((rc = esp_pt_swap(h, (int)((l + 1) % 2) + 1, h->next_swap++, s.seed))) return rc;
+        }
+    }
+    if (!s.pt) u.units_done += n;
+    return ESP_OK;
+}
+
+int esp_collect(esp_handle *h, esp_results *res)
+{
+    int rc = require(h, true, true);
+    if (rc) return rc;
+    RunState &u = h->run;
+    if (!u.active) { h->err = "esp_begin has not been called"; return ESP_ESTATE; }
+    if (!res) { h->err = "null results"; return ESP_EINVAL; }
+    if (u.meas_done < 1) { h->err = "no measurement has been made (esp_advance)"; return ESP_ESTATE; }
+    const int R = h->R, N = h->N, nlev = u.nlev;
+    const esp_schedule &s = u.s;
+    const int64_t steps_mc = u.meas_done;
+    std::vector<double> e_add(R), e_dir(R);
+    if ((rc = by_slot(h, h->d_e_run, 1, e_add.data()))) return rc;
+    if ((rc = do_energy(h))) return rc;
+    if ((rc = by_slot(h, h->d_tmp_e, 1, e_dir.data()))) return rc;
+    const double norm = 1.0 / (double)steps_mc;
+    std::vector<double> data((size_t)R * 6);
+    if ((rc = d2h(h, data.data(), h->d_data, sizeof(double) * 6 * R))) return rc;
+    std::vector<unsigned long long> rej((size_t)R * 2);
+    if ((rc = d2h(h, rej.data(), h->d_rej, sizeof(unsigned long long) * 2 * R))) return rc;
+    res->steps_mc_eff = steps_mc;
+    if (res->steps_tot) { res->steps_tot[0] = u.steps_tot[0]; res->steps_tot[1] = steps_mc * s.steps_measure * (int64_t)N; }
+    if (res->rejected)
+        for (int t = 0; t < 2 * R; ++t) res->rejected[t] = (int64_t)rej[t];
+    if (res->energy)
+        for (int t = 0; t < R; ++t) {
+            res->energy[3 * t] = u.e_init[t]; res->energy[3 * t + 1] = e_add[t]; res->energy[3 * t + 2] = e_dir[t];
+        }
+    if (res->data)
+        for (int i = 0; i < 6 * R; ++i) res->data[i] = data[i] * norm;
+    if (res->pm) {
+        std::vector<unsigned long long> cnt((size_t)R * h->nf);
+        if ((rc = d2h(h, cnt.data(), h->d_pm, sizeof(unsigned long long) * R * h->nf))) return rc;
+        const double ncell = (double)(N / h->na);
+        for (int t = 0; t < R; ++t) {
+            if (h->na == 1) cnt[(size_t)t * h->nf + h->nf - 1] += (unsigned long long)(u.const_hits * (long long)ncell);
+            // each hit adds 1/d_m = 100 (get_quant.F90:487); normalised by
+            // steps_mc * num_supercell (mcarlo.F90:715)
+            for (int f = 0; f < h->nf; ++f)
+                res->pm[(size_t)t * h->nf + f] = (double)cnt[(size_t)t * h->nf + f] * (1.0 / 0.01) * norm / ncell;
+        }
+    }
+    if (res->binning && nlev > 0) {
+        std::vector<double> ls((size_t)R * nlev * 2), bn((size_t)R * nlev * 2);
+        if ((rc = d2h(h, ls.data(), h->d_lsum, sizeof(double) * ls.size()))) return rc;
+        if ((rc = d2h(h, bn.data(), h->d_bin, sizeof(double) * bn.size()))) return rc;
+        // mcarlo.F90:635-656 / pt.F90:914-936
+        for (int t = 0; t < R; ++t)
+            for (int l = 0; l < nlev; ++l) {
+                const double blk = (double)(1LL << u.levels[l]);
+                const double m_l = (double)(steps_mc / (1LL << u.levels[l]));
+                for (int c = 0; c < 2; ++c) {
+                    const size_t k = ((size_t)t * nlev + l) * 2 + c;
+                    const double tot = c == 0 ? data[6 * t] / (double)N : data[6 * t + 3];
+                    double v = (tot - ls[k]) / blk / m_l;
+                    double b = bn[k] / m_l;
+                    b = (b - v * v) / (m_l - 1.0);
+                    if (s.pt) b = b / (double)N;
+                    res->binning[k] = b;
+                }
+            }
+    }
+    if (res->num_swaps || res->map) {
+        std::vector<long long> sw((size_t)R * 2);
+        if ((rc = d2h(h, sw.data(), h->d_swaps, sizeof(long long) * 2 * R))) return rc;
+        if (res->num_swaps) for (int i = 0; i < 2 * R; ++i) res->num_swaps[i] = sw[i];
+        if (res->map) {
+            std::vector<int32_t> ra;
+            if ((rc = get_repl_at(h, ra))) return rc;
+            for (int t = 0; t < R; ++t) res->map[t] = ra[t] + 1;
+        }
+    }
+    return ESP_OK;
+}
+
+int esp_run(esp_handle *h, const esp_schedule *s, esp_results *res)
+{
+    int rc = esp_begin(h, s);
+    if (rc) return rc;
+    if ((rc = esp_advance(h, h->run.total_units))) return rc;
+    return esp_collect(h, res);
+}
+
+}  // extern "C"

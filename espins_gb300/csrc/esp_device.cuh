@@ -1,0 +1,106 @@
+// Device-side building blocks shared by the Monte Carlo kernels.
+//
+// Random numbers: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), a
+// counter-based generator, replaces the reference's per-rank MT19937 stream
+// (ESpinS src/mtprng.f90).  One call yields the three uniforms one
+// Metropolis trial needs (get_quant.F90:80-93 draws two for the trial spin
+// and a third for the acceptance test only when dE > 0).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace esp {
+
+struct Philox4 {
+    uint32_t x, y, z, w;
+};
+
+__host__ __device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
+// Ten rounds; the key is bumped by the Weyl constants before rounds 2..10.
+__host__ __device__ __forceinline__ Philox4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                          uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint32_t hi0 = mulhi32(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        const uint32_t hi1 = mulhi32(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+    return Philox4{c0, c1, c2, c3};
+}
+
+// Uniform in [0,1) with 24 bits: exact in float and in double.
+__host__ __device__ __forceinline__ float u24f(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+// Uniform in [0,1) with 53 bits for FP64 decisions (PT swaps).
+__host__ __device__ __forceinline__ double u53(uint32_t a, uint32_t b)
+{
+    return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+// Trial spin of metropolis (get_quant.F90:80-162) in FP32.
+//  mode 0 'random': cos(theta) = 2u0-1, phi = 2 pi u1, length |mag|
+//  mode 1 'const' : theta = tilt*acos(2u0-1) about the old direction,
+//                   rotated as M = Rz(phi0) Ry(theta0) (get_quant.F90:136-159)
+__device__ __forceinline__ void trial_spin(int mode, float tilt, float mag, float ox, float oy, float oz,
+                                           uint32_t x0, uint32_t x1, float &nx, float &ny, float &nz)
+{
+    const float u0 = u24f(x0), u1 = u24f(x1);
+    float sphi, cphi;
+    sincospif(2.0f * u1, &sphi, &cphi);
+    if (mode == 0) {
+        const float c = 2.0f * u0 - 1.0f;
+        const float s = sqrtf(fmaxf(0.0f, 1.0f - c * c));
+        nx = mag * s * cphi;
+        ny = mag * s * sphi;
+        nz = mag * c;
+    } else {
+        const float theta = tilt * acosf(2.0f * u0 - 1.0f);
+        float st, ct;
+        sincosf(theta, &st, &ct);
+        const float tx = st * cphi, ty = st * sphi, tz = ct;
+        const float sxy = sqrtf(ox * ox + oy * oy);
+        float c0 = 1.0f, s0 = 0.0f;
+        if (sxy > 1e-8f) { c0 = ox / sxy; s0 = oy / sxy; }
+        const float inv = rsqrtf(ox * ox + oy * oy + oz * oz);
+        const float ax = ox * inv, ay = oy * inv, az = oz * inv;
+        nx = mag * (c0 * az * tx - s0 * ty + ax * tz);
+        ny = mag * (s0 * az * tx + c0 * ty + ay * tz);
+        nz = mag * (-sqrtf(ax * ax + ay * ay) * tx + az * tz);
+    }
+}
+
+// Arguments of the colour-class sweep over the merged ELL tables.
+struct SweepArgs {
+    // tables, permuted site order (colour-major); entry k of site p at k*N+p
+    const int32_t *nnb;
+    const int32_t *nbr;
+    const float *J, *B, *Dx, *Dy, *Dz;
+    const int32_t *perm;      // permuted -> reference site index (0-based)
+    const float *mag;         // [N] permuted
+    const float4 *si;         // [num_atoms] (ax, ay, az, Delta) or null
+    const float4 *fld;        // [num_atoms] (f ax, f ay, f az, 0) or null
+    // state, spin (p, r) at p*R + r
+    float *sx, *sy, *sz;
+    const int32_t *temp_of;   // replica -> temperature slot
+    const float *beta;        // slot -> 1/T
+    double *e_run;            // [R] running energy per replica
+    double *m_run;            // [R][3] running sum of spins per replica
+    unsigned long long *rej;  // [R slots][2]
+    int32_t N, R, num_atoms;
+    int32_t off_c, n_c;       // colour class: permuted sites [off_c, off_c + n_c)
+    int32_t phase, mode;
+    float tilt;
+    uint32_t key0, key1, sw_lo, sw_hi;
+};
+
+}  // namespace esp

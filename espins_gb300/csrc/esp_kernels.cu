@@ -1,0 +1,534 @@
+// Monte Carlo kernels for sm_103a.
+//
+//   k_sweep_ell      one colour class of a Metropolis sweep, every replica
+//                    (metropolis + delta_energy_get, get_quant.F90:52-182,264-337)
+//   k_energy_part    energy_get (get_quant.F90:186-261) and sum_i s_i per
+//                    replica: per-block partials into scratch ...
+//   k_energy_reduce  ... reduced in a fixed order (deterministic FP64)
+//   k_local_terms    the per-site linear/quadratic coefficients (parity checks)
+//   k_measure        per-measurement accumulators and binning
+//                    (mcarlo.F90:536-590, pt.F90:789-849)
+//   k_pm_hist        Pm_get (get_quant.F90:425-493) as an integer histogram
+//   k_pt_swap        pt_swap (pt.F90:1235-1288) on temperature labels
+//   k_init_spins     ferro / rand start configurations (mcarlo.F90:271-293)
+//
+// Layout: spins are FP32 SoA (sx, sy, sz), element (p, r) at p*R + r, with p
+// the colour-major permuted site index and r the replica.  Consecutive threads
+// take consecutive replicas of one site, so spin loads and stores of a warp
+// are contiguous and the table entries of a site are read once per warp.
+#include "esp_device.cuh"
+#include "esp_kernels.h"
+
+namespace esp {
+
+// ---------------------------------------------------------------------------
+// Block reduction of per-thread (dE, dMx, dMy, dMz, rejects) by replica.
+// Thread t of the block handles replica (base + t) % R, so the threads of one
+// replica are t0, t0+R, t0+2R, ...; thread t < min(R, blockDim) sums them.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void flush_replica_sums(double e, double mx, double my, double mz,
+                                                   unsigned int nrej, int r, int temp, int R, int phase,
+                                                   double *e_run, double *m_run, unsigned long long *rej,
+                                                   bool active)
+{
+    __shared__ double s_part[256][4];
+    __shared__ unsigned int s_rej[256];
+    __shared__ int s_r[256], s_t[256];
+    const int t = threadIdx.x;
+    const int nt = blockDim.x;
+    if (R >= nt) {
+        if (active) {
+            if (e != 0.0) atomicAdd(e_run + r, e);
+            if (mx != 0.0) atomicAdd(m_run + 3 * r, mx);
+            if (my != 0.0) atomicAdd(m_run + 3 * r + 1, my);
+            if (mz != 0.0) atomicAdd(m_run + 3 * r + 2, mz);
+            if (nrej) atomicAdd(rej + 2 * temp + phase, (unsigned long long)nrej);
+        }
+        return;
+    }
+    s_part[t][0] = active ? e : 0.0;
+    s_part[t][1] = active ? mx : 0.0;
+    s_part[t][2] = active ? my : 0.0;
+    s_part[t][3] = active ? mz : 0.0;
+    s_rej[t] = active ? nrej : 0u;
+    s_r[t] = active ? r : -1;
+    s_t[t] = temp;
+    __syncthreads();
+    if (t < R && s_r[t] >= 0) {
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        unsigned long long nr = 0;
+        for (int u = t; u < nt; u += R) {
+            if (s_r[u] < 0) continue;
+            a0 += s_part[u][0]; a1 += s_part[u][1]; a2 += s_part[u][2]; a3 += s_part[u][3];
+            nr += s_rej[u];
+        }
+        const int rr = s_r[t];
+        if (a0 != 0.0) atomicAdd(e_run + rr, a0);
+        if (a1 != 0.0) atomicAdd(m_run + 3 * rr, a1);
+        if (a2 != 0.0) atomicAdd(m_run + 3 * rr + 1, a2);
+        if (a3 != 0.0) atomicAdd(m_run + 3 * rr + 2, a3);
+        if (nr) atomicAdd(rej + 2 * s_t[t] + phase, nr);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// One colour class, all replicas.  Grid-stride with a stride that is a
+// multiple of R, so each thread keeps one replica for its whole life.
+// ---------------------------------------------------------------------------
+template <bool HB, bool HD>
+__global__ void __launch_bounds__(256) k_sweep_ell(const SweepArgs a)
+{
+    const int R = a.R;
+    const long long nthreads = (long long)gridDim.x * blockDim.x;
+    const long long S = (nthreads / R) * R;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = tid < S;
+    const int r = (int)(tid % R);
+    const int temp = a.temp_of[r];
+    double accE = 0.0, accX = 0.0, accY = 0.0, accZ = 0.0;
+    unsigned int nrej = 0;
+    if (live) {
+        const float beta = a.beta[temp];
+        const int pstep = (int)(S / R);
+        const bool has_si = a.si != nullptr, has_f = a.fld != nullptr;
+        for (int pi = (int)(tid / R); pi < a.n_c; pi += pstep) {
+            const int p = a.off_c + pi;
+            const size_t idx = (size_t)p * R + r;
+            const float ox = a.sx[idx], oy = a.sy[idx], oz = a.sz[idx];
+            float gx = 0.f, gy = 0.f, gz = 0.f;
+            float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
+            const int nn = __ldg(a.nnb + p);
+            for (int k = 0; k < nn; ++k) {
+                const size_t e = (size_t)k * a.N + p;
+                const int q = __ldg(a.nbr + e);
+                const size_t iq = (size_t)q * R + r;
+                const float tx = __ldg(a.sx + iq), ty = __ldg(a.sy + iq), tz = __ldg(a.sz + iq);
+                const float J = __ldg(a.J + e);
+                gx = fmaf(-J, tx, gx); gy = fmaf(-J, ty, gy); gz = fmaf(-J, tz, gz);
+                if (HB) {
+                    const float Bv = __ldg(a.B + e);
+                    const float bx = Bv * tx, by = Bv * ty, bz = Bv * tz;
+                    qxx = fmaf(bx, tx, qxx); qyy = fmaf(by, ty, qyy); qzz = fmaf(bz, tz, qzz);
+                    qxy = fmaf(bx, ty, qxy); qxz = fmaf(bx, tz, qxz); qyz = fmaf(by, tz, qyz);
+                }
+                if (HD) {
+                    const float dx = __ldg(a.Dx + e), dy = __ldg(a.Dy + e), dz = __ldg(a.Dz + e);
+                    // s_k x D_ik (the DM term of delta_energy_get as s_i . (s_k x D))
+                    gx += ty * dz - tz * dy;
+                    gy += tz * dx - tx * dz;
+                    gz += tx * dy - ty * dx;
+                }
+            }
+            const int orig = __ldg(a.perm + p);
+            if (has_si || has_f) {
+                const int at = orig % a.num_atoms;
+                if (has_si) {
+                    const float4 s = __ldg(a.si + at);
+                    const float dx = s.w * s.x, dy = s.w * s.y, dz = s.w * s.z;
+                    qxx = fmaf(dx, s.x, qxx); qyy = fmaf(dy, s.y, qyy); qzz = fmaf(dz, s.z, qzz);
+                    qxy = fmaf(dx, s.y, qxy); qxz = fmaf(dx, s.z, qxz); qyz = fmaf(dy, s.z, qyz);
+                }
+                if (has_f) {
+                    const float4 f = __ldg(a.fld + at);
+                    gx += f.x; gy += f.y; gz += f.z;
+                }
+            }
+            const Philox4 x = philox4x32_10((uint32_t)orig, (uint32_t)r, a.sw_lo, a.sw_hi, a.key0, a.key1);
+            float nx, ny, nz;
+            trial_spin(a.mode, a.tilt, __ldg(a.mag + p), ox, oy, oz, x.x, x.y, nx, ny, nz);
+            const float dx = nx - ox, dy = ny - oy, dz = nz - oz;
+            float de = gx * dx + gy * dy + gz * dz;
+            if (HB || has_si) {
+                // s_new^T Q s_new - s_old^T Q s_old = d^T Q (s_new + s_old)
+                const float px = nx + ox, py = ny + oy, pz = nz + oz;
+                de += dx * (qxx * px + qxy * py + qxz * pz)
+                    + dy * (qxy * px + qyy * py + qyz * pz)
+                    + dz * (qxz * px + qyz * py + qzz * pz);
+            }
+            bool acc = true;
+            if (de > 0.0f) acc = expf(-beta * de) >= u24f(x.z);
+            if (acc) {
+                a.sx[idx] = nx; a.sy[idx] = ny; a.sz[idx] = nz;
+                accE += (double)de;
+                accX += (double)dx; accY += (double)dy; accZ += (double)dz;
+            } else {
+                ++nrej;
+            }
+        }
+    }
+    flush_replica_sums(accE, accX, accY, accZ, nrej, r, temp, R, a.phase, a.e_run, a.m_run, a.rej, live);
+}
+
+// ---------------------------------------------------------------------------
+// Direct energy and magnetisation, stage 1: thread-local FP64 sums of the
+// per-site energies e_i = 1/2 sum_k pair_ik + Delta (s.a)^2 + f.s, then a
+// fixed-order block reduction per replica into scratch[block][R][4].
+// ---------------------------------------------------------------------------
+struct EnergyArgs {
+    const int32_t *nnb, *nbr;
+    const float *J, *B, *Dx, *Dy, *Dz;
+    const int32_t *perm;
+    const float4 *si, *fld;
+    const float *sx, *sy, *sz;
+    double *scratch;          // [gridDim.x][R][4]
+    int32_t N, R, num_atoms;
+};
+
+template <bool HB, bool HD>
+__global__ void __launch_bounds__(256) k_energy_part(const EnergyArgs a)
+{
+    __shared__ double s_acc[256][4];
+    const int R = a.R;
+    const long long nthreads = (long long)gridDim.x * blockDim.x;
+    const long long S = (nthreads / R) * R;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0, mx = 0, my = 0, mz = 0;
+    if (tid < S) {
+        const int r = (int)(tid % R);
+        const int pstep = (int)(S / R);
+        for (int p = (int)(tid / R); p < a.N; p += pstep) {
+            const size_t idx = (size_t)p * R + r;
+            const float ox = a.sx[idx], oy = a.sy[idx], oz = a.sz[idx];
+            float pair = 0.f;
+            const int nn = a.nnb[p];
+            for (int k = 0; k < nn; ++k) {
+                const size_t ee = (size_t)k * a.N + p;
+                const size_t iq = (size_t)a.nbr[ee] * R + r;
+                const float tx = a.sx[iq], ty = a.sy[iq], tz = a.sz[iq];
+                const float d = ox * tx + oy * ty + oz * tz;
+                pair -= a.J[ee] * d;
+                if (HB) pair += a.B[ee] * d * d;
+                if (HD) {
+                    const float cx = oy * tz - oz * ty, cy = oz * tx - ox * tz, cz = ox * ty - oy * tx;
+                    pair += a.Dx[ee] * cx + a.Dy[ee] * cy + a.Dz[ee] * cz;
+                }
+            }
+            float site = 0.5f * pair;
+            if (a.si || a.fld) {
+                const int at = a.perm[p] % a.num_atoms;
+                if (a.si) {
+                    const float4 s = a.si[at];
+                    const float sa = ox * s.x + oy * s.y + oz * s.z;
+                    site += s.w * sa * sa;
+                }
+                if (a.fld) {
+                    const float4 f = a.fld[at];
+                    site += f.x * ox + f.y * oy + f.z * oz;
+                }
+            }
+            e += (double)site;
+            mx += (double)ox; my += (double)oy; mz += (double)oz;
+        }
+    }
+    const int t = threadIdx.x;
+    s_acc[t][0] = e; s_acc[t][1] = mx; s_acc[t][2] = my; s_acc[t][3] = mz;
+    __syncthreads();
+    // replica of thread t is (blockIdx.x*blockDim.x + t) % R
+    const int base = (int)(((long long)blockIdx.x * blockDim.x) % R);
+    for (int rr = t; rr < R; rr += blockDim.x) {
+        // first thread of this block holding replica rr
+        int u0 = rr - base;
+        if (u0 < 0) u0 += R;
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        for (int u = u0; u < (int)blockDim.x; u += R) {
+            const long long g = (long long)blockIdx.x * blockDim.x + u;
+            if (g >= S) break;
+            a0 += s_acc[u][0]; a1 += s_acc[u][1]; a2 += s_acc[u][2]; a3 += s_acc[u][3];
+        }
+        double *o = a.scratch + ((size_t)blockIdx.x * R + rr) * 4;
+        o[0] = a0; o[1] = a1; o[2] = a2; o[3] = a3;
+    }
+}
+
+// Stage 2: out_e[r] = sum over blocks, in block order; out_m[r][3] likewise.
+__global__ void k_energy_reduce(const double *scratch, int nblocks, int R, double *out_e, double *out_m)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    for (int b = 0; b < nblocks; ++b) {
+        const double *o = scratch + ((size_t)b * R + r) * 4;
+        a0 += o[0]; a1 += o[1]; a2 += o[2]; a3 += o[3];
+    }
+    out_e[r] = a0;
+    if (out_m) { out_m[3 * r] = a1; out_m[3 * r + 1] = a2; out_m[3 * r + 2] = a3; }
+}
+
+// ---------------------------------------------------------------------------
+// Local terms g_i (3) and Q_i (6) of every (site, replica), FP32.
+// ---------------------------------------------------------------------------
+template <bool HB, bool HD>
+__global__ void k_local_terms(const EnergyArgs a, float *g, float *q)
+{
+    const long long total = (long long)a.N * a.R;
+    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
+         it += (long long)gridDim.x * blockDim.x) {
+        const int p = (int)(it / a.R), r = (int)(it % a.R);
+        float gx = 0, gy = 0, gz = 0, qxx = 0, qyy = 0, qzz = 0, qxy = 0, qxz = 0, qyz = 0;
+        const int nn = a.nnb[p];
+        for (int k = 0; k < nn; ++k) {
+            const size_t e = (size_t)k * a.N + p;
+            const size_t iq = (size_t)a.nbr[e] * a.R + r;
+            const float tx = a.sx[iq], ty = a.sy[iq], tz = a.sz[iq];
+            const float J = a.J[e];
+            gx = fmaf(-J, tx, gx); gy = fmaf(-J, ty, gy); gz = fmaf(-J, tz, gz);
+            if (HB) {
+                const float Bv = a.B[e];
+                const float bx = Bv * tx, by = Bv * ty, bz = Bv * tz;
+                qxx = fmaf(bx, tx, qxx); qyy = fmaf(by, ty, qyy); qzz = fmaf(bz, tz, qzz);
+                qxy = fmaf(bx, ty, qxy); qxz = fmaf(bx, tz, qxz); qyz = fmaf(by, tz, qyz);
+            }
+            if (HD) {
+                const float dx = a.Dx[e], dy = a.Dy[e], dz = a.Dz[e];
+                gx += ty * dz - tz * dy; gy += tz * dx - tx * dz; gz += tx * dy - ty * dx;
+            }
+        }
+        if (a.si || a.fld) {
+            const int at = a.perm[p] % a.num_atoms;
+            if (a.si) {
+                const float4 s = a.si[at];
+                const float dx = s.w * s.x, dy = s.w * s.y, dz = s.w * s.z;
+                qxx = fmaf(dx, s.x, qxx); qyy = fmaf(dy, s.y, qyy); qzz = fmaf(dz, s.z, qzz);
+                qxy = fmaf(dx, s.y, qxy); qxz = fmaf(dx, s.z, qxz); qyz = fmaf(dy, s.z, qyz);
+            }
+            if (a.fld) { const float4 f = a.fld[at]; gx += f.x; gy += f.y; gz += f.z; }
+        }
+        float *go = g + (size_t)it * 3;
+        go[0] = gx; go[1] = gy; go[2] = gz;
+        float *qo = q + (size_t)it * 6;
+        qo[0] = qxx; qo[1] = qyy; qo[2] = qzz; qo[3] = qxy; qo[4] = qxz; qo[5] = qyz;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-measurement accumulators, one thread per temperature slot.
+// data[t][6] += E, E^2, E^4, |m|, m^2, m^4 with m = M/N (mcarlo.F90:536-543);
+// binning sums as mcarlo.F90:548-590 (pt_quirk: pt.F90:841-849 divides a
+// completed block by 2**l, l being the level's position).
+// ---------------------------------------------------------------------------
+__global__ void k_measure(MeasureArgs a)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.R) return;
+    const int r = a.repl_at[t];
+    const double e = a.e_run[r];
+    const double mx = a.m_run[3 * r] / (double)a.N;
+    const double my = a.m_run[3 * r + 1] / (double)a.N;
+    const double mz = a.m_run[3 * r + 2] / (double)a.N;
+    const double m2 = mx * mx + my * my + mz * mz;
+    const double ee = e * e;
+    double *d = a.data + 6 * t;
+    d[0] += e; d[1] += ee; d[2] += ee * ee;
+    const double am = sqrt(m2);
+    d[3] += am; d[4] += m2; d[5] += m2 * m2;
+    if (a.nlev > 0) {
+        double *ls = a.lsum + (size_t)t * a.nlev * 2;
+        double *bn = a.binning + (size_t)t * a.nlev * 2;
+        for (int l = 0; l < a.nlev; ++l) {
+            ls[2 * l] += e / (double)a.N;
+            ls[2 * l + 1] += am;
+            const long long blk = 1LL << a.levels[l];
+            if (a.step % blk == 0) {
+                const double div = a.pt_quirk ? (double)(1LL << (l + 1)) : (double)blk;
+                for (int c = 0; c < 2; ++c) {
+                    const double v = ls[2 * l + c] / div;
+                    bn[2 * l + c] += v * v;
+                    ls[2 * l + c] = 0.0;
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// P(M) histogram (Pm_get): per unit cell |sum_atoms s| -> bin
+// max(nint((|m| - m_min)/(m_max - m_min) * (nf-1)) + 1, 1), counted as
+// integers per temperature slot (the reference adds 1/d_m = 100 per hit).
+// Block: a tile of cells x all replicas, shared histogram [R][nf] when it fits.
+// ---------------------------------------------------------------------------
+__global__ void k_pm_hist(PmArgs a)
+{
+    extern __shared__ unsigned int s_hist[];
+    const int R = a.R;
+    const bool shared = a.use_shared;
+    if (shared) {
+        for (int i = threadIdx.x; i < R * a.nf; i += blockDim.x) s_hist[i] = 0u;
+        __syncthreads();
+    }
+    const long long total = (long long)a.ncell * R;
+    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
+         it += (long long)gridDim.x * blockDim.x) {
+        const int cell = (int)(it / R), r = (int)(it % R);
+        double mx = 0, my = 0, mz = 0;
+        for (int at = 0; at < a.num_atoms; ++at) {
+            const int p = a.inv[cell * a.num_atoms + at];
+            const size_t idx = (size_t)p * R + r;
+            mx += (double)a.sx[idx]; my += (double)a.sy[idx]; mz += (double)a.sz[idx];
+        }
+        const double m = sqrt(mx * mx + my * my + mz * mz);
+        long long bin = llround(((m - a.m_min) / (a.m_max - a.m_min)) * (double)(a.nf - 1)) + 1;
+        if (bin < 1) bin = 1;
+        if (bin > a.nf) bin = a.nf;
+        const int t = a.temp_of[r];
+        if (shared) atomicAdd(s_hist + t * a.nf + (int)(bin - 1), 1u);
+        else atomicAdd(a.counts + (size_t)t * a.nf + (bin - 1), 1ULL);
+    }
+    if (shared) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < R * a.nf; i += blockDim.x)
+            if (s_hist[i]) atomicAdd(a.counts + i, (unsigned long long)s_hist[i]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pt_swap on labels: pairs (a, a+1), a = start0, start0+2, ...; one thread.
+// x = (1/T_a - 1/T_{a+1}) (E_a - E_{a+1}) with the running energies; accept
+// if x > 0 or u < exp(x).  The replicas keep their spins; the slot->replica
+// map (the reference's `map`) and replica->slot map are exchanged.
+// ---------------------------------------------------------------------------
+__global__ void k_pt_swap(PtSwapArgs a)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int s = a.start0; s + 1 < a.R; s += 2) {
+        const int ra = a.repl_at[s], rb = a.repl_at[s + 1];
+        const double x = (a.inv_t[s] - a.inv_t[s + 1]) * (a.e_run[ra] - a.e_run[rb]);
+        a.num_swaps[2 * s] += 1;
+        a.num_swaps[2 * (s + 1)] += 1;
+        bool swap = x > 0.0;
+        if (!swap) {
+            const Philox4 v = philox4x32_10((uint32_t)s, a.idx_lo, a.idx_hi, 0xFFFFFFFFu, a.key0, a.key1);
+            swap = u53(v.x, v.y) < exp(x);
+        }
+        if (swap) {
+            a.repl_at[s] = rb; a.repl_at[s + 1] = ra;
+            a.temp_of[rb] = s; a.temp_of[ra] = s + 1;
+            a.num_swaps[2 * s + 1] += 1;
+            a.num_swaps[2 * (s + 1) + 1] += 1;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Start configurations: kind 0 ferro (0,0,m); kind 1 rand with
+// theta = pi*u1, phi = 2 pi*u2 (mcarlo.F90:279-293), one configuration for
+// all replicas as pt.F90:448-459 does.
+// ---------------------------------------------------------------------------
+__global__ void k_init_spins(const int32_t *perm, const float *mag, float *sx, float *sy, float *sz,
+                             int N, int R, int kind, uint32_t k0, uint32_t k1)
+{
+    const long long total = (long long)N * R;
+    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
+         it += (long long)gridDim.x * blockDim.x) {
+        const int p = (int)(it / R);
+        const float m = mag[p];
+        float x = 0.f, y = 0.f, z = m;
+        if (kind == 1) {
+            const Philox4 v = philox4x32_10((uint32_t)perm[p], 0xFFFFFFFEu, 0u, 0u, k0, k1);
+            const double u1 = (double)v.x * (1.0 / 4294967296.0), u2 = (double)v.y * (1.0 / 4294967296.0);
+            double st, ct, sp, cp;
+            sincospi(u1, &st, &ct);
+            sincospi(2.0 * u2, &sp, &cp);
+            x = (float)(m * st * cp); y = (float)(m * st * sp); z = (float)(m * ct);
+        }
+        sx[it] = x; sy[it] = y; sz[it] = z;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launchers
+// ---------------------------------------------------------------------------
+static int grid_for(long long items, int threads, int max_blocks)
+{
+    long long b = (items + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > max_blocks) b = max_blocks;
+    return (int)b;
+}
+
+cudaError_t launch_sweep(const SweepArgs &a, bool hb, bool hd, int max_blocks, cudaStream_t st)
+{
+    const int threads = 256;
+    const long long items = (long long)a.n_c * a.R;
+    int blocks = grid_for(items, threads, max_blocks);
+    // the stride must hold at least one copy of every replica
+    const int need = (a.R + threads - 1) / threads;
+    if (blocks < need) blocks = need;
+    if (hb && hd) k_sweep_ell<true, true><<<blocks, threads, 0, st>>>(a);
+    else if (hb) k_sweep_ell<true, false><<<blocks, threads, 0, st>>>(a);
+    else if (hd) k_sweep_ell<false, true><<<blocks, threads, 0, st>>>(a);
+    else k_sweep_ell<false, false><<<blocks, threads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+int energy_blocks(int N, int R, int max_blocks)
+{
+    const int threads = 256;
+    int blocks = grid_for((long long)N * R, threads, max_blocks);
+    const int need = (R + threads - 1) / threads;
+    return blocks < need ? need : blocks;
+}
+
+cudaError_t launch_energy(const EnergyArgsHost &h, double *out_e, double *out_m, int blocks, cudaStream_t st)
+{
+    EnergyArgs a;
+    a.nnb = h.nnb; a.nbr = h.nbr; a.J = h.J; a.B = h.B; a.Dx = h.Dx; a.Dy = h.Dy; a.Dz = h.Dz;
+    a.perm = h.perm; a.si = h.si; a.fld = h.fld; a.sx = h.sx; a.sy = h.sy; a.sz = h.sz;
+    a.scratch = h.scratch; a.N = h.N; a.R = h.R; a.num_atoms = h.num_atoms;
+    const bool hb = h.B != nullptr, hd = h.Dx != nullptr;
+    if (hb && hd) k_energy_part<true, true><<<blocks, 256, 0, st>>>(a);
+    else if (hb) k_energy_part<true, false><<<blocks, 256, 0, st>>>(a);
+    else if (hd) k_energy_part<false, true><<<blocks, 256, 0, st>>>(a);
+    else k_energy_part<false, false><<<blocks, 256, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_energy_reduce<<<(h.R + 127) / 128, 128, 0, st>>>(h.scratch, blocks, h.R, out_e, out_m);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_local_terms(const EnergyArgsHost &h, float *g, float *q, cudaStream_t st)
+{
+    EnergyArgs a;
+    a.nnb = h.nnb; a.nbr = h.nbr; a.J = h.J; a.B = h.B; a.Dx = h.Dx; a.Dy = h.Dy; a.Dz = h.Dz;
+    a.perm = h.perm; a.si = h.si; a.fld = h.fld; a.sx = h.sx; a.sy = h.sy; a.sz = h.sz;
+    a.scratch = nullptr; a.N = h.N; a.R = h.R; a.num_atoms = h.num_atoms;
+    const int blocks = grid_for((long long)h.N * h.R, 256, 4096);
+    const bool hb = h.B != nullptr, hd = h.Dx != nullptr;
+    if (hb && hd) k_local_terms<true, true><<<blocks, 256, 0, st>>>(a, g, q);
+    else if (hb) k_local_terms<true, false><<<blocks, 256, 0, st>>>(a, g, q);
+    else if (hd) k_local_terms<false, true><<<blocks, 256, 0, st>>>(a, g, q);
+    else k_local_terms<false, false><<<blocks, 256, 0, st>>>(a, g, q);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_measure(const MeasureArgs &a, cudaStream_t st)
+{
+    k_measure<<<(a.R + 127) / 128, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pm(const PmArgs &a0, int max_blocks, cudaStream_t st)
+{
+    PmArgs a = a0;
+    const size_t smem = (size_t)a.R * a.nf * sizeof(unsigned int);
+    a.use_shared = smem <= 48 * 1024 ? 1 : 0;
+    const int blocks = grid_for((long long)a.ncell * a.R, 256, max_blocks);
+    k_pm_hist<<<blocks, 256, a.use_shared ? smem : 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pt_swap(const PtSwapArgs &a, cudaStream_t st)
+{
+    k_pt_swap<<<1, 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_spins(const int32_t *perm, const float *mag, float *sx, float *sy, float *sz,
+                              int N, int R, int kind, uint64_t seed, cudaStream_t st)
+{
+    const int blocks = grid_for((long long)N * R, 256, 4096);
+    k_init_spins<<<blocks, 256, 0, st>>>(perm, mag, sx, sy, sz, N, R, kind, (uint32_t)seed,
+                                         (uint32_t)(seed >> 32));
+    return cudaGetLastError();
+}
+
+}  // namespace esp

@@ -1,0 +1,57 @@
+// Launchers of the Monte Carlo kernels (esp_kernels.cu); host-side only.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "esp_device.cuh"
+
+namespace esp {
+
+struct EnergyArgsHost {
+    const int32_t *nnb, *nbr;
+    const float *J, *B, *Dx, *Dy, *Dz;
+    const int32_t *perm;
+    const float4 *si, *fld;
+    const float *sx, *sy, *sz;
+    double *scratch;          // [blocks][R][4]
+    int32_t N, R, num_atoms;
+};
+
+struct MeasureArgs {
+    const double *e_run, *m_run;
+    const int32_t *repl_at;
+    double *data;             // [R][6]
+    double *lsum, *binning;   // [R][nlev][2]
+    const int32_t *levels;    // [nlev] (device)
+    int32_t R, N, nlev, pt_quirk;
+    long long step;
+};
+
+struct PmArgs {
+    const float *sx, *sy, *sz;
+    const int32_t *inv;       // reference site -> permuted index
+    const int32_t *temp_of;
+    unsigned long long *counts;  // [R slots][nf]
+    int32_t R, ncell, num_atoms, nf, use_shared;
+    double m_min, m_max;
+};
+
+struct PtSwapArgs {
+    int32_t *repl_at, *temp_of;
+    const double *e_run, *inv_t;
+    long long *num_swaps;     // [R][2]
+    int32_t R, start0;
+    uint32_t key0, key1, idx_lo, idx_hi;
+};
+
+cudaError_t launch_sweep(const SweepArgs &a, bool hb, bool hd, int max_blocks, cudaStream_t st);
+int energy_blocks(int N, int R, int max_blocks);
+cudaError_t launch_energy(const EnergyArgsHost &h, double *out_e, double *out_m, int blocks, cudaStream_t st);
+cudaError_t launch_local_terms(const EnergyArgsHost &h, float *g, float *q, cudaStream_t st);
+cudaError_t launch_measure(const MeasureArgs &a, cudaStream_t st);
+cudaError_t launch_pm(const PmArgs &a, int max_blocks, cudaStream_t st);
+cudaError_t launch_pt_swap(const PtSwapArgs &a, cudaStream_t st);
+cudaError_t launch_init_spins(const int32_t *perm, const float *mag, float *sx, float *sy, float *sz,
+                              int N, int R, int kind, uint64_t seed, cudaStream_t st);
+
+}  // namespace esp

@@ -1,0 +1,30 @@
+// Host-side table preparation (esp_tables.cpp).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace esp {
+
+struct PrepInput {
+    int N, num_atoms, L[3];
+    const double *mag;
+    int j_maxnb; const int32_t *j_nn, *j_nbors; const double *j_val;
+    int b_maxnb; const int32_t *b_nn, *b_nbors; const double *b_val;
+    int d_maxnb; const int32_t *d_nn, *d_nbors; const double *d_val;
+};
+
+struct PrepOutput {
+    int maxnb = 0, num_colours = 0;
+    bool has_b = false, has_d = false;
+    std::vector<int> colour;      // reference site -> colour
+    std::vector<int> off;         // colour c owns permuted sites [off[c], off[c+1])
+    std::vector<int> perm, inv;   // permuted -> reference site, and back
+    std::vector<int32_t> nnb, nbr;
+    std::vector<float> J, B, Dx, Dy, Dz, mag;
+};
+
+// Returns 0 on success, 1 for invalid tables, 2 if the colouring check fails.
+int prepare_tables(const PrepInput &in, PrepOutput &out, std::string &err);
+
+}  // namespace esp

@@ -1,0 +1,338 @@
+"""ctypes binding of libespins_gpu.so (the C ABI in include/espins_gpu.h).
+
+This is the same binding a Python host of the library would write; a Fortran
+host uses the iso_c_binding interface block shown in INTEGRATION.md.  There is
+no CPU fallback: if the library cannot be loaded or no GPU is present, the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+
+ESP_OK, ESP_EINVAL, ESP_ECUDA, ESP_ENOMEM, ESP_ESTATE, ESP_ETIMEOUT, ESP_ECOLOR = range(7)
+
+EXPORTED = [
+    "esp_create", "esp_destroy", "esp_last_error", "esp_set_stream", "esp_upload_tables",
+    "esp_set_temperatures", "esp_set_spins", "esp_init_spins", "esp_run", "esp_begin",
+    "esp_advance", "esp_collect", "esp_sweep",
+    "esp_sweep_colour", "esp_pt_swap", "esp_energy", "esp_running_energy",
+    "esp_running_magnetization", "esp_local_terms", "esp_get_spins", "esp_get_colouring",
+    "esp_get_rejected", "esp_get_replica_of_slot", "esp_num_freq", "esp_launch_count",
+]
+
+
+class EspError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"libespins_gpu error {code}: {msg}")
+        self.code = code
+
+
+class Dims(C.Structure):
+    _fields_ = [("num_sites", C.c_int32), ("num_atoms", C.c_int32), ("supercell", C.c_int32 * 3),
+                ("num_replicas", C.c_int32), ("open_boundary", C.c_int32)]
+
+
+class Tables(C.Structure):
+    _fields_ = [("mag", C.c_void_p),
+                ("j_maxnb", C.c_int32), ("j_nn", C.c_void_p), ("j_nbors", C.c_void_p), ("j_val", C.c_void_p),
+                ("b_maxnb", C.c_int32), ("b_nn", C.c_void_p), ("b_nbors", C.c_void_p), ("b_val", C.c_void_p),
+                ("d_maxnb", C.c_int32), ("d_nn", C.c_void_p), ("d_nbors", C.c_void_p), ("d_val", C.c_void_p),
+                ("si_axis", C.c_void_p), ("si_delta", C.c_void_p),
+                ("field_axis", C.c_void_p), ("field_val", C.c_void_p)]
+
+
+class Schedule(C.Structure):
+    _fields_ = [("steps_warmup", C.c_int64), ("steps_mc", C.c_int64), ("steps_measure", C.c_int64),
+                ("pt", C.c_int32), ("mcarlo_mode", C.c_int32), ("pt_steps_swap", C.c_int64),
+                ("tilt_angles_max", C.c_double), ("seed", C.c_uint64), ("lbinerror", C.c_int32),
+                ("num_binning_level", C.c_int32), ("binning_level", C.c_void_p)]
+
+
+class Results(C.Structure):
+    _fields_ = [("rejected", C.c_void_p), ("steps_tot", C.c_void_p), ("energy", C.c_void_p),
+                ("data", C.c_void_p), ("pm", C.c_void_p), ("binning", C.c_void_p),
+                ("num_swaps", C.c_void_p), ("map", C.c_void_p), ("steps_mc_eff", C.c_int64)]
+
+
+class SweepOpts(C.Structure):
+    _fields_ = [("mcarlo_mode", C.c_int32), ("tilt_angles_max", C.c_double), ("seed", C.c_uint64),
+                ("phase", C.c_int32)]
+
+
+_lib = None
+
+
+def load(build_if_missing: bool = True):
+    """Load libespins_gpu.so from the package directory (building it if asked)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError(f"{path} is missing: run espins_gb300.build.build()")
+        _build.build()
+    lib = C.CDLL(path)
+    P, vp = C.POINTER, C.c_void_p
+    lib.esp_create.argtypes = [P(Dims), P(vp)]
+    lib.esp_destroy.argtypes = [vp]
+    lib.esp_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+    lib.esp_set_stream.argtypes = [vp, vp]
+    lib.esp_upload_tables.argtypes = [vp, P(Tables)]
+    lib.esp_set_temperatures.argtypes = [vp, vp]
+    lib.esp_set_spins.argtypes = [vp, vp]
+    lib.esp_init_spins.argtypes = [vp, C.c_int32, C.c_uint64]
+    lib.esp_run.argtypes = [vp, P(Schedule), P(Results)]
+    lib.esp_begin.argtypes = [vp, P(Schedule)]
+    lib.esp_advance.argtypes = [vp, C.c_int64]
+    lib.esp_collect.argtypes = [vp, P(Results)]
+    lib.esp_sweep.argtypes = [vp, C.c_int64, C.c_int64, P(SweepOpts)]
+    lib.esp_sweep_colour.argtypes = [vp, C.c_int32, C.c_int64, P(SweepOpts)]
+    lib.esp_pt_swap.argtypes = [vp, C.c_int32, C.c_int64, C.c_uint64]
+    for f in ("esp_energy", "esp_running_energy", "esp_running_magnetization", "esp_get_spins",
+              "esp_get_rejected", "esp_get_replica_of_slot"):
+        getattr(lib, f).argtypes = [vp, vp]
+    lib.esp_local_terms.argtypes = [vp, vp, vp]
+    lib.esp_get_colouring.argtypes = [vp, vp, P(C.c_int32)]
+    lib.esp_num_freq.argtypes = [vp, P(C.c_int32)]
+    lib.esp_launch_count.argtypes = [vp, P(C.c_int64)]
+    for f in EXPORTED:
+        getattr(lib, f).restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
+
+
+class Engine:
+    """One lattice with R replicas on the GPU (an ``esp_handle``)."""
+
+    def __init__(self, n: int, num_atoms: int, supercell, num_replicas: int, open_boundary: bool = False):
+        self.lib = load()
+        d = Dims()
+        d.num_sites, d.num_atoms = int(n), int(num_atoms)
+        for c in range(3):
+            d.supercell[c] = int(supercell[c])
+        d.num_replicas, d.open_boundary = int(num_replicas), int(bool(open_boundary))
+        h = C.c_void_p()
+        rc = self.lib.esp_create(C.byref(d), C.byref(h))
+        if rc != ESP_OK:
+            buf = C.create_string_buffer(512)
+            self.lib.esp_last_error(None, buf, 512)
+            raise EspError(rc, buf.value.decode())
+        self.h = h
+        self.n, self.na, self.R = int(n), int(num_atoms), int(num_replicas)
+        self._keep = []
+
+    # -- plumbing -------------------------------------------------------------
+    def _check(self, rc: int):
+        if rc != ESP_OK:
+            buf = C.create_string_buffer(1024)
+            self.lib.esp_last_error(self.h, buf, 1024)
+            raise EspError(rc, buf.value.decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.esp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- data in --------------------------------------------------------------
+    def upload(self, ham) -> None:
+        """Upload a Hamiltonian (espins_gb300.tables.Hamiltonian or equivalent)."""
+        keep = []
+
+        def arr(a, dt):
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a.ctypes.data
+
+        t = Tables()
+        t.mag = arr(ham.mag, np.float64)
+
+        def ell(tab):
+            nn = arr(tab.nn, np.int32)
+            nb1 = (np.asarray(tab.nb, dtype=np.int32) + 1)
+            nbp = arr(nb1, np.int32)
+            # (maxnb, N[, 3]) C order is the memory order of jij_matrix(N,maxnb)
+            # and dij_matrix(3,N,maxnb)
+            val = arr(tab.val, np.float64)
+            return int(tab.nb.shape[0]), nn, nbp, val
+
+        t.j_maxnb, t.j_nn, t.j_nbors, t.j_val = ell(ham.jij)
+        if getattr(ham, "bij", None) is not None:
+            t.b_maxnb, t.b_nn, t.b_nbors, t.b_val = ell(ham.bij)
+        if getattr(ham, "dij", None) is not None:
+            t.d_maxnb, t.d_nn, t.d_nbors, t.d_val = ell(ham.dij)
+        if getattr(ham, "si_axis", None) is not None:
+            t.si_axis = arr(ham.si_axis, np.float64)
+            t.si_delta = arr(ham.si_delta, np.float64)
+        if getattr(ham, "field_axis", None) is not None:
+            t.field_axis = arr(ham.field_axis, np.float64)
+            t.field_val = arr(ham.field_val, np.float64)
+        self._check(self.lib.esp_upload_tables(self.h, C.byref(t)))
+
+    def set_temperatures(self, tems) -> None:
+        t = np.ascontiguousarray(tems, dtype=np.float64)
+        assert t.size == self.R
+        self._check(self.lib.esp_set_temperatures(self.h, _p(t)))
+
+    def set_spins(self, spins: np.ndarray) -> None:
+        """spins: (R, N, 3) in temperature-slot order."""
+        s = np.ascontiguousarray(spins, dtype=np.float64)
+        assert s.shape == (self.R, self.n, 3)
+        self._check(self.lib.esp_set_spins(self.h, _p(s)))
+
+    def init_spins(self, kind: str = "ferro", seed: int = 0) -> None:
+        k = {"ferro": 0, "rand": 1}[kind]
+        self._check(self.lib.esp_init_spins(self.h, k, int(seed) & 0xFFFFFFFFFFFFFFFF))
+
+    def set_stream(self, stream_ptr: int) -> None:
+        self._check(self.lib.esp_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    # -- hot path ---------------------------------------------------------------
+    @staticmethod
+    def _opts(mode: int, tilt: float, seed: int, phase: int) -> SweepOpts:
+        o = SweepOpts()
+        o.mcarlo_mode, o.tilt_angles_max, o.seed, o.phase = int(mode), float(tilt), int(seed) & (2 ** 64 - 1), int(phase)
+        return o
+
+    def sweep(self, n: int, first_sweep: int, seed: int, mode: int = 0, tilt: float = 0.125, phase: int = 1):
+        o = self._opts(mode, tilt, seed, phase)
+        self._check(self.lib.esp_sweep(self.h, int(n), int(first_sweep), C.byref(o)))
+
+    def sweep_colour(self, colour: int, sweep: int, seed: int, mode: int = 0, tilt: float = 0.125, phase: int = 1):
+        o = self._opts(mode, tilt, seed, phase)
+        self._check(self.lib.esp_sweep_colour(self.h, int(colour), int(sweep), C.byref(o)))
+
+    def pt_swap(self, start: int, swap_index: int, seed: int):
+        self._check(self.lib.esp_pt_swap(self.h, int(start), int(swap_index), int(seed) & (2 ** 64 - 1)))
+
+    def schedule(self, steps_warmup: int, steps_mc: int, steps_measure: int, pt: bool = False,
+                 pt_steps_swap: int = 1, mode: int = 0, tilt: float = 0.125, seed: int = 1,
+                 binning_level=None) -> Schedule:
+        s = Schedule()
+        s.steps_warmup, s.steps_mc, s.steps_measure = int(steps_warmup), int(steps_mc), int(steps_measure)
+        s.pt, s.mcarlo_mode, s.pt_steps_swap = int(bool(pt)), int(mode), int(pt_steps_swap)
+        s.tilt_angles_max, s.seed = float(tilt), int(seed) & (2 ** 64 - 1)
+        bl = np.ascontiguousarray(binning_level if binning_level else [], dtype=np.int32)
+        s.lbinerror = int(bl.size > 0)
+        s.num_binning_level = int(bl.size)
+        s.binning_level = _p(bl) if bl.size else None
+        s._levels = bl  # keep the array alive with the struct
+        return s
+
+    def _results(self, nlev: int):
+        R = self.R
+        out = {
+            "rejected": np.zeros((R, 2), dtype=np.int64), "steps_tot": np.zeros(2, dtype=np.int64),
+            "energy": np.zeros((R, 3)), "data": np.zeros((R, 6)), "pm": np.zeros((R, self.num_freq())),
+            "binning": np.zeros((R, max(nlev, 1), 2)), "num_swaps": np.zeros((R, 2), dtype=np.int64),
+            "map": np.zeros(R, dtype=np.int32),
+        }
+        r = Results()
+        for k in ("rejected", "steps_tot", "energy", "data", "pm", "binning", "num_swaps", "map"):
+            setattr(r, k, _p(out[k]))
+        return out, r
+
+    def begin(self, sched: Schedule) -> None:
+        self._sched = sched
+        self._check(self.lib.esp_begin(self.h, C.byref(sched)))
+
+    def advance(self, n: int) -> None:
+        self._check(self.lib.esp_advance(self.h, int(n)))
+
+    def collect(self) -> dict:
+        nlev = self._sched.num_binning_level
+        out, r = self._results(nlev)
+        self._check(self.lib.esp_collect(self.h, C.byref(r)))
+        out["steps_mc_eff"] = r.steps_mc_eff
+        if nlev == 0:
+            out["binning"] = None
+        return out
+
+    def run(self, steps_warmup: int, steps_mc: int, steps_measure: int, pt: bool = False,
+            pt_steps_swap: int = 1, mode: int = 0, tilt: float = 0.125, seed: int = 1,
+            binning_level=None) -> dict:
+        """esp_run: the whole schedule of mcarlo_main / pt_main."""
+        s = self.schedule(steps_warmup, steps_mc, steps_measure, pt, pt_steps_swap, mode, tilt, seed,
+                          binning_level)
+        nlev = s.num_binning_level
+        out, r = self._results(nlev)
+        self._check(self.lib.esp_run(self.h, C.byref(s), C.byref(r)))
+        out["steps_mc_eff"] = r.steps_mc_eff
+        if nlev == 0:
+            out["binning"] = None
+        return out
+
+    # -- observables --------------------------------------------------------------
+    def energy(self) -> np.ndarray:
+        e = np.zeros(self.R)
+        self._check(self.lib.esp_energy(self.h, _p(e)))
+        return e
+
+    def running_energy(self) -> np.ndarray:
+        e = np.zeros(self.R)
+        self._check(self.lib.esp_running_energy(self.h, _p(e)))
+        return e
+
+    def running_magnetization(self) -> np.ndarray:
+        m = np.zeros((self.R, 3))
+        self._check(self.lib.esp_running_magnetization(self.h, _p(m)))
+        return m
+
+    def local_terms(self):
+        g = np.zeros((self.R, self.n, 3))
+        q = np.zeros((self.R, self.n, 6))
+        self._check(self.lib.esp_local_terms(self.h, _p(g), _p(q)))
+        return g, q
+
+    def get_spins(self) -> np.ndarray:
+        s = np.zeros((self.R, self.n, 3))
+        self._check(self.lib.esp_get_spins(self.h, _p(s)))
+        return s
+
+    def colouring(self):
+        c = np.zeros(self.n, dtype=np.int32)
+        k = C.c_int32()
+        self._check(self.lib.esp_get_colouring(self.h, _p(c), C.byref(k)))
+        return c, k.value
+
+    def rejected(self) -> np.ndarray:
+        r = np.zeros((self.R, 2), dtype=np.int64)
+        self._check(self.lib.esp_get_rejected(self.h, _p(r)))
+        return r
+
+    def replica_of_slot(self) -> np.ndarray:
+        r = np.zeros(self.R, dtype=np.int32)
+        self._check(self.lib.esp_get_replica_of_slot(self.h, _p(r)))
+        return r
+
+    def num_freq(self) -> int:
+        k = C.c_int32()
+        self._check(self.lib.esp_num_freq(self.h, C.byref(k)))
+        return k.value
+
+    def launch_count(self) -> int:
+        k = C.c_int64()
+        self._check(self.lib.esp_launch_count(self.h, C.byref(k)))
+        return k.value

@@ -1,0 +1,182 @@
+"""Writers of the reference's output files, byte-compatible in layout.
+
+Formats follow ESpinS src/mcarlo.F90:106-200 (headers), :784-818 (rows) and
+src/pt.F90:1040-1085:
+* ``seed_mc.dat``       format 125: (f9.4,2x,6(E15.8,2x)) per temperature
+* ``seed_pm.dat``       '#T=' line (1x,a,2x,f9.4), rows (2x,E15.8,10x,E15.8)
+* ``seed_sconfig.dat``  date line, (3I6) supercell, (2I6) N and tems_num, then
+                        per temperature (F12.6) T and (3F12.6) spins
+* ``seed_binerror.dat`` '#T=' line, rows (2x,I8,8x,E15.8,3x,E15.8)
+* ``seed.mcout``        the MONTECARLO summary block of mcarlo.F90:736-753 /
+                        pt.F90:1000-1010 (format 124)
+"""
+from __future__ import annotations
+
+import datetime
+import math
+from typing import Sequence
+
+import numpy as np
+
+
+def fortran_e(x: float, w: int = 15, d: int = 8) -> str:
+    """Fortran Ew.d: 0.ddddddddE+xx, right-justified in w characters."""
+    x = float(x)
+    if x == 0.0 or not math.isfinite(x):
+        if not math.isfinite(x):
+            return ("NaN" if math.isnan(x) else ("-Infinity" if x < 0 else "Infinity")).rjust(w)
+        body = "0." + "0" * d + "E+00"
+        return body.rjust(w)
+    sign = "-" if x < 0 else ""
+    a = abs(x)
+    e = math.floor(math.log10(a)) + 1
+    m = a / 10.0 ** e
+    digits = round(m * 10 ** d)
+    if digits >= 10 ** d:  # rounding carried into a new digit
+        digits //= 10
+        e += 1
+    if digits < 10 ** (d - 1):
+        digits *= 10
+        e -= 1
+    s = f"{sign}0.{digits:0{d}d}E{'+' if e >= 0 else '-'}{abs(e):02d}"
+    return s.rjust(w)
+
+
+def fortran_f(x: float, w: int, d: int) -> str:
+    s = f"{x:.{d}f}"
+    if s.startswith("0.") and len(s) > w:
+        s = s[1:]
+    elif s.startswith("-0.") and len(s) > w:
+        s = "-" + s[2:]
+    return s.rjust(w) if len(s) <= w else "*" * w
+
+
+def _date() -> str:
+    now = datetime.datetime.now()
+    return now.strftime("%d%b%Y").lstrip("0").rjust(9), now.strftime("%H:%M:%S")
+
+
+def write_mc_dat(path: str, tems: Sequence[float], data: np.ndarray, n: int) -> None:
+    """data: (R, 6) normalised <E>,<E2>,<E4>,<|m|>,<m2>,<m4> (mcarlo.F90:713-757)."""
+    d, t = _date()
+    with open(path, "w") as fh:
+        fh.write(f" #written on {d} at {t} \n")
+        fh.write(" #------------------------------------------------- MONTECARLO --------"
+                 "-----------------------------------------#\n")
+        fh.write(" # Temp      Magnetization     Energy_ave          C_M              Sus"
+                 "              U_E              U_M       #\n")
+        fh.write(" #-----------------------------------------------------------------------"
+                 "---------------------------------------#\n")
+        for T, row in zip(tems, data):
+            for line in [mc_dat_row(T, row, n)]:
+                fh.write(line + "\n")
+
+
+def observables(T: float, row: np.ndarray, n: int):
+    beta = 1.0 / T
+    E, E2, E4, M, M2, M4 = row
+    C = beta * beta * (E2 - E ** 2) / n
+    chi = beta * (M2 - M ** 2) * n
+    UE = 1.0 - (1.0 / 3.0) * (E4 / E2 ** 2)
+    UM = 1.0 - (1.0 / 3.0) * (M4 / M2 ** 2)
+    return M, E / n, C, chi, UE, UM
+
+
+def mc_dat_row(T: float, row: np.ndarray, n: int) -> str:
+    vals = observables(T, row, n)
+    return fortran_f(T, 9, 4) + "".join("  " + fortran_e(v) for v in vals)
+
+
+def write_pm_dat(path: str, tems, pm: np.ndarray, m_min: float, m_max: float) -> None:
+    nf = pm.shape[1]
+    dm = (m_max - m_min) / (nf - 1)
+    m_array = [m_min + i * dm for i in range(nf)]
+    d, t = _date()
+    with open(path, "w") as fh:
+        fh.write(f" #written on {d} at {t} \n")
+        fh.write(" #----------------- MONTECARLO -------------------#\n")
+        fh.write(" #        M                      P(M)             #\n")
+        fh.write(" #------------------------------------------------#\n")
+        for T, row in zip(tems, pm):
+            fh.write(" #T=  " + fortran_f(T, 9, 4) + "\n")
+            for m, p in zip(m_array, row):
+                fh.write("  " + fortran_e(m) + " " * 10 + fortran_e(p) + "\n")
+
+
+def write_sconfig(path: str, supercell, tems, spins: np.ndarray) -> None:
+    """spins: (R, N, 3) as the reference's global_spin_matrix(3,N,R)."""
+    d, t = _date()
+    R, N, _ = spins.shape
+    with open(path, "w") as fh:
+        fh.write(f" Created on {d} at {t} \n")
+        fh.write("".join(f"{int(v):6d}" for v in supercell) + "\n")
+        fh.write(f"{N:6d}{R:6d}\n")
+        for T, blk in zip(tems, spins):
+            fh.write(fortran_f(T, 12, 6) + "\n")
+            for s in blk:
+                fh.write("".join(fortran_f(v, 12, 6) for v in s) + "\n")
+
+
+def read_sconfig(path: str, n: int, tems) -> np.ndarray:
+    """``mcarlo_read_sconfig`` (get_quant.F90:543-598): spins normalised to unit length."""
+    with open(path) as fh:
+        lines = fh.read().splitlines()
+    nw, nt = (int(x) for x in lines[2].split())
+    if nw != n:
+        raise ValueError("Wrong matrix size in mcarlo: read_sconfig")
+    if nt != len(tems):
+        raise ValueError("Wrong temperature number in mcarlo: read_sconfig")
+    out = np.zeros((nt, n, 3))
+    pos = 3
+    for k in range(nt):
+        tt = float(lines[pos]); pos += 1
+        if abs(tt - tems[k]) > 1e-4:
+            raise ValueError("Mismatch in temperatures: read_sconfig")
+        blk = np.array([[float(v) for v in lines[pos + j].split()[:3]] for j in range(n)])
+        pos += n
+        if np.any(np.all(np.abs(blk) < 1e-4, axis=1)):
+            raise ValueError("All components of an spin in block are zero")
+        out[k] = blk / np.sqrt((blk * blk).sum(axis=1, keepdims=True))
+    return out
+
+
+def write_binerror(path: str, tems, binning: np.ndarray, levels, n: int, pt: bool) -> None:
+    with open(path, "w") as fh:
+        fh.write(" #------------------- MONTECARLO -----------------#\n")
+        fh.write(" #  Block_length      Error(E)          Error(M)  #\n")
+        fh.write(" #------------------------------------------------#\n")
+        for T, b in zip(tems, binning):
+            fh.write(" #T=  " + (fortran_f(T, 6, 2) if pt else fortran_f(T, 9, 4)) + "\n")
+            for lv, row in zip(levels, b):
+                vals = np.sqrt(np.maximum(row, 0.0)) if pt else np.sqrt(np.maximum(row / n, 0.0))
+                fh.write(f"  {int(lv):8d}        " + fortran_e(vals[0]) + "   " + fortran_e(vals[1]) + "\n")
+
+
+def mcout_block(tems, res: dict, n: int, pt: bool) -> str:
+    """Accept/reject table and energy triple per temperature (mcarlo.F90:736-753)."""
+    out = []
+    norm = 1.0 / res["steps_mc_eff"]
+    for t, T in enumerate(tems):
+        tot = int(res["steps_tot"][1])
+        rej = int(res["rejected"][t][1])
+        out.append(f"   {fortran_f(T, 9, 4)} {tot:14d} {rej:14d}     {tot - rej:14d}       "
+                   f"{(tot - rej) / tot:10.8f} {' ' * 3 if pt else ''} <-- MCARLO")
+        E = res["energy"][t]
+        out.append(f"     Initial Energy                           = {fortran_e(E[0], 15, 7)}  <-- ENERGY")
+        out.append(f"     Final Energy by adding differences       = {fortran_e(E[1], 15, 7)}  <-- ENERGY")
+        out.append(f"     Final Energy by direct calculations      = {fortran_e(E[2], 15, 7)}  <-- ENERGY")
+        d = res["data"][t]
+        dE = math.sqrt(max(d[1] - d[0] ** 2, 0.0) * norm) / n
+        dM = math.sqrt(max(d[4] - d[3] ** 2, 0.0) * norm)
+        out.append(f"                                 Delta E      = +/- {dE:15.9f}")
+        out.append(f"                                 Delta M      = +/- {dM:15.9f}")
+        out.append(" " + "-" * 85)
+    if pt:
+        out.append(" |  Temp_i     Temp_f         Tot-Swaps       Rej-Swaps      Acc-Swaps  Acc/Tot Ratio|")
+        for t, T in enumerate(tems):
+            tries, acc = (int(x) for x in res["num_swaps"][t])
+            Tf = tems[int(res["map"][t]) - 1]
+            ratio = acc / tries if tries else 0.0
+            out.append(f"  {fortran_f(T, 9, 4)}  {fortran_f(Tf, 9, 4)} {tries:14d} {tries - acc:14d} "
+                       f"{acc:14d}   {ratio:14.8f}  ")
+    return "\n".join(out) + "\n"

@@ -1,0 +1,199 @@
+/*
+ * espins_gpu.h -- C ABI of the GB300 Monte Carlo library (libespins_gpu.so).
+ *
+ * The library replaces the Monte Carlo hot path of ESpinS, which the Fortran
+ * program reaches by direct calls from mc_prog (src/mc_prog.F90:170-186:
+ * `call mcarlo_main()` / `call pt_main()`), with all data held in module
+ * globals.  A Fortran host keeps param_read and jij_get/bij_get/dij_get,
+ * hands the resulting ELL tables to esp_upload_tables, and calls esp_run in
+ * place of mcarlo_main/pt_main.  INTEGRATION.md shows the iso_c_binding
+ * interface block.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: ESP_OK (0) or an ESP_E* code;
+ *    esp_last_error() returns the message.  The Fortran shim passes a nonzero
+ *    status to io_error (src/io.F90:217-266), which is how the reference stops.
+ *  - Arrays use the reference's Fortran layouts: spin_matrix(3,N[,R]),
+ *    jij_nbors_matrix(N,maxnb) (column-major, 1-based neighbour indices),
+ *    dij_matrix(3,N,maxnb).  Energies are in Kelvin, as after jij.F90:163.
+ *  - The caller owns every host array; the library copies what it needs.
+ *    Device memory belongs to the handle.  One handle per host thread; calls
+ *    on one handle are not thread-safe.  All work runs on the handle's CUDA
+ *    stream (its own, or one given with esp_set_stream).
+ *  - Device-side waits are bounded; a wait that runs out returns ESP_ETIMEOUT.
+ */
+#ifndef ESPINS_GPU_H
+#define ESPINS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    ESP_OK = 0,
+    ESP_EINVAL = 1,    /* bad argument or inconsistent tables */
+    ESP_ECUDA = 2,     /* CUDA runtime error */
+    ESP_ENOMEM = 3,    /* device allocation failed */
+    ESP_ESTATE = 4,    /* call out of order (e.g. run before tables) */
+    ESP_ETIMEOUT = 5,  /* a bounded device wait gave up */
+    ESP_ECOLOR = 6     /* no valid colouring of the interaction graph */
+};
+
+typedef struct esp_handle esp_handle;
+
+/* Sizes of one lattice (mc_parameters: num_total_atoms, num_atoms,
+ * supercell_size, tems_num, boundary; src/parameters.F90:37-170). */
+typedef struct {
+    int32_t num_sites;      /* num_total_atoms = prod(supercell) * num_atoms */
+    int32_t num_atoms;      /* atoms per unit cell */
+    int32_t supercell[3];   /* supercell_size */
+    int32_t num_replicas;   /* tems_num: one replica per temperature */
+    int32_t open_boundary;  /* boundary = open (1) or periodic (0) */
+} esp_dims;
+
+/* The Hamiltonian as the reference's table builders leave it
+ * (mc_jij jij.F90:32-39, mc_bij bij.F90:32-34, mc_dij dij.F90:32-34,
+ * single-ion/field parameters.F90:129-131,926-995).  Absent terms: NULL. */
+typedef struct {
+    const double *mag;          /* mag_moments_matrix(N) */
+    int32_t j_maxnb;            /* second extent of jij_matrix */
+    const int32_t *j_nn;        /* jij_num_nbors_matrix(N) */
+    const int32_t *j_nbors;     /* jij_nbors_matrix(N,maxnb), 1-based */
+    const double *j_val;        /* jij_matrix(N,maxnb), Kelvin */
+    int32_t b_maxnb;
+    const int32_t *b_nn;        /* bij_num_nbors_matrix(N) or NULL */
+    const int32_t *b_nbors;     /* bij_nbors_matrix(N,maxnb) */
+    const double *b_val;        /* bij_matrix(N,maxnb) */
+    int32_t d_maxnb;
+    const int32_t *d_nn;        /* dij_num_nbors_matrix(N) or NULL */
+    const int32_t *d_nbors;     /* dij_nbors_matrix(N,maxnb) */
+    const double *d_val;        /* dij_matrix(3,N,maxnb) */
+    const double *si_axis;      /* singleion_axes_cart(3,num_atoms) or NULL */
+    const double *si_delta;     /* singleion_parameters(num_atoms), Kelvin */
+    const double *field_axis;   /* field_axes_cart(3,num_atoms) or NULL */
+    const double *field_val;    /* field_parameters(num_atoms), Kelvin */
+} esp_tables;
+
+/* The schedule of mcarlo (mcarlo.F90:496-659) or pt_mcarlo (pt.F90:524-942). */
+typedef struct {
+    int64_t steps_warmup;
+    int64_t steps_mc;
+    int64_t steps_measure;
+    int32_t pt;                 /* 0: independent temperatures, 1: parallel tempering */
+    int32_t mcarlo_mode;        /* 0: 'random' (uniform sphere), 1: 'const' (cone) */
+    int64_t pt_steps_swap;
+    double tilt_angles_max;
+    uint64_t seed;              /* key of the Philox stream (replaces mtprng) */
+    int32_t lbinerror;          /* binning_error */
+    int32_t num_binning_level;
+    const int32_t *binning_level;
+} esp_schedule;
+
+/* Results, caller-allocated.  R = num_replicas (temperatures), nf = num_freq
+ * (esp_num_freq), nl = num_binning_level.  NULL members are skipped.
+ * Values are normalised exactly as mcarlo.F90:713-733 / pt.F90:995-1024
+ * normalise them before writing _mc.dat, _pm.dat and _binerror.dat. */
+typedef struct {
+    int64_t *rejected;          /* [R][2]: warm-up and measurement phase (pt: [R][2] = warmup2, main) */
+    int64_t *steps_tot;         /* [2]: updates per temperature in each phase */
+    double *energy;             /* [R][3]: initial, final by differences, final direct */
+    double *data;               /* [R][6]: <E>,<E^2>,<E^4>,<|m|>,<m^2>,<m^4> */
+    double *pm;                 /* [R][nf]: P(M) */
+    double *binning;            /* [R][nl][2]: binning variances of E/N and |m| */
+    int64_t *num_swaps;         /* [R][2]: tries, accepts (pt) */
+    int32_t *map;               /* [R]: configuration index at each temperature, 1-based (pt) */
+    int64_t steps_mc_eff;       /* steps_mc after pt rounding (pt.F90:537-544) */
+} esp_results;
+
+/* Options of one low-level sweep call. */
+typedef struct {
+    int32_t mcarlo_mode;        /* 0 random, 1 const */
+    double tilt_angles_max;
+    uint64_t seed;
+    int32_t phase;              /* rejected-counter column: 0 or 1 */
+} esp_sweep_opts;
+
+/* ---- lifetime --------------------------------------------------------- */
+/* Replaces the allocations of mcarlo_setup (mcarlo.F90:242-460) and
+ * pt_setup (pt.F90:270-500). */
+int esp_create(const esp_dims *dims, esp_handle **out);
+int esp_destroy(esp_handle *h);
+/* Message of the last failed call on h (or of esp_create when h is NULL). */
+int esp_last_error(const esp_handle *h, char *buf, size_t len);
+/* Launch on an existing CUDA stream (cudaStream_t) instead of the handle's. */
+int esp_set_stream(esp_handle *h, void *cuda_stream);
+
+/* ---- data in ---------------------------------------------------------- */
+/* Tables of jij_get/bij_get/dij_get (jij.F90:394-446 etc.) plus single-ion
+ * and field data; builds the device ELL, merges duplicate neighbours, colours
+ * the interaction graph and checks the colouring on the host. */
+int esp_upload_tables(esp_handle *h, const esp_tables *t);
+/* tems(R) in Kelvin, in the order of the temperature slots. */
+int esp_set_temperatures(esp_handle *h, const double *tems);
+/* spin_matrix(3,N,R) (mcarlo.F90:269-322, pt.F90:442-491). */
+int esp_set_spins(esp_handle *h, const double *spins);
+/* Start configurations of the reference: 0 ferro (0,0,m), 1 rand
+ * (theta = pi*u1, phi = 2 pi*u2, the same for every temperature as in
+ * pt.F90:448-459), drawn from the Philox stream keyed by seed. */
+int esp_init_spins(esp_handle *h, int32_t kind, uint64_t seed);
+
+/* ---- the hot path ------------------------------------------------------ */
+/* mcarlo_main / pt_main without file output: runs the whole schedule on the
+ * device and fills *res. */
+int esp_run(esp_handle *h, const esp_schedule *s, esp_results *res);
+/* The same schedule in three parts, so a host can interleave its own work
+ * (progress lines, energy series) with the measurement phase:
+ *  esp_begin   zeroes the accumulators and runs the warm-up: plain sweeps
+ *              (mcarlo.F90:506-521), or warm-up 1 and warm-up 2 with swaps
+ *              (pt.F90:524-735);
+ *  esp_advance runs n units of the measurement phase: a unit is one
+ *              measurement (steps_measure sweeps + accumulators,
+ *              mcarlo.F90:526-590) or, with pt, one swap interval
+ *              (pt_steps_swap measurements followed by pt_swap, pt.F90:773-907);
+ *  esp_collect computes the final direct energy and fills *res, normalised
+ *              by the number of measurements made so far.
+ * esp_run == esp_begin + esp_advance(all units of the schedule) + esp_collect. */
+int esp_begin(esp_handle *h, const esp_schedule *s);
+int esp_advance(esp_handle *h, int64_t n);
+int esp_collect(esp_handle *h, esp_results *res);
+/* n full sweeps (every colour once) of every replica, starting at global
+ * sweep index first_sweep; the metropolis + delta_energy_get loop of
+ * mcarlo.F90:511-535 in colour order. */
+int esp_sweep(esp_handle *h, int64_t n, int64_t first_sweep, const esp_sweep_opts *o);
+/* One colour class of one sweep (for parity checks of a single pass). */
+int esp_sweep_colour(esp_handle *h, int32_t colour, int64_t sweep, const esp_sweep_opts *o);
+/* pt_swap (pt.F90:1235-1288) on device: start = 1 or 2 (1-based first pair),
+ * swap_index selects the Philox counter of the draws. */
+int esp_pt_swap(esp_handle *h, int32_t start, int64_t swap_index, uint64_t seed);
+
+/* ---- observables ------------------------------------------------------- */
+/* energy_get (get_quant.F90:186-261) per temperature slot, FP64 accumulated;
+ * also resets the running energies used by the sweeps to these values. */
+int esp_energy(esp_handle *h, double *energy_out);
+/* Running ("by adding differences") energies per temperature slot. */
+int esp_running_energy(esp_handle *h, double *energy_out);
+/* Running magnetisation sum_i s_i per temperature slot, [R][3]. */
+int esp_running_magnetization(esp_handle *h, double *m_out);
+/* Local terms of every site: energy of site i as a function of its spin s is
+ * g_i.s + s^T Q_i s;  g: (3,N,R), q: (6,N,R) as xx,yy,zz,xy,xz,yz.
+ * The exchange local field of delta_energy_get is -g without the Zeeman part. */
+int esp_local_terms(esp_handle *h, double *g_out, double *q_out);
+int esp_get_spins(esp_handle *h, double *spins_out);
+/* Colour of every site (0-based, N entries) and the number of colours. */
+int esp_get_colouring(esp_handle *h, int32_t *colour_out, int32_t *num_colours);
+/* Rejected counters per temperature slot, [R][2]. */
+int esp_get_rejected(esp_handle *h, int64_t *rejected_out);
+/* Temperature slot -> replica (0-based) after PT swaps. */
+int esp_get_replica_of_slot(esp_handle *h, int32_t *replica_out);
+/* num_freq of the P(M) grid (mcarlo.F90:432-442). */
+int esp_num_freq(const esp_handle *h, int32_t *nf);
+/* Number of kernels this handle has launched so far. */
+int esp_launch_count(const esp_handle *h, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ESPINS_GPU_H */

@@ -810,3 +810,105 @@ int or_build_ell(int num_atoms, const double *atoms_frac, const double *mag_cell
     free(tot_nb); free(tot_val); free(num);
     return rc;
 }
+
+/* ------------------------------------------------------------------------ */
+/* CPU baseline: the reference's PT main phase on host threads.             */
+/*                                                                          */
+/* Temperatures are block-split over threads as comms_array_split does      */
+/* (comms.F90:153-176, one thread standing for one MPI rank); each thread   */
+/* runs pt_steps_swap typewriter sweeps of its temperatures with its own    */
+/* MT19937 stream, measuring after every steps_measure sweeps               */
+/* (pt.F90:773-864: E accumulators, magnetization_get, Pm_get), then thread */
+/* 0 performs pt_swap.  Returns the number of site updates done.            */
+/* ------------------------------------------------------------------------ */
+#include <pthread.h>
+
+typedef struct {
+    const or_ham *h;
+    int R, nthreads, tid, mode;
+    double tilt;
+    const double *tems;
+    double *spins, *e2, *data, *pm;
+    int64_t *rejected, *num_swaps;
+    int32_t *map;
+    int64_t n_swap_intervals, pss, steps_measure;
+    int32_t seed;
+    pthread_barrier_t *bar;
+    double *tmp;
+    or_mt root_mt;
+    int64_t updates;
+} or_bench_ctx;
+
+static void *or_bench_worker(void *arg)
+{
+    or_bench_ctx *c = (or_bench_ctx *)arg;
+    const or_ham *h = c->h;
+    const int n = h->n;
+    int base = c->R / c->nthreads, rem = c->R % c->nthreads;
+    int t0 = c->tid * base + (c->tid < rem ? c->tid : rem);
+    int t1 = t0 + base + (c->tid < rem ? 1 : 0);
+    int nf = or_num_freq(h);
+    or_mt mt;
+    or_mt_init(&mt, c->seed + c->tid);
+    c->updates = 0;
+    for (int64_t lsw = 1; lsw <= c->n_swap_intervals; ++lsw) {
+        for (int t = t0; t < t1; ++t) {
+            double beta = 1.0 / c->tems[t];
+            double *s = c->spins + (size_t)3 * n * t;
+            for (int64_t mc = 0; mc < c->pss; ++mc) {
+                for (int64_t ms = 0; ms < c->steps_measure; ++ms)
+                    for (int i = 0; i < n; ++i)
+                        or_metropolis(h, &mt, i, beta, s, &c->e2[t], &c->rejected[t], c->mode, c->tilt);
+                c->updates += (int64_t)n * c->steps_measure;
+                double e = c->e2[t], ee = e * e, *d = c->data + 6 * t;
+                d[0] += e; d[1] += ee; d[2] += ee * ee;
+                double m2 = or_magnetization2(h, s);
+                d[3] += sqrt(m2); d[4] += m2; d[5] += m2 * m2;
+                or_pm(h, s, nf, c->pm + (size_t)nf * t);
+            }
+        }
+        pthread_barrier_wait(c->bar);
+        if (c->tid == 0)
+            or_pt_swap((int)((lsw + 1) % 2) + 1, c->R, c->tems, n, c->spins, c->e2, c->map, c->num_swaps,
+                       &c->root_mt, c->tmp);
+        pthread_barrier_wait(c->bar);
+    }
+    return NULL;
+}
+
+int64_t or_pt_bench(const or_ham *h, int nthreads, int R, const double *tems, double *spins,
+                    int64_t n_swap_intervals, int64_t pss, int64_t steps_measure, int mode,
+                    double tilt, int32_t seed)
+{
+    if (nthreads > R) nthreads = R;
+    if (nthreads < 1) nthreads = 1;
+    const int n = h->n;
+    int nf = or_num_freq(h);
+    double *e2 = (double *)calloc((size_t)R, sizeof(double));
+    double *data = (double *)calloc((size_t)6 * R, sizeof(double));
+    double *pm = (double *)calloc((size_t)nf * R, sizeof(double));
+    int64_t *rej = (int64_t *)calloc((size_t)R, sizeof(int64_t));
+    int64_t *sw = (int64_t *)calloc((size_t)2 * R, sizeof(int64_t));
+    int32_t *map = (int32_t *)malloc(sizeof(int32_t) * R);
+    double *tmp = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    for (int t = 0; t < R; ++t) { map[t] = t + 1; e2[t] = or_energy(h, spins + (size_t)3 * n * t); }
+    pthread_barrier_t bar;
+    pthread_barrier_init(&bar, NULL, (unsigned)nthreads);
+    or_bench_ctx *ctx = (or_bench_ctx *)calloc((size_t)nthreads, sizeof(or_bench_ctx));
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    for (int k = 0; k < nthreads; ++k) {
+        or_bench_ctx *c = &ctx[k];
+        c->h = h; c->R = R; c->nthreads = nthreads; c->tid = k; c->mode = mode; c->tilt = tilt;
+        c->tems = tems; c->spins = spins; c->e2 = e2; c->data = data; c->pm = pm;
+        c->rejected = rej; c->num_swaps = sw; c->map = map;
+        c->n_swap_intervals = n_swap_intervals; c->pss = pss; c->steps_measure = steps_measure;
+        c->seed = seed; c->bar = &bar; c->tmp = tmp;
+        if (k == 0) or_mt_init(&c->root_mt, seed - 1);
+        pthread_create(&th[k], NULL, or_bench_worker, c);
+    }
+    int64_t total = 0;
+    for (int k = 0; k < nthreads; ++k) { pthread_join(th[k], NULL); total += ctx[k].updates; }
+    pthread_barrier_destroy(&bar);
+    free(ctx); free(th); free(e2); free(data); free(pm); free(rej); free(sw); free(map); free(tmp);
+    return total;
+}

@@ -1,0 +1,85 @@
+"""Shared helpers of the tests: fixtures of the reference examples and small
+synthetic lattices with the shapes of the benchmark configurations."""
+import json
+import os
+
+import numpy as np
+
+from espins_gb300.mcin import K_B, parse_mcin, read_mcin
+from espins_gb300.tables import build_hamiltonian
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def example(name, nodes=None):
+    if nodes is None:
+        nodes = 32 if name.startswith(("ex02", "ex04")) else 4
+    inp = read_mcin(os.path.join(GOLDEN, name + ".mcin"), num_nodes=nodes)
+    with open(os.path.join(GOLDEN, name + "_golden.json")) as fh:
+        g = json.load(fh)
+    return inp, g
+
+
+def example_spins(name):
+    z = np.load(os.path.join(GOLDEN, name + "_sconfig.npz"))
+    return z["temps"], z["spins"]
+
+
+def sc_mcin(L, shells, tems, extra="", bq=None, dm=None, si=None, steps=(100, 1000, 1)):
+    """A simple-cubic input: shells = [(J_eV, offsets...)], optional NN biquadratic
+    (eV), NN DM (eV, along the unit bond vector) and single-ion (Delta eV along z)."""
+    lines = ["begin unit_cell_cart", "1 0 0", "0 1 0", "0 0 1", "end unit_cell_cart",
+             "begin atoms_frac", "Fe 0 0 0 1.0", "end atoms_frac",
+             f"supercell_size = {L} {L} {L}", "tems_mode = man", f"tems_num = {len(tems)}",
+             "tems = " + " ".join(repr(float(t)) for t in tems),
+             f"steps_warmup = {steps[0]}", f"steps_mc = {steps[1]}", f"steps_measure = {steps[2]}"]
+    lines.append("begin jij_parameters")
+    for J, offs in shells:
+        for o in offs:
+            lines.append(f"f1=0,0,0:f2={o[0]},{o[1]},{o[2]}:jij={J}")
+    lines.append("end jij_parameters")
+    nn = [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)]
+    if bq is not None:
+        lines += ["ham_bij = .true.", "begin bij_parameters"]
+        lines += [f"f1=0,0,0:f2={o[0]},{o[1]},{o[2]}:bij={bq}" for o in nn]
+        lines.append("end bij_parameters")
+    if dm is not None:
+        lines += ["ham_dij = .true.", "begin dij_parameters"]
+        lines += [f"f1=0,0,0:f2={o[0]},{o[1]},{o[2]}:dij={dm}" for o in nn]
+        lines += ["end dij_parameters", "begin dij_vectors_cart"]
+        lines += [f"{o[0]} {o[1]} {o[2]}" for o in nn]
+        lines.append("end dij_vectors_cart")
+    if si is not None:
+        lines += ["ham_singleion = .true.", "begin singleion_axes_cart", f"Fe 0 0 1 {si}", "end singleion_axes_cart"]
+    lines += [l for l in extra.splitlines() if l.strip()]
+    return parse_mcin("\n".join(lines) + "\n", seedname="sc")
+
+
+NN = [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)]
+NNN = [(a, b, 0) for a in (1, -1) for b in (1, -1)] + [(a, 0, b) for a in (1, -1) for b in (1, -1)] + \
+      [(0, a, b) for a in (1, -1) for b in (1, -1)]
+N3 = [(a, b, c) for a in (1, -1) for b in (1, -1) for c in (1, -1)]
+
+
+def energy_scale(h):
+    """Sum of |coupling| magnitudes: the floor for relative energy errors."""
+    s = 0.5 * np.abs(h.jij.val).sum()
+    if h.bij is not None:
+        s += 0.5 * np.abs(h.bij.val).sum()
+    if h.dij is not None:
+        s += 0.5 * np.abs(h.dij.val).sum()
+    if h.si_delta is not None:
+        s += h.n * np.abs(h.si_delta).max()
+    return s
+
+
+def site_scale(h):
+    """Per-site sum of |J| + |B| + |D| (floor for local-field errors)."""
+    sc = np.abs(h.jij.val).sum(axis=0)
+    if h.bij is not None:
+        sc = sc + np.abs(h.bij.val).sum(axis=0)
+    if h.dij is not None:
+        sc = sc + np.abs(h.dij.val).sum(axis=(0, 2))
+    if h.si_delta is not None:
+        sc = sc + np.abs(h.si_delta).max()
+    return sc
