@@ -1,0 +1,359 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 Monte Carlo path.
+
+Workload (default ``bcc24_pt``): parallel tempering on a bcc lattice of 24^3
+conventional cells (27,648 spins), J1=+2.0, J2=+0.5, J3=-0.1 meV, easy-axis
+single-ion 0.05 meV along z, 48 replicas geometrically spaced 10-80 K, a
+replica exchange every 10 sweeps, FP32 spins and fields with FP64 energy
+totals and swap exponent, uniform random start on S^2 from seed 2.  Inputs are
+synthetic (the reference ships no benchmark data).
+
+A step is one swap interval of the measurement phase for all replicas:
+10 sweeps (every colour class), 10 measurements (energy/magnetisation
+accumulators, binning, P(M) histogram) and one exchange (esp_advance(1)).
+Metric: site updates/s = steps * 10 * N * R / time.
+
+* ``value``: device time of the timed steps, CUDA events on the library's
+  stream, L2 flushed (256 MB write) before every timed step, outside the events.
+* ``e2e``: the same metric through the C ABI with host buffers: set spins from
+  host memory, run the steps, collect results and read the spins back, wall
+  clock, copies included.
+* ``roofline``: the sweep kernel, 24 B of compulsory spin traffic per site
+  update (read + write of one FP32 3-vector), against the measured HBM copy
+  bandwidth.
+* ``cpu_baseline``: the FP64 oracle (a restatement of the reference's Fortran:
+  typewriter sweeps, MT19937) on the host cores, one thread per block of
+  temperatures as the reference's MPI ranks, on a bounded sample.
+
+``--impl reference`` times that CPU implementation alone (the reference itself
+is Fortran + MPI and cannot be built in this image).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", default="bcc24_pt")
+    p.add_argument("--L", type=int, default=None)
+    p.add_argument("--replicas", type=int, default=None)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--seed", type=int, default=2)
+    return p.parse_args()
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _uniform_spins(R, n, mag, seed):
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=(R, n, 3))
+    v /= np.linalg.norm(v, axis=2, keepdims=True)
+    return v * mag[None, :, None]
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0])); mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(inp, ham, seconds: float, threads: int, seed: int, max_intervals=None):
+    """The oracle's PT main phase on host threads, bounded to about `seconds`."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ctypes as C
+
+    import oracle as O
+    lib = O.lib()
+    lib.or_pt_bench.argtypes = [C.POINTER(O.OrHam), C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int64,
+                                C.c_int64, C.c_int64, C.c_int, C.c_double, C.c_int32]
+    lib.or_pt_bench.restype = C.c_int64
+    H = O.Ham(ham)
+    R = inp.tems_num
+    tems = np.ascontiguousarray(inp.tems, dtype=np.float64)
+    spins = np.ascontiguousarray(_uniform_spins(R, ham.n, ham.mag, seed).reshape(-1))
+    pss = inp.pt_steps_swap if inp.pt else 1
+    mode = 1 if inp.mcarlo_mode.startswith("const") else 0
+
+    def run(k):
+        t0 = time.perf_counter()
+        n = lib.or_pt_bench(H.ref, threads, R, tems.ctypes.data, spins.ctypes.data, k, pss,
+                            inp.steps_measure, mode, inp.tilt_angles_max, seed)
+        return n, time.perf_counter() - t0
+
+    n1, t1 = run(1)
+    k = max(1, int(seconds / max(t1, 1e-6)))
+    if max_intervals:
+        k = min(k, max_intervals)
+    n, t = run(k)
+    return n / t, {"swap_intervals": k, "updates": int(n), "seconds": t,
+                   "sweeps_per_interval": pss * inp.steps_measure}
+
+
+def reference_arm(a, ws, rank):
+    """--impl reference: the CPU implementation of the path on all host threads."""
+    from espins_gb300.tables import build_hamiltonian
+    from espins_gb300.workloads import workload
+    if rank != 0:
+        return
+    inp = workload(a.workload, L=a.L, replicas=a.replicas)
+    ham = build_hamiltonian(inp, check=False)
+    threads = os.cpu_count() or 1
+    R = inp.tems_num
+    spins_per_step = (inp.pt_steps_swap if inp.pt else 1) * inp.steps_measure * ham.n * R
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    # each step: one swap interval of every temperature; bounded sample per step
+    rates = []
+    for _ in range(a.warmup):
+        cpu_baseline(inp, ham, 0.0, threads, a.seed, max_intervals=1)
+    t_tot, u_tot = 0.0, 0
+    for _ in range(a.steps):
+        r, info = cpu_baseline(inp, ham, 0.0, threads, a.seed, max_intervals=1)
+        t_tot += info["seconds"]; u_tot += info["updates"]
+    value = u_tot / t_tot
+    line = {
+        "impl": "reference", "metric": "site updates/s", "value": value, "unit": "site updates/s",
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * t_tot / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": _config(inp, ham, a.workload),
+        "cpu_baseline": {"value": value, "unit": "site updates/s", "cores": threads, "kind": "port",
+                         "sample": f"{a.steps} steps of one swap interval ({spins_per_step} site updates) each; "
+                                   "FP64 C restatement of the Fortran (typewriter order, MT19937), "
+                                   "temperatures block-split over threads"},
+        "e2e": {"value": value, "unit": "site updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _config(inp, ham, name):
+    return {"workload": name, "sites": ham.n, "atoms_per_cell": ham.num_atoms,
+            "supercell": list(inp.supercell_size), "replicas": inp.tems_num,
+            "temperatures_K": [float(inp.tems[0]), float(inp.tems[-1])],
+            "pt": bool(inp.pt), "pt_steps_swap": inp.pt_steps_swap, "steps_measure": inp.steps_measure,
+            "sweeps_per_step": (inp.pt_steps_swap if inp.pt else 1) * inp.steps_measure,
+            "l2": "flushed before every timed step (256 MB write, outside the events)",
+            "parallelism": "all replicas in one device; independent jobs per GPU when n_gpus > 1"}
+
+
+def main():
+    a = _args()
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if a.impl == "reference":
+        reference_arm(a, ws, rank)
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import torch
+
+    from espins_gb300.lib import Engine
+    from espins_gb300.tables import build_hamiltonian
+    from espins_gb300.workloads import workload
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    inp = workload(a.workload, L=a.L, replicas=a.replicas)
+    ham = build_hamiltonian(inp, check=False)
+    R, N = inp.tems_num, ham.n
+    pss = inp.pt_steps_swap if inp.pt else 1
+    sweeps_per_step = pss * inp.steps_measure
+    updates_per_step = sweeps_per_step * N * R
+    seed = a.seed + 1000 * rank
+    spins0 = _uniform_spins(R, N, ham.mag, seed)
+    stream = torch.cuda.current_stream(dev)
+    eng = Engine(N, ham.num_atoms, ham.supercell, R, inp.boundary_open)
+    eng.upload(ham)
+    eng.set_temperatures(inp.tems)
+    eng.set_stream(stream.cuda_stream)
+    _, ncol = eng.colouring()
+    mode = 1 if inp.mcarlo_mode.startswith("const") else 0
+    total_units = a.warmup + a.steps
+    sched = eng.schedule(0, total_units * pss, inp.steps_measure, pt=inp.pt, pt_steps_swap=pss, mode=mode,
+                         tilt=inp.tilt_angles_max, seed=seed, binning_level=[1, 2, 3, 4, 5])
+    eng.set_spins(spins0)
+    eng.begin(sched)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    for _ in range(a.warmup):
+        eng.advance(1)
+    torch.cuda.synchronize(dev)
+    sampler = ClockSampler(local)
+    sampler.start()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    l0 = eng.launch_count()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    for k in range(a.steps):
+        flush.fill_(k & 0xFF)
+        starts[k].record(stream)
+        eng.advance(1)
+        ends[k].record(stream)
+    torch.cuda.synchronize(dev)
+    launches = eng.launch_count() - l0
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    clocks = sampler.stop()
+    res = eng.collect()
+
+    # sweep-kernel duration, live: back-to-back sweeps (every colour) on the same stream
+    nsw = max(4, min(200, int(2e8 // max(N * R, 1))))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    eng.sweep(2, 10 ** 9, seed)
+    ev0.record(stream)
+    eng.sweep(nsw, 10 ** 9 + 2, seed)
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    sweep_ms = ev0.elapsed_time(ev1)
+    per_launch_s = sweep_ms * 1e-3 / (nsw * ncol)
+    bytes_per_launch = 24.0 * N * R / ncol
+    peak, peak_kind = _peaks()
+    achieved = bytes_per_launch / per_launch_s / 1e9
+
+    # end to end through the C ABI with host buffers
+    e2e_steps = max(1, min(a.steps, 50))
+    eng2 = Engine(N, ham.num_atoms, ham.supercell, R, inp.boundary_open)
+    eng2.upload(ham)
+    eng2.set_temperatures(inp.tems)
+    sched2 = eng2.schedule(0, e2e_steps * pss, inp.steps_measure, pt=inp.pt, pt_steps_swap=pss, mode=mode,
+                           tilt=inp.tilt_angles_max, seed=seed)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    eng2.set_spins(spins0)
+    eng2.begin(sched2)
+    eng2.advance(e2e_steps)
+    r2 = eng2.collect()
+    out_spins = eng2.get_spins()
+    t_e2e = time.perf_counter() - t0
+    eng2.close()
+    h2d = 12 * N * R + 8 * R
+    d2h = 12 * N * R + 8 * R * (6 + 3 + 4) + 8 * R * eng.num_freq()
+
+    t_local = ms / 1e3
+    if ws > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_local], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+        te = torch.tensor([t_e2e], dtype=torch.float64)
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        t_e2e = float(te.item())
+    else:
+        t_max = t_local
+    value = ws * a.steps * updates_per_step / t_max
+    e2e_value = ws * e2e_steps * updates_per_step / t_e2e
+    if rank == 0:
+        line = {
+            "metric": "site updates/s", "value": value, "unit": "site updates/s", "n_gpus": ws,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * t_max / a.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": _config(inp, ham, a.workload),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "k_sweep_ell", "bytes_per_launch": bytes_per_launch,
+                         "launch_us": per_launch_s * 1e6, "peak_source": peak_kind,
+                         "note": "state is L2-resident inside a step (16 MB)"},
+            "e2e": {"value": e2e_value, "unit": "site updates/s", "h2d_bytes_per_step": h2d / e2e_steps,
+                    "d2h_bytes_per_step": d2h / e2e_steps, "steps": e2e_steps,
+                    "path": "esp_set_spins + esp_begin + esp_advance + esp_collect + esp_get_spins"},
+            "gpu_launches": int(launches), "colours": ncol,
+            "clocks": clocks,
+            "swap_acceptance": float(np.mean(res["num_swaps"][:, 1] / np.maximum(res["num_swaps"][:, 0], 1))),
+        }
+        if not a.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            v, info = cpu_baseline(inp, ham, a.cpu_seconds, threads, a.seed)
+            line["cpu_baseline"] = {"value": v, "unit": "site updates/s", "cores": threads, "kind": "port",
+                                    "sample": f"{info['swap_intervals']} swap intervals x "
+                                              f"{info['sweeps_per_interval']} sweeps of all {R} temperatures "
+                                              f"({info['updates']} site updates, {info['seconds']:.1f} s)"}
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

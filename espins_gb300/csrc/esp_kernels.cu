@@ -97,26 +97,38 @@ __global__ void __launch_bounds__(256) k_sweep_ell(const SweepArgs a)
             const float ox = a.sx[idx], oy = a.sy[idx], oz = a.sz[idx];
             float gx = 0.f, gy = 0.f, gz = 0.f;
             float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
+            // entries come in groups of 8 (the host pads every list with
+            // zero-coupling entries pointing at the site itself), so each
+            // group issues 8 independent index loads and then 24 spin loads
             const int nn = __ldg(a.nnb + p);
-            for (int k = 0; k < nn; ++k) {
-                const size_t e = (size_t)k * a.N + p;
-                const int q = __ldg(a.nbr + e);
-                const size_t iq = (size_t)q * R + r;
-                const float tx = __ldg(a.sx + iq), ty = __ldg(a.sy + iq), tz = __ldg(a.sz + iq);
-                const float J = __ldg(a.J + e);
-                gx = fmaf(-J, tx, gx); gy = fmaf(-J, ty, gy); gz = fmaf(-J, tz, gz);
-                if (HB) {
-                    const float Bv = __ldg(a.B + e);
-                    const float bx = Bv * tx, by = Bv * ty, bz = Bv * tz;
-                    qxx = fmaf(bx, tx, qxx); qyy = fmaf(by, ty, qyy); qzz = fmaf(bz, tz, qzz);
-                    qxy = fmaf(bx, ty, qxy); qxz = fmaf(bx, tz, qxz); qyz = fmaf(by, tz, qyz);
+            for (int k0 = 0; k0 < nn; k0 += 8) {
+                int q[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) q[j] = __ldg(a.nbr + (size_t)(k0 + j) * a.N + p);
+                float tx[8], ty[8], tz[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const size_t iq = (size_t)q[j] * R + r;
+                    tx[j] = __ldg(a.sx + iq); ty[j] = __ldg(a.sy + iq); tz[j] = __ldg(a.sz + iq);
                 }
-                if (HD) {
-                    const float dx = __ldg(a.Dx + e), dy = __ldg(a.Dy + e), dz = __ldg(a.Dz + e);
-                    // s_k x D_ik (the DM term of delta_energy_get as s_i . (s_k x D))
-                    gx += ty * dz - tz * dy;
-                    gy += tz * dx - tx * dz;
-                    gz += tx * dy - ty * dx;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const size_t e = (size_t)(k0 + j) * a.N + p;
+                    const float J = __ldg(a.J + e);
+                    gx = fmaf(-J, tx[j], gx); gy = fmaf(-J, ty[j], gy); gz = fmaf(-J, tz[j], gz);
+                    if (HB) {
+                        const float Bv = __ldg(a.B + e);
+                        const float bx = Bv * tx[j], by = Bv * ty[j], bz = Bv * tz[j];
+                        qxx = fmaf(bx, tx[j], qxx); qyy = fmaf(by, ty[j], qyy); qzz = fmaf(bz, tz[j], qzz);
+                        qxy = fmaf(bx, ty[j], qxy); qxz = fmaf(bx, tz[j], qxz); qyz = fmaf(by, tz[j], qyz);
+                    }
+                    if (HD) {
+                        const float dx = __ldg(a.Dx + e), dy = __ldg(a.Dy + e), dz = __ldg(a.Dz + e);
+                        // s_k x D_ik (the DM term of delta_energy_get as s_i . (s_k x D))
+                        gx += ty[j] * dz - tz[j] * dy;
+                        gy += tz[j] * dx - tx[j] * dz;
+                        gz += tx[j] * dy - ty[j] * dx;
+                    }
                 }
             }
             const int orig = __ldg(a.perm + p);

@@ -120,7 +120,9 @@ int prepare_tables(const PrepInput &in, PrepOutput &out, std::string &err)
     }
     int maxnb = 0;
     for (int i = 0; i < N; ++i) maxnb = std::max(maxnb, (int)cnt[i]);
-    out.maxnb = maxnb;
+    // device lists are padded to a multiple of kGroup entries
+    const int maxnb_pad = ((maxnb + kGroup - 1) / kGroup) * kGroup;
+    out.maxnb = maxnb_pad;
 
     // ---- colouring ---------------------------------------------------------
     std::vector<int> colour(N, -1);
@@ -200,7 +202,7 @@ int prepare_tables(const PrepInput &in, PrepOutput &out, std::string &err)
         }
     }
     // ---- pack in permuted order (entry k of site p at k*N + p) -------------
-    const size_t M = (size_t)maxnb * N;
+    const size_t M = (size_t)maxnb_pad * N;
     out.nnb.assign(N, 0);
     out.nbr.assign(M, 0);
     out.J.assign(M, 0.f);
@@ -209,8 +211,10 @@ int prepare_tables(const PrepInput &in, PrepOutput &out, std::string &err)
     out.mag.assign(N, 0.f);
     for (int p = 0; p < N; ++p) {
         const int i = out.perm[p];
-        out.nnb[p] = cnt[i];
+        out.nnb[p] = ((cnt[i] + kGroup - 1) / kGroup) * kGroup;
         out.mag[p] = (float)in.mag[i];
+        // padding: zero couplings to the site itself
+        for (int k = cnt[i]; k < out.nnb[p]; ++k) out.nbr[(size_t)k * N + p] = p;
         int k = 0;
         for (int64_t e = start[i]; e < start[i + 1]; ++e, ++k) {
             const size_t o = (size_t)k * N + p;

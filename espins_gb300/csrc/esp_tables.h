@@ -6,6 +6,9 @@
 
 namespace esp {
 
+// Neighbour lists on the device are padded to multiples of this.
+constexpr int kGroup = 8;
+
 struct PrepInput {
     int N, num_atoms, L[3];
     const double *mag;
@@ -15,7 +18,7 @@ struct PrepInput {
 };
 
 struct PrepOutput {
-    int maxnb = 0, num_colours = 0;
+    int maxnb = 0, num_colours = 0;  // maxnb: padded list length
     bool has_b = false, has_d = false;
     std::vector<int> colour;      // reference site -> colour
     std::vector<int> off;         // colour c owns permuted sites [off[c], off[c+1])

@@ -1,0 +1,111 @@
+"""Statistical parity: GPU colour-class chains against the oracle's typewriter
+chains (the reference's algorithm: mcarlo.F90:496-733, pt.F90:504-1024).
+
+The two samplers use different site orders and random streams, so only
+stationary averages can agree.  For every temperature the test requires
+|<x>_gpu - <x>_oracle| <= 3 sigma for x = E/N and |m|, with sigma combined
+from both runs' binning analysis (mcarlo.F90:635-656): the largest of the
+binning error estimates over block sizes 2^5..2^9.  Seeds are fixed, so the
+outcome is deterministic.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from espins_gb300.lib import Engine
+from espins_gb300.tables import build_hamiltonian
+from helpers import NN, NNN, sc_mcin
+
+pytestmark = pytest.mark.gpu
+
+LEVELS = [1, 2, 3, 4, 5, 6, 7, 8, 9]
+
+
+def _sigma(binning):
+    """binning: (levels, 2) variances of the mean of E/N and |m|."""
+    b = np.asarray(binning)[4:9]
+    return np.sqrt(np.max(np.maximum(b, 0.0), axis=0))
+
+
+def _gpu_run(h, tems, pt, warm, mc, pss=10, mode=0, tilt=0.125, seed=12345):
+    R = len(tems)
+    with Engine(h.n, h.num_atoms, h.supercell, R) as e:
+        e.upload(h)
+        e.set_temperatures(tems)
+        e.init_spins("ferro")
+        return e.run(warm, mc, 1, pt=pt, pt_steps_swap=pss, mode=mode, tilt=tilt, seed=seed,
+                     binning_level=LEVELS)
+
+
+def _check(h, tems, gpu_data, gpu_bin, or_data, or_bin, what):
+    n = h.n
+    for t, T in enumerate(tems):
+        g = np.array([gpu_data[t][0] / n, gpu_data[t][3]])
+        o = np.array([or_data[t][0] / n, or_data[t][3]])
+        sg, so = _sigma(gpu_bin[t]), _sigma(or_bin[t])
+        s = np.sqrt(sg ** 2 + so ** 2)
+        assert np.all(np.abs(g - o) <= 3.0 * s), (what, T, g, o, s)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_plain_metropolis_matches_reference_algorithm(mode):
+    inp = sc_mcin(6, [(1e-3, NN)], [8.0, 14.0, 20.0, 30.0])
+    h = build_hamiltonian(inp)
+    tems = inp.tems
+    warm, mc = 2000, 40000
+    res = _gpu_run(h, tems, False, warm, mc, mode=mode, tilt=0.3)
+    H = O.Ham(h)
+    or_data, or_bin = [], []
+    for t, T in enumerate(tems):
+        s = np.zeros((h.n, 3)); s[:, 2] = 1.0
+        r = H.mcarlo(O.MT(1000 + t), 1.0 / T, s, warm, mc, 1, mode=mode, tilt=0.3, binning_level=LEVELS,
+                     want_pm=False)
+        or_data.append(r["data"] / mc)
+        or_bin.append(r["binning"])
+    _check(h, tems, res["data"], res["binning"], or_data, or_bin, f"plain mode={mode}")
+    # the energy bookkeeping of the run: final by differences == direct
+    e = res["energy"]
+    assert np.max(np.abs(e[:, 1] - e[:, 2])) <= 1e-6 * h.n * 12.0
+
+
+def test_plain_metropolis_biquadratic_dm_singleion():
+    inp = sc_mcin(6, [(1e-3, NN), (3e-4, NNN)], [5.0, 12.0, 25.0], bq=1e-4, dm=2e-4, si=-3e-5)
+    h = build_hamiltonian(inp)
+    tems = inp.tems
+    warm, mc = 2000, 30000
+    res = _gpu_run(h, tems, False, warm, mc)
+    H = O.Ham(h)
+    or_data, or_bin = [], []
+    for t, T in enumerate(tems):
+        s = np.zeros((h.n, 3)); s[:, 2] = 1.0
+        r = H.mcarlo(O.MT(77 + t), 1.0 / T, s, warm, mc, 1, binning_level=LEVELS, want_pm=False)
+        or_data.append(r["data"] / mc)
+        or_bin.append(r["binning"])
+    _check(h, tems, res["data"], res["binning"], or_data, or_bin, "J+B+D+SI")
+
+
+def test_parallel_tempering_matches_reference_algorithm():
+    inp = sc_mcin(6, [(1e-3, NN)], list(np.geomspace(8.0, 30.0, 8)))
+    h = build_hamiltonian(inp)
+    tems = inp.tems
+    warm, mc, pss = 4000, 40000, 10
+    res = _gpu_run(h, tems, True, warm, mc, pss=pss)
+    H = O.Ham(h)
+    s = np.zeros((len(tems), h.n, 3)); s[:, :, 2] = 1.0
+    r = H.pt(O.MT(4242), tems, s.reshape(-1), warm, mc, 1, pss, binning_level=LEVELS, want_pm=False)
+    steps = r["steps_mc_eff"]
+    or_data = r["data"] / steps
+    # PT binning variances carry an extra 1/N (pt.F90:935); undo it for sigma
+    gb = res["binning"] * h.n
+    ob = r["binning"] * h.n
+    _check(h, tems, res["data"], gb, or_data, ob, "pt")
+    # swap acceptance per temperature: binomial tolerance
+    ga = res["num_swaps"][:, 1] / np.maximum(res["num_swaps"][:, 0], 1)
+    oa = r["num_swaps"][:, 1] / np.maximum(r["num_swaps"][:, 0], 1)
+    ntries = np.maximum(res["num_swaps"][:, 0], 1)
+    sig = np.sqrt(np.maximum(oa * (1 - oa), 1e-4) / ntries) * 2.0
+    assert np.all(np.abs(ga - oa) <= 4 * sig + 0.02), (ga, oa)
+    # map is a permutation, tries are counted as the reference counts them
+    assert sorted(res["map"].tolist()) == list(range(1, len(tems) + 1))
+    nsw = steps // pss
+    assert res["num_swaps"][0, 0] == (nsw + 1) // 2
