@@ -22,7 +22,7 @@ CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17"]
 
 CU_SOURCES = ["esp_kernels.cu", "esp_api.cu"]
 CXX_SOURCES = ["esp_tables.cpp"]
-HEADERS = ["esp_device.cuh", "esp_kernels.h", "esp_tables.h"]
+HEADERS = ["esp_device.cuh", "esp_kernels.h", "esp_tables.h", "esp_errors.h"]
 
 
 def _nvcc() -> str:

@@ -3,6 +3,7 @@
 // and pt_mcarlo (src/pt.F90:504-1024) driven from the host.
 #include <algorithm>
 #include <cmath>
+#include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -12,6 +13,7 @@
 #include "../../include/espins_gpu.h"
 #include "esp_kernels.h"
 #include "esp_tables.h"
+#include "esp_errors.h"
 
 using namespace esp;
 
@@ -51,6 +53,12 @@ struct esp_handle {
     unsigned long long *d_rej = nullptr;
     double *d_scratch = nullptr;
     int e_blocks = 0;
+    // per-block partial sums of the sweeps (see add_block_slots / k_fold)
+    double *d_part = nullptr;
+    unsigned long long *d_part_rej = nullptr;
+    int sweep_grid = 0, slots = 0;
+    int pending_phase = 0;
+    long long pending_sweeps = 0;
     double *d_tmp_e = nullptr, *d_tmp_m = nullptr;
     // accumulators
     double *d_data = nullptr, *d_lsum = nullptr, *d_bin = nullptr;
@@ -65,7 +73,9 @@ struct esp_handle {
 
 namespace {
 
-std::string g_create_err;
+// Message of the last failure that has no handle to hold it (esp_create and
+// calls without a handle); a fixed buffer, so recording it allocates nothing.
+char g_global_err[512] = "";
 
 #define CK(call)                                                                                   \
     do {                                                                                           \
@@ -94,7 +104,7 @@ void free_tables(esp_handle *h)
 {
     dfree(h->d_nnb); dfree(h->d_nbr); dfree(h->d_perm); dfree(h->d_inv);
     dfree(h->d_J); dfree(h->d_B); dfree(h->d_Dx); dfree(h->d_Dy); dfree(h->d_Dz); dfree(h->d_mag);
-    dfree(h->d_si); dfree(h->d_fld); dfree(h->d_scratch);
+    dfree(h->d_si); dfree(h->d_fld); dfree(h->d_scratch); dfree(h->d_part); dfree(h->d_part_rej);
 }
 
 void free_all(esp_handle *h)
@@ -114,10 +124,10 @@ SweepArgs sweep_args(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *
     a.perm = h->d_perm; a.mag = h->d_mag; a.si = h->hsi ? h->d_si : nullptr; a.fld = h->hfld ? h->d_fld : nullptr;
     a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz;
     a.temp_of = h->d_temp_of; a.beta = h->d_beta;
-    a.e_run = h->d_e_run; a.m_run = h->d_m_run; a.rej = h->d_rej;
+    a.part = h->d_part; a.part_rej = h->d_part_rej; a.slots = h->slots;
     a.N = h->N; a.R = h->R; a.num_atoms = h->na;
     a.off_c = h->prep.off[c]; a.n_c = h->prep.off[c + 1] - h->prep.off[c];
-    a.phase = o->phase ? 1 : 0; a.mode = o->mcarlo_mode ? 1 : 0; a.tilt = (float)o->tilt_angles_max;
+    a.mode = o->mcarlo_mode ? 1 : 0; a.tilt = (float)o->tilt_angles_max;
     a.key0 = (uint32_t)o->seed; a.key1 = (uint32_t)(o->seed >> 32);
     a.sw_lo = (uint32_t)sweep; a.sw_hi = (uint32_t)((uint64_t)sweep >> 32);
     return a;
@@ -142,22 +152,50 @@ int require(esp_handle *h, bool tables, bool temps)
     return ESP_OK;
 }
 
+// Adds the sweeps' per-block partial sums to the running energies,
+// magnetisations and rejected counters (k_fold), in block order.
+int fold(esp_handle *h)
+{
+    if (h->pending_sweeps == 0) return ESP_OK;
+    FoldArgs f;
+    f.part = h->d_part; f.part_rej = h->d_part_rej; f.e_run = h->d_e_run; f.m_run = h->d_m_run;
+    f.rej = h->d_rej; f.temp_of = h->d_temp_of; f.R = h->R; f.nblocks = h->sweep_grid; f.slots = h->slots;
+    f.block_threads = 256; f.phase = h->pending_phase;
+    CK(launch_fold(f, h->st));
+    h->launches++;
+    h->pending_sweeps = 0;
+    return ESP_OK;
+}
+
 int do_sweep_colour(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o)
 {
+    const int phase = o->phase ? 1 : 0;
+    if (phase != h->pending_phase) {
+        int rc = fold(h);
+        if (rc) return rc;
+        h->pending_phase = phase;
+    }
     SweepArgs a = sweep_args(h, c, sweep, o);
     if (a.n_c == 0) return ESP_OK;
-    CK(launch_sweep(a, h->prep.has_b, h->prep.has_d, h->max_blocks, h->st));
+    CK(launch_sweep(a, h->prep.has_b, h->prep.has_d, h->sweep_grid, h->st));
     h->launches++;
+    h->pending_sweeps++;
     return ESP_OK;
 }
 
 int do_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o)
 {
-    for (int64_t w = 0; w < n; ++w)
+    for (int64_t w = 0; w < n; ++w) {
         for (int c = 0; c < h->prep.num_colours; ++c) {
             int rc = do_sweep_colour(h, c, first + w, o);
             if (rc) return rc;
         }
+        // keep the partial counters far from overflow on long warm-ups
+        if (h->pending_sweeps >= 4096 * (long long)h->prep.num_colours) {
+            int rc = fold(h);
+            if (rc) return rc;
+        }
+    }
     return ESP_OK;
 }
 
@@ -171,8 +209,11 @@ int do_energy(esp_handle *h)
 
 int reset_running(esp_handle *h)
 {
-    int rc = do_energy(h);
+    // keep the rejected counts of pending sweeps, then overwrite the running
+    // energies and magnetisations with direct ones
+    int rc = fold(h);
     if (rc) return rc;
+    if ((rc = do_energy(h))) return rc;
     CK(cudaMemcpyAsync(h->d_e_run, h->d_tmp_e, sizeof(double) * h->R, cudaMemcpyDeviceToDevice, h->st));
     CK(cudaMemcpyAsync(h->d_m_run, h->d_tmp_m, sizeof(double) * 3 * h->R, cudaMemcpyDeviceToDevice, h->st));
     return ESP_OK;
@@ -211,6 +252,8 @@ int by_slot(esp_handle *h, const double *d_by_rep, int width, double *out)
 
 int measure(esp_handle *h, long long step, int nlev, bool pt_quirk, long long &const_hits)
 {
+    int rc = fold(h);
+    if (rc) return rc;
     MeasureArgs m;
     m.e_run = h->d_e_run; m.m_run = h->d_m_run; m.repl_at = h->d_repl_at;
     m.data = h->d_data; m.lsum = h->d_lsum; m.binning = h->d_bin; m.levels = h->d_levels;
@@ -269,23 +312,33 @@ int d2h(esp_handle *h, void *dst, const void *src, size_t bytes)
 
 }  // namespace
 
+namespace esp {
+void set_global_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(g_global_err, sizeof(g_global_err), fmt, ap);
+    va_end(ap);
+}
+}  // namespace esp
+
 extern "C" {
 
 int esp_create(const esp_dims *dims, esp_handle **out)
 {
-    if (!dims || !out) { g_create_err = "null argument"; return ESP_EINVAL; }
+    if (!dims || !out) { set_global_error("null argument"); return ESP_EINVAL; }
     *out = nullptr;
     if (dims->num_sites <= 0 || dims->num_atoms <= 0 || dims->num_replicas <= 0 ||
         dims->supercell[0] <= 0 || dims->supercell[1] <= 0 || dims->supercell[2] <= 0) {
-        g_create_err = "dimensions must be positive";
+        set_global_error("dimensions must be positive");
         return ESP_EINVAL;
     }
     if ((long long)dims->supercell[0] * dims->supercell[1] * dims->supercell[2] * dims->num_atoms != dims->num_sites) {
-        g_create_err = "num_sites != prod(supercell) * num_atoms";
+        set_global_error("num_sites != prod(supercell) * num_atoms");
         return ESP_EINVAL;
     }
     esp_handle *h = new (std::nothrow) esp_handle();
-    if (!h) { g_create_err = "host allocation failed"; return ESP_ENOMEM; }
+    if (!h) { set_global_error("host allocation failed"); return ESP_ENOMEM; }
     h->N = dims->num_sites; h->R = dims->num_replicas; h->na = dims->num_atoms;
     for (int c = 0; c < 3; ++c) h->L[c] = dims->supercell[c];
     h->open = dims->open_boundary != 0;
@@ -293,7 +346,7 @@ int esp_create(const esp_dims *dims, esp_handle **out)
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
-        g_create_err = std::string("CUDA unavailable: ") + cudaGetErrorString(e);
+        set_global_error("CUDA unavailable: %s", cudaGetErrorString(e));
         delete h;
         return ESP_ECUDA;
     }
@@ -316,7 +369,7 @@ int esp_create(const esp_dims *dims, esp_handle **out)
     if (e == cudaSuccess) e = dalloc(&h->d_data, 6 * (size_t)h->R);
     if (e == cudaSuccess) e = dalloc(&h->d_swaps, 2 * (size_t)h->R);
     if (e != cudaSuccess) {
-        g_create_err = std::string("device allocation failed: ") + cudaGetErrorString(e);
+        set_global_error("device allocation failed: %s", cudaGetErrorString(e));
         free_all(h);
         cudaStreamDestroy(h->own);
         delete h;
@@ -342,8 +395,7 @@ int esp_destroy(esp_handle *h)
 int esp_last_error(const esp_handle *h, char *buf, size_t len)
 {
     if (!buf || len == 0) return ESP_EINVAL;
-    const std::string &s = h ? h->err : g_create_err;
-    std::snprintf(buf, len, "%s", s.c_str());
+    std::snprintf(buf, len, "%s", h ? h->err.c_str() : g_global_err);
     return ESP_OK;
 }
 
@@ -351,7 +403,7 @@ int esp_set_stream(esp_handle *h, void *stream)
 {
     if (!h) return ESP_EINVAL;
     CK(cudaStreamSynchronize(h->st));
-    h->st = stream ? (cudaStream_t)stream : h->own;
+    h->st = (cudaStream_t)stream;  // NULL is the legacy default stream
     return ESP_OK;
 }
 
@@ -412,6 +464,17 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
     CK(dalloc(&h->d_fld, h->na));
     if ((rc = h2d(h, h->d_si, si.data(), sizeof(float4) * h->na))) return rc;
     if ((rc = h2d(h, h->d_fld, fl.data(), sizeof(float4) * h->na))) return rc;
+    {
+        int maxc = 0;
+        for (int c = 0; c < prep.num_colours; ++c) maxc = std::max(maxc, prep.off[c + 1] - prep.off[c]);
+        h->sweep_grid = sweep_blocks((long long)maxc * h->R, h->R, h->max_blocks);
+        h->slots = std::min(h->R, 256);
+        CK(dalloc(&h->d_part, (size_t)4 * h->sweep_grid * h->slots));
+        CK(dalloc(&h->d_part_rej, (size_t)h->sweep_grid * h->slots));
+        CK(cudaMemsetAsync(h->d_part, 0, sizeof(double) * 4 * (size_t)h->sweep_grid * h->slots, h->st));
+        CK(cudaMemsetAsync(h->d_part_rej, 0, sizeof(unsigned long long) * (size_t)h->sweep_grid * h->slots, h->st));
+        h->pending_sweeps = 0;
+    }
     h->e_blocks = energy_blocks(h->N, h->R, h->max_blocks);
     CK(dalloc(&h->d_scratch, (size_t)h->e_blocks * h->R * 4));
     // P(M) grid (mcarlo.F90:432-442)
@@ -528,6 +591,7 @@ int esp_pt_swap(esp_handle *h, int32_t start, int64_t swap_index, uint64_t seed)
     int rc = require(h, true, true);
     if (rc) return rc;
     if (start != 1 && start != 2) { h->err = "start must be 1 or 2"; return ESP_EINVAL; }
+    if ((rc = fold(h))) return rc;
     PtSwapArgs a;
     a.repl_at = h->d_repl_at; a.temp_of = h->d_temp_of; a.e_run = h->d_e_run; a.inv_t = h->d_inv_t;
     a.num_swaps = h->d_swaps; a.R = h->R; a.start0 = start - 1;
@@ -552,6 +616,7 @@ int esp_running_energy(esp_handle *h, double *out)
 {
     int rc = require(h, true, false);
     if (rc) return rc;
+    if ((rc = fold(h))) return rc;
     return by_slot(h, h->d_e_run, 1, out);
 }
 
@@ -559,6 +624,7 @@ int esp_running_magnetization(esp_handle *h, double *out)
 {
     int rc = require(h, true, false);
     if (rc) return rc;
+    if ((rc = fold(h))) return rc;
     return by_slot(h, h->d_m_run, 3, out);
 }
 
@@ -603,6 +669,10 @@ int esp_get_colouring(esp_handle *h, int32_t *colour_out, int32_t *num_colours)
 int esp_get_rejected(esp_handle *h, int64_t *out)
 {
     if (!h || !out) return ESP_EINVAL;
+    if (h->have_tables) {
+        int rc = fold(h);
+        if (rc) return rc;
+    }
     CK(cudaMemcpyAsync(out, h->d_rej, sizeof(int64_t) * 2 * h->R, cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     return ESP_OK;
@@ -664,6 +734,7 @@ int esp_begin(esp_handle *h, const esp_schedule *s)
         if ((rc = esp_energy(h, u.e_init.data()))) return rc;
         if ((rc = do_sweeps(h, s->steps_warmup * s->steps_measure, h->next_sweep, &o))) return rc;
         h->next_sweep += s->steps_warmup * s->steps_measure;
+        if ((rc = fold(h))) return rc;
         u.steps_tot[0] = s->steps_warmup * s->steps_measure * (int64_t)N;
         u.total_units = s->steps_mc;
     } else {
@@ -685,6 +756,7 @@ int esp_begin(esp_handle *h, const esp_schedule *s)
             }
         }
         u.steps_tot[0] = 2 * sw * s->steps_measure * (int64_t)N;
+        if ((rc = fold(h))) return rc;
         if ((rc = by_slot(h, h->d_e_run, 1, u.e_init.data()))) return rc;
         CK(cudaMemsetAsync(h->d_swaps, 0, sizeof(long long) * 2 * R, h->st));
     }
@@ -737,6 +809,7 @@ int esp_collect(esp_handle *h, esp_results *res)
     const esp_schedule &s = u.s;
     const int64_t steps_mc = u.meas_done;
     std::vector<double> e_add(R), e_dir(R);
+    if ((rc = fold(h))) return rc;
     if ((rc = by_slot(h, h->d_e_run, 1, e_add.data()))) return rc;
     if ((rc = do_energy(h))) return rc;
     if ((rc = by_slot(h, h->d_tmp_e, 1, e_dir.data()))) return rc;

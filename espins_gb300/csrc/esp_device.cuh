@@ -93,12 +93,12 @@ struct SweepArgs {
     float *sx, *sy, *sz;
     const int32_t *temp_of;   // replica -> temperature slot
     const float *beta;        // slot -> 1/T
-    double *e_run;            // [R] running energy per replica
-    double *m_run;            // [R][3] running sum of spins per replica
-    unsigned long long *rej;  // [R slots][2]
+    double *part;             // [blocks][slots][4]: dE, dMx, dMy, dMz of accepted moves
+    unsigned long long *part_rej;   // [blocks][slots]: rejected trials
+    int32_t slots;            // min(R, blockDim)
     int32_t N, R, num_atoms;
     int32_t off_c, n_c;       // colour class: permuted sites [off_c, off_c + n_c)
-    int32_t phase, mode;
+    int32_t mode;
     float tilt;
     uint32_t key0, key1, sw_lo, sw_hi;
 };

@@ -22,52 +22,80 @@
 namespace esp {
 
 // ---------------------------------------------------------------------------
-// Block reduction of per-thread (dE, dMx, dMy, dMz, rejects) by replica.
-// Thread t of the block handles replica (base + t) % R, so the threads of one
-// replica are t0, t0+R, t0+2R, ...; thread t < min(R, blockDim) sums them.
+// Per-block partial sums, no atomics.  Thread t of block b works on replica
+// (b*blockDim + t) % R for the whole launch, so the threads of one replica in
+// a block are t0, t0+R, ...; thread t < slots (= min(R, blockDim)) sums them
+// and adds the result to its block's own slot part[b][t].  Every launch of the
+// sweep uses the same grid, so slot (b, t) always belongs to the same block and
+// the same replica; k_fold later sums the slots of each replica in block order
+// (deterministic) into the running totals.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void flush_replica_sums(double e, double mx, double my, double mz,
-                                                   unsigned int nrej, int r, int temp, int R, int phase,
-                                                   double *e_run, double *m_run, unsigned long long *rej,
-                                                   bool active)
+__device__ __forceinline__ void add_block_slots(double e, double mx, double my, double mz, unsigned int nrej,
+                                                int R, int slots, double *part, unsigned long long *part_rej)
 {
     __shared__ double s_part[256][4];
     __shared__ unsigned int s_rej[256];
-    __shared__ int s_r[256], s_t[256];
     const int t = threadIdx.x;
     const int nt = blockDim.x;
+    const size_t slot = (size_t)blockIdx.x * slots + t;
     if (R >= nt) {
-        if (active) {
-            if (e != 0.0) atomicAdd(e_run + r, e);
-            if (mx != 0.0) atomicAdd(m_run + 3 * r, mx);
-            if (my != 0.0) atomicAdd(m_run + 3 * r + 1, my);
-            if (mz != 0.0) atomicAdd(m_run + 3 * r + 2, mz);
-            if (nrej) atomicAdd(rej + 2 * temp + phase, (unsigned long long)nrej);
-        }
+        double *o = part + 4 * slot;
+        o[0] += e; o[1] += mx; o[2] += my; o[3] += mz;
+        part_rej[slot] += (unsigned long long)nrej;
         return;
     }
-    s_part[t][0] = active ? e : 0.0;
-    s_part[t][1] = active ? mx : 0.0;
-    s_part[t][2] = active ? my : 0.0;
-    s_part[t][3] = active ? mz : 0.0;
-    s_rej[t] = active ? nrej : 0u;
-    s_r[t] = active ? r : -1;
-    s_t[t] = temp;
+    s_part[t][0] = e; s_part[t][1] = mx; s_part[t][2] = my; s_part[t][3] = mz;
+    s_rej[t] = nrej;
     __syncthreads();
-    if (t < R && s_r[t] >= 0) {
+    if (t < R) {
         double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
         unsigned long long nr = 0;
         for (int u = t; u < nt; u += R) {
-            if (s_r[u] < 0) continue;
             a0 += s_part[u][0]; a1 += s_part[u][1]; a2 += s_part[u][2]; a3 += s_part[u][3];
             nr += s_rej[u];
         }
-        const int rr = s_r[t];
-        if (a0 != 0.0) atomicAdd(e_run + rr, a0);
-        if (a1 != 0.0) atomicAdd(m_run + 3 * rr, a1);
-        if (a2 != 0.0) atomicAdd(m_run + 3 * rr + 1, a2);
-        if (a3 != 0.0) atomicAdd(m_run + 3 * rr + 2, a3);
-        if (nr) atomicAdd(rej + 2 * s_t[t] + phase, nr);
+        double *o = part + 4 * slot;
+        o[0] += a0; o[1] += a1; o[2] += a2; o[3] += a3;
+        part_rej[slot] += nr;
+    }
+}
+
+// Sum every block's slot of replica r, add it to the running energy /
+// magnetisation and to the rejected counter of r's temperature slot, and
+// clear the slots.  One block per replica: thread t takes blocks t, t+256, ...
+// and a fixed-shape tree combines the threads, so the sum is deterministic.
+__global__ void __launch_bounds__(256) k_fold(FoldArgs a)
+{
+    __shared__ double s_v[4][256];
+    __shared__ unsigned long long s_n[256];
+    const int r = blockIdx.x;
+    double e = 0, mx = 0, my = 0, mz = 0;
+    unsigned long long nr = 0;
+    for (int b = threadIdx.x; b < a.nblocks; b += blockDim.x) {
+        long long t = ((long long)r - (long long)b * a.block_threads) % a.R;
+        if (t < 0) t += a.R;
+        if (t >= a.slots) continue;
+        const size_t slot = (size_t)b * a.slots + t;
+        double *o = a.part + 4 * slot;
+        e += o[0]; mx += o[1]; my += o[2]; mz += o[3];
+        o[0] = 0.0; o[1] = 0.0; o[2] = 0.0; o[3] = 0.0;
+        nr += a.part_rej[slot];
+        a.part_rej[slot] = 0ull;
+    }
+    const int t = threadIdx.x;
+    s_v[0][t] = e; s_v[1][t] = mx; s_v[2][t] = my; s_v[3][t] = mz; s_n[t] = nr;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) {
+            for (int c = 0; c < 4; ++c) s_v[c][t] += s_v[c][t + w];
+            s_n[t] += s_n[t + w];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        a.e_run[r] += s_v[0][0];
+        a.m_run[3 * r] += s_v[1][0]; a.m_run[3 * r + 1] += s_v[2][0]; a.m_run[3 * r + 2] += s_v[3][0];
+        a.rej[2 * a.temp_of[r] + a.phase] += s_n[0];
     }
 }
 
@@ -168,7 +196,7 @@ __global__ void __launch_bounds__(256) k_sweep_ell(const SweepArgs a)
             }
         }
     }
-    flush_replica_sums(accE, accX, accY, accZ, nrej, r, temp, R, a.phase, a.e_run, a.m_run, a.rej, live);
+    add_block_slots(accE, accX, accY, accZ, nrej, R, a.slots, a.part, a.part_rej);
 }
 
 // ---------------------------------------------------------------------------
@@ -358,37 +386,38 @@ __global__ void k_measure(MeasureArgs a)
 // integers per temperature slot (the reference adds 1/d_m = 100 per hit).
 // Block: a tile of cells x all replicas, shared histogram [R][nf] when it fits.
 // ---------------------------------------------------------------------------
-__global__ void k_pm_hist(PmArgs a)
+__global__ void __launch_bounds__(256) k_pm_hist(PmArgs a)
 {
+    // block (x, y): a chunk of cells x the replica tile [y*rt, y*rt + nrt)
     extern __shared__ unsigned int s_hist[];
-    const int R = a.R;
-    const bool shared = a.use_shared;
-    if (shared) {
-        for (int i = threadIdx.x; i < R * a.nf; i += blockDim.x) s_hist[i] = 0u;
-        __syncthreads();
-    }
-    const long long total = (long long)a.ncell * R;
+    const int R = a.R, nf = a.nf;
+    const int r0 = blockIdx.y * a.rt;
+    const int nrt = min(a.rt, R - r0);
+    for (int i = threadIdx.x; i < nrt * nf; i += blockDim.x) s_hist[i] = 0u;
+    __syncthreads();
+    const long long total = (long long)a.ncell * nrt;
     for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
          it += (long long)gridDim.x * blockDim.x) {
-        const int cell = (int)(it / R), r = (int)(it % R);
+        const int cell = (int)(it / nrt), rr = (int)(it % nrt), r = r0 + rr;
         double mx = 0, my = 0, mz = 0;
         for (int at = 0; at < a.num_atoms; ++at) {
-            const int p = a.inv[cell * a.num_atoms + at];
+            const int p = __ldg(a.inv + cell * a.num_atoms + at);
             const size_t idx = (size_t)p * R + r;
             mx += (double)a.sx[idx]; my += (double)a.sy[idx]; mz += (double)a.sz[idx];
         }
         const double m = sqrt(mx * mx + my * my + mz * mz);
-        long long bin = llround(((m - a.m_min) / (a.m_max - a.m_min)) * (double)(a.nf - 1)) + 1;
+        long long bin = llround(((m - a.m_min) / (a.m_max - a.m_min)) * (double)(nf - 1)) + 1;
         if (bin < 1) bin = 1;
-        if (bin > a.nf) bin = a.nf;
-        const int t = a.temp_of[r];
-        if (shared) atomicAdd(s_hist + t * a.nf + (int)(bin - 1), 1u);
-        else atomicAdd(a.counts + (size_t)t * a.nf + (bin - 1), 1ULL);
+        if (bin > nf) bin = nf;
+        atomicAdd(s_hist + rr * nf + (int)(bin - 1), 1u);
     }
-    if (shared) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < R * a.nf; i += blockDim.x)
-            if (s_hist[i]) atomicAdd(a.counts + i, (unsigned long long)s_hist[i]);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nrt * nf; i += blockDim.x) {
+        const unsigned int c = s_hist[i];
+        if (c) {
+            const int t = a.temp_of[r0 + i / nf];
+            atomicAdd(a.counts + (size_t)t * nf + (i % nf), (unsigned long long)c);
+        }
     }
 }
 
@@ -400,23 +429,23 @@ __global__ void k_pm_hist(PmArgs a)
 // ---------------------------------------------------------------------------
 __global__ void k_pt_swap(PtSwapArgs a)
 {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    for (int s = a.start0; s + 1 < a.R; s += 2) {
-        const int ra = a.repl_at[s], rb = a.repl_at[s + 1];
-        const double x = (a.inv_t[s] - a.inv_t[s + 1]) * (a.e_run[ra] - a.e_run[rb]);
-        a.num_swaps[2 * s] += 1;
-        a.num_swaps[2 * (s + 1)] += 1;
-        bool swap = x > 0.0;
-        if (!swap) {
-            const Philox4 v = philox4x32_10((uint32_t)s, a.idx_lo, a.idx_hi, 0xFFFFFFFFu, a.key0, a.key1);
-            swap = u53(v.x, v.y) < exp(x);
-        }
-        if (swap) {
-            a.repl_at[s] = rb; a.repl_at[s + 1] = ra;
-            a.temp_of[rb] = s; a.temp_of[ra] = s + 1;
-            a.num_swaps[2 * s + 1] += 1;
-            a.num_swaps[2 * (s + 1) + 1] += 1;
-        }
+    // pairs are disjoint, one thread each
+    const int s = a.start0 + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (s + 1 >= a.R) return;
+    const int ra = a.repl_at[s], rb = a.repl_at[s + 1];
+    const double x = (a.inv_t[s] - a.inv_t[s + 1]) * (a.e_run[ra] - a.e_run[rb]);
+    a.num_swaps[2 * s] += 1;
+    a.num_swaps[2 * (s + 1)] += 1;
+    bool swap = x > 0.0;
+    if (!swap) {
+        const Philox4 v = philox4x32_10((uint32_t)s, a.idx_lo, a.idx_hi, 0xFFFFFFFFu, a.key0, a.key1);
+        swap = u53(v.x, v.y) < exp(x);
+    }
+    if (swap) {
+        a.repl_at[s] = rb; a.repl_at[s + 1] = ra;
+        a.temp_of[rb] = s; a.temp_of[ra] = s + 1;
+        a.num_swaps[2 * s + 1] += 1;
+        a.num_swaps[2 * (s + 1) + 1] += 1;
     }
 }
 
@@ -457,14 +486,24 @@ static int grid_for(long long items, int threads, int max_blocks)
     return (int)b;
 }
 
-cudaError_t launch_sweep(const SweepArgs &a, bool hb, bool hd, int max_blocks, cudaStream_t st)
+int sweep_blocks(long long max_items, int R, int max_blocks)
 {
     const int threads = 256;
-    const long long items = (long long)a.n_c * a.R;
-    int blocks = grid_for(items, threads, max_blocks);
+    int blocks = grid_for(max_items, threads, max_blocks);
     // the stride must hold at least one copy of every replica
-    const int need = (a.R + threads - 1) / threads;
-    if (blocks < need) blocks = need;
+    const int need = (R + threads - 1) / threads;
+    return blocks < need ? need : blocks;
+}
+
+cudaError_t launch_fold(const FoldArgs &a, cudaStream_t st)
+{
+    k_fold<<<a.R, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sweep(const SweepArgs &a, bool hb, bool hd, int blocks, cudaStream_t st)
+{
+    const int threads = 256;
     if (hb && hd) k_sweep_ell<true, true><<<blocks, threads, 0, st>>>(a);
     else if (hb) k_sweep_ell<true, false><<<blocks, threads, 0, st>>>(a);
     else if (hd) k_sweep_ell<false, true><<<blocks, threads, 0, st>>>(a);
@@ -521,16 +560,36 @@ cudaError_t launch_measure(const MeasureArgs &a, cudaStream_t st)
 cudaError_t launch_pm(const PmArgs &a0, int max_blocks, cudaStream_t st)
 {
     PmArgs a = a0;
-    const size_t smem = (size_t)a.R * a.nf * sizeof(unsigned int);
-    a.use_shared = smem <= 48 * 1024 ? 1 : 0;
-    const int blocks = grid_for((long long)a.ncell * a.R, 256, max_blocks);
-    k_pm_hist<<<blocks, 256, a.use_shared ? smem : 0, st>>>(a);
+    // replica tile: its [rt][nf] histogram fits in 96 KB of shared memory
+    const size_t cap = 96 * 1024;
+    a.rt = (int)(cap / ((size_t)a.nf * sizeof(unsigned int)));
+    if (a.rt < 1) return cudaErrorInvalidValue;
+    if (a.rt > a.R) a.rt = a.R;
+    a.use_shared = 1;
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!attr_set[dev]) {
+        e = cudaFuncSetAttribute(k_pm_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
+        if (e != cudaSuccess) return e;
+        attr_set[dev] = true;
+    }
+    const int tiles = (a.R + a.rt - 1) / a.rt;
+    // few blocks, many items each: the flush of the block histograms is a
+    // global atomic per non-empty bin, so fewer blocks means less contention
+    const int cap_blocks = max_blocks / 8 / tiles > 0 ? max_blocks / 8 / tiles : 1;
+    int bx = grid_for((long long)a.ncell * a.rt, 256, cap_blocks);
+    const size_t smem = (size_t)a.rt * a.nf * sizeof(unsigned int);
+    k_pm_hist<<<dim3(bx, tiles), 256, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pt_swap(const PtSwapArgs &a, cudaStream_t st)
 {
-    k_pt_swap<<<1, 32, 0, st>>>(a);
+    const int pairs = (a.R + 1) / 2;
+    k_pt_swap<<<(pairs + 127) / 128, 128, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -17,6 +17,15 @@ struct EnergyArgsHost {
     int32_t N, R, num_atoms;
 };
 
+struct FoldArgs {
+    double *part;
+    unsigned long long *part_rej;
+    double *e_run, *m_run;
+    unsigned long long *rej;  // [R slots][2]
+    const int32_t *temp_of;
+    int32_t R, nblocks, slots, block_threads, phase;
+};
+
 struct MeasureArgs {
     const double *e_run, *m_run;
     const int32_t *repl_at;
@@ -32,7 +41,7 @@ struct PmArgs {
     const int32_t *inv;       // reference site -> permuted index
     const int32_t *temp_of;
     unsigned long long *counts;  // [R slots][nf]
-    int32_t R, ncell, num_atoms, nf, use_shared;
+    int32_t R, ncell, num_atoms, nf, use_shared, rt;
     double m_min, m_max;
 };
 
@@ -44,7 +53,9 @@ struct PtSwapArgs {
     uint32_t key0, key1, idx_lo, idx_hi;
 };
 
-cudaError_t launch_sweep(const SweepArgs &a, bool hb, bool hd, int max_blocks, cudaStream_t st);
+int sweep_blocks(long long max_items, int R, int max_blocks);
+cudaError_t launch_sweep(const SweepArgs &a, bool hb, bool hd, int blocks, cudaStream_t st);
+cudaError_t launch_fold(const FoldArgs &a, cudaStream_t st);
 int energy_blocks(int N, int R, int max_blocks);
 cudaError_t launch_energy(const EnergyArgsHost &h, double *out_e, double *out_m, int blocks, cudaStream_t st);
 cudaError_t launch_local_terms(const EnergyArgsHost &h, float *g, float *q, cudaStream_t st);

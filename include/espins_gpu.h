@@ -123,7 +123,8 @@ int esp_create(const esp_dims *dims, esp_handle **out);
 int esp_destroy(esp_handle *h);
 /* Message of the last failed call on h (or of esp_create when h is NULL). */
 int esp_last_error(const esp_handle *h, char *buf, size_t len);
-/* Launch on an existing CUDA stream (cudaStream_t) instead of the handle's. */
+/* Launch on an existing CUDA stream (cudaStream_t) instead of the handle's
+ * own; NULL selects the legacy default stream. */
 int esp_set_stream(esp_handle *h, void *cuda_stream);
 
 /* ---- data in ---------------------------------------------------------- */
