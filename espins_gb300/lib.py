@@ -24,6 +24,7 @@ EXPORTED = [
     "esp_sweep_colour", "esp_pt_swap", "esp_energy", "esp_running_energy",
     "esp_running_magnetization", "esp_local_terms", "esp_get_spins", "esp_get_colouring",
     "esp_get_rejected", "esp_get_replica_of_slot", "esp_num_freq", "esp_launch_count",
+    "esp_energy_noalloc",
 ]
 
 
@@ -58,6 +59,17 @@ class Results(C.Structure):
     _fields_ = [("rejected", C.c_void_p), ("steps_tot", C.c_void_p), ("energy", C.c_void_p),
                 ("data", C.c_void_p), ("pm", C.c_void_p), ("binning", C.c_void_p),
                 ("num_swaps", C.c_void_p), ("map", C.c_void_p), ("steps_mc_eff", C.c_int64)]
+
+
+class EnergyArgs(C.Structure):
+    """esp_energy_args: device pointers in the reference's layouts."""
+    _fields_ = [("num_sites", C.c_int32), ("num_atoms", C.c_int32), ("num_replicas", C.c_int32),
+                ("spins", C.c_void_p),
+                ("j_nn", C.c_void_p), ("j_nbors", C.c_void_p), ("j_val", C.c_void_p),
+                ("b_nn", C.c_void_p), ("b_nbors", C.c_void_p), ("b_val", C.c_void_p),
+                ("d_nn", C.c_void_p), ("d_nbors", C.c_void_p), ("d_val", C.c_void_p),
+                ("si_axis", C.c_void_p), ("si_delta", C.c_void_p),
+                ("field_axis", C.c_void_p), ("field_val", C.c_void_p)]
 
 
 class SweepOpts(C.Structure):
@@ -102,10 +114,18 @@ def load(build_if_missing: bool = True):
     lib.esp_get_colouring.argtypes = [vp, vp, P(C.c_int32)]
     lib.esp_num_freq.argtypes = [vp, P(C.c_int32)]
     lib.esp_launch_count.argtypes = [vp, P(C.c_int64)]
+    lib.esp_energy_noalloc.argtypes = [P(EnergyArgs), vp, vp]
     for f in EXPORTED:
         getattr(lib, f).restype = C.c_int
     _lib = lib
     return lib
+
+
+def last_global_error() -> str:
+    """esp_last_error(NULL, ...): the message of a failed call without a handle."""
+    buf = C.create_string_buffer(512)
+    load().esp_last_error(None, buf, 512)
+    return buf.value.decode()
 
 
 def _p(a: Optional[np.ndarray]):

@@ -194,6 +194,32 @@ int esp_num_freq(const esp_handle *h, int32_t *nf);
 /* Number of kernels this handle has launched so far. */
 int esp_launch_count(const esp_handle *h, int64_t *count);
 
+/* ---- allocation-free direct energy ---------------------------------------
+ * No counterpart in the reference: an extra entry point for hosts that own
+ * all device memory and cannot let a library allocate (a Fortran program
+ * whose arrays sit in its own device data regions, a framework with its own
+ * caching allocator, a run that must not change its device footprint).
+ * Every pointer below is a DEVICE pointer owned by the caller, in the
+ * reference's layouts (as esp_tables, with spins = spin_matrix(3,N,R)).
+ * The partial sums live in a 1 MiB array inside the library (held by every
+ * GPU that loads it), so: num_replicas <= ESP_NOALLOC_MAX_REPLICAS and
+ * num_sites * num_replicas < 2^31, else ESP_EINVAL.  The first call on each
+ * device looks up that array's device address; make it before any stream
+ * capture.  Calls that overlap on the GPU share the array and race. */
+#define ESP_NOALLOC_MAX_REPLICAS 4096
+typedef struct {
+    int32_t num_sites, num_atoms, num_replicas;
+    const double *spins;        /* (3,N,R) */
+    const int32_t *j_nn, *j_nbors; const double *j_val;
+    const int32_t *b_nn, *b_nbors; const double *b_val;   /* or NULL */
+    const int32_t *d_nn, *d_nbors; const double *d_val;   /* or NULL */
+    const double *si_axis, *si_delta;                     /* or NULL */
+    const double *field_axis, *field_val;                 /* or NULL */
+} esp_energy_args;
+/* energy_out: device array [R]; runs on `stream` (a cudaStream_t, or NULL);
+ * calls no cudaMalloc/cudaFree and allocates nothing. */
+int esp_energy_noalloc(const esp_energy_args *a, double *energy_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
