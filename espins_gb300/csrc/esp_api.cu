@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/espins_gpu.h"
+#include "esp_cluster.h"
 #include "esp_kernels.h"
 #include "esp_tables.h"
 #include "esp_errors.h"
@@ -59,6 +60,16 @@ struct esp_handle {
     int sweep_grid = 0, slots = 0;
     int pending_phase = 0;
     long long pending_sweeps = 0;
+    // cluster-resident path (translation-invariant lattices)
+    int kernel_choice = 0;          // 0 auto, 1 ELL, 2 cluster
+    bool cluster_ok = false;
+    int csize = 0, pz = 0;
+    size_t cluster_smem = 0;
+    double *d_series = nullptr;
+    long long series_cap = 0;
+    unsigned char *d_stencil_blob = nullptr;
+    uint32_t *d_nbidx = nullptr;
+    int stencil_words = 0;
     double *d_tmp_e = nullptr, *d_tmp_m = nullptr;
     // accumulators
     double *d_data = nullptr, *d_lsum = nullptr, *d_bin = nullptr;
@@ -105,6 +116,8 @@ void free_tables(esp_handle *h)
     dfree(h->d_nnb); dfree(h->d_nbr); dfree(h->d_perm); dfree(h->d_inv);
     dfree(h->d_J); dfree(h->d_B); dfree(h->d_Dx); dfree(h->d_Dy); dfree(h->d_Dz); dfree(h->d_mag);
     dfree(h->d_si); dfree(h->d_fld); dfree(h->d_scratch); dfree(h->d_part); dfree(h->d_part_rej);
+    dfree(h->d_stencil_blob); dfree(h->d_nbidx);
+    h->cluster_ok = false;
 }
 
 void free_all(esp_handle *h)
@@ -114,6 +127,7 @@ void free_all(esp_handle *h)
     dfree(h->d_temp_of); dfree(h->d_repl_at); dfree(h->d_beta); dfree(h->d_inv_t);
     dfree(h->d_e_run); dfree(h->d_m_run); dfree(h->d_rej); dfree(h->d_tmp_e); dfree(h->d_tmp_m);
     dfree(h->d_data); dfree(h->d_lsum); dfree(h->d_bin); dfree(h->d_levels); dfree(h->d_pm); dfree(h->d_swaps);
+    dfree(h->d_series);
 }
 
 SweepArgs sweep_args(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o)
@@ -167,6 +181,55 @@ int fold(esp_handle *h)
     return ESP_OK;
 }
 
+bool use_cluster(const esp_handle *h)
+{
+    return h->cluster_ok && h->kernel_choice != 1;
+}
+
+// One launch of the cluster-resident kernel: n_meas units of steps_measure
+// sweeps starting at global sweep `first`, each unit followed by a
+// measurement when `measure` is set.
+int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first, int measure, long long meas_base,
+                const esp_sweep_opts *o, int phase, int nlev, bool pt_quirk)
+{
+    int rc = fold(h);
+    if (rc) return rc;
+    ClusterArgs a;
+    a.stencil = reinterpret_cast<const ClusterStencil *>(h->d_stencil_blob);
+    a.stencil_words = h->stencil_words;
+    a.nbidx = h->d_nbidx;
+    a.Lx = h->L[0]; a.Ly = h->L[1]; a.Lz = h->L[2]; a.na = h->na; a.N = h->N; a.R = h->R;
+    a.nclass = 8 * h->na; a.pz = h->pz;
+    a.has_b = h->prep.has_b; a.has_d = h->prep.has_d; a.has_si = h->hsi; a.has_f = h->hfld;
+    a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz; a.inv = h->d_inv;
+    a.temp_of = h->d_temp_of; a.beta = h->d_beta; a.e_run = h->d_e_run; a.m_run = h->d_m_run; a.rej = h->d_rej;
+    a.phase = phase;
+    a.measure = measure; a.n_meas = (int)n_meas; a.steps_measure = steps_measure; a.meas_base = meas_base;
+    a.data = h->d_data; a.lsum = h->d_lsum; a.binning = h->d_bin; a.levels = h->d_levels;
+    a.nlev = nlev; a.pt_quirk = pt_quirk ? 1 : 0;
+    a.pm_counts = h->d_pm; a.nf = h->nf; a.m_min = h->m_min; a.m_max = h->m_max;
+    a.series = h->d_series; a.series_cap = h->series_cap;
+    a.sweep_base = (unsigned long long)first;
+    a.key0 = (uint32_t)o->seed; a.key1 = (uint32_t)(o->seed >> 32);
+    a.mode = o->mcarlo_mode ? 1 : 0; a.tilt = (float)o->tilt_angles_max;
+    CK(launch_cluster(a, h->csize, h->cluster_smem, h->st));
+    h->launches++;
+    return ESP_OK;
+}
+
+// plain sweeps on the cluster path, in launches of at most kChunk sweeps
+constexpr int64_t kChunk = 1000;
+
+int cluster_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o)
+{
+    for (int64_t done = 0; done < n; done += kChunk) {
+        const int64_t k = std::min(kChunk, n - done);
+        int rc = cluster_run(h, k, 1, first + done, 0, 0, o, o->phase ? 1 : 0, 0, false);
+        if (rc) return rc;
+    }
+    return ESP_OK;
+}
+
 int do_sweep_colour(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o)
 {
     const int phase = o->phase ? 1 : 0;
@@ -185,6 +248,7 @@ int do_sweep_colour(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o
 
 int do_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o)
 {
+    if (use_cluster(h)) return cluster_sweeps(h, n, first, o);
     for (int64_t w = 0; w < n; ++w) {
         for (int c = 0; c < h->prep.num_colours; ++c) {
             int rc = do_sweep_colour(h, c, first + w, o);
@@ -258,6 +322,7 @@ int measure(esp_handle *h, long long step, int nlev, bool pt_quirk, long long &c
     m.e_run = h->d_e_run; m.m_run = h->d_m_run; m.repl_at = h->d_repl_at;
     m.data = h->d_data; m.lsum = h->d_lsum; m.binning = h->d_bin; m.levels = h->d_levels;
     m.R = h->R; m.N = h->N; m.nlev = nlev; m.pt_quirk = pt_quirk ? 1 : 0; m.step = step;
+    m.series = h->d_series; m.series_cap = h->series_cap;
     CK(launch_measure(m, h->st));
     h->launches++;
     if (h->na == 1) {
@@ -412,6 +477,7 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
     if (!h || !t) return ESP_EINVAL;
     PrepInput in;
     in.N = h->N; in.num_atoms = h->na; in.L[0] = h->L[0]; in.L[1] = h->L[1]; in.L[2] = h->L[2];
+    in.open_boundary = h->open;
     in.mag = t->mag;
     in.j_maxnb = t->j_maxnb; in.j_nn = t->j_nn; in.j_nbors = t->j_nbors; in.j_val = t->j_val;
     in.b_maxnb = t->b_maxnb; in.b_nn = t->b_nn; in.b_nbors = t->b_nbors; in.b_val = t->b_val;
@@ -475,14 +541,119 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
         CK(cudaMemsetAsync(h->d_part_rej, 0, sizeof(unsigned long long) * (size_t)h->sweep_grid * h->slots, h->st));
         h->pending_sweeps = 0;
     }
-    h->e_blocks = energy_blocks(h->N, h->R, h->max_blocks);
-    CK(dalloc(&h->d_scratch, (size_t)h->e_blocks * h->R * 4));
     // P(M) grid (mcarlo.F90:432-442)
     double mmax = 0.0;
     for (int a = 0; a < h->na; ++a) mmax += std::fabs(t->mag[a]);
     h->m_max = mmax; h->m_min = -mmax;
     h->nf = (int)std::llround((h->m_max - h->m_min) / 0.01) + 1;
     if (h->nf == 1) h->nf = 2;
+    // cluster-resident path: translation-invariant lattice whose replica fits
+    // in the distributed shared memory of one cluster
+    h->cluster_ok = false;
+    if (prep.invariant && h->na <= kMaxClusterAtoms && prep.num_colours <= kMaxClasses &&
+        (int)prep.class_colour.size() == 8 * h->na && h->L[0] % 2 == 0 && h->L[1] % 2 == 0 && h->L[2] % 2 == 0) {
+        const int nclass = 8 * h->na;
+        int maxst = 0;
+        for (int at = 0; at < h->na; ++at) maxst = std::max(maxst, (int)prep.stencil[at].size());
+        maxst = (maxst + 7) & ~7;  // the kernel reads neighbours in groups of 8
+        const size_t sbytes = (cluster_stencil_bytes(nclass, maxst) + 15) & ~(size_t)15;
+        std::vector<unsigned char> blob(sbytes, 0);
+        ClusterStencil &hs = *reinterpret_cast<ClusterStencil *>(blob.data());
+        ClusterNbr *nbs = reinterpret_cast<ClusterNbr *>(blob.data() + sizeof(ClusterStencil));
+        bool fits = true;
+        hs.nclass = nclass; hs.maxst = maxst; hs.ncolour = prep.num_colours;
+        auto fdiv2 = [](int v) { return v >= 0 ? v / 2 : -((-v + 1) / 2); };  // floor(v / 2)
+        for (int k = 0; k < nclass; ++k) {
+            const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
+            const auto &lst = prep.stencil[at];
+            hs.count[k] = (int)lst.size();
+            for (size_t e = 0; e < lst.size(); ++e) {
+                const StencilEntry &x = lst[e];
+                ClusterNbr &nb = nbs[(size_t)k * maxst + e];
+                const int qx = px + x.dx, qy = py + x.dy, qz = pz + x.dz;
+                nb.kn = (x.b << 3) | ((qx & 1) << 2) | ((qy & 1) << 1) | (qz & 1);
+                nb.dhx = fdiv2(qx); nb.dhy = fdiv2(qy); nb.dhz = fdiv2(qz);
+                nb.J = x.J; nb.B = x.B; nb.Dx = x.Dx; nb.Dy = x.Dy; nb.Dz = x.Dz;
+            }
+        }
+        for (int at = 0; at < h->na; ++at) {
+            if (h->hsi)
+                hs.si[at] = make_float4((float)t->si_axis[3 * at], (float)t->si_axis[3 * at + 1],
+                                        (float)t->si_axis[3 * at + 2], (float)t->si_delta[at]);
+            if (h->hfld)
+                hs.fld[at] = make_float4((float)(t->field_val[at] * t->field_axis[3 * at]),
+                                         (float)(t->field_val[at] * t->field_axis[3 * at + 1]),
+                                         (float)(t->field_val[at] * t->field_axis[3 * at + 2]), 0.f);
+            hs.mag[at] = (float)t->mag[at];
+        }
+        // every site of an atom must carry that atom's moment
+        for (int i = 0; i < h->N && fits; ++i)
+            if ((float)t->mag[i] != hs.mag[i % h->na]) fits = false;
+        {
+            int n = 0;
+            for (int c = 0; c < prep.num_colours; ++c) {
+                hs.colour_start[c] = n;
+                for (int k = 0; k < nclass; ++k)
+                    if (prep.class_colour[k] == c) hs.class_order[n++] = k;
+            }
+            hs.colour_start[prep.num_colours] = n;
+        }
+        // cluster size (portable, <= 8): slabs of an even number of planes,
+        // shared memory within the per-CTA limit, and the fewest waves of R
+        // clusters as the occupancy calculator counts them, per CTA of work
+        int best = 0;
+        double best_cost = 1e300;
+        for (int cs = 1; cs <= 8 && fits; ++cs) {
+            if (h->L[2] % (2 * cs) != 0) continue;
+            const size_t smem = cluster_smem_bytes(h->N / cs, h->nf, sbytes);
+            if (smem > 226 * 1024) continue;
+            const int active = cluster_max_active(cs, smem, h->R);
+            if (active <= 0) continue;
+            const double waves = std::ceil((double)h->R / (double)active);
+            const double cost = waves / cs;
+            if (cost < best_cost - 1e-12) { best_cost = cost; best = cs; }
+        }
+        if (fits && best > 0) {
+            h->csize = best;
+            h->pz = h->L[2] / best;
+            h->cluster_smem = cluster_smem_bytes(h->N / best, h->nf, sbytes);
+            h->stencil_words = (int)(sbytes / 4);
+            CK(dalloc(&h->d_stencil_blob, sbytes));
+            if ((rc = h2d(h, h->d_stencil_blob, blob.data(), sbytes))) return rc;
+            CK(cluster_configure(h->cluster_smem, best));
+            // neighbour table of every CTA rank: (owner rank << 24) | local index
+            const int cs = best, pz = h->pz, n_local = h->N / cs;
+            const int Lx = h->L[0], Ly = h->L[1], Lz = h->L[2], Hx = Lx / 2, Hy = Ly / 2, Hzl = pz / 2;
+            const int per_class = Hx * Hy * Hzl;
+            std::vector<uint32_t> tab((size_t)cs * maxst * n_local);
+            for (int q = 0; q < cs; ++q)
+                for (int l = 0; l < n_local; ++l) {
+                    const int k = l / per_class, rem = l % per_class;
+                    const int hx = rem % Hx, hy = (rem / Hx) % Hy, hzl = rem / (Hx * Hy);
+                    const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pzb = k & 1;
+                    const int x = 2 * hx + px, y = 2 * hy + py, z = q * pz + 2 * hzl + pzb;
+                    const auto &lst = prep.stencil[at];
+                    for (int e = 0; e < maxst; ++e) {
+                        uint32_t v = ((uint32_t)q << 24) | (uint32_t)l;  // padding: the site itself
+                        if (e < (int)lst.size()) {
+                            const StencilEntry &se = lst[e];
+                            const int xn = ((x + se.dx) % Lx + Lx) % Lx, yn = ((y + se.dy) % Ly + Ly) % Ly;
+                            const int zn = ((z + se.dz) % Lz + Lz) % Lz;
+                            const int kn = (se.b << 3) | ((xn & 1) << 2) | ((yn & 1) << 1) | (zn & 1);
+                            const int rn = zn / pz;
+                            const int ln = kn * per_class + ((((zn - rn * pz) >> 1) * Hy + (yn >> 1)) * Hx + (xn >> 1));
+                            v = ((uint32_t)rn << 24) | (uint32_t)ln;
+                        }
+                        tab[((size_t)q * maxst + e) * n_local + l] = v;
+                    }
+                }
+            CK(dalloc(&h->d_nbidx, tab.size()));
+            if ((rc = h2d(h, h->d_nbidx, tab.data(), sizeof(uint32_t) * tab.size()))) return rc;
+            h->cluster_ok = true;
+        }
+    }
+    h->e_blocks = energy_blocks(h->N, h->R, h->max_blocks);
+    CK(dalloc(&h->d_scratch, (size_t)h->e_blocks * h->R * 4));
     dfree(h->d_pm);
     CK(dalloc(&h->d_pm, (size_t)h->R * h->nf));
     h->prep = std::move(prep);
@@ -688,6 +859,58 @@ int esp_get_replica_of_slot(esp_handle *h, int32_t *out)
     return ESP_OK;
 }
 
+int esp_set_series(esp_handle *h, int64_t capacity)
+{
+    if (!h || capacity < 0) return ESP_EINVAL;
+    CK(cudaStreamSynchronize(h->st));
+    dfree(h->d_series);
+    h->series_cap = 0;
+    if (capacity > 0) {
+        CK(dalloc(&h->d_series, (size_t)capacity * h->R * 2));
+        h->series_cap = capacity;
+    }
+    return ESP_OK;
+}
+
+int esp_get_series(esp_handle *h, double *out, int64_t *count)
+{
+    if (!h || !count) return ESP_EINVAL;
+    const long long done = h->run.meas_done;
+    const long long n = std::min<long long>(done, h->series_cap);
+    *count = n;
+    if (!out || n == 0) return ESP_OK;
+    std::vector<double> all((size_t)h->series_cap * h->R * 2);
+    int rc = d2h(h, all.data(), h->d_series, sizeof(double) * all.size());
+    if (rc) return rc;
+    const long long first = done - n;  // 0-based index of the oldest kept measurement
+    for (long long k = 0; k < n; ++k) {
+        const long long row = (first + k) % h->series_cap;
+        std::memcpy(out + (size_t)k * h->R * 2, all.data() + (size_t)row * h->R * 2, sizeof(double) * h->R * 2);
+    }
+    return ESP_OK;
+}
+
+int esp_set_sweep_kernel(esp_handle *h, int32_t kind)
+{
+    if (!h || kind < 0 || kind > 2) return ESP_EINVAL;
+    if (kind == 2 && !h->cluster_ok) {
+        h->err = "the cluster-resident sweep needs a periodic, translation-invariant lattice that fits a cluster";
+        return ESP_EINVAL;
+    }
+    int rc = fold(h);
+    if (rc) return rc;
+    h->kernel_choice = kind;
+    return ESP_OK;
+}
+
+int esp_get_sweep_kernel(const esp_handle *h, int32_t *kind, int32_t *cluster_size)
+{
+    if (!h || !kind) return ESP_EINVAL;
+    *kind = use_cluster(h) ? 2 : 1;
+    if (cluster_size) *cluster_size = h->cluster_ok ? h->csize : 0;
+    return ESP_OK;
+}
+
 int esp_num_freq(const esp_handle *h, int32_t *nf)
 {
     if (!h || !nf) return ESP_EINVAL;
@@ -774,6 +997,32 @@ int esp_advance(esp_handle *h, int64_t n)
     const esp_schedule &s = u.s;
     esp_sweep_opts o;
     o.mcarlo_mode = s.mcarlo_mode; o.tilt_angles_max = s.tilt_angles_max; o.seed = s.seed; o.phase = 1;
+    if (use_cluster(h)) {
+        if (!s.pt) {
+            // independent temperatures: many measurement units per launch
+            for (int64_t done = 0; done < n; done += kChunk) {
+                const int64_t k = std::min(kChunk, n - done);
+                if ((rc = cluster_run(h, k, (int)s.steps_measure, h->next_sweep, 1, u.meas_done, &o, 1, u.nlev, false)))
+                    return rc;
+                h->next_sweep += k * s.steps_measure;
+                u.meas_done += k;
+                if (h->na == 1) u.const_hits += k;
+            }
+            u.units_done += n;
+        } else {
+            for (int64_t k = 0; k < n; ++k) {
+                const int64_t l = ++u.units_done;
+                if ((rc = cluster_run(h, s.pt_steps_swap, (int)s.steps_measure, h->next_sweep, 1, u.meas_done, &o, 1,
+                                      u.nlev, true)))
+                    return rc;
+                h->next_sweep += s.pt_steps_swap * s.steps_measure;
+                u.meas_done += s.pt_steps_swap;
+                if (h->na == 1) u.const_hits += s.pt_steps_swap;
+                if ((rc = esp_pt_swap(h, (int)((l + 1) % 2) + 1, h->next_swap++, s.seed))) return rc;
+            }
+        }
+        return ESP_OK;
+    }
     for (int64_t k = 0; k < n; ++k) {
         if (!s.pt) {
             // mcarlo.F90:526-590: steps_measure sweeps, then one measurement

@@ -1,0 +1,366 @@
+// Cluster-resident sweeps for translation-invariant periodic lattices.
+//
+// One thread-block cluster holds one replica's whole lattice in distributed
+// shared memory for the length of a launch: each CTA of the cluster owns a
+// slab of z planes, stored class-major (parity class k = atom*8 + px*4 + py*2
+// + pz, then half-cell coordinates), so a colour pass (a set of classes) reads
+// its neighbours from its own or a peer CTA's shared memory and writes only its
+// own.  A launch runs `n_meas` units of `steps_measure` sweeps, each unit
+// followed by the measurement of mcarlo.F90:536-590 / pt.F90:789-849
+// (accumulators, binning, Pm_get histogram), all without touching global
+// memory; spins are read at the start and written back at the end.
+//
+// Updates, random numbers and the order of the local-field sums are those of
+// k_sweep_ell (same colouring, same Philox counter (site, replica, sweep), the
+// stencil lists in the merged-list order), so both kernels produce the same
+// trajectory.  Waits are cluster barriers only (hardware, no spinning).
+#include <cooperative_groups.h>
+
+#include "esp_cluster.h"
+#include "esp_device.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace esp {
+
+__global__ void __launch_bounds__(kClusterThreads, 1) k_sweep_cluster(const ClusterArgs a)
+{
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int csize = (int)cluster.num_blocks();
+    const int r = blockIdx.x / csize;  // replica of this cluster
+    const int Hx = a.Lx >> 1, Hy = a.Ly >> 1;
+    const int Hzl = a.pz >> 1;                      // half planes per CTA
+    const int per_class = Hx * Hy * Hzl;
+    const int n_local = per_class * a.nclass;
+    const int z0 = rank * a.pz;
+
+    // shared memory: stencil copy | P(M) histogram | reduction scratch | spins
+    // (stencil_words is a multiple of 4, so every part stays 16-byte aligned)
+    extern __shared__ __align__(16) unsigned char smem[];
+    ClusterStencil *st = reinterpret_cast<ClusterStencil *>(smem);
+    const ClusterNbr *nbt = reinterpret_cast<const ClusterNbr *>(st + 1);
+    unsigned int *hist = reinterpret_cast<unsigned int *>(smem) + a.stencil_words;
+    double *red = reinterpret_cast<double *>(hist + ((a.nf + 3) & ~3));
+    float *sx = reinterpret_cast<float *>(red + 136);
+    float *sy = sx + n_local;
+    float *sz = sy + n_local;
+
+    // ---- set-up: stencil and own spins -------------------------------------
+    {
+        const int *src = reinterpret_cast<const int *>(a.stencil);
+        int *dst = reinterpret_cast<int *>(st);
+        for (int i = threadIdx.x; i < a.stencil_words; i += blockDim.x) dst[i] = src[i];
+        for (int i = threadIdx.x; i < a.nf; i += blockDim.x) hist[i] = 0u;
+    }
+    for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
+        const int k = l / per_class, rem = l % per_class;
+        const int hx = rem % Hx, hy = (rem / Hx) % Hy, hzl = rem / (Hx * Hy);
+        const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
+        const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pz;
+        const int orig = ((z * a.Ly + y) * a.Lx + x) * a.na + at;
+        const size_t g = (size_t)__ldg(a.inv + orig) * a.R + r;
+        sx[l] = a.sx[g]; sy[l] = a.sy[g]; sz[l] = a.sz[g];
+    }
+    cluster.sync();
+
+    const int temp = a.temp_of[r];
+    const float beta = a.beta[temp];
+    double accE = 0.0, accX = 0.0, accY = 0.0, accZ = 0.0;  // since the last measurement
+    unsigned long long nrej = 0;
+    const float pm_scale = (float)((double)(a.nf - 1) / (a.m_max - a.m_min));
+    // replica totals, held by thread 0 of rank 0
+    double e_run = 0.0, m_run[3] = {0.0, 0.0, 0.0};
+    if (rank == 0 && threadIdx.x == 0) {
+        e_run = a.e_run[r];
+        m_run[0] = a.m_run[3 * r]; m_run[1] = a.m_run[3 * r + 1]; m_run[2] = a.m_run[3 * r + 2];
+    }
+
+    for (int m = 0; m < a.n_meas; ++m) {
+        for (int sm = 0; sm < a.steps_measure; ++sm) {
+            const unsigned long long sweep = a.sweep_base + (unsigned long long)m * a.steps_measure + sm;
+            const uint32_t sw_lo = (uint32_t)sweep, sw_hi = (uint32_t)(sweep >> 32);
+            // FP32 sums of one sweep, added to the FP64 ones after it
+            float fE = 0.f, fX = 0.f, fY = 0.f, fZ = 0.f;
+            for (int c = 0; c < st->ncolour; ++c) {
+                const int c0 = st->colour_start[c];
+                const int items = (st->colour_start[c + 1] - c0) * per_class;
+                for (int it = threadIdx.x; it < items; it += blockDim.x) {
+                    const int k = st->class_order[c0 + it / per_class];
+                    const int rem = it % per_class;
+                    const int l = k * per_class + rem;
+                    const int hx = rem % Hx, hy = (rem / Hx) % Hy, hzl = rem / (Hx * Hy);
+                    const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pzb = k & 1;
+                    const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pzb;
+                    const float ox = sx[l], oy = sy[l], oz = sz[l];
+                    float gx = 0.f, gy = 0.f, gz = 0.f;
+                    float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
+                    // neighbour k of site l: (owner rank << 24) | local index, from the
+                    // precomputed table shared by every replica's cluster; lists are
+                    // padded to multiples of 8 with zero-coupling self entries
+                    const int ne8 = (st->count[k] + 7) & ~7;
+                    const ClusterNbr *nb = nbt + k * st->maxst;
+                    const uint32_t *tab = a.nbidx + (size_t)rank * st->maxst * n_local + l;
+                    for (int e0 = 0; e0 < ne8; e0 += 8) {
+                        uint32_t id[8];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) id[j] = __ldg(tab + (size_t)(e0 + j) * n_local);
+                        float tx[8], ty[8], tz[8];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const int rn = (int)(id[j] >> 24), ln = (int)(id[j] & 0xffffffu);
+                            if (rn == rank) {
+                                tx[j] = sx[ln]; ty[j] = sy[ln]; tz[j] = sz[ln];
+                            } else {
+                                const float *px_ = cluster.map_shared_rank(sx, rn);
+                                tx[j] = px_[ln]; ty[j] = px_[ln + n_local]; tz[j] = px_[ln + 2 * n_local];
+                            }
+                        }
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const ClusterNbr &se = nb[e0 + j];
+                            const float J = se.J;
+                            gx = fmaf(-J, tx[j], gx); gy = fmaf(-J, ty[j], gy); gz = fmaf(-J, tz[j], gz);
+                            if (a.has_b) {
+                                const float Bv = se.B;
+                                const float bx = Bv * tx[j], by = Bv * ty[j], bz = Bv * tz[j];
+                                qxx = fmaf(bx, tx[j], qxx); qyy = fmaf(by, ty[j], qyy); qzz = fmaf(bz, tz[j], qzz);
+                                qxy = fmaf(bx, ty[j], qxy); qxz = fmaf(bx, tz[j], qxz); qyz = fmaf(by, tz[j], qyz);
+                            }
+                            if (a.has_d) {
+                                const float dx = se.Dx, dy = se.Dy, dz = se.Dz;
+                                gx += ty[j] * dz - tz[j] * dy;
+                                gy += tz[j] * dx - tx[j] * dz;
+                                gz += tx[j] * dy - ty[j] * dx;
+                            }
+                        }
+                    }
+                    if (a.has_si) {
+                        const float4 s = st->si[at];
+                        const float dx = s.w * s.x, dy = s.w * s.y, dz = s.w * s.z;
+                        qxx = fmaf(dx, s.x, qxx); qyy = fmaf(dy, s.y, qyy); qzz = fmaf(dz, s.z, qzz);
+                        qxy = fmaf(dx, s.y, qxy); qxz = fmaf(dx, s.z, qxz); qyz = fmaf(dy, s.z, qyz);
+                    }
+                    if (a.has_f) {
+                        const float4 f = st->fld[at];
+                        gx += f.x; gy += f.y; gz += f.z;
+                    }
+                    const int orig = ((z * a.Ly + y) * a.Lx + x) * a.na + at;
+                    const Philox4 xr = philox4x32_10((uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
+                    float nx, ny, nz;
+                    trial_spin(a.mode, a.tilt, st->mag[at], ox, oy, oz, xr.x, xr.y, nx, ny, nz);
+                    const float dx = nx - ox, dy = ny - oy, dz = nz - oz;
+                    float de = gx * dx + gy * dy + gz * dz;
+                    if (a.has_b || a.has_si) {
+                        const float px2 = nx + ox, py2 = ny + oy, pz2 = nz + oz;
+                        de += dx * (qxx * px2 + qxy * py2 + qxz * pz2)
+                            + dy * (qxy * px2 + qyy * py2 + qyz * pz2)
+                            + dz * (qxz * px2 + qyz * py2 + qzz * pz2);
+                    }
+                    bool acc = true;
+                    if (de > 0.0f) acc = expf(-beta * de) >= u24f(xr.z);
+                    if (acc) {
+                        sx[l] = nx; sy[l] = ny; sz[l] = nz;
+                        fE += de;
+                        fX += dx; fY += dy; fZ += dz;
+                    } else {
+                        ++nrej;
+                    }
+                }
+                cluster.sync();
+            }
+            accE += (double)fE; accX += (double)fX; accY += (double)fY; accZ += (double)fZ;
+        }
+        if (!a.measure) continue;
+        // ---- measurement: cluster-wide sums of dE and dM -------------------
+        {
+            double v[4] = {accE, accX, accY, accZ};
+            accE = accX = accY = accZ = 0.0;
+            for (int c = 0; c < 4; ++c)
+                for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+            const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            if (lane == 0)
+                for (int c = 0; c < 4; ++c) red[4 * warp + c] = v[c];
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double t4[4] = {0, 0, 0, 0};
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+                    for (int c = 0; c < 4; ++c) t4[c] += red[4 * w + c];
+                for (int c = 0; c < 4; ++c) red[128 + c] = t4[c];  // this CTA's total
+            }
+            // P(M) of this CTA's cells
+            if (a.na > 1) {
+                const int ncells_local = Hx * Hy * Hzl * 8;  // cells of the slab
+                const int cl_end = (ncells_local + 31) & ~31;   // whole warps take part in the vote
+                for (int cl = threadIdx.x; cl < cl_end; cl += blockDim.x) {
+                    int bin = -1;
+                    if (cl < ncells_local) {
+                        const int x = cl % a.Lx, y = (cl / a.Lx) % a.Ly, zl = cl / (a.Lx * a.Ly);
+                        const int z = z0 + zl;
+                        float mx = 0.f, my = 0.f, mz = 0.f;
+                        for (int at = 0; at < a.na; ++at) {
+                            const int k = (at << 3) | ((x & 1) << 2) | ((y & 1) << 1) | (z & 1);
+                            const int l = k * per_class + (((zl >> 1) * Hy + (y >> 1)) * Hx + (x >> 1));
+                            mx += sx[l]; my += sy[l]; mz += sz[l];
+                        }
+                        bin = pm_bin(mx, my, mz, (float)a.m_min, pm_scale, a.nf);
+                    }
+                    // lanes with the same bin add once (low temperatures put
+                    // almost every cell in one bin)
+                    const unsigned int peers = __match_any_sync(0xffffffffu, bin);
+                    if (bin > 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+                        atomicAdd(hist + (bin - 1), (unsigned)__popc(peers));
+                }
+            }
+            cluster.sync();
+            if (rank == 0 && threadIdx.x == 0) {
+                double d4[4] = {0, 0, 0, 0};
+                for (int q = 0; q < csize; ++q) {
+                    const double *pr = cluster.map_shared_rank(red, q);
+                    for (int c = 0; c < 4; ++c) d4[c] += pr[128 + c];
+                }
+                e_run += d4[0];
+                m_run[0] += d4[1]; m_run[1] += d4[2]; m_run[2] += d4[3];
+                // accumulators of mcarlo.F90:536-590 for this temperature slot
+                const double e = e_run;
+                const double mx = m_run[0] / (double)a.N, my = m_run[1] / (double)a.N, mz = m_run[2] / (double)a.N;
+                const double m2 = mx * mx + my * my + mz * mz;
+                const double ee = e * e, am = sqrt(m2);
+                double *d = a.data + 6 * temp;
+                d[0] += e; d[1] += ee; d[2] += ee * ee;
+                d[3] += am; d[4] += m2; d[5] += m2 * m2;
+                const long long step = a.meas_base + m + 1;
+                if (a.series) {
+                    double *o = a.series + (((step - 1) % a.series_cap) * a.R + temp) * 2;
+                    o[0] = e; o[1] = am;
+                }
+                for (int lv = 0; lv < a.nlev; ++lv) {
+                    double *ls = a.lsum + ((size_t)temp * a.nlev + lv) * 2;
+                    double *bn = a.binning + ((size_t)temp * a.nlev + lv) * 2;
+                    ls[0] += e / (double)a.N;
+                    ls[1] += am;
+                    const long long blk = 1LL << a.levels[lv];
+                    if (step % blk == 0) {
+                        const double div = a.pt_quirk ? (double)(1LL << (lv + 1)) : (double)blk;
+                        for (int c = 0; c < 2; ++c) {
+                            const double v2 = ls[c] / div;
+                            bn[c] += v2 * v2;
+                            ls[c] = 0.0;
+                        }
+                    }
+                }
+            }
+            cluster.sync();
+        }
+    }
+
+    // ---- end of launch: totals, rejected counts, histogram, spins ----------
+    {
+        double v[4] = {accE, accX, accY, accZ};
+        unsigned long long nr = nrej;
+        for (int c = 0; c < 4; ++c)
+            for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+        for (int o = 16; o > 0; o >>= 1) nr += __shfl_down_sync(0xffffffffu, nr, o);
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (lane == 0) {
+            for (int c = 0; c < 4; ++c) red[4 * warp + c] = v[c];
+            reinterpret_cast<unsigned long long *>(red + 96)[warp] = nr;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t4[4] = {0, 0, 0, 0};
+            unsigned long long tn = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                for (int c = 0; c < 4; ++c) t4[c] += red[4 * w + c];
+                tn += reinterpret_cast<unsigned long long *>(red + 96)[w];
+            }
+            for (int c = 0; c < 4; ++c) red[128 + c] = t4[c];
+            reinterpret_cast<unsigned long long *>(red)[132] = tn;
+        }
+        if (a.na > 1)
+            for (int i = threadIdx.x; i < a.nf; i += blockDim.x)
+                if (hist[i]) atomicAdd(a.pm_counts + (size_t)temp * a.nf + i, (unsigned long long)hist[i]);
+        cluster.sync();
+        if (rank == 0 && threadIdx.x == 0) {
+            double d4[4] = {0, 0, 0, 0};
+            unsigned long long tn = 0;
+            for (int q = 0; q < csize; ++q) {
+                const double *pr = cluster.map_shared_rank(red, q);
+                for (int c = 0; c < 4; ++c) d4[c] += pr[128 + c];
+                tn += reinterpret_cast<const unsigned long long *>(pr)[132];
+            }
+            a.e_run[r] = e_run + d4[0];
+            a.m_run[3 * r] = m_run[0] + d4[1];
+            a.m_run[3 * r + 1] = m_run[1] + d4[2];
+            a.m_run[3 * r + 2] = m_run[2] + d4[3];
+            a.rej[2 * temp + a.phase] += tn;
+        }
+    }
+    for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
+        const int k = l / per_class, rem = l % per_class;
+        const int hx = rem % Hx, hy = (rem / Hx) % Hy, hzl = rem / (Hx * Hy);
+        const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
+        const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pz;
+        const int orig = ((z * a.Ly + y) * a.Lx + x) * a.na + at;
+        const size_t g = (size_t)__ldg(a.inv + orig) * a.R + r;
+        a.sx[g] = sx[l]; a.sy[g] = sy[l]; a.sz[g] = sz[l];
+    }
+    // peers may still read this CTA's shared memory until every CTA is done
+    cluster.sync();
+}
+
+size_t cluster_smem_bytes(int n_local, int nf, size_t stencil_bytes)
+{
+    return ((stencil_bytes + 15) & ~(size_t)15) + (size_t)((nf + 3) & ~3) * sizeof(unsigned int) +
+           (size_t)136 * sizeof(double) + (size_t)3 * n_local * sizeof(float);
+}
+
+cudaError_t cluster_configure(size_t smem, int csize)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_sweep_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (csize > 8) e = cudaFuncSetAttribute(k_sweep_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+}
+
+int cluster_max_active(int csize, size_t smem, int R)
+{
+    if (cudaFuncSetAttribute(k_sweep_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(csize * R, 1, 1);
+    cfg.blockDim = dim3(kClusterThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = csize;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_sweep_cluster, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+cudaError_t launch_cluster(const ClusterArgs &a, int csize, size_t smem, cudaStream_t st)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(csize * a.R, 1, 1);
+    cfg.blockDim = dim3(kClusterThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = csize;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_sweep_cluster, a);
+}
+
+}  // namespace esp

@@ -1,0 +1,77 @@
+// Cluster-resident sweep kernel (esp_cluster.cu): arguments and launchers.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace esp {
+
+constexpr int kClusterThreads = 512;
+constexpr int kMaxClusterAtoms = 8;
+constexpr int kMaxStencil = 64;
+constexpr int kMaxClasses = 8 * kMaxClusterAtoms;
+
+// Neighbour of a site of parity class k through stencil entry e: class kn
+// and half-cell offsets (dhx, dhy, dhz); the couplings are those of the
+// entry.  Stored per class, so no parity arithmetic is done per neighbour.
+struct ClusterNbr {
+    int kn, dhx, dhy, dhz;
+    float J, B, Dx, Dy, Dz, pad0, pad1, pad2;
+};
+
+// Everything the kernel needs about the lattice's couplings; the header is
+// followed in memory by nclass * maxst ClusterNbr entries (class-major).
+struct ClusterStencil {
+    int nclass, maxst, ncolour, pad;
+    int count[kMaxClasses];            // entries of each class
+    float4 si[kMaxClusterAtoms];       // (ax, ay, az, Delta)
+    float4 fld[kMaxClusterAtoms];      // (f ax, f ay, f az, 0)
+    float mag[kMaxClusterAtoms];
+    int colour_start[kMaxClasses + 1]; // classes of colour c: class_order[colour_start[c] .. colour_start[c+1])
+    int class_order[kMaxClasses];
+};
+
+inline size_t cluster_stencil_bytes(int nclass, int maxst)
+{
+    return sizeof(ClusterStencil) + (size_t)nclass * maxst * sizeof(ClusterNbr);
+}
+
+struct ClusterArgs {
+    const ClusterStencil *stencil;  // device copy (header + entries)
+    int stencil_words;              // size of that copy in 4-byte words
+    const uint32_t *nbidx;          // [rank][entry][local site]: (owner rank << 24) | local index
+    int Lx, Ly, Lz, na, N, R, nclass, pz;  // pz: z planes per CTA (even)
+    int has_b, has_d, has_si, has_f;
+    // state
+    float *sx, *sy, *sz;            // element (p, r) at p*R + r
+    const int32_t *inv;             // reference site -> p
+    const int32_t *temp_of;
+    const float *beta;
+    double *e_run, *m_run;
+    unsigned long long *rej;        // [R slots][2]
+    int phase;
+    // measurement
+    int measure, n_meas, steps_measure;
+    long long meas_base;
+    double *data, *lsum, *binning;
+    const int32_t *levels;
+    int nlev, pt_quirk;
+    unsigned long long *pm_counts;
+    double *series;                 // [cap][R slots][2] or null
+    long long series_cap;
+    int nf;
+    double m_min, m_max;
+    // random stream
+    unsigned long long sweep_base;
+    uint32_t key0, key1;
+    int mode;
+    float tilt;
+};
+
+size_t cluster_smem_bytes(int n_local, int nf, size_t stencil_bytes);
+cudaError_t cluster_configure(size_t smem, int csize);
+// Clusters of csize CTAs with `smem` bytes each that fit on the GPU at once.
+int cluster_max_active(int csize, size_t smem, int R);
+cudaError_t launch_cluster(const ClusterArgs &a, int csize, size_t smem, cudaStream_t st);
+
+}  // namespace esp

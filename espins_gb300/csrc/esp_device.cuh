@@ -79,6 +79,18 @@ __device__ __forceinline__ void trial_spin(int mode, float tilt, float mag, floa
     }
 }
 
+// Bin of a unit cell's |sum of spins| on the P(M) grid of Pm_get
+// (get_quant.F90:425-493): max(nint((|m| - m_min) / (m_max - m_min) * (nf-1)) + 1, 1),
+// clamped to nf; FP32 (an edge flip needs |m| within ~1e-7 of a bin edge).
+// scale = (nf - 1) / (m_max - m_min).  Returns the 1-based bin.
+__device__ __forceinline__ int pm_bin(float mx, float my, float mz, float m_min, float scale, int nf)
+{
+    const float m = sqrtf(mx * mx + my * my + mz * mz);
+    int bin = (int)floorf((m - m_min) * scale + 0.5f) + 1;  // nint of a non-negative value
+    bin = bin < 1 ? 1 : bin;
+    return bin > nf ? nf : bin;
+}
+
 // Arguments of the colour-class sweep over the merged ELL tables.
 struct SweepArgs {
     // tables, permuted site order (colour-major); entry k of site p at k*N+p

@@ -30,7 +30,7 @@ namespace esp {
 // the same replica; k_fold later sums the slots of each replica in block order
 // (deterministic) into the running totals.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void add_block_slots(double e, double mx, double my, double mz, unsigned int nrej,
+__device__ __forceinline__ void add_block_slots(float e, float mx, float my, float mz, unsigned int nrej,
                                                 int R, int slots, double *part, unsigned long long *part_rej)
 {
     __shared__ double s_part[256][4];
@@ -40,11 +40,11 @@ __device__ __forceinline__ void add_block_slots(double e, double mx, double my, 
     const size_t slot = (size_t)blockIdx.x * slots + t;
     if (R >= nt) {
         double *o = part + 4 * slot;
-        o[0] += e; o[1] += mx; o[2] += my; o[3] += mz;
+        o[0] += (double)e; o[1] += (double)mx; o[2] += (double)my; o[3] += (double)mz;
         part_rej[slot] += (unsigned long long)nrej;
         return;
     }
-    s_part[t][0] = e; s_part[t][1] = mx; s_part[t][2] = my; s_part[t][3] = mz;
+    s_part[t][0] = (double)e; s_part[t][1] = (double)mx; s_part[t][2] = (double)my; s_part[t][3] = (double)mz;
     s_rej[t] = nrej;
     __syncthreads();
     if (t < R) {
@@ -113,7 +113,8 @@ __global__ void __launch_bounds__(256) k_sweep_ell(const SweepArgs a)
     const bool live = tid < S;
     const int r = (int)(tid % R);
     const int temp = a.temp_of[r];
-    double accE = 0.0, accX = 0.0, accY = 0.0, accZ = 0.0;
+    // FP32 per thread (a few updates each); FP64 from the block sums on
+    float accE = 0.f, accX = 0.f, accY = 0.f, accZ = 0.f;
     unsigned int nrej = 0;
     if (live) {
         const float beta = a.beta[temp];
@@ -189,8 +190,8 @@ __global__ void __launch_bounds__(256) k_sweep_ell(const SweepArgs a)
             if (de > 0.0f) acc = expf(-beta * de) >= u24f(x.z);
             if (acc) {
                 a.sx[idx] = nx; a.sy[idx] = ny; a.sz[idx] = nz;
-                accE += (double)de;
-                accX += (double)dx; accY += (double)dy; accZ += (double)dz;
+                accE += de;
+                accX += dx; accY += dy; accZ += dz;
             } else {
                 ++nrej;
             }
@@ -361,6 +362,10 @@ __global__ void k_measure(MeasureArgs a)
     d[0] += e; d[1] += ee; d[2] += ee * ee;
     const double am = sqrt(m2);
     d[3] += am; d[4] += m2; d[5] += m2 * m2;
+    if (a.series) {
+        double *o = a.series + (((a.step - 1) % a.series_cap) * a.R + t) * 2;
+        o[0] = e; o[1] = am;
+    }
     if (a.nlev > 0) {
         double *ls = a.lsum + (size_t)t * a.nlev * 2;
         double *bn = a.binning + (size_t)t * a.nlev * 2;
@@ -399,17 +404,14 @@ __global__ void __launch_bounds__(256) k_pm_hist(PmArgs a)
     for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
          it += (long long)gridDim.x * blockDim.x) {
         const int cell = (int)(it / nrt), rr = (int)(it % nrt), r = r0 + rr;
-        double mx = 0, my = 0, mz = 0;
+        float mx = 0.f, my = 0.f, mz = 0.f;
         for (int at = 0; at < a.num_atoms; ++at) {
             const int p = __ldg(a.inv + cell * a.num_atoms + at);
             const size_t idx = (size_t)p * R + r;
-            mx += (double)a.sx[idx]; my += (double)a.sy[idx]; mz += (double)a.sz[idx];
+            mx += a.sx[idx]; my += a.sy[idx]; mz += a.sz[idx];
         }
-        const double m = sqrt(mx * mx + my * my + mz * mz);
-        long long bin = llround(((m - a.m_min) / (a.m_max - a.m_min)) * (double)(nf - 1)) + 1;
-        if (bin < 1) bin = 1;
-        if (bin > nf) bin = nf;
-        atomicAdd(s_hist + rr * nf + (int)(bin - 1), 1u);
+        const int bin = pm_bin(mx, my, mz, (float)a.m_min, (float)((double)(nf - 1) / (a.m_max - a.m_min)), nf);
+        atomicAdd(s_hist + rr * nf + (bin - 1), 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nrt * nf; i += blockDim.x) {

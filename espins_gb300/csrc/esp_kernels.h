@@ -33,7 +33,9 @@ struct MeasureArgs {
     double *lsum, *binning;   // [R][nlev][2]
     const int32_t *levels;    // [nlev] (device)
     int32_t R, N, nlev, pt_quirk;
-    long long step;
+    long long step;           // 1-based measurement index
+    double *series;           // [cap][R][2]: (E, |m|) per measurement, or null
+    long long series_cap;
 };
 
 struct PmArgs {

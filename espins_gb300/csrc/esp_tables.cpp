@@ -161,6 +161,8 @@ int prepare_tables(const PrepInput &in, PrepOutput &out, std::string &err)
                         if (col[c] >= 0 && remap[col[c]] < 0) remap[col[c]] = used++;
                     for (int i = 0; i < N; ++i) colour[i] = remap[col[cls_of(i)]];
                     C = used;
+                    out.class_colour.assign(K, 0);
+                    for (int k = 0; k < K; ++k) out.class_colour[k] = remap[col[k]];
                 }
             }
         }
@@ -185,6 +187,72 @@ int prepare_tables(const PrepInput &in, PrepOutput &out, std::string &err)
         for (int64_t e = start[i]; e < start[i + 1]; ++e)
             if (colour[merged[e].j] == colour[i]) { err = "colouring check failed"; return 2; }
 
+    // ---- translation invariance (stencil form) -------------------------------
+    if (!out.class_colour.empty() && !in.open_boundary) {
+        const int L0 = in.L[0], L1 = in.L[1], L2 = in.L[2];
+        auto cell_xyz = [&](int i, int &x, int &y, int &z) {
+            const int cell = i / na;
+            x = cell % L0; y = (cell / L0) % L1; z = cell / (L0 * L1);
+        };
+        auto wrap = [](int v, int L) { v %= L; return v < 0 ? v + L : v; };
+        auto signed_off = [](int d, int L) { d %= L; if (d < 0) d += L; return d > L / 2 ? d - L : d; };
+        bool ok = true;
+        std::vector<std::vector<StencilEntry>> st(na);
+        for (int a = 0; a < na && ok; ++a) {
+            const int i0 = a;  // atom a of cell (0,0,0)
+            for (int64_t e = start[i0]; e < start[i0 + 1]; ++e) {
+                int x, y, z;
+                cell_xyz(merged[e].j, x, y, z);
+                StencilEntry se;
+                se.dx = signed_off(x, L0); se.dy = signed_off(y, L1); se.dz = signed_off(z, L2);
+                se.b = merged[e].j % na;
+                se.J = (float)merged[e].J; se.B = (float)merged[e].B;
+                se.Dx = (float)merged[e].D[0]; se.Dy = (float)merged[e].D[1]; se.Dz = (float)merged[e].D[2];
+                st[a].push_back(se);
+            }
+        }
+        // every site must carry exactly its atom's list, with equal couplings
+        // (in the same order, or reordered below to that order)
+        for (int i = 0; i < N && ok; ++i) {
+            const int a = i % na;
+            int x, y, z;
+            cell_xyz(i, x, y, z);
+            const int64_t n_i = start[i + 1] - start[i];
+            if (n_i != (int64_t)st[a].size()) { ok = false; break; }
+            auto same = [&](const Entry &m, const StencilEntry &se, int j) {
+                return m.j == j && (float)m.J == se.J && (float)m.B == se.B && (float)m.D[0] == se.Dx &&
+                       (float)m.D[1] == se.Dy && (float)m.D[2] == se.Dz;
+            };
+            auto target = [&](const StencilEntry &se) {
+                return ((wrap(z + se.dz, L2) * L1 + wrap(y + se.dy, L1)) * L0 + wrap(x + se.dx, L0)) * na + se.b;
+            };
+            // usual case: the list is already in the stencil's order
+            bool in_order = true;
+            for (int64_t k = 0; k < n_i && in_order; ++k)
+                in_order = same(merged[start[i] + k], st[a][k], target(st[a][k]));
+            if (in_order) continue;
+            std::vector<Entry> want;
+            want.reserve(n_i);
+            for (const auto &se : st[a]) {
+                const int j = target(se);
+                bool found = false;
+                for (int64_t e = start[i]; e < start[i + 1]; ++e) {
+                    if (same(merged[e], se, j)) {
+                        want.push_back(merged[e]);
+                        found = true;
+                        break;
+                    }
+                }
+                if (!found) { ok = false; break; }
+            }
+            if (ok) std::copy(want.begin(), want.end(), merged.begin() + start[i]);
+        }
+        if (ok) {
+            out.invariant = true;
+            out.stencil = std::move(st);
+        }
+    }
+
     // ---- colour-major permutation ------------------------------------------
     out.num_colours = C;
     out.colour = colour;
@@ -193,7 +261,26 @@ int prepare_tables(const PrepInput &in, PrepOutput &out, std::string &err)
     for (int c = 0; c < C; ++c) out.off[c + 1] += out.off[c];
     out.perm.assign(N, 0);
     out.inv.assign(N, 0);
-    {
+    if (!out.class_colour.empty()) {
+        // parity-class colouring: inside a colour, class by class (ascending
+        // class index), and inside a class in site order, which is half-cell
+        // order (hz, hy, hx); every class then owns a contiguous block
+        const int K = 8 * na;
+        std::vector<std::vector<int>> members(K);
+        for (int i = 0; i < N; ++i) members[cls_of(i)].push_back(i);
+        out.class_off.assign(K, 0);
+        int p = 0;
+        for (int c = 0; c < C; ++c)
+            for (int k = 0; k < K; ++k) {
+                if (out.class_colour[k] != c) continue;
+                out.class_off[k] = p;
+                for (int i : members[k]) {
+                    out.perm[p] = i;
+                    out.inv[i] = p;
+                    ++p;
+                }
+            }
+    } else {
         std::vector<int> fill(out.off.begin(), out.off.end() - 1);
         for (int i = 0; i < N; ++i) {
             const int p = fill[colour[i]]++;

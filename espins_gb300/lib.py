@@ -24,7 +24,7 @@ EXPORTED = [
     "esp_sweep_colour", "esp_pt_swap", "esp_energy", "esp_running_energy",
     "esp_running_magnetization", "esp_local_terms", "esp_get_spins", "esp_get_colouring",
     "esp_get_rejected", "esp_get_replica_of_slot", "esp_num_freq", "esp_launch_count",
-    "esp_energy_noalloc",
+    "esp_energy_noalloc", "esp_set_sweep_kernel", "esp_get_sweep_kernel", "esp_set_series", "esp_get_series",
 ]
 
 
@@ -115,6 +115,10 @@ def load(build_if_missing: bool = True):
     lib.esp_num_freq.argtypes = [vp, P(C.c_int32)]
     lib.esp_launch_count.argtypes = [vp, P(C.c_int64)]
     lib.esp_energy_noalloc.argtypes = [P(EnergyArgs), vp, vp]
+    lib.esp_set_sweep_kernel.argtypes = [vp, C.c_int32]
+    lib.esp_set_series.argtypes = [vp, C.c_int64]
+    lib.esp_get_series.argtypes = [vp, vp, P(C.c_int64)]
+    lib.esp_get_sweep_kernel.argtypes = [vp, P(C.c_int32), P(C.c_int32)]
     for f in EXPORTED:
         getattr(lib, f).restype = C.c_int
     _lib = lib
@@ -346,6 +350,29 @@ class Engine:
         r = np.zeros(self.R, dtype=np.int32)
         self._check(self.lib.esp_get_replica_of_slot(self.h, _p(r)))
         return r
+
+    def set_series(self, capacity: int) -> None:
+        self._check(self.lib.esp_set_series(self.h, int(capacity)))
+
+    def series(self) -> np.ndarray:
+        """(measurements, R, 2): E and |m| per measurement and temperature slot."""
+        n = C.c_int64()
+        self._check(self.lib.esp_get_series(self.h, None, C.byref(n)))
+        out = np.zeros((n.value, self.R, 2))
+        if n.value:
+            self._check(self.lib.esp_get_series(self.h, _p(out), C.byref(n)))
+        return out
+
+    def set_sweep_kernel(self, kind: str) -> None:
+        """'auto', 'ell' (any lattice) or 'cluster' (translation-invariant, cluster-resident)."""
+        k = {"auto": 0, "ell": 1, "cluster": 2}[kind]
+        self._check(self.lib.esp_set_sweep_kernel(self.h, k))
+
+    def sweep_kernel(self):
+        """('ell' | 'cluster', cluster size)."""
+        k, cs = C.c_int32(), C.c_int32()
+        self._check(self.lib.esp_get_sweep_kernel(self.h, C.byref(k), C.byref(cs)))
+        return ("cluster" if k.value == 2 else "ell"), cs.value
 
     def num_freq(self) -> int:
         k = C.c_int32()

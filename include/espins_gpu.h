@@ -189,6 +189,21 @@ int esp_get_colouring(esp_handle *h, int32_t *colour_out, int32_t *num_colours);
 int esp_get_rejected(esp_handle *h, int64_t *rejected_out);
 /* Temperature slot -> replica (0-based) after PT swaps. */
 int esp_get_replica_of_slot(esp_handle *h, int32_t *replica_out);
+/* Sweep kernel: 0 automatic, 1 the ELL kernel (any lattice), 2 the
+ * cluster-resident kernel (periodic, translation-invariant lattices whose
+ * replica fits the shared memory of one thread-block cluster).  Both follow the
+ * same colouring, random stream and summation order. */
+int esp_set_sweep_kernel(esp_handle *h, int32_t kind);
+/* The kernel in use (1 or 2) and the cluster size of the cluster path. */
+int esp_get_sweep_kernel(const esp_handle *h, int32_t *kind, int32_t *cluster_size);
+/* Keep the per-measurement series (E, |m|) of every temperature slot for
+ * the last `capacity` measurements of a run (0 switches it off): the data of
+ * the reference's energy series files (energy_write, get_quant.F90:1130-1223)
+ * and of autocorrelation analyses. */
+int esp_set_series(esp_handle *h, int64_t capacity);
+/* *count = kept measurements; out (if not NULL) receives them oldest first,
+ * out[(k*R + t)*2 + 0] = E, [.. + 1] = |m| of measurement k at slot t. */
+int esp_get_series(esp_handle *h, double *out, int64_t *count);
 /* num_freq of the P(M) grid (mcarlo.F90:432-442). */
 int esp_num_freq(const esp_handle *h, int32_t *nf);
 /* Number of kernels this handle has launched so far. */

@@ -157,3 +157,27 @@ def test_colouring_is_proper_and_minimal_on_lattices():
         assert C == expect
         for k in range(h.jij.maxnb):
             assert np.all(col[h.jij.nb[k]] != col)
+
+
+def test_pt_swap_kernel_takes_the_host_protocol_decisions():
+    """k_pt_swap == espins_gb300.distributed.swap_decisions on the same energies."""
+    from espins_gb300 import distributed as D
+    inp = sc_mcin(4, [(1e-3, NN)], list(np.geomspace(5.0, 40.0, 10)))
+    h = build_hamiltonian(inp)
+    R = len(inp.tems)
+    rng = np.random.default_rng(3)
+    seed = 0x5EED5EED12345
+    with _engine(h, R, inp.tems) as e:
+        for step in range(6):
+            v = rng.normal(size=(R, h.n, 3))
+            e.set_spins(v / np.linalg.norm(v, axis=2, keepdims=True))   # resets labels? no: keeps them
+            e_slot = e.running_energy()
+            before = e.replica_of_slot()
+            start = step % 2 + 1
+            want = D.swap_decisions(start, 1.0 / np.asarray(inp.tems), e_slot, step, seed)
+            e.pt_swap(start, step, seed)
+            after = e.replica_of_slot()
+            expect = before.copy()
+            for s in want:
+                expect[s], expect[s + 1] = before[s + 1], before[s]
+            assert np.array_equal(after, expect), (step, want)
