@@ -562,17 +562,13 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
         ClusterNbr *nbs = reinterpret_cast<ClusterNbr *>(blob.data() + sizeof(ClusterStencil));
         bool fits = true;
         hs.nclass = nclass; hs.maxst = maxst; hs.ncolour = prep.num_colours;
-        auto fdiv2 = [](int v) { return v >= 0 ? v / 2 : -((-v + 1) / 2); };  // floor(v / 2)
         for (int k = 0; k < nclass; ++k) {
-            const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
+            const int at = k >> 3;
             const auto &lst = prep.stencil[at];
             hs.count[k] = (int)lst.size();
             for (size_t e = 0; e < lst.size(); ++e) {
                 const StencilEntry &x = lst[e];
                 ClusterNbr &nb = nbs[(size_t)k * maxst + e];
-                const int qx = px + x.dx, qy = py + x.dy, qz = pz + x.dz;
-                nb.kn = (x.b << 3) | ((qx & 1) << 2) | ((qy & 1) << 1) | (qz & 1);
-                nb.dhx = fdiv2(qx); nb.dhy = fdiv2(qy); nb.dhz = fdiv2(qz);
                 nb.J = x.J; nb.B = x.B; nb.Dx = x.Dx; nb.Dy = x.Dy; nb.Dz = x.Dz;
             }
         }

@@ -223,7 +223,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sweep_cluster(const Clus
                 m_run[0] += d4[1]; m_run[1] += d4[2]; m_run[2] += d4[3];
                 // accumulators of mcarlo.F90:536-590 for this temperature slot
                 const double e = e_run;
-                const double mx = m_run[0] / (double)a.N, my = m_run[1] / (double)a.N, mz = m_run[2] / (double)a.N;
+                const double rn_inv = 1.0 / (double)a.N;
+                const double mx = m_run[0] * rn_inv, my = m_run[1] * rn_inv, mz = m_run[2] * rn_inv;
                 const double m2 = mx * mx + my * my + mz * mz;
                 const double ee = e * e, am = sqrt(m2);
                 double *d = a.data + 6 * temp;
@@ -237,13 +238,14 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sweep_cluster(const Clus
                 for (int lv = 0; lv < a.nlev; ++lv) {
                     double *ls = a.lsum + ((size_t)temp * a.nlev + lv) * 2;
                     double *bn = a.binning + ((size_t)temp * a.nlev + lv) * 2;
-                    ls[0] += e / (double)a.N;
+                    ls[0] += e * rn_inv;
                     ls[1] += am;
                     const long long blk = 1LL << a.levels[lv];
-                    if (step % blk == 0) {
-                        const double div = a.pt_quirk ? (double)(1LL << (lv + 1)) : (double)blk;
+                    if ((step & (blk - 1)) == 0) {
+                        // 1/2^n is exact, so the product equals the division
+                        const double inv_div = 1.0 / (a.pt_quirk ? (double)(1LL << (lv + 1)) : (double)blk);
                         for (int c = 0; c < 2; ++c) {
-                            const double v2 = ls[c] / div;
+                            const double v2 = ls[c] * inv_div;
                             bn[c] += v2 * v2;
                             ls[c] = 0.0;
                         }

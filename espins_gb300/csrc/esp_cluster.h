@@ -11,11 +11,9 @@ constexpr int kMaxClusterAtoms = 8;
 constexpr int kMaxStencil = 64;
 constexpr int kMaxClasses = 8 * kMaxClusterAtoms;
 
-// Neighbour of a site of parity class k through stencil entry e: class kn
-// and half-cell offsets (dhx, dhy, dhz); the couplings are those of the
-// entry.  Stored per class, so no parity arithmetic is done per neighbour.
+// Couplings of stencil entry e of parity class k (the neighbour's position
+// comes from the index table); padded to 32 bytes.
 struct ClusterNbr {
-    int kn, dhx, dhy, dhz;
     float J, B, Dx, Dy, Dz, pad0, pad1, pad2;
 };
 
