@@ -27,6 +27,13 @@ Metric: site updates/s = steps * 10 * N * R / time.
 
 ``--impl reference`` times that CPU implementation alone (the reference itself
 is Fortran + MPI and cannot be built in this image).
+
+``--proposal compare`` (with ``--workload sc48_frustrated_pt``) measures the
+learned proposal instead: it collects 10^7 (environment, spin) pairs from the
+plain PT sampler, trains the network on the GPU, then runs the plain and the
+learned sampler from the same state and reports independent samples/s =
+sum over temperature slots of sweeps/s / (2 tau_int), tau_int the larger of
+E's and |m|'s (Sokal windowing), for both.
 """
 from __future__ import annotations
 
@@ -56,6 +63,10 @@ def _args():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--seed", type=int, default=2)
+    p.add_argument("--proposal", choices=["plain", "compare"], default="plain")
+    p.add_argument("--train-pairs", type=int, default=10_000_000)
+    p.add_argument("--train-steps", type=int, default=3000)
+    p.add_argument("--measure-sweeps", type=int, default=20000)
     return p.parse_args()
 
 
@@ -211,9 +222,106 @@ def _config(inp, ham, name):
             "parallelism": "all replicas in one device; independent jobs per GPU when n_gpus > 1"}
 
 
+def learned_compare(a, rank, local):
+    """Learned vs plain PT sampler: training, site updates/s, tau_int, independent samples/s."""
+    import torch
+
+    from espins_gb300 import analysis
+    from espins_gb300.lib import Engine
+    from espins_gb300.tables import build_hamiltonian
+    from espins_gb300.workloads import workload
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    inp = workload(a.workload, L=a.L, replicas=a.replicas)
+    ham = build_hamiltonian(inp, check=False)
+    R, N = inp.tems_num, ham.n
+    pss = inp.pt_steps_swap if inp.pt else 1
+    seed = 4 + 1000 * rank
+    stream = torch.cuda.current_stream(dev)
+    eng = Engine(N, ham.num_atoms, ham.supercell, R, inp.boundary_open)
+    eng.upload(ham)
+    eng.set_temperatures(inp.tems)
+    eng.set_stream(stream.cuda_stream)
+    _, ncol = eng.colouring()
+    # plain PT warm-up, then one colour class of every replica per swap interval
+    eng.set_spins(_uniform_spins(R, N, ham.mag, seed))
+    warm = 2000
+    n_coll = -(-a.train_pairs // (N * R // ncol))
+    sched = eng.schedule(0, (warm // pss + n_coll + 1) * pss, 1, pt=inp.pt, pt_steps_swap=pss, seed=seed)
+    eng.begin(sched)
+    eng.advance(warm // pss)
+    eng.lp_reserve(a.train_pairs)
+    t0 = time.perf_counter()
+    rows = 0
+    for k in range(n_coll):
+        eng.advance(1)
+        rows = eng.lp_collect(k % ncol)
+    torch.cuda.synchronize(dev)
+    t_collect = time.perf_counter() - t0
+    start = eng.get_spins()
+    eng.lp_init(seed=seed)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    loss = eng.lp_train(a.train_steps, batch=4096, lr=1e-3, seed=seed)
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    t_train = ev0.elapsed_time(ev1) * 1e-3
+    out = {}
+    for kind in ("plain", "learned"):
+        eng.set_proposal(kind)
+        eng.set_spins(start)
+        eng.set_series(a.measure_sweeps)
+        sched = eng.schedule(0, a.measure_sweeps, 1, pt=inp.pt, pt_steps_swap=pss, seed=seed + 17)
+        eng.begin(sched)
+        eng.advance(max(1, 500 // pss))          # settle after the switch (not in the series window)
+        units = -(-a.measure_sweeps // pss) - max(1, 500 // pss)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        eng.advance(units)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        secs = e0.elapsed_time(e1) * 1e-3
+        res = eng.collect()
+        ser = eng.series()[-units * pss:]
+        tau_e = np.array([analysis.tau_int(ser[:, t, 0]) for t in range(R)])
+        tau_m = np.array([analysis.tau_int(ser[:, t, 1]) for t in range(R)])
+        tau = np.maximum(tau_e, tau_m)
+        sweeps_per_s = units * pss / secs
+        ups = sweeps_per_s * N * R
+        trials = -(-a.measure_sweeps // pss) * pss * N     # per temperature slot, whole run
+        acc = 1.0 - res["rejected"][:, 1] / trials
+        out[kind] = {
+            "site_updates_per_s": ups,
+            "independent_samples_per_s": float(np.sum(sweeps_per_s / (2.0 * tau))),
+            "tau_int_E": tau_e.tolist(), "tau_int_absM": tau_m.tolist(),
+            "tau_int_binning_E": [analysis.binning_tau(ser[:, t, 0]) for t in range(R)],
+            "acceptance": acc.tolist(), "kernel": eng.sweep_kernel()[0],
+            "mean_E_per_site": (res["data"][:, 0] / N).tolist(), "mean_absM": res["data"][:, 3].tolist(),
+        }
+    eng.close()
+    if rank == 0:
+        line = {
+            "metric": "independent samples/s", "value": out["learned"]["independent_samples_per_s"],
+            "unit": "samples/s", "n_gpus": 1, "steps": a.measure_sweeps, "warmup": 500,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32",
+            "data": "synthetic", "config": _config(inp, ham, a.workload) | {"proposal": "learned vs plain"},
+            "plain": out["plain"], "learned": out["learned"],
+            "ratio_independent_samples": out["learned"]["independent_samples_per_s"]
+            / out["plain"]["independent_samples_per_s"],
+            "training": {"pairs": int(rows), "collect_s": t_collect, "steps": a.train_steps, "batch": 4096,
+                         "seconds": t_train, "loss_first": float(np.mean(loss[:20])),
+                         "loss_last": float(np.mean(loss[-50:]))},
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     a = _args()
     ws, rank, local = _dist()
+    if a.proposal == "compare":
+        learned_compare(a, rank, local)
+        return
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")

@@ -13,6 +13,7 @@
 #include "../../include/espins_gpu.h"
 #include "esp_cluster.h"
 #include "esp_kernels.h"
+#include "esp_learned.h"
 #include "esp_tables.h"
 #include "esp_errors.h"
 
@@ -58,6 +59,7 @@ struct esp_handle {
     double *d_part = nullptr;
     unsigned long long *d_part_rej = nullptr;
     int sweep_grid = 0, slots = 0;
+    int part_blocks = 0;            // 256-thread blocks with partial slots (>= sweep_grid)
     int pending_phase = 0;
     long long pending_sweeps = 0;
     // cluster-resident path (translation-invariant lattices)
@@ -80,6 +82,24 @@ struct esp_handle {
     std::vector<double> tems;
     int nf = 2;
     double m_min = 0, m_max = 0;
+    // learned proposal: network (fp32 master + Adam moments + bf16 copies),
+    // training set, mini-batch buffers
+    int proposal = 0;               // 0 plain Metropolis, 1 learned
+    bool lp_weights = false;
+    int lp_grid = 0;
+    float *d_lp_p = nullptr, *d_lp_g = nullptr, *d_lp_m = nullptr, *d_lp_v = nullptr;
+    __nv_bfloat16 *d_lp_w1 = nullptr, *d_lp_w2 = nullptr, *d_lp_w3 = nullptr;
+    float4 *d_lp_axis = nullptr;
+    long long lp_adam_t = 0;
+    __nv_bfloat16 *d_lp_x = nullptr;
+    float *d_lp_t = nullptr;
+    long long lp_cap = 0, lp_n = 0;
+    int lp_bcap = 0;
+    __nv_bfloat16 *d_lp_xb = nullptr, *d_lp_h1 = nullptr, *d_lp_h2 = nullptr, *d_lp_do = nullptr,
+                  *d_lp_dz2 = nullptr, *d_lp_dz1 = nullptr;
+    float *d_lp_tb = nullptr, *d_lp_o = nullptr;
+    double *d_lp_loss = nullptr;
+    long long lp_loss_cap = 0;
 };
 
 namespace {
@@ -116,8 +136,15 @@ void free_tables(esp_handle *h)
     dfree(h->d_nnb); dfree(h->d_nbr); dfree(h->d_perm); dfree(h->d_inv);
     dfree(h->d_J); dfree(h->d_B); dfree(h->d_Dx); dfree(h->d_Dy); dfree(h->d_Dz); dfree(h->d_mag);
     dfree(h->d_si); dfree(h->d_fld); dfree(h->d_scratch); dfree(h->d_part); dfree(h->d_part_rej);
-    dfree(h->d_stencil_blob); dfree(h->d_nbidx);
+    dfree(h->d_stencil_blob); dfree(h->d_nbidx); dfree(h->d_lp_axis);
     h->cluster_ok = false;
+}
+
+void free_lp_batch(esp_handle *h)
+{
+    dfree(h->d_lp_xb); dfree(h->d_lp_h1); dfree(h->d_lp_h2); dfree(h->d_lp_do); dfree(h->d_lp_dz2);
+    dfree(h->d_lp_dz1); dfree(h->d_lp_tb); dfree(h->d_lp_o);
+    h->lp_bcap = 0;
 }
 
 void free_all(esp_handle *h)
@@ -128,6 +155,10 @@ void free_all(esp_handle *h)
     dfree(h->d_e_run); dfree(h->d_m_run); dfree(h->d_rej); dfree(h->d_tmp_e); dfree(h->d_tmp_m);
     dfree(h->d_data); dfree(h->d_lsum); dfree(h->d_bin); dfree(h->d_levels); dfree(h->d_pm); dfree(h->d_swaps);
     dfree(h->d_series);
+    free_lp_batch(h);
+    dfree(h->d_lp_p); dfree(h->d_lp_g); dfree(h->d_lp_m); dfree(h->d_lp_v);
+    dfree(h->d_lp_w1); dfree(h->d_lp_w2); dfree(h->d_lp_w3);
+    dfree(h->d_lp_x); dfree(h->d_lp_t); dfree(h->d_lp_loss);
 }
 
 SweepArgs sweep_args(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o)
@@ -173,7 +204,7 @@ int fold(esp_handle *h)
     if (h->pending_sweeps == 0) return ESP_OK;
     FoldArgs f;
     f.part = h->d_part; f.part_rej = h->d_part_rej; f.e_run = h->d_e_run; f.m_run = h->d_m_run;
-    f.rej = h->d_rej; f.temp_of = h->d_temp_of; f.R = h->R; f.nblocks = h->sweep_grid; f.slots = h->slots;
+    f.rej = h->d_rej; f.temp_of = h->d_temp_of; f.R = h->R; f.nblocks = h->part_blocks; f.slots = h->slots;
     f.block_threads = 256; f.phase = h->pending_phase;
     CK(launch_fold(f, h->st));
     h->launches++;
@@ -183,7 +214,7 @@ int fold(esp_handle *h)
 
 bool use_cluster(const esp_handle *h)
 {
-    return h->cluster_ok && h->kernel_choice != 1;
+    return h->cluster_ok && h->kernel_choice != 1 && h->proposal == 0;
 }
 
 // One launch of the cluster-resident kernel: n_meas units of steps_measure
@@ -240,7 +271,16 @@ int do_sweep_colour(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o
     }
     SweepArgs a = sweep_args(h, c, sweep, o);
     if (a.n_c == 0) return ESP_OK;
-    CK(launch_sweep(a, h->prep.has_b, h->prep.has_d, h->sweep_grid, h->st));
+    if (h->proposal == 1) {
+        LpSweepArgs la;
+        la.s = a;
+        la.w.w1 = h->d_lp_w1; la.w.w2 = h->d_lp_w2; la.w.w3 = h->d_lp_w3;
+        la.w.b1 = h->d_lp_p + kPadB1; la.w.b2 = h->d_lp_p + kPadB2; la.w.b3 = h->d_lp_p + kPadB3;
+        la.axis = h->hsi ? h->d_lp_axis : nullptr;
+        CK(launch_sweep_lp(la, h->prep.has_b, h->prep.has_d, h->lp_grid, h->st));
+    } else {
+        CK(launch_sweep(a, h->prep.has_b, h->prep.has_d, h->sweep_grid, h->st));
+    }
     h->launches++;
     h->pending_sweeps++;
     return ESP_OK;
@@ -410,6 +450,7 @@ int esp_create(const esp_dims *dims, esp_handle **out)
     cudaError_t e = cudaGetDevice(&h->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = lp_configure(h->device);
     if (e != cudaSuccess) {
         set_global_error("CUDA unavailable: %s", cudaGetErrorString(e));
         delete h;
@@ -530,15 +571,22 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
     CK(dalloc(&h->d_fld, h->na));
     if ((rc = h2d(h, h->d_si, si.data(), sizeof(float4) * h->na))) return rc;
     if ((rc = h2d(h, h->d_fld, fl.data(), sizeof(float4) * h->na))) return rc;
+    // reference axis of the learned proposal's local frame: the single-ion axis
+    CK(dalloc(&h->d_lp_axis, h->na));
+    if ((rc = h2d(h, h->d_lp_axis, si.data(), sizeof(float4) * h->na))) return rc;
     {
         int maxc = 0;
         for (int c = 0; c < prep.num_colours; ++c) maxc = std::max(maxc, prep.off[c + 1] - prep.off[c]);
         h->sweep_grid = sweep_blocks((long long)maxc * h->R, h->R, h->max_blocks);
         h->slots = std::min(h->R, 256);
-        CK(dalloc(&h->d_part, (size_t)4 * h->sweep_grid * h->slots));
-        CK(dalloc(&h->d_part_rej, (size_t)h->sweep_grid * h->slots));
-        CK(cudaMemsetAsync(h->d_part, 0, sizeof(double) * 4 * (size_t)h->sweep_grid * h->slots, h->st));
-        CK(cudaMemsetAsync(h->d_part_rej, 0, sizeof(unsigned long long) * (size_t)h->sweep_grid * h->slots, h->st));
+        // the learned sweep's 512-thread blocks count as two 256-thread blocks
+        h->lp_grid = lp_sweep_blocks((long long)maxc * h->R, h->R, h->num_sms);
+        h->part_blocks = std::max(h->sweep_grid, 2 * h->lp_grid);
+        const size_t nslot = (size_t)h->part_blocks * h->slots;
+        CK(dalloc(&h->d_part, 4 * nslot));
+        CK(dalloc(&h->d_part_rej, nslot));
+        CK(cudaMemsetAsync(h->d_part, 0, sizeof(double) * 4 * nslot, h->st));
+        CK(cudaMemsetAsync(h->d_part_rej, 0, sizeof(unsigned long long) * nslot, h->st));
         h->pending_sweeps = 0;
     }
     // P(M) grid (mcarlo.F90:432-442)
@@ -902,7 +950,7 @@ int esp_set_sweep_kernel(esp_handle *h, int32_t kind)
 int esp_get_sweep_kernel(const esp_handle *h, int32_t *kind, int32_t *cluster_size)
 {
     if (!h || !kind) return ESP_EINVAL;
-    *kind = use_cluster(h) ? 2 : 1;
+    *kind = h->proposal == 1 ? 3 : use_cluster(h) ? 2 : 1;
     if (cluster_size) *cluster_size = h->cluster_ok ? h->csize : 0;
     return ESP_OK;
 }
@@ -1124,6 +1172,359 @@ int esp_run(esp_handle *h, const esp_schedule *s, esp_results *res)
     if (rc) return rc;
     if ((rc = esp_advance(h, h->run.total_units))) return rc;
     return esp_collect(h, res);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Learned proposal: network storage, training set, training passes.
+// ---------------------------------------------------------------------------
+namespace {
+
+// logical parameter order: W1[128][12] b1[128] W2[128][128] b2[128] W3[20][128] b3[20]
+void lp_logical_to_padded(const float *in, std::vector<float> &p)
+{
+    p.assign(kPadParams, 0.f);
+    size_t o = 0;
+    for (int n = 0; n < kMlpHid; ++n)
+        for (int k = 0; k < kMlpIn; ++k) p[kPadW1 + n * kMlpInPad + k] = in[o++];
+    for (int n = 0; n < kMlpHid; ++n) p[kPadB1 + n] = in[o++];
+    for (int i = 0; i < kMlpHid * kMlpHid; ++i) p[kPadW2 + i] = in[o++];
+    for (int n = 0; n < kMlpHid; ++n) p[kPadB2 + n] = in[o++];
+    for (int n = 0; n < kMlpOut; ++n)
+        for (int k = 0; k < kMlpHid; ++k) p[kPadW3 + n * kMlpHid + k] = in[o++];
+    for (int n = 0; n < kMlpOut; ++n) p[kPadB3 + n] = in[o++];
+}
+
+void lp_padded_to_logical(const std::vector<float> &p, float *out)
+{
+    size_t o = 0;
+    for (int n = 0; n < kMlpHid; ++n)
+        for (int k = 0; k < kMlpIn; ++k) out[o++] = p[kPadW1 + n * kMlpInPad + k];
+    for (int n = 0; n < kMlpHid; ++n) out[o++] = p[kPadB1 + n];
+    for (int i = 0; i < kMlpHid * kMlpHid; ++i) out[o++] = p[kPadW2 + i];
+    for (int n = 0; n < kMlpHid; ++n) out[o++] = p[kPadB2 + n];
+    for (int n = 0; n < kMlpOut; ++n)
+        for (int k = 0; k < kMlpHid; ++k) out[o++] = p[kPadW3 + n * kMlpHid + k];
+    for (int n = 0; n < kMlpOut; ++n) out[o++] = p[kPadB3 + n];
+}
+
+int lp_alloc_net(esp_handle *h)
+{
+    if (h->d_lp_p) return ESP_OK;
+    CK(dalloc(&h->d_lp_p, kPadParams));
+    CK(dalloc(&h->d_lp_g, kPadParams));
+    CK(dalloc(&h->d_lp_m, kPadParams));
+    CK(dalloc(&h->d_lp_v, kPadParams));
+    CK(dalloc(&h->d_lp_w1, kMlpHid * kMlpInPad));
+    CK(dalloc(&h->d_lp_w2, kMlpHid * kMlpHid));
+    CK(dalloc(&h->d_lp_w3, kMlpOutPad * kMlpHid));
+    return ESP_OK;
+}
+
+// Upload padded fp32 parameters, reset Adam, refresh the bf16 copies.
+int lp_upload(esp_handle *h, const std::vector<float> &p)
+{
+    int rc = lp_alloc_net(h);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h->d_lp_p, p.data(), sizeof(float) * kPadParams, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemsetAsync(h->d_lp_m, 0, sizeof(float) * kPadParams, h->st));
+    CK(cudaMemsetAsync(h->d_lp_v, 0, sizeof(float) * kPadParams, h->st));
+    CK(launch_lp_to_bf16(h->d_lp_p, h->d_lp_w1, h->d_lp_w2, h->d_lp_w3, h->st));
+    h->launches++;
+    CK(cudaStreamSynchronize(h->st));
+    h->lp_adam_t = 0;
+    h->lp_weights = true;
+    return ESP_OK;
+}
+
+int lp_ensure_batch(esp_handle *h, int B)
+{
+    if (B <= h->lp_bcap) return ESP_OK;
+    free_lp_batch(h);
+    const size_t b = (size_t)B;
+    CK(dalloc(&h->d_lp_xb, b * kMlpInPad));
+    CK(dalloc(&h->d_lp_h1, b * kMlpHid));
+    CK(dalloc(&h->d_lp_h2, b * kMlpHid));
+    CK(dalloc(&h->d_lp_do, b * kMlpOutPad));
+    CK(dalloc(&h->d_lp_dz2, b * kMlpHid));
+    CK(dalloc(&h->d_lp_dz1, b * kMlpHid));
+    CK(dalloc(&h->d_lp_tb, b * 4));
+    CK(dalloc(&h->d_lp_o, b * kMlpOutPad));
+    h->lp_bcap = B;
+    return ESP_OK;
+}
+
+int lp_ensure_loss(esp_handle *h, long long n)
+{
+    if (n <= h->lp_loss_cap) return ESP_OK;
+    dfree(h->d_lp_loss);
+    CK(dalloc(&h->d_lp_loss, (size_t)n));
+    h->lp_loss_cap = n;
+    return ESP_OK;
+}
+
+// Forward and backward pass over the B rows in the batch buffers, the first
+// n_real of which are samples: loss (mean -log q over those) into *d_loss,
+// gradients into d_lp_g (padded layout).
+int lp_pass(esp_handle *h, int B, int n_real, double *d_loss)
+{
+    cudaStream_t st = h->st;
+    const float *P = h->d_lp_p;
+    float *G = h->d_lp_g;
+    GemmArgs g;
+    auto reset = [&]() { std::memset(&g, 0, sizeof(g)); };
+    // H1 = relu(X W1^T + b1)
+    reset(); g.A = h->d_lp_xb; g.lda = kMlpInPad; g.B = h->d_lp_w1; g.ldb = kMlpInPad;
+    g.M = B; g.N = kMlpHid; g.K = kMlpInPad; g.Cb = h->d_lp_h1; g.ldcb = kMlpHid; g.bias = P + kPadB1; g.relu = 1;
+    CK(launch_gemm(g, false, false, st));
+    // H2 = relu(H1 W2^T + b2)
+    reset(); g.A = h->d_lp_h1; g.lda = kMlpHid; g.B = h->d_lp_w2; g.ldb = kMlpHid;
+    g.M = B; g.N = kMlpHid; g.K = kMlpHid; g.Cb = h->d_lp_h2; g.ldcb = kMlpHid; g.bias = P + kPadB2; g.relu = 1;
+    CK(launch_gemm(g, false, false, st));
+    // O = H2 W3^T + b3
+    reset(); g.A = h->d_lp_h2; g.lda = kMlpHid; g.B = h->d_lp_w3; g.ldb = kMlpHid;
+    g.M = B; g.N = kMlpOutPad; g.K = kMlpHid; g.C = h->d_lp_o; g.ldc = kMlpOutPad; g.bias = P + kPadB3;
+    CK(launch_gemm(g, false, false, st));
+    // dO
+    CK(launch_lp_head(h->d_lp_o, h->d_lp_tb, n_real, B, 1.f / (float)n_real, h->d_lp_do, d_loss, st));
+    // dW3 = dO^T H2, db3
+    reset(); g.A = h->d_lp_do; g.lda = kMlpOutPad; g.B = h->d_lp_h2; g.ldb = kMlpHid;
+    g.M = kMlpOutPad; g.N = kMlpHid; g.K = B; g.C = G + kPadW3; g.ldc = kMlpHid;
+    CK(launch_gemm(g, true, true, st));
+    CK(launch_colsum(h->d_lp_do, B, kMlpOutPad, kMlpOutPad, G + kPadB3, st));
+    // dZ2 = (dO W3) . [H2 > 0]
+    reset(); g.A = h->d_lp_do; g.lda = kMlpOutPad; g.B = h->d_lp_w3; g.ldb = kMlpHid;
+    g.M = B; g.N = kMlpHid; g.K = kMlpOutPad; g.Cb = h->d_lp_dz2; g.ldcb = kMlpHid; g.mask = h->d_lp_h2; g.ldm = kMlpHid;
+    CK(launch_gemm(g, false, true, st));
+    // dW2 = dZ2^T H1, db2
+    reset(); g.A = h->d_lp_dz2; g.lda = kMlpHid; g.B = h->d_lp_h1; g.ldb = kMlpHid;
+    g.M = kMlpHid; g.N = kMlpHid; g.K = B; g.C = G + kPadW2; g.ldc = kMlpHid;
+    CK(launch_gemm(g, true, true, st));
+    CK(launch_colsum(h->d_lp_dz2, B, kMlpHid, kMlpHid, G + kPadB2, st));
+    // dZ1 = (dZ2 W2) . [H1 > 0]
+    reset(); g.A = h->d_lp_dz2; g.lda = kMlpHid; g.B = h->d_lp_w2; g.ldb = kMlpHid;
+    g.M = B; g.N = kMlpHid; g.K = kMlpHid; g.Cb = h->d_lp_dz1; g.ldcb = kMlpHid; g.mask = h->d_lp_h1; g.ldm = kMlpHid;
+    CK(launch_gemm(g, false, true, st));
+    // dW1 = dZ1^T X, db1
+    reset(); g.A = h->d_lp_dz1; g.lda = kMlpHid; g.B = h->d_lp_xb; g.ldb = kMlpInPad;
+    g.M = kMlpHid; g.N = kMlpInPad; g.K = B; g.C = G + kPadW1; g.ldc = kMlpInPad;
+    CK(launch_gemm(g, true, true, st));
+    CK(launch_colsum(h->d_lp_dz1, B, kMlpHid, kMlpHid, G + kPadB1, st));
+    h->launches += 13;
+    return ESP_OK;
+}
+
+void bf16_rows(const float *f, int64_t n, std::vector<__nv_bfloat16> &x)
+{
+    x.assign((size_t)n * kMlpInPad, __float2bfloat16_rn(0.f));
+    for (int64_t i = 0; i < n; ++i)
+        for (int k = 0; k < kMlpIn; ++k) x[(size_t)i * kMlpInPad + k] = __float2bfloat16_rn(f[(size_t)i * kMlpIn + k]);
+}
+
+int64_t round8(int64_t n) { return (n + 7) & ~(int64_t)7; }
+
+}  // namespace
+
+extern "C" {
+
+int esp_lp_num_params(void) { return kLpParams; }
+
+int esp_lp_set_weights(esp_handle *h, const float *params)
+{
+    if (!h || !params) return ESP_EINVAL;
+    for (int i = 0; i < kLpParams; ++i)
+        if (!std::isfinite(params[i])) { h->err = "non-finite network parameter"; return ESP_EINVAL; }
+    std::vector<float> p;
+    lp_logical_to_padded(params, p);
+    return lp_upload(h, p);
+}
+
+int esp_lp_get_weights(esp_handle *h, float *params)
+{
+    if (!h || !params) return ESP_EINVAL;
+    if (!h->lp_weights) { h->err = "no network weights (esp_lp_init_weights / esp_lp_set_weights)"; return ESP_ESTATE; }
+    std::vector<float> p(kPadParams);
+    int rc = d2h(h, p.data(), h->d_lp_p, sizeof(float) * kPadParams);
+    if (rc) return rc;
+    lp_padded_to_logical(p, params);
+    return ESP_OK;
+}
+
+int esp_lp_init_weights(esp_handle *h, uint64_t seed)
+{
+    if (!h) return ESP_EINVAL;
+    // splitmix64 uniforms: He-uniform hidden layers, a small output layer so
+    // that the initial proposal is close to the Heisenberg conditional
+    uint64_t state = seed ^ 0x6A09E667F3BCC909ull;
+    auto uni = [&]() {
+        uint64_t z = (state += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+    };
+    std::vector<float> l(kLpParams, 0.f);
+    size_t o = 0;
+    const double a1 = std::sqrt(6.0 / kMlpIn), a2 = std::sqrt(6.0 / kMlpHid), a3 = 0.01 / std::sqrt((double)kMlpHid);
+    for (int i = 0; i < kMlpHid * kMlpIn; ++i) l[o++] = (float)(a1 * uni());
+    o += kMlpHid;
+    for (int i = 0; i < kMlpHid * kMlpHid; ++i) l[o++] = (float)(a2 * uni());
+    o += kMlpHid;
+    for (int i = 0; i < kMlpOut * kMlpHid; ++i) l[o++] = (float)(a3 * uni());
+    std::vector<float> p;
+    lp_logical_to_padded(l.data(), p);
+    return lp_upload(h, p);
+}
+
+int esp_lp_reserve(esp_handle *h, int64_t capacity)
+{
+    if (!h || capacity < 0) return ESP_EINVAL;
+    CK(cudaStreamSynchronize(h->st));
+    dfree(h->d_lp_x); dfree(h->d_lp_t);
+    h->lp_cap = 0; h->lp_n = 0;
+    if (capacity == 0) return ESP_OK;
+    CK(dalloc(&h->d_lp_x, (size_t)capacity * kMlpInPad));
+    CK(dalloc(&h->d_lp_t, (size_t)capacity * 4));
+    h->lp_cap = capacity;
+    return ESP_OK;
+}
+
+int esp_lp_collect(esp_handle *h, int32_t colour, int64_t *rows)
+{
+    int rc = require(h, true, true);
+    if (rc) return rc;
+    if (colour < 0 || colour >= h->prep.num_colours) { h->err = "bad colour"; return ESP_EINVAL; }
+    if (h->lp_cap == 0) { h->err = "no training-set storage (esp_lp_reserve)"; return ESP_ESTATE; }
+    esp_sweep_opts o{};
+    LpCollectArgs c;
+    c.s = sweep_args(h, colour, 0, &o);
+    c.axis = h->hsi ? h->d_lp_axis : nullptr;
+    c.x = h->d_lp_x; c.t = h->d_lp_t;
+    c.first = h->lp_n;
+    c.count = std::min((long long)c.s.n_c * h->R, h->lp_cap - h->lp_n);
+    CK(launch_lp_collect(c, h->prep.has_b, h->prep.has_d, h->max_blocks, h->st));
+    h->launches++;
+    h->lp_n += c.count;
+    if (rows) *rows = h->lp_n;
+    return ESP_OK;
+}
+
+int esp_lp_get_data(esp_handle *h, int64_t first, int64_t n, float *features, float *targets)
+{
+    if (!h || first < 0 || n < 0 || first + n > h->lp_n) return ESP_EINVAL;
+    if (n == 0) return ESP_OK;
+    std::vector<__nv_bfloat16> x((size_t)n * kMlpInPad);
+    std::vector<float> t((size_t)n * 4);
+    int rc = d2h(h, x.data(), h->d_lp_x + (size_t)first * kMlpInPad, sizeof(__nv_bfloat16) * x.size());
+    if (rc) return rc;
+    if ((rc = d2h(h, t.data(), h->d_lp_t + (size_t)first * 4, sizeof(float) * t.size()))) return rc;
+    for (int64_t i = 0; i < n; ++i) {
+        if (features)
+            for (int k = 0; k < kMlpIn; ++k) features[i * kMlpIn + k] = __bfloat162float(x[(size_t)i * kMlpInPad + k]);
+        if (targets)
+            for (int k = 0; k < 4; ++k) targets[i * 4 + k] = t[(size_t)i * 4 + k];
+    }
+    return ESP_OK;
+}
+
+int esp_lp_train(esp_handle *h, const esp_lp_train_opts *o, double *loss)
+{
+    if (!h || !o) return ESP_EINVAL;
+    if (!h->lp_weights) { h->err = "no network weights (esp_lp_init_weights / esp_lp_set_weights)"; return ESP_ESTATE; }
+    if (h->lp_n <= 0) { h->err = "empty training set (esp_lp_collect)"; return ESP_ESTATE; }
+    if (o->steps < 0 || o->batch < 8 || o->batch > (1 << 20) || !(o->lr > 0.0)) {
+        h->err = "bad training options";
+        return ESP_EINVAL;
+    }
+    const int B = (int)round8(o->batch);
+    int rc = lp_ensure_batch(h, B);
+    if (rc) return rc;
+    if ((rc = lp_ensure_loss(h, std::max(1, o->steps)))) return rc;
+    for (int s = 0; s < o->steps; ++s) {
+        CK(launch_lp_gather(h->d_lp_x, h->d_lp_t, h->lp_n, B, o->seed, (uint64_t)(h->lp_adam_t), h->d_lp_xb,
+                            h->d_lp_tb, h->st));
+        if ((rc = lp_pass(h, B, B, h->d_lp_loss + s))) return rc;
+        ++h->lp_adam_t;
+        CK(launch_adam(h->d_lp_p, h->d_lp_g, h->d_lp_m, h->d_lp_v, kPadParams, (float)o->lr, (float)o->beta1,
+                       (float)o->beta2, (float)o->eps, h->lp_adam_t, h->st));
+        CK(launch_lp_to_bf16(h->d_lp_p, h->d_lp_w1, h->d_lp_w2, h->d_lp_w3, h->st));
+        h->launches += 3;
+    }
+    if (loss && o->steps > 0) {
+        if ((rc = d2h(h, loss, h->d_lp_loss, sizeof(double) * o->steps))) return rc;
+    } else {
+        CK(cudaStreamSynchronize(h->st));
+    }
+    return ESP_OK;
+}
+
+int esp_lp_loss_grad(esp_handle *h, const float *features, const float *targets, int64_t n, double *loss,
+                     float *grad)
+{
+    if (!h || !features || !targets || n <= 0 || n > (1 << 20)) return ESP_EINVAL;
+    if (!h->lp_weights) { h->err = "no network weights (esp_lp_init_weights / esp_lp_set_weights)"; return ESP_ESTATE; }
+    const int B = (int)round8(n);
+    int rc = lp_ensure_batch(h, B);
+    if (rc) return rc;
+    if ((rc = lp_ensure_loss(h, 1))) return rc;
+    std::vector<__nv_bfloat16> x;
+    bf16_rows(features, n, x);
+    x.resize((size_t)B * kMlpInPad, __float2bfloat16_rn(0.f));   // zero rows up to the multiple of 8
+    std::vector<float> t((size_t)B * 4, 0.f);
+    std::memcpy(t.data(), targets, sizeof(float) * 4 * n);
+    if ((rc = h2d(h, h->d_lp_xb, x.data(), sizeof(__nv_bfloat16) * x.size()))) return rc;
+    if ((rc = h2d(h, h->d_lp_tb, t.data(), sizeof(float) * t.size()))) return rc;
+    if ((rc = lp_pass(h, B, (int)n, h->d_lp_loss))) return rc;
+    std::vector<float> g(kPadParams);
+    if ((rc = d2h(h, g.data(), h->d_lp_g, sizeof(float) * kPadParams))) return rc;
+    if (grad) lp_padded_to_logical(g, grad);
+    if (loss && (rc = d2h(h, loss, h->d_lp_loss, sizeof(double)))) return rc;
+    return ESP_OK;
+}
+
+int esp_lp_forward(esp_handle *h, const float *features, int64_t n, float *out)
+{
+    if (!h || !features || !out || n < 0 || n > (1 << 24)) return ESP_EINVAL;
+    if (!h->lp_weights) { h->err = "no network weights (esp_lp_init_weights / esp_lp_set_weights)"; return ESP_ESTATE; }
+    if (n == 0) return ESP_OK;
+    std::vector<__nv_bfloat16> x;
+    bf16_rows(features, n, x);
+    __nv_bfloat16 *dx = nullptr;
+    float *dout = nullptr;
+    CK(dalloc(&dx, x.size()));
+    cudaError_t e = dalloc(&dout, (size_t)n * kMlpOut);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x.data(), sizeof(__nv_bfloat16) * x.size(), cudaMemcpyHostToDevice, h->st);
+    LpWeights w;
+    w.w1 = h->d_lp_w1; w.w2 = h->d_lp_w2; w.w3 = h->d_lp_w3;
+    w.b1 = h->d_lp_p + kPadB1; w.b2 = h->d_lp_p + kPadB2; w.b3 = h->d_lp_p + kPadB3;
+    if (e == cudaSuccess) e = launch_lp_forward(w, dx, (int)n, dout, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, sizeof(float) * n * kMlpOut, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    h->launches++;
+    dfree(dx); dfree(dout);
+    if (e != cudaSuccess) { h->err = std::string("esp_lp_forward: ") + cudaGetErrorString(e); return ESP_ECUDA; }
+    return ESP_OK;
+}
+
+int esp_set_proposal(esp_handle *h, int32_t kind)
+{
+    if (!h || kind < 0 || kind > 1) return ESP_EINVAL;
+    if (kind == 1 && !h->lp_weights) {
+        h->err = "the learned proposal needs network weights (esp_lp_init_weights / esp_lp_set_weights)";
+        return ESP_ESTATE;
+    }
+    int rc = fold(h);
+    if (rc) return rc;
+    h->proposal = kind;
+    return ESP_OK;
+}
+
+int esp_get_proposal(const esp_handle *h, int32_t *kind)
+{
+    if (!h || !kind) return ESP_EINVAL;
+    *kind = h->proposal;
+    return ESP_OK;
 }
 
 }  // extern "C"

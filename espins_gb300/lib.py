@@ -25,13 +25,24 @@ EXPORTED = [
     "esp_running_magnetization", "esp_local_terms", "esp_get_spins", "esp_get_colouring",
     "esp_get_rejected", "esp_get_replica_of_slot", "esp_num_freq", "esp_launch_count",
     "esp_energy_noalloc", "esp_set_sweep_kernel", "esp_get_sweep_kernel", "esp_set_series", "esp_get_series",
+    "esp_lp_num_params", "esp_lp_init_weights", "esp_lp_set_weights", "esp_lp_get_weights", "esp_lp_reserve",
+    "esp_lp_collect", "esp_lp_get_data", "esp_lp_train", "esp_lp_loss_grad", "esp_lp_forward",
+    "esp_set_proposal", "esp_get_proposal",
 ]
+
+LP_NUM_PARAMS = 20756
+LP_IN, LP_OUT = 12, 20
 
 
 class EspError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"libespins_gpu error {code}: {msg}")
         self.code = code
+
+
+class LpTrainOpts(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("batch", C.c_int32), ("lr", C.c_double), ("beta1", C.c_double),
+                ("beta2", C.c_double), ("eps", C.c_double), ("seed", C.c_uint64)]
 
 
 class Dims(C.Structure):
@@ -119,6 +130,18 @@ def load(build_if_missing: bool = True):
     lib.esp_set_series.argtypes = [vp, C.c_int64]
     lib.esp_get_series.argtypes = [vp, vp, P(C.c_int64)]
     lib.esp_get_sweep_kernel.argtypes = [vp, P(C.c_int32), P(C.c_int32)]
+    lib.esp_lp_num_params.argtypes = []
+    lib.esp_lp_init_weights.argtypes = [vp, C.c_uint64]
+    lib.esp_lp_set_weights.argtypes = [vp, vp]
+    lib.esp_lp_get_weights.argtypes = [vp, vp]
+    lib.esp_lp_reserve.argtypes = [vp, C.c_int64]
+    lib.esp_lp_collect.argtypes = [vp, C.c_int32, P(C.c_int64)]
+    lib.esp_lp_get_data.argtypes = [vp, C.c_int64, C.c_int64, vp, vp]
+    lib.esp_lp_train.argtypes = [vp, P(LpTrainOpts), vp]
+    lib.esp_lp_loss_grad.argtypes = [vp, vp, vp, C.c_int64, P(C.c_double), vp]
+    lib.esp_lp_forward.argtypes = [vp, vp, C.c_int64, vp]
+    lib.esp_set_proposal.argtypes = [vp, C.c_int32]
+    lib.esp_get_proposal.argtypes = [vp, P(C.c_int32)]
     for f in EXPORTED:
         getattr(lib, f).restype = C.c_int
     _lib = lib
@@ -369,10 +392,69 @@ class Engine:
         self._check(self.lib.esp_set_sweep_kernel(self.h, k))
 
     def sweep_kernel(self):
-        """('ell' | 'cluster', cluster size)."""
+        """('ell' | 'cluster' | 'learned', cluster size)."""
         k, cs = C.c_int32(), C.c_int32()
         self._check(self.lib.esp_get_sweep_kernel(self.h, C.byref(k), C.byref(cs)))
-        return ("cluster" if k.value == 2 else "ell"), cs.value
+        return {1: "ell", 2: "cluster", 3: "learned"}[k.value], cs.value
+
+    # -- learned proposal -----------------------------------------------------
+    def lp_init(self, seed: int = 0) -> None:
+        self._check(self.lib.esp_lp_init_weights(self.h, int(seed)))
+
+    def lp_set_weights(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != LP_NUM_PARAMS:
+            raise ValueError(f"expected {LP_NUM_PARAMS} parameters")
+        self._check(self.lib.esp_lp_set_weights(self.h, _p(p)))
+
+    def lp_weights(self) -> np.ndarray:
+        p = np.zeros(LP_NUM_PARAMS, dtype=np.float32)
+        self._check(self.lib.esp_lp_get_weights(self.h, _p(p)))
+        return p
+
+    def lp_reserve(self, capacity: int) -> None:
+        self._check(self.lib.esp_lp_reserve(self.h, int(capacity)))
+
+    def lp_collect(self, colour: int) -> int:
+        n = C.c_int64()
+        self._check(self.lib.esp_lp_collect(self.h, int(colour), C.byref(n)))
+        return n.value
+
+    def lp_data(self, first: int, n: int):
+        f = np.zeros((n, LP_IN), dtype=np.float32)
+        t = np.zeros((n, 4), dtype=np.float32)
+        self._check(self.lib.esp_lp_get_data(self.h, int(first), int(n), _p(f), _p(t)))
+        return f, t
+
+    def lp_train(self, steps: int, batch: int = 4096, lr: float = 1e-3, beta1: float = 0.9,
+                 beta2: float = 0.999, eps: float = 1e-8, seed: int = 0) -> np.ndarray:
+        o = LpTrainOpts(int(steps), int(batch), float(lr), float(beta1), float(beta2), float(eps), int(seed))
+        loss = np.zeros(max(1, int(steps)))
+        self._check(self.lib.esp_lp_train(self.h, C.byref(o), _p(loss)))
+        return loss[:steps]
+
+    def lp_loss_grad(self, features: np.ndarray, targets: np.ndarray):
+        f = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, LP_IN)
+        t = np.ascontiguousarray(targets, dtype=np.float32).reshape(-1, 4)
+        g = np.zeros(LP_NUM_PARAMS, dtype=np.float32)
+        loss = C.c_double()
+        self._check(self.lib.esp_lp_loss_grad(self.h, _p(f), _p(t), f.shape[0], C.byref(loss), _p(g)))
+        return loss.value, g
+
+    def lp_forward(self, features: np.ndarray) -> np.ndarray:
+        f = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, LP_IN)
+        out = np.zeros((f.shape[0], LP_OUT), dtype=np.float32)
+        self._check(self.lib.esp_lp_forward(self.h, _p(f), f.shape[0], _p(out)))
+        return out
+
+    def set_proposal(self, kind: str) -> None:
+        """'plain' (the reference's trial moves) or 'learned'."""
+        self._check(self.lib.esp_set_proposal(self.h, {"plain": 0, "learned": 1}[kind]))
+
+    def proposal(self) -> str:
+        k = C.c_int32()
+        self._check(self.lib.esp_get_proposal(self.h, C.byref(k)))
+        return ("plain", "learned")[k.value]
 
     def num_freq(self) -> int:
         k = C.c_int32()

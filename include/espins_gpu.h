@@ -194,7 +194,8 @@ int esp_get_replica_of_slot(esp_handle *h, int32_t *replica_out);
  * replica fits the shared memory of one thread-block cluster).  Both follow the
  * same colouring, random stream and summation order. */
 int esp_set_sweep_kernel(esp_handle *h, int32_t kind);
-/* The kernel in use (1 or 2) and the cluster size of the cluster path. */
+/* The kernel in use (1 ELL, 2 cluster, 3 the learned-proposal sweep) and the
+ * cluster size of the cluster path. */
 int esp_get_sweep_kernel(const esp_handle *h, int32_t *kind, int32_t *cluster_size);
 /* Keep the per-measurement series (E, |m|) of every temperature slot for
  * the last `capacity` measurements of a run (0 switches it off): the data of
@@ -208,6 +209,51 @@ int esp_get_series(esp_handle *h, double *out, int64_t *count);
 int esp_num_freq(const esp_handle *h, int32_t *nf);
 /* Number of kernels this handle has launched so far. */
 int esp_launch_count(const esp_handle *h, int64_t *count);
+
+/* ---- learned proposal ------------------------------------------------------
+ * No counterpart in the reference (whose trial spins are uniform on the sphere
+ * or in a cone, get_quant.F90:80-162).  The trial spin of a site is drawn from
+ * a 4-component von Mises-Fisher mixture whose parameters an MLP
+ * (12 -> 128 -> 128 -> 20, ReLU, BF16 weights, FP32 accumulation) computes
+ * from the site's environment (local field, quadratic form, beta) in a local
+ * frame; the Metropolis-Hastings test uses the exact mixture density of the
+ * old and the new spin, so the chain samples the same Boltzmann distribution.
+ * The network is trained on the GPU on (environment, spin) pairs taken from
+ * the plain sampler's configurations, by maximum likelihood (Adam).
+ * Parameters travel as ESP_LP_NUM_PARAMS floats in the order
+ * W1[128][12] b1[128] W2[128][128] b2[128] W3[20][128] b3[20] (row = output). */
+#define ESP_LP_NUM_PARAMS 20756
+typedef struct {
+    int32_t steps;              /* optimiser steps */
+    int32_t batch;              /* samples per step (rounded up to a multiple of 8) */
+    double lr, beta1, beta2, eps;   /* Adam */
+    uint64_t seed;              /* mini-batch draws */
+} esp_lp_train_opts;
+int esp_lp_num_params(void);
+int esp_lp_init_weights(esp_handle *h, uint64_t seed);
+int esp_lp_set_weights(esp_handle *h, const float *params);
+int esp_lp_get_weights(esp_handle *h, float *params);
+/* Training-set storage for `capacity` pairs (clears the set). */
+int esp_lp_reserve(esp_handle *h, int64_t capacity);
+/* Append the pairs of every site of one colour class in every replica of the
+ * current configurations (until the storage is full); *rows = set size. */
+int esp_lp_collect(esp_handle *h, int32_t colour, int64_t *rows);
+/* Copy pairs [first, first+n) of the set: features (n,12) as stored (bf16
+ * values), targets (n,4) = unit spin in the local frame and kappa0. */
+int esp_lp_get_data(esp_handle *h, int64_t first, int64_t n, float *features, float *targets);
+/* o->steps Adam steps on random mini-batches of the set; loss (if not NULL)
+ * receives the mean negative log-likelihood of every step's batch. */
+int esp_lp_train(esp_handle *h, const esp_lp_train_opts *o, double *loss);
+/* Mean negative log-likelihood of n given pairs and its gradient with respect
+ * to the parameters (ESP_LP_NUM_PARAMS floats), by the training kernels. */
+int esp_lp_loss_grad(esp_handle *h, const float *features, const float *targets, int64_t n, double *loss,
+                     float *grad);
+/* Raw network outputs (n,20) of n feature rows by the sweep's fused forward pass. */
+int esp_lp_forward(esp_handle *h, const float *features, int64_t n, float *out);
+/* 0: the reference's trial moves (default); 1: the learned proposal (needs
+ * weights).  Applies to esp_sweep, esp_sweep_colour, esp_run and esp_advance. */
+int esp_set_proposal(esp_handle *h, int32_t kind);
+int esp_get_proposal(const esp_handle *h, int32_t *kind);
 
 /* ---- allocation-free direct energy ---------------------------------------
  * No counterpart in the reference: an extra entry point for hosts that own

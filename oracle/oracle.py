@@ -22,8 +22,8 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
-    src = os.path.join(HERE, "espins_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("espins_oracle.c", "lp_oracle.c", "Makefile")]
+    if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(LIB_PATH) < os.path.getmtime(s) for s in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
@@ -107,6 +107,15 @@ def _declare(L):
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                C.c_void_p, C.c_void_p, C.c_void_p, P(C.c_int32)]
     L.or_build_ell.restype = C.c_int
+    L.or_lp_num_params.restype = C.c_int
+    L.or_lp_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    L.or_lp_loss_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    L.or_lp_loss_grad.restype = C.c_double
+    L.or_vmf_logpdf.argtypes = [C.c_void_p, C.c_double, C.c_void_p]
+    L.or_vmf_logpdf.restype = C.c_double
+    L.or_vmf_sample.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]
+    L.or_lp_features.argtypes = [C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 P(C.c_double), C.c_void_p]
 
 
 def _ptr(a: np.ndarray) -> int:
@@ -314,3 +323,56 @@ def read_sconfig(path: str):
         blk = np.array([[float(v) for v in lines[pos + j].split()] for j in range(nw)])
         spins.append(blk); pos += nw
     return sc, np.array(temps), np.array(spins)
+
+
+# ---- learned proposal: FP64 network, mixture head and gradient (lp_oracle.c) ----
+
+LP_IN, LP_HID, LP_OUT = 12, 128, 20
+
+
+def lp_num_params() -> int:
+    return int(lib().or_lp_num_params())
+
+
+def lp_forward(params: np.ndarray, x: np.ndarray) -> np.ndarray:
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, LP_IN)
+    out = np.zeros((x.shape[0], LP_OUT))
+    lib().or_lp_forward(_ptr(p), _ptr(x), x.shape[0], _ptr(out))
+    return out
+
+
+def lp_loss_grad(params: np.ndarray, x: np.ndarray, t: np.ndarray):
+    """Mean negative log-likelihood of (features, targets) and its gradient."""
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, LP_IN)
+    t = np.ascontiguousarray(t, dtype=np.float64).reshape(-1, 4)
+    g = np.zeros(p.size)
+    loss = lib().or_lp_loss_grad(_ptr(p), _ptr(x), _ptr(t), x.shape[0], _ptr(g))
+    return float(loss), g
+
+
+def vmf_logpdf(o, kappa0: float, s) -> float:
+    o = np.ascontiguousarray(o, dtype=np.float64)
+    s = np.ascontiguousarray(s, dtype=np.float64)
+    return float(lib().or_vmf_logpdf(_ptr(o), float(kappa0), _ptr(s)))
+
+
+def vmf_sample(o, kappa0: float, u) -> np.ndarray:
+    o = np.ascontiguousarray(o, dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    s = np.zeros(3)
+    lib().or_vmf_sample(_ptr(o), float(kappa0), _ptr(u), _ptr(s))
+    return s
+
+
+def lp_features(beta: float, mag: float, g, q, axis):
+    """(frame rows (3,3), kappa0, features (12,)) of one site."""
+    g = np.ascontiguousarray(g, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    a = np.ascontiguousarray(axis, dtype=np.float64)
+    e = np.zeros(9)
+    k0 = C.c_double(0.0)
+    f = np.zeros(LP_IN)
+    lib().or_lp_features(float(beta), float(mag), _ptr(g), _ptr(q), _ptr(a), _ptr(e), C.byref(k0), _ptr(f))
+    return e.reshape(3, 3), float(k0.value), f
