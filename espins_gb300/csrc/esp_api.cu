@@ -2,6 +2,7 @@
 // device memory, and the schedules of mcarlo (ESpinS src/mcarlo.F90:463-733)
 // and pt_mcarlo (src/pt.F90:504-1024) driven from the host.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -100,6 +101,17 @@ struct esp_handle {
     float *d_lp_tb = nullptr, *d_lp_o = nullptr;
     double *d_lp_loss = nullptr;
     long long lp_loss_cap = 0;
+    // PT: temperatures per independent lattice (0: all R are one lattice)
+    int pt_group = 0;
+    // run counters on the device [sweep, swap, measurement, unit], used by
+    // kernels launched inside a captured graph: their arguments hold values
+    // relative to the counters at capture time and every replay advances
+    // the counters (k_bump) instead of repeating the same random numbers
+    unsigned long long *d_ctr = nullptr;
+    unsigned long long ctr_shadow[4] = {0, 0, 0, 0};   // what d_ctr holds
+    bool ctr_valid = false;
+    bool capturing = false;
+    int64_t cap_base[4] = {0, 0, 0, 0};
 };
 
 namespace {
@@ -159,6 +171,7 @@ void free_all(esp_handle *h)
     dfree(h->d_lp_p); dfree(h->d_lp_g); dfree(h->d_lp_m); dfree(h->d_lp_v);
     dfree(h->d_lp_w1); dfree(h->d_lp_w2); dfree(h->d_lp_w3);
     dfree(h->d_lp_x); dfree(h->d_lp_t); dfree(h->d_lp_loss);
+    dfree(h->d_ctr);
 }
 
 SweepArgs sweep_args(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o)
@@ -174,6 +187,11 @@ SweepArgs sweep_args(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *
     a.off_c = h->prep.off[c]; a.n_c = h->prep.off[c + 1] - h->prep.off[c];
     a.mode = o->mcarlo_mode ? 1 : 0; a.tilt = (float)o->tilt_angles_max;
     a.key0 = (uint32_t)o->seed; a.key1 = (uint32_t)(o->seed >> 32);
+    a.ctr = nullptr;
+    if (h->capturing) {
+        sweep -= h->cap_base[0];
+        a.ctr = h->d_ctr;
+    }
     a.sw_lo = (uint32_t)sweep; a.sw_hi = (uint32_t)((uint64_t)sweep >> 32);
     return a;
 }
@@ -240,6 +258,12 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     a.nlev = nlev; a.pt_quirk = pt_quirk ? 1 : 0;
     a.pm_counts = h->d_pm; a.nf = h->nf; a.m_min = h->m_min; a.m_max = h->m_max;
     a.series = h->d_series; a.series_cap = h->series_cap;
+    a.ctr = nullptr;
+    if (h->capturing) {
+        first -= h->cap_base[0];
+        a.meas_base -= h->cap_base[2];
+        a.ctr = h->d_ctr;
+    }
     a.sweep_base = (unsigned long long)first;
     a.key0 = (uint32_t)o->seed; a.key1 = (uint32_t)(o->seed >> 32);
     a.mode = o->mcarlo_mode ? 1 : 0; a.tilt = (float)o->tilt_angles_max;
@@ -363,6 +387,11 @@ int measure(esp_handle *h, long long step, int nlev, bool pt_quirk, long long &c
     m.data = h->d_data; m.lsum = h->d_lsum; m.binning = h->d_bin; m.levels = h->d_levels;
     m.R = h->R; m.N = h->N; m.nlev = nlev; m.pt_quirk = pt_quirk ? 1 : 0; m.step = step;
     m.series = h->d_series; m.series_cap = h->series_cap;
+    m.ctr = nullptr;
+    if (h->capturing) {
+        m.step -= h->cap_base[2];
+        m.ctr = h->d_ctr + 2;
+    }
     CK(launch_measure(m, h->st));
     h->launches++;
     if (h->na == 1) {
@@ -801,19 +830,55 @@ int esp_sweep_colour(esp_handle *h, int32_t colour, int64_t sweep, const esp_swe
     return do_sweep_colour(h, colour, sweep, o);
 }
 
+}  // extern "C"
+
+namespace {
+
+// pt_swap of every lattice (group of temperatures); `unit` is the 1-based
+// unit index whose parity gives `start` (used when capturing a graph).
+int pt_swap_launch(esp_handle *h, int32_t start, int64_t swap_index, uint64_t seed, int64_t unit)
+{
+    int rc = fold(h);
+    if (rc) return rc;
+    PtSwapArgs a;
+    a.repl_at = h->d_repl_at; a.temp_of = h->d_temp_of; a.e_run = h->d_e_run; a.inv_t = h->d_inv_t;
+    a.num_swaps = h->d_swaps; a.R = h->R; a.start0 = start - 1;
+    a.group = h->pt_group > 0 ? h->pt_group : h->R;
+    a.key0 = (uint32_t)seed; a.key1 = (uint32_t)(seed >> 32);
+    a.ctr = nullptr; a.unit_off = 0;
+    if (h->capturing) {
+        swap_index -= h->cap_base[1];
+        a.unit_off = (int32_t)(unit - h->cap_base[3]);
+        a.ctr = h->d_ctr;
+    }
+    a.idx_lo = (uint32_t)swap_index; a.idx_hi = (uint32_t)((uint64_t)swap_index >> 32);
+    CK(launch_pt_swap(a, h->st));
+    h->launches++;
+    return ESP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int esp_pt_swap(esp_handle *h, int32_t start, int64_t swap_index, uint64_t seed)
 {
     int rc = require(h, true, true);
     if (rc) return rc;
     if (start != 1 && start != 2) { h->err = "start must be 1 or 2"; return ESP_EINVAL; }
-    if ((rc = fold(h))) return rc;
-    PtSwapArgs a;
-    a.repl_at = h->d_repl_at; a.temp_of = h->d_temp_of; a.e_run = h->d_e_run; a.inv_t = h->d_inv_t;
-    a.num_swaps = h->d_swaps; a.R = h->R; a.start0 = start - 1;
-    a.key0 = (uint32_t)seed; a.key1 = (uint32_t)(seed >> 32);
-    a.idx_lo = (uint32_t)swap_index; a.idx_hi = (uint32_t)((uint64_t)swap_index >> 32);
-    CK(launch_pt_swap(a, h->st));
-    h->launches++;
+    return pt_swap_launch(h, start, swap_index, seed, 0);
+}
+
+int esp_set_pt_groups(esp_handle *h, int32_t group_size)
+{
+    if (!h) return ESP_EINVAL;
+    if (group_size < 1 || h->R % group_size != 0) {
+        h->err = "the PT group size must divide the number of replicas";
+        return ESP_EINVAL;
+    }
+    int rc = fold(h);
+    if (rc) return rc;
+    h->pt_group = group_size;
     return ESP_OK;
 }
 
@@ -1062,7 +1127,7 @@ int esp_advance(esp_handle *h, int64_t n)
                 h->next_sweep += s.pt_steps_swap * s.steps_measure;
                 u.meas_done += s.pt_steps_swap;
                 if (h->na == 1) u.const_hits += s.pt_steps_swap;
-                if ((rc = esp_pt_swap(h, (int)((l + 1) % 2) + 1, h->next_swap++, s.seed))) return rc;
+                if ((rc = pt_swap_launch(h, (int)((l + 1) % 2) + 1, h->next_swap++, s.seed, l))) return rc;
             }
         }
         return ESP_OK;
@@ -1083,7 +1148,7 @@ int esp_advance(esp_handle *h, int64_t n)
                 ++u.meas_done;
                 if ((rc = measure(h, u.meas_done, u.nlev, true, u.const_hits))) return rc;
             }
-            if ((rc = esp_pt_swap(h, (int)((l + 1) % 2) + 1, h->next_swap++, s.seed))) return rc;
+            if ((rc = pt_swap_launch(h, (int)((l + 1) % 2) + 1, h->next_swap++, s.seed, l))) return rc;
         }
     }
     if (!s.pt) u.units_done += n;
@@ -1524,6 +1589,309 @@ int esp_get_proposal(const esp_handle *h, int32_t *kind)
 {
     if (!h || !kind) return ESP_EINVAL;
     *kind = h->proposal;
+    return ESP_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches: independent handles advanced together by one CUDA graph per
+// `units_per_graph` measurement units, and the autotuner that picks each
+// handle's sweep kernel and the units per graph by timing them.
+// ---------------------------------------------------------------------------
+struct esp_batch {
+    std::vector<esp_handle *> hs;
+    std::vector<cudaStream_t> prev;   // the handles' streams before the batch
+    cudaStream_t st = nullptr;
+    cudaStream_t own = nullptr;       // created when the caller passes no stream
+    std::string err;
+    int units_per_graph = 1;
+    cudaGraphExec_t exec = nullptr;
+    int exec_units = 0;
+    struct Delta {
+        int64_t c[4];
+        long long const_hits, launches;
+    };
+    std::vector<Delta> deltas;
+};
+
+namespace {
+
+void mirrors(const esp_handle *h, int64_t c[4])
+{
+    c[0] = h->next_sweep; c[1] = h->next_swap; c[2] = h->run.meas_done; c[3] = h->run.units_done;
+}
+
+void set_mirrors(esp_handle *h, const int64_t c[4])
+{
+    h->next_sweep = c[0]; h->next_swap = c[1]; h->run.meas_done = c[2]; h->run.units_done = c[3];
+}
+
+void batch_drop_graph(esp_batch *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    b->exec_units = 0;
+}
+
+int batch_fail(esp_batch *b, const char *what, const esp_handle *h)
+{
+    b->err = std::string(what) + (h ? ": " + h->err : std::string());
+    return ESP_ECUDA;
+}
+
+// Record K units of every handle into one graph.  The host counters are put
+// back afterwards; each replay advances them by the recorded deltas.
+int batch_capture(esp_batch *b, int K)
+{
+    batch_drop_graph(b);
+    const size_t n = b->hs.size();
+    std::vector<std::array<int64_t, 4>> base(n);
+    std::vector<long long> hits0(n), launches0(n);
+    for (size_t i = 0; i < n; ++i) {
+        esp_handle *h = b->hs[i];
+        if (!h->run.active) { b->err = "esp_begin has not been called on every handle"; return ESP_ESTATE; }
+        int rc = fold(h);
+        if (rc) return batch_fail(b, "fold", h);
+        if (!h->d_ctr) {
+            if (dalloc(&h->d_ctr, 4) != cudaSuccess) { b->err = "device allocation failed"; return ESP_ENOMEM; }
+            h->ctr_valid = false;
+        }
+        mirrors(h, base[i].data());
+        hits0[i] = h->run.const_hits;
+        launches0[i] = h->launches;
+    }
+    cudaError_t e = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) { b->err = std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e); return ESP_ECUDA; }
+    for (size_t i = 0; i < n; ++i) {
+        b->hs[i]->capturing = true;
+        for (int c = 0; c < 4; ++c) b->hs[i]->cap_base[c] = base[i][c];
+    }
+    int rc = ESP_OK;
+    const esp_handle *bad = nullptr;
+    for (int k = 0; k < K && rc == ESP_OK; ++k)
+        for (size_t i = 0; i < n && rc == ESP_OK; ++i)
+            if ((rc = esp_advance(b->hs[i], 1))) bad = b->hs[i];
+    b->deltas.assign(n, esp_batch::Delta{});
+    for (size_t i = 0; i < n; ++i) {
+        esp_handle *h = b->hs[i];
+        int64_t now[4];
+        mirrors(h, now);
+        unsigned long long d[4];
+        for (int c = 0; c < 4; ++c) {
+            b->deltas[i].c[c] = now[c] - base[i][c];
+            d[c] = (unsigned long long)b->deltas[i].c[c];
+        }
+        if (rc == ESP_OK && launch_bump(h->d_ctr, d, b->st) != cudaSuccess) { rc = ESP_ECUDA; bad = h; }
+        b->deltas[i].const_hits = h->run.const_hits - hits0[i];
+        b->deltas[i].launches = h->launches - launches0[i] + 1;
+        set_mirrors(h, base[i].data());
+        h->run.const_hits = hits0[i];
+        h->launches = launches0[i];
+        h->capturing = false;
+    }
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(b->st, &g);
+    if (rc != ESP_OK || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        if (rc == ESP_OK) b->err = std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e);
+        else batch_fail(b, "capture", bad);
+        return rc == ESP_OK ? ESP_ECUDA : rc;
+    }
+    e = cudaGraphInstantiate(&b->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { b->exec = nullptr; b->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e); return ESP_ECUDA; }
+    b->exec_units = K;
+    return ESP_OK;
+}
+
+int batch_replay(esp_batch *b)
+{
+    for (esp_handle *h : b->hs) {
+        int64_t now[4];
+        mirrors(h, now);
+        bool same = h->ctr_valid;
+        for (int c = 0; c < 4; ++c) same = same && h->ctr_shadow[c] == (unsigned long long)now[c];
+        if (!same) {
+            for (int c = 0; c < 4; ++c) h->ctr_shadow[c] = (unsigned long long)now[c];
+            cudaError_t e = cudaMemcpyAsync(h->d_ctr, h->ctr_shadow, sizeof(h->ctr_shadow), cudaMemcpyHostToDevice, b->st);
+            if (e != cudaSuccess) { b->err = std::string("counter upload: ") + cudaGetErrorString(e); return ESP_ECUDA; }
+            h->ctr_valid = true;
+        }
+    }
+    cudaError_t e = cudaGraphLaunch(b->exec, b->st);
+    if (e != cudaSuccess) { b->err = std::string("cudaGraphLaunch: ") + cudaGetErrorString(e); return ESP_ECUDA; }
+    for (size_t i = 0; i < b->hs.size(); ++i) {
+        esp_handle *h = b->hs[i];
+        int64_t now[4];
+        mirrors(h, now);
+        for (int c = 0; c < 4; ++c) {
+            now[c] += b->deltas[i].c[c];
+            h->ctr_shadow[c] += (unsigned long long)b->deltas[i].c[c];
+        }
+        set_mirrors(h, now);
+        h->run.const_hits += b->deltas[i].const_hits;
+        h->launches += b->deltas[i].launches;
+    }
+    return ESP_OK;
+}
+
+int batch_advance(esp_batch *b, int64_t n)
+{
+    while (n > 0) {
+        if (n >= b->units_per_graph) {
+            if (b->exec_units != b->units_per_graph) {
+                int rc = batch_capture(b, b->units_per_graph);
+                if (rc) return rc;
+            }
+            int rc = batch_replay(b);
+            if (rc) return rc;
+            n -= b->exec_units;
+        } else {
+            for (esp_handle *h : b->hs) {
+                int rc = esp_advance(h, 1);
+                if (rc) return batch_fail(b, "esp_advance", h);
+            }
+            --n;
+        }
+    }
+    return ESP_OK;
+}
+
+// Device time of `units` units of the whole batch (after one untimed unit).
+int batch_time(esp_batch *b, int64_t units, double *us)
+{
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return ESP_ECUDA;
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return ESP_ECUDA; }
+    int rc = batch_advance(b, std::min<int64_t>(units, b->units_per_graph));
+    if (!rc && cudaEventRecord(e0, b->st) != cudaSuccess) rc = ESP_ECUDA;
+    if (!rc) rc = batch_advance(b, units);
+    if (!rc && cudaEventRecord(e1, b->st) != cudaSuccess) rc = ESP_ECUDA;
+    float ms = 0.f;
+    if (!rc && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)) rc = ESP_ECUDA;
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    if (rc == ESP_ECUDA && b->err.empty()) b->err = "event timing failed";
+    *us = 1e3 * (double)ms / (double)units;
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int esp_batch_create(esp_handle *const *handles, int32_t n, void *stream, esp_batch **out)
+{
+    if (!handles || n <= 0 || !out) { set_global_error("esp_batch_create: bad arguments"); return ESP_EINVAL; }
+    *out = nullptr;
+    for (int i = 0; i < n; ++i)
+        if (!handles[i]) { set_global_error("esp_batch_create: null handle"); return ESP_EINVAL; }
+    esp_batch *b = new (std::nothrow) esp_batch();
+    if (!b) { set_global_error("host allocation failed"); return ESP_ENOMEM; }
+    b->hs.assign(handles, handles + n);
+    b->st = (cudaStream_t)stream;
+    if (!b->st) {
+        // graphs cannot be captured on the legacy default stream
+        cudaError_t e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { set_global_error("cudaStreamCreate: %s", cudaGetErrorString(e)); delete b; return ESP_ECUDA; }
+        b->st = b->own;
+    }
+    for (esp_handle *h : b->hs) {
+        b->prev.push_back(h->st);
+        int rc = esp_set_stream(h, (void *)b->st);
+        if (rc) {
+            set_global_error("esp_set_stream: %s", h->err.c_str());
+            for (size_t i = 0; i + 1 < b->prev.size(); ++i) esp_set_stream(b->hs[i], (void *)b->prev[i]);
+            if (b->own) cudaStreamDestroy(b->own);
+            delete b;
+            return rc;
+        }
+    }
+    *out = b;
+    return ESP_OK;
+}
+
+int esp_batch_destroy(esp_batch *b)
+{
+    if (!b) return ESP_EINVAL;
+    if (b->st) cudaStreamSynchronize(b->st);
+    batch_drop_graph(b);
+    for (size_t i = 0; i < b->hs.size(); ++i) esp_set_stream(b->hs[i], (void *)b->prev[i]);
+    if (b->own) cudaStreamDestroy(b->own);
+    delete b;
+    return ESP_OK;
+}
+
+int esp_batch_last_error(const esp_batch *b, char *buf, size_t len)
+{
+    if (!b || !buf || len == 0) return ESP_EINVAL;
+    std::snprintf(buf, len, "%s", b->err.c_str());
+    return ESP_OK;
+}
+
+int esp_batch_set_units_per_graph(esp_batch *b, int32_t units)
+{
+    if (!b || units < 1 || units > 4096) return ESP_EINVAL;
+    if (units != b->units_per_graph) batch_drop_graph(b);
+    b->units_per_graph = units;
+    return ESP_OK;
+}
+
+int esp_batch_advance(esp_batch *b, int64_t units)
+{
+    if (!b || units < 0) return ESP_EINVAL;
+    b->err.clear();
+    return batch_advance(b, units);
+}
+
+int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out)
+{
+    if (!b || units < 1) return ESP_EINVAL;
+    b->err.clear();
+    const size_t n = b->hs.size();
+    // 1. per handle: one colour class per launch (ELL kernel) or every colour
+    //    and sweep of a unit in one launch (cluster-resident kernel)
+    for (size_t i = 0; i < n; ++i) {
+        esp_handle *h = b->hs[i];
+        if (h->proposal != 0) continue;
+        double best = 1e300;
+        int best_kind = 1;
+        const int kinds[2] = {1, 2};
+        for (int kind : kinds) {
+            if (kind == 2 && !h->cluster_ok) continue;
+            int rc = esp_set_sweep_kernel(h, kind);
+            if (rc) return batch_fail(b, "esp_set_sweep_kernel", h);
+            esp_batch one;
+            one.hs.assign(1, h);
+            one.st = b->st;
+            double us = 0.0;
+            rc = batch_time(&one, units, &us);
+            batch_drop_graph(&one);
+            if (rc) { b->err = one.err; return rc; }
+            if (out && out->ell_us && kind == 1) out->ell_us[i] = us;
+            if (out && out->cluster_us && kind == 2) out->cluster_us[i] = us;
+            if (us < best) { best = us; best_kind = kind; }
+        }
+        if (out && out->cluster_us && !h->cluster_ok) out->cluster_us[i] = -1.0;
+        int rc = esp_set_sweep_kernel(h, best_kind);
+        if (rc) return batch_fail(b, "esp_set_sweep_kernel", h);
+        if (out && out->kernel) out->kernel[i] = best_kind;
+    }
+    // 2. units per graph replay
+    const int cands[4] = {1, 2, 4, 8};
+    double best = 1e300;
+    int best_u = 1;
+    for (int c = 0; c < 4; ++c) {
+        esp_batch_set_units_per_graph(b, cands[c]);
+        double us = 0.0;
+        const int64_t t_units = std::max<int64_t>(units, 2 * cands[c]);
+        int rc = batch_time(b, t_units - t_units % cands[c], &us);
+        if (rc) return rc;
+        if (out && out->graph_us) out->graph_us[c] = us;
+        if (us < best) { best = us; best_u = cands[c]; }
+    }
+    esp_batch_set_units_per_graph(b, best_u);
+    if (out) { out->units_per_graph = best_u; out->us_per_unit = best; }
     return ESP_OK;
 }
 

@@ -34,6 +34,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sweep_cluster(const Clus
     const int per_class = Hx * Hy * Hzl;
     const int n_local = per_class * a.nclass;
     const int z0 = rank * a.pz;
+    const unsigned long long sweep_base = a.sweep_base + (a.ctr ? a.ctr[0] : 0ull);
+    const long long meas_base = a.meas_base + (a.ctr ? (long long)a.ctr[2] : 0ll);
 
     // shared memory: stencil copy | P(M) histogram | reduction scratch | spins
     // (stencil_words is a multiple of 4, so every part stays 16-byte aligned)
@@ -78,7 +80,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sweep_cluster(const Clus
 
     for (int m = 0; m < a.n_meas; ++m) {
         for (int sm = 0; sm < a.steps_measure; ++sm) {
-            const unsigned long long sweep = a.sweep_base + (unsigned long long)m * a.steps_measure + sm;
+            const unsigned long long sweep = sweep_base + (unsigned long long)m * a.steps_measure + sm;
             const uint32_t sw_lo = (uint32_t)sweep, sw_hi = (uint32_t)(sweep >> 32);
             // FP32 sums of one sweep, added to the FP64 ones after it
             float fE = 0.f, fX = 0.f, fY = 0.f, fZ = 0.f;
@@ -230,7 +232,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_sweep_cluster(const Clus
                 double *d = a.data + 6 * temp;
                 d[0] += e; d[1] += ee; d[2] += ee * ee;
                 d[3] += am; d[4] += m2; d[5] += m2 * m2;
-                const long long step = a.meas_base + m + 1;
+                const long long step = meas_base + m + 1;
                 if (a.series) {
                     double *o = a.series + (((step - 1) % a.series_cap) * a.R + temp) * 2;
                     o[0] = e; o[1] = am;

@@ -61,6 +61,9 @@ struct ClusterArgs {
     double m_min, m_max;
     // random stream
     unsigned long long sweep_base;
+    // device counters [sweep, swap, measurement, unit] added to sweep_base
+    // and meas_base, or null
+    const unsigned long long *ctr;
     uint32_t key0, key1;
     int mode;
     float tilt;

@@ -113,6 +113,18 @@ struct SweepArgs {
     int32_t mode;
     float tilt;
     uint32_t key0, key1, sw_lo, sw_hi;
+    // device sweep counter added to (sw_hi, sw_lo), or null (replayed graphs
+    // keep their launch arguments and advance the counter instead)
+    const unsigned long long *ctr;
 };
+
+// The sweep index of a launch: the host value plus the device counter.
+__device__ __forceinline__ void sweep_index(const SweepArgs &a, uint32_t &lo, uint32_t &hi)
+{
+    unsigned long long s = ((unsigned long long)a.sw_hi << 32) | a.sw_lo;
+    if (a.ctr) s += *a.ctr;
+    lo = (uint32_t)s;
+    hi = (uint32_t)(s >> 32);
+}
 
 }  // namespace esp

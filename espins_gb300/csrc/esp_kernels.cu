@@ -116,6 +116,8 @@ __global__ void __launch_bounds__(256) k_sweep_ell(const SweepArgs a)
     // FP32 per thread (a few updates each); FP64 from the block sums on
     float accE = 0.f, accX = 0.f, accY = 0.f, accZ = 0.f;
     unsigned int nrej = 0;
+    uint32_t sw_lo, sw_hi;
+    sweep_index(a, sw_lo, sw_hi);
     if (live) {
         const float beta = a.beta[temp];
         const int pstep = (int)(S / R);
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(256) k_sweep_ell(const SweepArgs a)
                     gx += f.x; gy += f.y; gz += f.z;
                 }
             }
-            const Philox4 x = philox4x32_10((uint32_t)orig, (uint32_t)r, a.sw_lo, a.sw_hi, a.key0, a.key1);
+            const Philox4 x = philox4x32_10((uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
             float nx, ny, nz;
             trial_spin(a.mode, a.tilt, __ldg(a.mag + p), ox, oy, oz, x.x, x.y, nx, ny, nz);
             const float dx = nx - ox, dy = ny - oy, dz = nz - oz;
@@ -351,6 +353,7 @@ __global__ void k_measure(MeasureArgs a)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.R) return;
+    if (a.ctr) a.step += (long long)*a.ctr;
     const int r = a.repl_at[t];
     const double e = a.e_run[r];
     const double mx = a.m_run[3 * r] / (double)a.N;
@@ -431,16 +434,30 @@ __global__ void __launch_bounds__(256) k_pm_hist(PmArgs a)
 // ---------------------------------------------------------------------------
 __global__ void k_pt_swap(PtSwapArgs a)
 {
-    // pairs are disjoint, one thread each
-    const int s = a.start0 + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    if (s + 1 >= a.R) return;
+    // pairs are disjoint, one thread each; slots form groups of `group`
+    // consecutive temperatures (independent lattices) and pairs never cross
+    // a group boundary
+    uint32_t idx_lo = a.idx_lo, idx_hi = a.idx_hi;
+    int start0 = a.start0;
+    if (a.ctr) {
+        const unsigned long long idx = (((unsigned long long)a.idx_hi << 32) | a.idx_lo) + a.ctr[1];
+        idx_lo = (uint32_t)idx; idx_hi = (uint32_t)(idx >> 32);
+        start0 = (int)((a.ctr[3] + (unsigned long long)a.unit_off + 1ull) % 2ull);
+    }
+    const int per_group = a.group / 2;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = i / per_group, k = i % per_group;
+    if (g >= a.R / a.group) return;
+    const int sl = start0 + 2 * k;
+    if (sl + 1 >= a.group) return;
+    const int s = g * a.group + sl;
     const int ra = a.repl_at[s], rb = a.repl_at[s + 1];
     const double x = (a.inv_t[s] - a.inv_t[s + 1]) * (a.e_run[ra] - a.e_run[rb]);
     a.num_swaps[2 * s] += 1;
     a.num_swaps[2 * (s + 1)] += 1;
     bool swap = x > 0.0;
     if (!swap) {
-        const Philox4 v = philox4x32_10((uint32_t)s, a.idx_lo, a.idx_hi, 0xFFFFFFFFu, a.key0, a.key1);
+        const Philox4 v = philox4x32_10((uint32_t)s, idx_lo, idx_hi, 0xFFFFFFFFu, a.key0, a.key1);
         swap = u53(v.x, v.y) < exp(x);
     }
     if (swap) {
@@ -590,8 +607,21 @@ cudaError_t launch_pm(const PmArgs &a0, int max_blocks, cudaStream_t st)
 
 cudaError_t launch_pt_swap(const PtSwapArgs &a, cudaStream_t st)
 {
-    const int pairs = (a.R + 1) / 2;
-    k_pt_swap<<<(pairs + 127) / 128, 128, 0, st>>>(a);
+    if (a.group < 2 || a.R % a.group != 0) return a.group == 1 ? cudaSuccess : cudaErrorInvalidValue;
+    const int threads = (a.R / a.group) * (a.group / 2);
+    k_pt_swap<<<(threads + 127) / 128, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+__global__ void k_bump(unsigned long long *ctr, unsigned long long d0, unsigned long long d1, unsigned long long d2,
+                       unsigned long long d3)
+{
+    ctr[0] += d0; ctr[1] += d1; ctr[2] += d2; ctr[3] += d3;
+}
+
+cudaError_t launch_bump(unsigned long long *ctr, const unsigned long long d[4], cudaStream_t st)
+{
+    k_bump<<<1, 1, 0, st>>>(ctr, d[0], d[1], d[2], d[3]);
     return cudaGetLastError();
 }
 

@@ -36,6 +36,7 @@ struct MeasureArgs {
     long long step;           // 1-based measurement index
     double *series;           // [cap][R][2]: (E, |m|) per measurement, or null
     long long series_cap;
+    const unsigned long long *ctr;   // device measurement counter added to step, or null
 };
 
 struct PmArgs {
@@ -53,6 +54,11 @@ struct PtSwapArgs {
     long long *num_swaps;     // [R][2]
     int32_t R, start0;
     uint32_t key0, key1, idx_lo, idx_hi;
+    int32_t group;            // temperatures per independent lattice (R for one lattice)
+    // device counters [sweep, swap, measurement, unit] or null: the swap index
+    // adds ctr[1]; the start pair follows the parity of unit ctr[3] + unit_off
+    const unsigned long long *ctr;
+    int32_t unit_off;
 };
 
 int sweep_blocks(long long max_items, int R, int max_blocks);
@@ -64,6 +70,8 @@ cudaError_t launch_local_terms(const EnergyArgsHost &h, float *g, float *q, cuda
 cudaError_t launch_measure(const MeasureArgs &a, cudaStream_t st);
 cudaError_t launch_pm(const PmArgs &a, int max_blocks, cudaStream_t st);
 cudaError_t launch_pt_swap(const PtSwapArgs &a, cudaStream_t st);
+// ctr[i] += d[i] for the four run counters
+cudaError_t launch_bump(unsigned long long *ctr, const unsigned long long d[4], cudaStream_t st);
 cudaError_t launch_init_spins(const int32_t *perm, const float *mag, float *sx, float *sy, float *sz,
                               int N, int R, int kind, uint64_t seed, cudaStream_t st);
 

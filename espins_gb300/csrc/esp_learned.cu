@@ -157,6 +157,8 @@ __global__ void __launch_bounds__(kLpThreads, 1) k_sweep_lp(const LpSweepArgs la
     const int pstep = (int)(S / R);
     float accE = 0.f, accX = 0.f, accY = 0.f, accZ = 0.f;
     unsigned int nrej = 0;
+    uint32_t sw_lo, sw_hi;
+    sweep_index(a, sw_lo, sw_hi);
     int pi = tid < S ? (int)(tid / R) : a.n_c;
     while (__any_sync(0xffffffffu, pi < a.n_c)) {
         const bool act = pi < a.n_c;
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(kLpThreads, 1) k_sweep_lp(const LpSweepArgs la
             vmf_params(o, fr.kappa0, mix);
             const size_t idx = (size_t)p * R + r;
             const float ox = a.sx[idx], oy = a.sy[idx], oz = a.sz[idx];
-            const Philox4 x = philox4x32_10((uint32_t)orig, (uint32_t)r, a.sw_lo, a.sw_hi, a.key0, a.key1);
+            const Philox4 x = philox4x32_10((uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
             float ux, uy, uz;
             vmf_sample(mix, u24f(x.x), u24f(x.y), u24f(x.z), ux, uy, uz);
             const float nx = mag * (ux * fr.e[0][0] + uy * fr.e[1][0] + uz * fr.e[2][0]);

@@ -48,12 +48,17 @@ def u53(a: int, b: int) -> float:
     return ((a >> 5) * 67108864.0 + (b >> 6)) * (1.0 / 9007199254740992.0)
 
 
-def swap_decisions(start: int, inv_t: np.ndarray, e_slot: np.ndarray, swap_index: int, seed: int) -> List[int]:
-    """Slots s (0-based) whose pair (s, s+1) exchanges, as k_pt_swap decides."""
+def swap_decisions(start: int, inv_t: np.ndarray, e_slot: np.ndarray, swap_index: int, seed: int,
+                   group: int = 0) -> List[int]:
+    """Slots s (0-based) whose pair (s, s+1) exchanges, as k_pt_swap decides.
+    With group > 0 the slots form independent groups of `group` temperatures
+    and pairs stay inside a group."""
     R = len(inv_t)
+    G = group if group > 0 else R
     key = (seed & MASK, (seed >> 32) & MASK)
     out = []
-    for s in range(start - 1, R - 1, 2):
+    pairs = [g * G + s for g in range(R // G) for s in range(start - 1, G - 1, 2)]
+    for s in pairs:
         x = (inv_t[s] - inv_t[s + 1]) * (e_slot[s] - e_slot[s + 1])
         swap = x > 0.0
         if not swap:

@@ -28,6 +28,8 @@ EXPORTED = [
     "esp_lp_num_params", "esp_lp_init_weights", "esp_lp_set_weights", "esp_lp_get_weights", "esp_lp_reserve",
     "esp_lp_collect", "esp_lp_get_data", "esp_lp_train", "esp_lp_loss_grad", "esp_lp_forward",
     "esp_set_proposal", "esp_get_proposal",
+    "esp_set_pt_groups", "esp_batch_create", "esp_batch_destroy", "esp_batch_last_error",
+    "esp_batch_set_units_per_graph", "esp_batch_advance", "esp_batch_tune",
 ]
 
 LP_NUM_PARAMS = 20756
@@ -43,6 +45,11 @@ class EspError(RuntimeError):
 class LpTrainOpts(C.Structure):
     _fields_ = [("steps", C.c_int32), ("batch", C.c_int32), ("lr", C.c_double), ("beta1", C.c_double),
                 ("beta2", C.c_double), ("eps", C.c_double), ("seed", C.c_uint64)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("units_per_graph", C.c_int32), ("us_per_unit", C.c_double), ("kernel", C.c_void_p),
+                ("ell_us", C.c_void_p), ("cluster_us", C.c_void_p), ("graph_us", C.c_void_p)]
 
 
 class Dims(C.Structure):
@@ -142,6 +149,13 @@ def load(build_if_missing: bool = True):
     lib.esp_lp_forward.argtypes = [vp, vp, C.c_int64, vp]
     lib.esp_set_proposal.argtypes = [vp, C.c_int32]
     lib.esp_get_proposal.argtypes = [vp, P(C.c_int32)]
+    lib.esp_set_pt_groups.argtypes = [vp, C.c_int32]
+    lib.esp_batch_create.argtypes = [vp, C.c_int32, vp, P(vp)]
+    lib.esp_batch_destroy.argtypes = [vp]
+    lib.esp_batch_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+    lib.esp_batch_set_units_per_graph.argtypes = [vp, C.c_int32]
+    lib.esp_batch_advance.argtypes = [vp, C.c_int64]
+    lib.esp_batch_tune.argtypes = [vp, C.c_int32, P(BatchTuning)]
     for f in EXPORTED:
         getattr(lib, f).restype = C.c_int
     _lib = lib
@@ -447,6 +461,11 @@ class Engine:
         self._check(self.lib.esp_lp_forward(self.h, _p(f), f.shape[0], _p(out)))
         return out
 
+    def set_pt_groups(self, group_size: int) -> None:
+        """Replica exchange only inside consecutive groups of `group_size`
+        temperature slots (independent lattices of one shape in one handle)."""
+        self._check(self.lib.esp_set_pt_groups(self.h, int(group_size)))
+
     def set_proposal(self, kind: str) -> None:
         """'plain' (the reference's trial moves) or 'learned'."""
         self._check(self.lib.esp_set_proposal(self.h, {"plain": 0, "learned": 1}[kind]))
@@ -465,3 +484,59 @@ class Engine:
         k = C.c_int64()
         self._check(self.lib.esp_launch_count(self.h, C.byref(k)))
         return k.value
+
+
+class Batch:
+    """Handles advanced together by replayed CUDA graphs (``esp_batch``)."""
+
+    def __init__(self, engines, stream_ptr: int = 0):
+        self.lib = load()
+        self.engines = list(engines)
+        arr = (C.c_void_p * len(self.engines))(*[e.h.value for e in self.engines])
+        self._arr = arr
+        b = C.c_void_p()
+        rc = self.lib.esp_batch_create(arr, len(self.engines), C.c_void_p(stream_ptr), C.byref(b))
+        if rc != ESP_OK:
+            raise EspError(rc, last_global_error())
+        self.b = b
+
+    def _check(self, rc: int):
+        if rc != ESP_OK:
+            buf = C.create_string_buffer(1024)
+            self.lib.esp_batch_last_error(self.b, buf, 1024)
+            raise EspError(rc, buf.value.decode())
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.esp_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_units_per_graph(self, units: int) -> None:
+        self._check(self.lib.esp_batch_set_units_per_graph(self.b, int(units)))
+
+    def advance(self, units: int) -> None:
+        self._check(self.lib.esp_batch_advance(self.b, int(units)))
+
+    def tune(self, units: int = 2) -> dict:
+        n = len(self.engines)
+        kern = np.zeros(n, dtype=np.int32)
+        ell = np.zeros(n)
+        clu = np.zeros(n)
+        gr = np.zeros(4)
+        t = BatchTuning(0, 0.0, _p(kern), _p(ell), _p(clu), _p(gr))
+        self._check(self.lib.esp_batch_tune(self.b, int(units), C.byref(t)))
+        return {"units_per_graph": t.units_per_graph, "us_per_unit": t.us_per_unit,
+                "kernel": ["ell" if k == 1 else "cluster" for k in kern], "ell_us": ell.tolist(),
+                "cluster_us": clu.tolist(), "graph_us": dict(zip((1, 2, 4, 8), gr.tolist()))}

@@ -118,3 +118,29 @@ def workload_text(name: str, L: Optional[int] = None, replicas: Optional[int] = 
 
 def workload(name: str, **kw) -> McInput:
     return parse_mcin(workload_text(name, **kw), seedname=name)
+
+
+# ---------------------------------------------------------------------------
+# Many independent lattices: 512 simple-cubic lattices, L drawn uniformly
+# from {8, 12, ..., 48} with seed 3, J1 = +1.0 meV, nearest-neighbour
+# biquadratic 0.1 meV and DM 0.2 meV along the unit bond vector, 16 PT
+# replicas per lattice log-spaced 2-25 K, a swap every 10 sweeps.
+# Lattices of one size share their tables, so they become replica groups of
+# one handle (esp_set_pt_groups); the sizes are the handles of one batch.
+# ---------------------------------------------------------------------------
+BATCH_SIZES = tuple(range(8, 49, 4))
+
+
+def batch_lattice_sizes(count: int = 512, seed: int = 3) -> Dict[int, int]:
+    """L -> number of lattices of that size."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    Ls = rng.choice(np.array(BATCH_SIZES), size=count)
+    return {int(L): int((Ls == L).sum()) for L in BATCH_SIZES if (Ls == L).any()}
+
+
+def batch_lattice_mcin(L: int, replicas: int = 16, steps: Tuple[int, int, int] = (1000, 10000, 1)) -> McInput:
+    """The input of one lattice of the batch (its 16 temperatures)."""
+    text = lattice_mcin(SC, L, [(1e-3, NN)], tem_range=(2.0, 25.0, replicas), tems_mode="log",
+                        biquad=(1e-4, NN), dm=(2e-4, NN), pt=True, pt_steps_swap=10, steps=steps)
+    return parse_mcin(text, seedname=f"batch_L{L}")

@@ -210,6 +210,44 @@ int esp_num_freq(const esp_handle *h, int32_t *nf);
 /* Number of kernels this handle has launched so far. */
 int esp_launch_count(const esp_handle *h, int64_t *count);
 
+/* ---- many independent lattices -------------------------------------------
+ * No counterpart in the reference, which runs one lattice per invocation.
+ * Lattices of the same shape and Hamiltonian share their tables: put them in
+ * one handle as groups of replicas, each group its own temperature set, and
+ * restrict replica exchange to the group (pt.F90:1235-1288 within each
+ * lattice).  Lattices of different shapes live in different handles, which a
+ * batch advances together. */
+int esp_set_pt_groups(esp_handle *h, int32_t group_size);
+
+/* A batch advances every handle (each after its own esp_begin) by whole
+ * measurement units, recording `units_per_graph` units of all handles as one
+ * CUDA graph and replaying it; kernels read their sweep, swap and
+ * measurement indices from per-handle device counters that each replay
+ * advances, so the random stream and the results are those of calling
+ * esp_advance on every handle.  Every handle runs on `stream` (a
+ * cudaStream_t; NULL: a stream the batch creates, since graphs cannot be
+ * captured on the legacy default stream) until esp_batch_destroy gives the
+ * handles their previous streams back. */
+typedef struct esp_batch esp_batch;
+typedef struct {
+    int32_t units_per_graph;      /* chosen */
+    double us_per_unit;           /* device time of one unit of the batch, chosen setting */
+    int32_t *kernel;              /* [n] chosen sweep kernel per handle (1 ELL, 2 cluster), or NULL */
+    double *ell_us, *cluster_us;  /* [n] time per unit of each handle alone (-1: not possible), or NULL */
+    double *graph_us;             /* [4] time per unit with 1, 2, 4, 8 units per graph, or NULL */
+} esp_batch_tuning;
+int esp_batch_create(esp_handle *const *handles, int32_t n, void *stream, esp_batch **out);
+int esp_batch_destroy(esp_batch *b);
+int esp_batch_last_error(const esp_batch *b, char *buf, size_t len);
+int esp_batch_set_units_per_graph(esp_batch *b, int32_t units);
+int esp_batch_advance(esp_batch *b, int64_t units);
+/* Autotuner: times every handle alone with each sweep kernel it supports
+ * (one colour class per launch, or every colour and sweep of a unit per
+ * launch) and keeps the faster, then times the whole batch with 1, 2, 4 and 8
+ * units per graph and keeps the fastest.  It advances every handle by about
+ * 20 * units measurement units, which count as measurements of the run. */
+int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out);
+
 /* ---- learned proposal ------------------------------------------------------
  * No counterpart in the reference (whose trial spins are uniform on the sphere
  * or in a cone, get_quant.F90:80-162).  The trial spin of a site is drawn from
