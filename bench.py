@@ -63,7 +63,7 @@ def _args():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--seed", type=int, default=2)
-    p.add_argument("--proposal", choices=["plain", "compare"], default="plain")
+    p.add_argument("--proposal", choices=["plain", "learned", "compare"], default="plain")
     p.add_argument("--train-pairs", type=int, default=10_000_000)
     p.add_argument("--train-steps", type=int, default=3000)
     p.add_argument("--measure-sweeps", type=int, default=20000)
@@ -84,13 +84,18 @@ def _uniform_spins(R, n, mag, seed):
     return v * mag[None, :, None]
 
 
-def _peaks():
+def _peaks(kind: str = "hbm"):
+    """(peak, source): HBM GB/s, or dense BF16 TFLOP/s (burst) for kind 'tensor'."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
         with open(path) as fh:
             d = json.load(fh)
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        return float(d["hbm_gbs"] if kind == "hbm" else d["bf16_tflops"]), "measured"
+    return (6800.0 if kind == "hbm" else 1900.0), "fallback"
+
+
+# network FLOPs of one learned proposal: 2 (12*128 + 128*128 + 128*20)
+LP_FLOP = 2 * (12 * 128 + 128 * 128 + 128 * 20)
 
 
 class ClockSampler:
@@ -440,6 +445,10 @@ def main():
     eng.upload(ham)
     eng.set_temperatures(inp.tems)
     eng.set_stream(stream.cuda_stream)
+    if a.proposal == "learned":
+        # an untrained network (the learned sampler's cost does not depend on its weights)
+        eng.lp_init(seed=seed)
+        eng.set_proposal("learned")
     _, ncol = eng.colouring()
     mode = 1 if inp.mcarlo_mode.startswith("const") else 0
     total_units = a.warmup + a.steps
@@ -488,14 +497,34 @@ def main():
     sweep_ms = ev0.elapsed_time(ev1)
     per_launch_s = sweep_ms * 1e-3 / sweep_launches
     bytes_per_launch = 24.0 * N * R * nsw / sweep_launches
-    peak, peak_kind = _peaks()
-    achieved = bytes_per_launch / per_launch_s / 1e9
+    if kernel == "learned":
+        flop_per_launch = float(LP_FLOP) * N * R * nsw / sweep_launches
+        peak, peak_kind = _peaks("tensor")
+        achieved = flop_per_launch / per_launch_s / 1e12
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak, "traffic": None, "kernel": "k_sweep_lp",
+                    "flop_per_launch": flop_per_launch, "sweeps_timed": nsw, "launch_us": per_launch_s * 1e6,
+                    "peak_source": peak_kind,
+                    "hbm_equivalent_GBps": bytes_per_launch / per_launch_s / 1e9}
+    else:
+        peak, peak_kind = _peaks()
+        achieved = bytes_per_launch / per_launch_s / 1e9
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": None,
+                    "kernel": "k_sweep_cluster" if kernel == "cluster" else "k_sweep_ell",
+                    "cluster_size": csize if kernel == "cluster" else None,
+                    "bytes_per_launch": bytes_per_launch, "sweeps_timed": nsw,
+                    "launch_us": per_launch_s * 1e6, "peak_source": peak_kind,
+                    "note": "state is L2-resident inside a step (16 MB)"}
 
     # end to end through the C ABI with host buffers
     e2e_steps = max(1, min(a.steps, 50))
     eng2 = Engine(N, ham.num_atoms, ham.supercell, R, inp.boundary_open)
     eng2.upload(ham)
     eng2.set_temperatures(inp.tems)
+    if a.proposal == "learned":
+        eng2.lp_init(seed=seed)
+        eng2.set_proposal("learned")
     sched2 = eng2.schedule(0, e2e_steps * pss, inp.steps_measure, pt=inp.pt, pt_steps_swap=pss, mode=mode,
                            tilt=inp.tilt_angles_max, seed=seed)
     torch.cuda.synchronize(dev)
@@ -527,15 +556,10 @@ def main():
         line = {
             "metric": "site updates/s", "value": value, "unit": "site updates/s", "n_gpus": ws,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * t_max / a.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": _config(inp, ham, a.workload),
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "kernel": "k_sweep_cluster" if kernel == "cluster" else "k_sweep_ell",
-                         "cluster_size": csize if kernel == "cluster" else None,
-                         "bytes_per_launch": bytes_per_launch, "sweeps_timed": nsw,
-                         "launch_us": per_launch_s * 1e6, "peak_source": peak_kind,
-                         "note": "state is L2-resident inside a step (16 MB)"},
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16+f32" if a.proposal == "learned" else "f32",
+            "data": "synthetic", "config": _config(inp, ham, a.workload) | {"proposal": a.proposal},
+            "roofline": roofline,
             "e2e": {"value": e2e_value, "unit": "site updates/s", "h2d_bytes_per_step": h2d / e2e_steps,
                     "d2h_bytes_per_step": d2h / e2e_steps, "steps": e2e_steps,
                     "path": "esp_set_spins + esp_begin + esp_advance + esp_collect + esp_get_spins"},

@@ -671,12 +671,13 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
             }
             hs.colour_start[prep.num_colours] = n;
         }
-        // cluster size (portable, <= 8): slabs of an even number of planes,
-        // shared memory within the per-CTA limit, and the fewest waves of R
-        // clusters as the occupancy calculator counts them, per CTA of work
+        // cluster size (up to 16; above 8 where the GPU allows non-portable
+        // sizes): slabs of an even number of planes, shared memory within the
+        // per-CTA limit, and the fewest waves of R clusters as the occupancy
+        // calculator counts them, per CTA of work
         int best = 0;
         double best_cost = 1e300;
-        for (int cs = 1; cs <= 8 && fits; ++cs) {
+        for (int cs = 1; cs <= 16 && fits; ++cs) {
             if (h->L[2] % (2 * cs) != 0) continue;
             const size_t smem = cluster_smem_bytes(h->N / cs, h->nf, sbytes);
             if (smem > 226 * 1024) continue;

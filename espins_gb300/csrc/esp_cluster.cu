@@ -331,6 +331,10 @@ int cluster_max_active(int csize, size_t smem, int R)
 {
     if (cudaFuncSetAttribute(k_sweep_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return 0;
+    if (csize > 8 && cudaFuncSetAttribute(k_sweep_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(csize * R, 1, 1);
     cfg.blockDim = dim3(kClusterThreads, 1, 1);

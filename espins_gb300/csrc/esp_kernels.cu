@@ -283,18 +283,30 @@ __global__ void __launch_bounds__(256) k_energy_part(const EnergyArgs a)
     }
 }
 
-// Stage 2: out_e[r] = sum over blocks, in block order; out_m[r][3] likewise.
-__global__ void k_energy_reduce(const double *scratch, int nblocks, int R, double *out_e, double *out_m)
+// Stage 2: out_e[r] = sum over blocks, out_m[r][3] likewise.  One block per
+// replica: thread t takes blocks t, t+256, ... and a fixed-shape tree combines
+// the threads, so the sum is deterministic.
+__global__ void __launch_bounds__(256) k_energy_reduce(const double *scratch, int nblocks, int R, double *out_e,
+                                                       double *out_m)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= R) return;
+    __shared__ double s_v[4][256];
+    const int r = blockIdx.x, t = threadIdx.x;
     double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-    for (int b = 0; b < nblocks; ++b) {
+    for (int b = t; b < nblocks; b += blockDim.x) {
         const double *o = scratch + ((size_t)b * R + r) * 4;
         a0 += o[0]; a1 += o[1]; a2 += o[2]; a3 += o[3];
     }
-    out_e[r] = a0;
-    if (out_m) { out_m[3 * r] = a1; out_m[3 * r + 1] = a2; out_m[3 * r + 2] = a3; }
+    s_v[0][t] = a0; s_v[1][t] = a1; s_v[2][t] = a2; s_v[3][t] = a3;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w)
+            for (int c = 0; c < 4; ++c) s_v[c][t] += s_v[c][t + w];
+        __syncthreads();
+    }
+    if (t == 0) {
+        out_e[r] = s_v[0][0];
+        if (out_m) { out_m[3 * r] = s_v[1][0]; out_m[3 * r + 1] = s_v[2][0]; out_m[3 * r + 2] = s_v[3][0]; }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -551,7 +563,7 @@ cudaError_t launch_energy(const EnergyArgsHost &h, double *out_e, double *out_m,
     else k_energy_part<false, false><<<blocks, 256, 0, st>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_energy_reduce<<<(h.R + 127) / 128, 128, 0, st>>>(h.scratch, blocks, h.R, out_e, out_m);
+    k_energy_reduce<<<h.R, 256, 0, st>>>(h.scratch, blocks, h.R, out_e, out_m);
     return cudaGetLastError();
 }
 
