@@ -452,6 +452,14 @@ def main():
     _, ncol = eng.colouring()
     mode = 1 if inp.mcarlo_mode.startswith("const") else 0
     total_units = a.warmup + a.steps
+    # the library's autotuner picks the sweep kernel and cluster geometry on
+    # units that serve as extra warm-up; the run then starts over
+    from espins_gb300.lib import Batch
+    eng.set_spins(spins0)
+    eng.begin(eng.schedule(0, 64 * pss, inp.steps_measure, pt=inp.pt, pt_steps_swap=pss, mode=mode,
+                           tilt=inp.tilt_angles_max, seed=seed + 7))
+    with Batch([eng]) as tb:
+        tuning = tb.tune(units=2)
     sched = eng.schedule(0, total_units * pss, inp.steps_measure, pt=inp.pt, pt_steps_swap=pss, mode=mode,
                          tilt=inp.tilt_angles_max, seed=seed, binning_level=[1, 2, 3, 4, 5])
     eng.set_spins(spins0)
@@ -511,11 +519,13 @@ def main():
         achieved = bytes_per_launch / per_launch_s / 1e9
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "traffic": None,
-                    "kernel": "k_sweep_cluster" if kernel == "cluster" else "k_sweep_ell",
-                    "cluster_size": csize if kernel == "cluster" else None,
+                    "kernel": {"cluster": "k_sweep_cluster", "tile": "k_sweep_tile"}.get(kernel, "k_sweep_ell"),
+                    "cluster_geometry": list(eng.cluster_geometry()) if kernel == "cluster" else None,
+                    "tile_geometry": list(eng.tile_geometry()) if kernel == "tile" else None,
                     "bytes_per_launch": bytes_per_launch, "sweeps_timed": nsw,
                     "launch_us": per_launch_s * 1e6, "peak_source": peak_kind,
-                    "note": "state is L2-resident inside a step (16 MB)"}
+                    "note": (f"state {12 * N * R / 1e6:.0f} MB of spins"
+                             + (" (L2-resident inside a step)" if 12 * N * R < 100e6 else " (HBM-resident)"))}
 
     # end to end through the C ABI with host buffers
     e2e_steps = max(1, min(a.steps, 50))
@@ -525,6 +535,14 @@ def main():
     if a.proposal == "learned":
         eng2.lp_init(seed=seed)
         eng2.set_proposal("learned")
+    elif kernel == "cluster":
+        eng2.set_cluster_geometry(*eng.cluster_geometry())
+        eng2.set_sweep_kernel("cluster")
+    elif kernel == "tile":
+        eng2.set_tile_geometry(*eng.tile_geometry())
+        eng2.set_sweep_kernel("tile")
+    elif kernel == "ell":
+        eng2.set_sweep_kernel("ell")
     sched2 = eng2.schedule(0, e2e_steps * pss, inp.steps_measure, pt=inp.pt, pt_steps_swap=pss, mode=mode,
                            tilt=inp.tilt_angles_max, seed=seed)
     torch.cuda.synchronize(dev)
@@ -564,6 +582,8 @@ def main():
                     "d2h_bytes_per_step": d2h / e2e_steps, "steps": e2e_steps,
                     "path": "esp_set_spins + esp_begin + esp_advance + esp_collect + esp_get_spins"},
             "gpu_launches": int(launches), "colours": ncol,
+            "autotuner": {"kernel": tuning["kernel"][0], "cluster_geometry": tuning["cluster_geometry"][0],
+                          "ell_us_per_unit": tuning["ell_us"][0], "cluster_us_per_unit": tuning["cluster_us"][0]},
             "clocks": clocks,
             "swap_acceptance": float(np.mean(res["num_swaps"][:, 1] / np.maximum(res["num_swaps"][:, 0], 1))),
         }

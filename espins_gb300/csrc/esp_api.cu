@@ -15,6 +15,7 @@
 #include "esp_cluster.h"
 #include "esp_kernels.h"
 #include "esp_learned.h"
+#include "esp_tile.h"
 #include "esp_tables.h"
 #include "esp_errors.h"
 
@@ -66,8 +67,18 @@ struct esp_handle {
     // cluster-resident path (translation-invariant lattices)
     int kernel_choice = 0;          // 0 auto, 1 ELL, 2 cluster
     bool cluster_ok = false;
-    int csize = 0, pz = 0;
+    int csize = 0, pz = 0, cthreads = 512;
     size_t cluster_smem = 0;
+    int cl_maxst = 0;
+    size_t cl_sbytes = 0;
+    // tiled path (translation-invariant lattices with nearest-cell stencils)
+    bool tile_ok = false;
+    int tile_T = 0, tile_G = 0, tile_nt[3] = {0, 0, 0}, ntiles = 0;
+    size_t tile_smem = 0;
+    int4 *d_tile_offs = nullptr;
+    double *d_tile_part = nullptr;
+    unsigned long long *d_tile_rej = nullptr;
+    long long tile_pending = 0;
     double *d_series = nullptr;
     long long series_cap = 0;
     unsigned char *d_stencil_blob = nullptr;
@@ -149,7 +160,9 @@ void free_tables(esp_handle *h)
     dfree(h->d_J); dfree(h->d_B); dfree(h->d_Dx); dfree(h->d_Dy); dfree(h->d_Dz); dfree(h->d_mag);
     dfree(h->d_si); dfree(h->d_fld); dfree(h->d_scratch); dfree(h->d_part); dfree(h->d_part_rej);
     dfree(h->d_stencil_blob); dfree(h->d_nbidx); dfree(h->d_lp_axis);
+    dfree(h->d_tile_offs); dfree(h->d_tile_part); dfree(h->d_tile_rej);
     h->cluster_ok = false;
+    h->tile_ok = false;
 }
 
 void free_lp_batch(esp_handle *h)
@@ -219,6 +232,14 @@ int require(esp_handle *h, bool tables, bool temps)
 // magnetisations and rejected counters (k_fold), in block order.
 int fold(esp_handle *h)
 {
+    if (h->tile_pending > 0) {
+        TileFoldArgs t;
+        t.part = h->d_tile_part; t.part_rej = h->d_tile_rej; t.e_run = h->d_e_run; t.m_run = h->d_m_run;
+        t.rej = h->d_rej; t.temp_of = h->d_temp_of; t.R = h->R; t.ntiles = h->ntiles; t.phase = h->pending_phase;
+        CK(launch_tile_fold(t, h->st));
+        h->launches++;
+        h->tile_pending = 0;
+    }
     if (h->pending_sweeps == 0) return ESP_OK;
     FoldArgs f;
     f.part = h->d_part; f.part_rej = h->d_part_rej; f.e_run = h->d_e_run; f.m_run = h->d_m_run;
@@ -232,7 +253,51 @@ int fold(esp_handle *h)
 
 bool use_cluster(const esp_handle *h)
 {
-    return h->cluster_ok && h->kernel_choice != 1 && h->proposal == 0;
+    return h->cluster_ok && (h->kernel_choice == 0 || h->kernel_choice == 2) && h->proposal == 0;
+}
+
+// the tiled kernel: when chosen, or by default where no cluster fits
+bool use_tile(const esp_handle *h)
+{
+    return h->tile_ok && h->proposal == 0 &&
+           (h->kernel_choice == 4 || (h->kernel_choice == 0 && !h->cluster_ok));
+}
+
+// n sweeps of eight tile-parity launches each
+int tile_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o)
+{
+    const int phase = o->phase ? 1 : 0;
+    if (phase != h->pending_phase) {
+        int rc = fold(h);
+        if (rc) return rc;
+        h->pending_phase = phase;
+    }
+    TileArgs a;
+    a.stencil = reinterpret_cast<const ClusterStencil *>(h->d_stencil_blob);
+    a.offs = h->d_tile_offs;
+    a.maxst = h->cl_maxst;
+    for (int at = 0; at < kMaxClusterAtoms; ++at)
+        a.count[at] = at < h->na ? (int)h->prep.stencil[at].size() : 0;
+    a.Lx = h->L[0]; a.Ly = h->L[1]; a.Lz = h->L[2]; a.na = h->na; a.N = h->N; a.R = h->R;
+    a.T = h->tile_T; a.G = h->tile_G;
+    a.ntx = h->tile_nt[0]; a.nty = h->tile_nt[1]; a.ntz = h->tile_nt[2];
+    a.has_b = h->prep.has_b; a.has_d = h->prep.has_d; a.has_si = h->hsi; a.has_f = h->hfld;
+    a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz; a.inv = h->d_inv;
+    a.temp_of = h->d_temp_of; a.beta = h->d_beta;
+    a.part = h->d_tile_part; a.part_rej = h->d_tile_rej;
+    a.key0 = (uint32_t)o->seed; a.key1 = (uint32_t)(o->seed >> 32);
+    a.mode = o->mcarlo_mode ? 1 : 0; a.tilt = (float)o->tilt_angles_max;
+    a.ctr = h->capturing ? h->d_ctr : nullptr;
+    for (int64_t w = 0; w < n; ++w) {
+        a.sweep = (unsigned long long)(first + w - (h->capturing ? h->cap_base[0] : 0));
+        for (int ph = 0; ph < 8; ++ph) {
+            a.phase = ph;
+            CK(launch_tile(a, h->tile_smem, h->st));
+            h->launches++;
+        }
+        h->tile_pending++;
+    }
+    return ESP_OK;
 }
 
 // One launch of the cluster-resident kernel: n_meas units of steps_measure
@@ -267,7 +332,7 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     a.sweep_base = (unsigned long long)first;
     a.key0 = (uint32_t)o->seed; a.key1 = (uint32_t)(o->seed >> 32);
     a.mode = o->mcarlo_mode ? 1 : 0; a.tilt = (float)o->tilt_angles_max;
-    CK(launch_cluster(a, h->csize, h->cluster_smem, h->st));
+    CK(launch_cluster(a, h->csize, h->cthreads, h->cluster_smem, h->st));
     h->launches++;
     return ESP_OK;
 }
@@ -313,6 +378,7 @@ int do_sweep_colour(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o
 int do_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o)
 {
     if (use_cluster(h)) return cluster_sweeps(h, n, first, o);
+    if (use_tile(h)) return tile_sweeps(h, n, first, o);
     for (int64_t w = 0; w < n; ++w) {
         for (int c = 0; c < h->prep.num_colours; ++c) {
             int rc = do_sweep_colour(h, c, first + w, o);
@@ -441,6 +507,159 @@ int d2h(esp_handle *h, void *dst, const void *src, size_t bytes)
 {
     CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
+    return ESP_OK;
+}
+
+// Cluster geometries the GPU can run, cheapest first by a model: cs CTAs of
+// nt threads per replica, slabs of an even number of z planes, shared memory
+// within the per-CTA limit; cost = waves of R clusters (occupancy calculator)
+// x sites one SM holds per wave.
+struct ClusterGeom {
+    int cs, nt;
+    double cost;
+};
+
+std::vector<ClusterGeom> cluster_candidates(const esp_handle *h)
+{
+    std::vector<ClusterGeom> out;
+    if (!h->d_stencil_blob) return out;
+    const int nts[2] = {512, 256};
+    for (int nt : nts)
+        for (int cs = 1; cs <= 16; ++cs) {
+            if (h->L[2] % (2 * cs) != 0) continue;
+            const size_t smem = cluster_smem_bytes(h->N / cs, h->nf, h->cl_sbytes);
+            if (smem > 226 * 1024) continue;
+            const int active = cluster_max_active(cs, nt, smem, h->R);
+            if (active <= 0) continue;
+            const double waves = std::ceil((double)h->R / (double)active);
+            const double conc = (double)std::min(h->R, active) * cs;
+            const double per_sm = std::ceil(conc / (double)std::max(1, h->num_sms));
+            out.push_back({cs, nt, waves * ((double)h->N / cs) * per_sm});
+        }
+    std::stable_sort(out.begin(), out.end(), [](const ClusterGeom &a, const ClusterGeom &b) { return a.cost < b.cost; });
+    return out;
+}
+
+// Tile geometries (edge T cells, G replicas per CTA), cheapest first by a
+// model: HBM bytes per site update 12 ((T+2)^3/T^3 + 1), divided by the
+// 32-byte-sector use of G contiguous replicas, and scaled up when one launch
+// has fewer than two CTAs per SM.  Shared memory stays within two CTAs per SM.
+struct TileGeom {
+    int T, G;
+    double cost;
+};
+
+std::vector<TileGeom> tile_candidates(const esp_handle *h)
+{
+    std::vector<TileGeom> out;
+    if (!h->d_tile_offs) return out;
+    const int Gs[5] = {16, 8, 4, 2, 1};
+    for (int T = 2; T <= 32; T += 2) {
+        if (h->L[0] % (2 * T) || h->L[1] % (2 * T) || h->L[2] % (2 * T)) continue;
+        const int ntiles = (h->L[0] / T) * (h->L[1] / T) * (h->L[2] / T);
+        for (int G : Gs) {
+            if (h->R % G || 256 % G) continue;
+            const size_t smem = tile_smem_bytes(T, G, h->na, h->cl_maxst);
+            if (smem > 113 * 1024) continue;
+            const double b = (double)(T + 2) / T;
+            double cost = 12.0 * (b * b * b + 1.0) / std::min(1.0, G / 8.0);
+            const double ctas = (double)(ntiles / 8) * (h->R / G);
+            if (ctas < 2.0 * h->num_sms) cost *= 2.0 * h->num_sms / ctas;
+            out.push_back({T, G, cost});
+        }
+    }
+    std::stable_sort(out.begin(), out.end(), [](const TileGeom &a, const TileGeom &b) { return a.cost < b.cost; });
+    return out;
+}
+
+int tile_geometry(esp_handle *h, int T, int G)
+{
+    const size_t smem = tile_smem_bytes(T, G, h->na, h->cl_maxst);
+    CK(tile_configure(smem));
+    CK(cudaStreamSynchronize(h->st));
+    int rc = fold(h);
+    if (rc) return rc;
+    const int nt[3] = {h->L[0] / T, h->L[1] / T, h->L[2] / T};
+    const int ntiles = nt[0] * nt[1] * nt[2];
+    if (ntiles != h->ntiles) {
+        dfree(h->d_tile_part); dfree(h->d_tile_rej);
+        CK(dalloc(&h->d_tile_part, (size_t)ntiles * h->R * 4));
+        CK(dalloc(&h->d_tile_rej, (size_t)ntiles * h->R));
+        CK(cudaMemsetAsync(h->d_tile_part, 0, sizeof(double) * 4 * (size_t)ntiles * h->R, h->st));
+        CK(cudaMemsetAsync(h->d_tile_rej, 0, sizeof(unsigned long long) * (size_t)ntiles * h->R, h->st));
+    }
+    h->tile_T = T; h->tile_G = G;
+    for (int d = 0; d < 3; ++d) h->tile_nt[d] = nt[d];
+    h->ntiles = ntiles;
+    h->tile_smem = smem;
+    h->tile_ok = true;
+    return ESP_OK;
+}
+
+// Stencil offsets of the tiled path, if every entry stays within one cell.
+int tile_setup(esp_handle *h)
+{
+    const int maxst = h->cl_maxst;
+    std::vector<int4> offs((size_t)h->na * maxst, make_int4(0, 0, 0, 0));
+    for (int at = 0; at < h->na; ++at) {
+        const auto &lst = h->prep.stencil[at];
+        for (size_t e = 0; e < lst.size(); ++e) {
+            const StencilEntry &x = lst[e];
+            if (std::abs(x.dx) > 1 || std::abs(x.dy) > 1 || std::abs(x.dz) > 1) return ESP_OK;
+            offs[(size_t)at * maxst + e] = make_int4(x.dx, x.dy, x.dz, x.b);
+        }
+    }
+    CK(dalloc(&h->d_tile_offs, offs.size()));
+    int rc = h2d(h, h->d_tile_offs, offs.data(), sizeof(int4) * offs.size());
+    if (rc) return rc;
+    const std::vector<TileGeom> c = tile_candidates(h);
+    if (c.empty()) return ESP_OK;
+    return tile_geometry(h, c[0].T, c[0].G);
+}
+
+// Set up the cluster path for cs CTAs of nt threads: slab height, shared
+// memory, the neighbour table of every CTA rank.
+int cluster_geometry(esp_handle *h, int cs, int nt)
+{
+    const int maxst = h->cl_maxst;
+    const int pz = h->L[2] / cs, n_local = h->N / cs;
+    const size_t smem = cluster_smem_bytes(n_local, h->nf, h->cl_sbytes);
+    CK(cluster_configure(smem, cs, nt));
+    const int Lx = h->L[0], Ly = h->L[1], Lz = h->L[2], Hx = Lx / 2, Hy = Ly / 2, Hzl = pz / 2;
+    const int per_class = Hx * Hy * Hzl;
+    // (owner rank << 24) | local index of stencil entry e of local site l on rank q
+    std::vector<uint32_t> tab((size_t)cs * maxst * n_local);
+    for (int q = 0; q < cs; ++q)
+        for (int l = 0; l < n_local; ++l) {
+            const int k = l / per_class, rem = l % per_class;
+            const int hx = rem % Hx, hy = (rem / Hx) % Hy, hzl = rem / (Hx * Hy);
+            const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pzb = k & 1;
+            const int x = 2 * hx + px, y = 2 * hy + py, z = q * pz + 2 * hzl + pzb;
+            const auto &lst = h->prep.stencil[at];
+            for (int e = 0; e < maxst; ++e) {
+                uint32_t v = ((uint32_t)q << 24) | (uint32_t)l;  // padding: the site itself
+                if (e < (int)lst.size()) {
+                    const StencilEntry &se = lst[e];
+                    const int xn = ((x + se.dx) % Lx + Lx) % Lx, yn = ((y + se.dy) % Ly + Ly) % Ly;
+                    const int zn = ((z + se.dz) % Lz + Lz) % Lz;
+                    const int kn = (se.b << 3) | ((xn & 1) << 2) | ((yn & 1) << 1) | (zn & 1);
+                    const int rn = zn / pz;
+                    const int ln = kn * per_class + ((((zn - rn * pz) >> 1) * Hy + (yn >> 1)) * Hx + (xn >> 1));
+                    v = ((uint32_t)rn << 24) | (uint32_t)ln;
+                }
+                tab[((size_t)q * maxst + e) * n_local + l] = v;
+            }
+        }
+    CK(cudaStreamSynchronize(h->st));
+    dfree(h->d_nbidx);
+    CK(dalloc(&h->d_nbidx, tab.size()));
+    int rc = h2d(h, h->d_nbidx, tab.data(), sizeof(uint32_t) * tab.size());
+    if (rc) return rc;
+    h->csize = cs;
+    h->cthreads = nt;
+    h->pz = pz;
+    h->cluster_smem = smem;
+    h->cluster_ok = true;
     return ESP_OK;
 }
 
@@ -671,59 +890,12 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
             }
             hs.colour_start[prep.num_colours] = n;
         }
-        // cluster size (up to 16; above 8 where the GPU allows non-portable
-        // sizes): slabs of an even number of planes, shared memory within the
-        // per-CTA limit, and the fewest waves of R clusters as the occupancy
-        // calculator counts them, per CTA of work
-        int best = 0;
-        double best_cost = 1e300;
-        for (int cs = 1; cs <= 16 && fits; ++cs) {
-            if (h->L[2] % (2 * cs) != 0) continue;
-            const size_t smem = cluster_smem_bytes(h->N / cs, h->nf, sbytes);
-            if (smem > 226 * 1024) continue;
-            const int active = cluster_max_active(cs, smem, h->R);
-            if (active <= 0) continue;
-            const double waves = std::ceil((double)h->R / (double)active);
-            const double cost = waves / cs;
-            if (cost < best_cost - 1e-12) { best_cost = cost; best = cs; }
-        }
-        if (fits && best > 0) {
-            h->csize = best;
-            h->pz = h->L[2] / best;
-            h->cluster_smem = cluster_smem_bytes(h->N / best, h->nf, sbytes);
+        if (fits) {
+            h->cl_maxst = maxst;
+            h->cl_sbytes = sbytes;
             h->stencil_words = (int)(sbytes / 4);
             CK(dalloc(&h->d_stencil_blob, sbytes));
             if ((rc = h2d(h, h->d_stencil_blob, blob.data(), sbytes))) return rc;
-            CK(cluster_configure(h->cluster_smem, best));
-            // neighbour table of every CTA rank: (owner rank << 24) | local index
-            const int cs = best, pz = h->pz, n_local = h->N / cs;
-            const int Lx = h->L[0], Ly = h->L[1], Lz = h->L[2], Hx = Lx / 2, Hy = Ly / 2, Hzl = pz / 2;
-            const int per_class = Hx * Hy * Hzl;
-            std::vector<uint32_t> tab((size_t)cs * maxst * n_local);
-            for (int q = 0; q < cs; ++q)
-                for (int l = 0; l < n_local; ++l) {
-                    const int k = l / per_class, rem = l % per_class;
-                    const int hx = rem % Hx, hy = (rem / Hx) % Hy, hzl = rem / (Hx * Hy);
-                    const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pzb = k & 1;
-                    const int x = 2 * hx + px, y = 2 * hy + py, z = q * pz + 2 * hzl + pzb;
-                    const auto &lst = prep.stencil[at];
-                    for (int e = 0; e < maxst; ++e) {
-                        uint32_t v = ((uint32_t)q << 24) | (uint32_t)l;  // padding: the site itself
-                        if (e < (int)lst.size()) {
-                            const StencilEntry &se = lst[e];
-                            const int xn = ((x + se.dx) % Lx + Lx) % Lx, yn = ((y + se.dy) % Ly + Ly) % Ly;
-                            const int zn = ((z + se.dz) % Lz + Lz) % Lz;
-                            const int kn = (se.b << 3) | ((xn & 1) << 2) | ((yn & 1) << 1) | (zn & 1);
-                            const int rn = zn / pz;
-                            const int ln = kn * per_class + ((((zn - rn * pz) >> 1) * Hy + (yn >> 1)) * Hx + (xn >> 1));
-                            v = ((uint32_t)rn << 24) | (uint32_t)ln;
-                        }
-                        tab[((size_t)q * maxst + e) * n_local + l] = v;
-                    }
-                }
-            CK(dalloc(&h->d_nbidx, tab.size()));
-            if ((rc = h2d(h, h->d_nbidx, tab.data(), sizeof(uint32_t) * tab.size()))) return rc;
-            h->cluster_ok = true;
         }
     }
     h->e_blocks = energy_blocks(h->N, h->R, h->max_blocks);
@@ -731,6 +903,12 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
     dfree(h->d_pm);
     CK(dalloc(&h->d_pm, (size_t)h->R * h->nf));
     h->prep = std::move(prep);
+    h->ntiles = 0;
+    if (h->d_stencil_blob) {
+        const std::vector<ClusterGeom> c = cluster_candidates(h);
+        if (!c.empty() && (rc = cluster_geometry(h, c[0].cs, c[0].nt))) return rc;
+        if ((rc = tile_setup(h))) return rc;
+    }
     h->have_tables = true;
     return ESP_OK;
 }
@@ -1002,9 +1180,14 @@ int esp_get_series(esp_handle *h, double *out, int64_t *count)
 
 int esp_set_sweep_kernel(esp_handle *h, int32_t kind)
 {
-    if (!h || kind < 0 || kind > 2) return ESP_EINVAL;
+    if (!h || kind < 0 || kind > 4 || kind == 3) return ESP_EINVAL;
     if (kind == 2 && !h->cluster_ok) {
         h->err = "the cluster-resident sweep needs a periodic, translation-invariant lattice that fits a cluster";
+        return ESP_EINVAL;
+    }
+    if (kind == 4 && !h->tile_ok) {
+        h->err = "the tiled sweep needs a periodic, translation-invariant lattice with nearest-cell couplings "
+                 "and even tile counts";
         return ESP_EINVAL;
     }
     int rc = fold(h);
@@ -1013,10 +1196,52 @@ int esp_set_sweep_kernel(esp_handle *h, int32_t kind)
     return ESP_OK;
 }
 
+int esp_set_tile_geometry(esp_handle *h, int32_t tile, int32_t replicas)
+{
+    if (!h) return ESP_EINVAL;
+    for (const TileGeom &g : tile_candidates(h))
+        if (g.T == tile && g.G == replicas) return tile_geometry(h, tile, replicas);
+    h->err = "tile geometry not possible for this lattice";
+    return ESP_EINVAL;
+}
+
+int esp_get_tile_geometry(const esp_handle *h, int32_t *tile, int32_t *replicas)
+{
+    if (!h || !tile || !replicas) return ESP_EINVAL;
+    *tile = h->tile_ok ? h->tile_T : 0;
+    *replicas = h->tile_ok ? h->tile_G : 0;
+    return ESP_OK;
+}
+
+int esp_set_cluster_geometry(esp_handle *h, int32_t cluster_size, int32_t threads)
+{
+    if (!h) return ESP_EINVAL;
+    if (!h->have_tables || !h->d_stencil_blob) {
+        h->err = "the cluster-resident sweep needs a periodic, translation-invariant lattice that fits a cluster";
+        return ESP_EINVAL;
+    }
+    for (const ClusterGeom &g : cluster_candidates(h))
+        if (g.cs == cluster_size && g.nt == threads) {
+            int rc = fold(h);
+            if (rc) return rc;
+            return cluster_geometry(h, cluster_size, threads);
+        }
+    h->err = "cluster geometry not possible for this lattice on this GPU";
+    return ESP_EINVAL;
+}
+
+int esp_get_cluster_geometry(const esp_handle *h, int32_t *cluster_size, int32_t *threads)
+{
+    if (!h || !cluster_size || !threads) return ESP_EINVAL;
+    *cluster_size = h->cluster_ok ? h->csize : 0;
+    *threads = h->cluster_ok ? h->cthreads : 0;
+    return ESP_OK;
+}
+
 int esp_get_sweep_kernel(const esp_handle *h, int32_t *kind, int32_t *cluster_size)
 {
     if (!h || !kind) return ESP_EINVAL;
-    *kind = h->proposal == 1 ? 3 : use_cluster(h) ? 2 : 1;
+    *kind = h->proposal == 1 ? 3 : use_cluster(h) ? 2 : use_tile(h) ? 4 : 1;
     if (cluster_size) *cluster_size = h->cluster_ok ? h->csize : 0;
     return ESP_OK;
 }
@@ -1851,17 +2076,29 @@ int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out)
     b->err.clear();
     const size_t n = b->hs.size();
     // 1. per handle: one colour class per launch (ELL kernel) or every colour
-    //    and sweep of a unit in one launch (cluster-resident kernel)
+    //    and sweep of a unit in one launch (cluster-resident kernel) with the
+    //    model's three best cluster geometries (CTAs per cluster, threads per CTA)
     for (size_t i = 0; i < n; ++i) {
         esp_handle *h = b->hs[i];
         if (h->proposal != 0) continue;
-        double best = 1e300;
-        int best_kind = 1;
-        const int kinds[2] = {1, 2};
-        for (int kind : kinds) {
-            if (kind == 2 && !h->cluster_ok) continue;
-            int rc = esp_set_sweep_kernel(h, kind);
-            if (rc) return batch_fail(b, "esp_set_sweep_kernel", h);
+        struct Cand { int kind, cs, nt; };
+        std::vector<Cand> cands{{1, 0, 0}};
+        if (h->cluster_ok) {
+            const std::vector<ClusterGeom> g = cluster_candidates(h);
+            for (size_t k = 0; k < g.size() && k < 3; ++k) cands.push_back({2, g[k].cs, g[k].nt});
+        }
+        if (h->tile_ok) {
+            // kind 4: cs, nt carry the tile edge and the replicas per CTA
+            const std::vector<TileGeom> g = tile_candidates(h);
+            for (size_t k = 0; k < g.size() && k < 2; ++k) cands.push_back({4, g[k].T, g[k].G});
+        }
+        double best = 1e300, best_cl = 1e300;
+        Cand pick{1, 0, 0};
+        for (const Cand &c : cands) {
+            int rc = ESP_OK;
+            if (c.kind == 2 && (rc = cluster_geometry(h, c.cs, c.nt))) return batch_fail(b, "cluster geometry", h);
+            if (c.kind == 4 && (rc = tile_geometry(h, c.cs, c.nt))) return batch_fail(b, "tile geometry", h);
+            if ((rc = esp_set_sweep_kernel(h, c.kind))) return batch_fail(b, "esp_set_sweep_kernel", h);
             esp_batch one;
             one.hs.assign(1, h);
             one.st = b->st;
@@ -1869,14 +2106,18 @@ int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out)
             rc = batch_time(&one, units, &us);
             batch_drop_graph(&one);
             if (rc) { b->err = one.err; return rc; }
-            if (out && out->ell_us && kind == 1) out->ell_us[i] = us;
-            if (out && out->cluster_us && kind == 2) out->cluster_us[i] = us;
-            if (us < best) { best = us; best_kind = kind; }
+            if (out && out->ell_us && c.kind == 1) out->ell_us[i] = us;
+            if (c.kind != 1) best_cl = std::min(best_cl, us);
+            if (us < best) { best = us; pick = c; }
         }
-        if (out && out->cluster_us && !h->cluster_ok) out->cluster_us[i] = -1.0;
-        int rc = esp_set_sweep_kernel(h, best_kind);
-        if (rc) return batch_fail(b, "esp_set_sweep_kernel", h);
-        if (out && out->kernel) out->kernel[i] = best_kind;
+        if (out && out->cluster_us) out->cluster_us[i] = cands.size() > 1 ? best_cl : -1.0;
+        int rc = ESP_OK;
+        if (pick.kind == 2 && (rc = cluster_geometry(h, pick.cs, pick.nt))) return batch_fail(b, "cluster geometry", h);
+        if (pick.kind == 4 && (rc = tile_geometry(h, pick.cs, pick.nt))) return batch_fail(b, "tile geometry", h);
+        if ((rc = esp_set_sweep_kernel(h, pick.kind))) return batch_fail(b, "esp_set_sweep_kernel", h);
+        if (out && out->kernel) out->kernel[i] = pick.kind;
+        if (out && out->cluster_size) out->cluster_size[i] = h->cluster_ok ? h->csize : 0;
+        if (out && out->cluster_threads) out->cluster_threads[i] = h->cluster_ok ? h->cthreads : 0;
     }
     // 2. units per graph replay
     const int cands[4] = {1, 2, 4, 8};

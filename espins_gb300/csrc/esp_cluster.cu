@@ -23,7 +23,10 @@ namespace cg = cooperative_groups;
 
 namespace esp {
 
-__global__ void __launch_bounds__(kClusterThreads, 1) k_sweep_cluster(const ClusterArgs a)
+// NT threads per CTA: 512 (one CTA per SM) or 256 (two per SM), both within
+// 128 registers per thread.
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArgs a)
 {
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
@@ -319,25 +322,39 @@ size_t cluster_smem_bytes(int n_local, int nf, size_t stencil_bytes)
            (size_t)136 * sizeof(double) + (size_t)3 * n_local * sizeof(float);
 }
 
-cudaError_t cluster_configure(size_t smem, int csize)
+namespace {
+
+using ClusterKernel = void (*)(ClusterArgs);
+
+ClusterKernel cluster_kernel(int nt) { return nt == 256 ? k_sweep_cluster<256> : k_sweep_cluster<512>; }
+
+}  // namespace
+
+cudaError_t cluster_configure(size_t smem, int csize, int nt)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_sweep_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nt != 256 && nt != 512) return cudaErrorInvalidValue;
+    const ClusterKernel k = cluster_kernel(nt);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    if (csize > 8) e = cudaFuncSetAttribute(k_sweep_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (csize > 8) e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     return e;
 }
 
-int cluster_max_active(int csize, size_t smem, int R)
+int cluster_max_active(int csize, int nt, size_t smem, int R)
 {
-    if (cudaFuncSetAttribute(k_sweep_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    if (nt != 256 && nt != 512) return 0;
+    const ClusterKernel k = cluster_kernel(nt);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
         return 0;
-    if (csize > 8 && cudaFuncSetAttribute(k_sweep_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    }
+    if (csize > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(csize * R, 1, 1);
-    cfg.blockDim = dim3(kClusterThreads, 1, 1);
+    cfg.blockDim = dim3(nt, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -347,18 +364,19 @@ int cluster_max_active(int csize, size_t smem, int R)
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, k_sweep_cluster, &cfg) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
     return n;
 }
 
-cudaError_t launch_cluster(const ClusterArgs &a, int csize, size_t smem, cudaStream_t st)
+cudaError_t launch_cluster(const ClusterArgs &a, int csize, int nt, size_t smem, cudaStream_t st)
 {
+    if (nt != 256 && nt != 512) return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(csize * a.R, 1, 1);
-    cfg.blockDim = dim3(kClusterThreads, 1, 1);
+    cfg.blockDim = dim3(nt, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
@@ -368,7 +386,7 @@ cudaError_t launch_cluster(const ClusterArgs &a, int csize, size_t smem, cudaStr
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_sweep_cluster, a);
+    return cudaLaunchKernelEx(&cfg, cluster_kernel(nt), a);
 }
 
 }  // namespace esp

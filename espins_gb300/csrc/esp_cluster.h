@@ -70,9 +70,10 @@ struct ClusterArgs {
 };
 
 size_t cluster_smem_bytes(int n_local, int nf, size_t stencil_bytes);
-cudaError_t cluster_configure(size_t smem, int csize);
-// Clusters of csize CTAs with `smem` bytes each that fit on the GPU at once.
-int cluster_max_active(int csize, size_t smem, int R);
-cudaError_t launch_cluster(const ClusterArgs &a, int csize, size_t smem, cudaStream_t st);
+// nt: threads per CTA, 256 or 512
+cudaError_t cluster_configure(size_t smem, int csize, int nt);
+// Clusters of csize CTAs of nt threads with `smem` bytes each that fit on the GPU at once.
+int cluster_max_active(int csize, int nt, size_t smem, int R);
+cudaError_t launch_cluster(const ClusterArgs &a, int csize, int nt, size_t smem, cudaStream_t st);
 
 }  // namespace esp

@@ -1,0 +1,50 @@
+// Tiled sweep kernel (esp_tile.cu): arguments and launchers.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "esp_cluster.h"
+#include "esp_device.cuh"
+
+namespace esp {
+
+struct TileArgs {
+    const ClusterStencil *stencil;  // device copy of the cluster path's stencil (header + entries)
+    const int4 *offs;               // [na][maxst]: (dx, dy, dz, target atom) in cells
+    int maxst;
+    int count[kMaxClusterAtoms];    // entries of each atom's list
+    int Lx, Ly, Lz, na, N, R;
+    int T, G;                       // tile edge (cells, even), replicas per CTA
+    int ntx, nty, ntz;              // tiles per axis (even)
+    int phase;                      // tile parity: bit 0 x, bit 1 y, bit 2 z
+    int has_b, has_d, has_si, has_f;
+    float *sx, *sy, *sz;
+    const int32_t *inv;             // reference site -> p
+    const int32_t *temp_of;
+    const float *beta;
+    double *part;                   // [tiles][R][4]: dE, dMx, dMy, dMz
+    unsigned long long *part_rej;   // [tiles][R]
+    unsigned long long sweep;
+    const unsigned long long *ctr;  // device sweep counter added to sweep, or null
+    uint32_t key0, key1;
+    int mode;
+    float tilt;
+};
+
+struct TileFoldArgs {
+    double *part;
+    unsigned long long *part_rej;
+    double *e_run, *m_run;
+    unsigned long long *rej;
+    const int32_t *temp_of;
+    int R, ntiles, phase;
+};
+
+size_t tile_smem_bytes(int T, int G, int na, int maxst);
+cudaError_t tile_configure(size_t smem);
+// one launch = the tiles of one parity (a.phase); eight make a sweep
+cudaError_t launch_tile(const TileArgs &a, size_t smem, cudaStream_t st);
+cudaError_t launch_tile_fold(const TileFoldArgs &a, cudaStream_t st);
+
+}  // namespace esp

@@ -28,7 +28,8 @@ EXPORTED = [
     "esp_lp_num_params", "esp_lp_init_weights", "esp_lp_set_weights", "esp_lp_get_weights", "esp_lp_reserve",
     "esp_lp_collect", "esp_lp_get_data", "esp_lp_train", "esp_lp_loss_grad", "esp_lp_forward",
     "esp_set_proposal", "esp_get_proposal",
-    "esp_set_pt_groups", "esp_batch_create", "esp_batch_destroy", "esp_batch_last_error",
+    "esp_set_pt_groups", "esp_set_cluster_geometry", "esp_get_cluster_geometry",
+    "esp_set_tile_geometry", "esp_get_tile_geometry", "esp_batch_create", "esp_batch_destroy", "esp_batch_last_error",
     "esp_batch_set_units_per_graph", "esp_batch_advance", "esp_batch_tune",
 ]
 
@@ -49,7 +50,8 @@ class LpTrainOpts(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("units_per_graph", C.c_int32), ("us_per_unit", C.c_double), ("kernel", C.c_void_p),
-                ("ell_us", C.c_void_p), ("cluster_us", C.c_void_p), ("graph_us", C.c_void_p)]
+                ("ell_us", C.c_void_p), ("cluster_us", C.c_void_p), ("graph_us", C.c_void_p),
+                ("cluster_size", C.c_void_p), ("cluster_threads", C.c_void_p)]
 
 
 class Dims(C.Structure):
@@ -150,6 +152,10 @@ def load(build_if_missing: bool = True):
     lib.esp_set_proposal.argtypes = [vp, C.c_int32]
     lib.esp_get_proposal.argtypes = [vp, P(C.c_int32)]
     lib.esp_set_pt_groups.argtypes = [vp, C.c_int32]
+    lib.esp_set_cluster_geometry.argtypes = [vp, C.c_int32, C.c_int32]
+    lib.esp_set_tile_geometry.argtypes = [vp, C.c_int32, C.c_int32]
+    lib.esp_get_tile_geometry.argtypes = [vp, P(C.c_int32), P(C.c_int32)]
+    lib.esp_get_cluster_geometry.argtypes = [vp, P(C.c_int32), P(C.c_int32)]
     lib.esp_batch_create.argtypes = [vp, C.c_int32, vp, P(vp)]
     lib.esp_batch_destroy.argtypes = [vp]
     lib.esp_batch_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
@@ -401,15 +407,16 @@ class Engine:
         return out
 
     def set_sweep_kernel(self, kind: str) -> None:
-        """'auto', 'ell' (any lattice) or 'cluster' (translation-invariant, cluster-resident)."""
-        k = {"auto": 0, "ell": 1, "cluster": 2}[kind]
+        """'auto', 'ell' (any lattice), 'cluster' (translation-invariant, cluster-resident)
+        or 'tile' (translation-invariant, tiles with frozen halos)."""
+        k = {"auto": 0, "ell": 1, "cluster": 2, "tile": 4}[kind]
         self._check(self.lib.esp_set_sweep_kernel(self.h, k))
 
     def sweep_kernel(self):
         """('ell' | 'cluster' | 'learned', cluster size)."""
         k, cs = C.c_int32(), C.c_int32()
         self._check(self.lib.esp_get_sweep_kernel(self.h, C.byref(k), C.byref(cs)))
-        return {1: "ell", 2: "cluster", 3: "learned"}[k.value], cs.value
+        return {1: "ell", 2: "cluster", 3: "learned", 4: "tile"}[k.value], cs.value
 
     # -- learned proposal -----------------------------------------------------
     def lp_init(self, seed: int = 0) -> None:
@@ -460,6 +467,24 @@ class Engine:
         out = np.zeros((f.shape[0], LP_OUT), dtype=np.float32)
         self._check(self.lib.esp_lp_forward(self.h, _p(f), f.shape[0], _p(out)))
         return out
+
+    def set_cluster_geometry(self, cluster_size: int, threads: int) -> None:
+        self._check(self.lib.esp_set_cluster_geometry(self.h, int(cluster_size), int(threads)))
+
+    def cluster_geometry(self):
+        """(CTAs per replica, threads per CTA) of the cluster path, (0, 0) without one."""
+        a, b = C.c_int32(), C.c_int32()
+        self._check(self.lib.esp_get_cluster_geometry(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def set_tile_geometry(self, tile: int, replicas: int) -> None:
+        self._check(self.lib.esp_set_tile_geometry(self.h, int(tile), int(replicas)))
+
+    def tile_geometry(self):
+        """(tile edge in cells, replicas per CTA) of the tiled path, (0, 0) without one."""
+        a, b = C.c_int32(), C.c_int32()
+        self._check(self.lib.esp_get_tile_geometry(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def set_pt_groups(self, group_size: int) -> None:
         """Replica exchange only inside consecutive groups of `group_size`
@@ -535,8 +560,12 @@ class Batch:
         ell = np.zeros(n)
         clu = np.zeros(n)
         gr = np.zeros(4)
-        t = BatchTuning(0, 0.0, _p(kern), _p(ell), _p(clu), _p(gr))
+        cs = np.zeros(n, dtype=np.int32)
+        nt = np.zeros(n, dtype=np.int32)
+        t = BatchTuning(0, 0.0, _p(kern), _p(ell), _p(clu), _p(gr), _p(cs), _p(nt))
         self._check(self.lib.esp_batch_tune(self.b, int(units), C.byref(t)))
         return {"units_per_graph": t.units_per_graph, "us_per_unit": t.us_per_unit,
-                "kernel": ["ell" if k == 1 else "cluster" for k in kern], "ell_us": ell.tolist(),
-                "cluster_us": clu.tolist(), "graph_us": dict(zip((1, 2, 4, 8), gr.tolist()))}
+                "kernel": [{1: "ell", 2: "cluster", 4: "tile"}.get(int(k), "ell") for k in kern],
+                "ell_us": ell.tolist(),
+                "cluster_us": clu.tolist(), "graph_us": dict(zip((1, 2, 4, 8), gr.tolist())),
+                "cluster_geometry": [(int(a), int(b)) for a, b in zip(cs, nt)]}

@@ -191,11 +191,24 @@ int esp_get_rejected(esp_handle *h, int64_t *rejected_out);
 int esp_get_replica_of_slot(esp_handle *h, int32_t *replica_out);
 /* Sweep kernel: 0 automatic, 1 the ELL kernel (any lattice), 2 the
  * cluster-resident kernel (periodic, translation-invariant lattices whose
- * replica fits the shared memory of one thread-block cluster).  Both follow the
- * same colouring, random stream and summation order. */
+ * replica fits the shared memory of one thread-block cluster), 4 the tiled
+ * kernel (periodic, translation-invariant lattices with nearest-cell
+ * couplings: cubes of T cells plus a one-cell halo of G replicas in shared
+ * memory, updated in a 2x2x2 checkerboard of tiles).  ELL and cluster follow
+ * the same colouring, random stream and summation order; the tiled kernel
+ * uses the same random stream and arithmetic in tile order. */
 int esp_set_sweep_kernel(esp_handle *h, int32_t kind);
-/* The kernel in use (1 ELL, 2 cluster, 3 the learned-proposal sweep) and the
- * cluster size of the cluster path. */
+/* Geometry of the cluster-resident sweep: CTAs per replica (slabs of z
+ * planes) and threads per CTA (256 or 512); ESP_EINVAL where the lattice or
+ * the GPU cannot run it.  Trajectories do not depend on it. */
+int esp_set_cluster_geometry(esp_handle *h, int32_t cluster_size, int32_t threads);
+int esp_get_cluster_geometry(const esp_handle *h, int32_t *cluster_size, int32_t *threads);
+/* Geometry of the tiled sweep: tile edge in cells (even, 2 * tile dividing
+ * every supercell edge) and replicas per CTA. */
+int esp_set_tile_geometry(esp_handle *h, int32_t tile, int32_t replicas);
+int esp_get_tile_geometry(const esp_handle *h, int32_t *tile, int32_t *replicas);
+/* The kernel in use (1 ELL, 2 cluster, 3 the learned-proposal sweep, 4
+ * tiled) and the cluster size of the cluster path. */
 int esp_get_sweep_kernel(const esp_handle *h, int32_t *kind, int32_t *cluster_size);
 /* Keep the per-measurement series (E, |m|) of every temperature slot for
  * the last `capacity` measurements of a run (0 switches it off): the data of
@@ -232,9 +245,11 @@ typedef struct esp_batch esp_batch;
 typedef struct {
     int32_t units_per_graph;      /* chosen */
     double us_per_unit;           /* device time of one unit of the batch, chosen setting */
-    int32_t *kernel;              /* [n] chosen sweep kernel per handle (1 ELL, 2 cluster), or NULL */
-    double *ell_us, *cluster_us;  /* [n] time per unit of each handle alone (-1: not possible), or NULL */
+    int32_t *kernel;              /* [n] chosen sweep kernel per handle (1 ELL, 2 cluster, 4 tiled), or NULL */
+    double *ell_us, *cluster_us;  /* [n] time per unit of each handle alone: ELL, and the best of the
+                                     cluster / tiled candidates (-1: none possible), or NULL */
     double *graph_us;             /* [4] time per unit with 1, 2, 4, 8 units per graph, or NULL */
+    int32_t *cluster_size, *cluster_threads;  /* [n] chosen cluster geometry per handle (0: none), or NULL */
 } esp_batch_tuning;
 int esp_batch_create(esp_handle *const *handles, int32_t n, void *stream, esp_batch **out);
 int esp_batch_destroy(esp_batch *b);
@@ -243,9 +258,10 @@ int esp_batch_set_units_per_graph(esp_batch *b, int32_t units);
 int esp_batch_advance(esp_batch *b, int64_t units);
 /* Autotuner: times every handle alone with each sweep kernel it supports
  * (one colour class per launch, or every colour and sweep of a unit per
- * launch) and keeps the faster, then times the whole batch with 1, 2, 4 and 8
- * units per graph and keeps the fastest.  It advances every handle by about
- * 20 * units measurement units, which count as measurements of the run. */
+ * launch with up to three cluster geometries) and keeps the fastest, then
+ * times the whole batch with 1, 2, 4 and 8 units per graph and keeps the
+ * fastest.  It advances every handle by about 25 * units measurement units,
+ * which count as measurements of the run. */
 int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out);
 
 /* ---- learned proposal ------------------------------------------------------

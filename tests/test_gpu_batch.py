@@ -102,7 +102,7 @@ def test_autotuner_chooses_and_batch_keeps_running():
         for i, (L, _, _, _) in enumerate(KINDS):
             assert t["ell_us"][i] > 0
             if t["cluster_us"][i] > 0:
-                assert t["kernel"][i] == ("cluster" if t["cluster_us"][i] < t["ell_us"][i] else "ell")
+                assert (t["kernel"][i] != "ell") == (t["cluster_us"][i] < t["ell_us"][i])
             else:
                 assert t["kernel"][i] == "ell"
         b.advance(5)

@@ -92,3 +92,32 @@ def test_cluster_kernel_is_chosen_for_invariant_lattices_only():
         e.upload(h)
         e.set_temperatures([5.0, 6.0])
         assert e.sweep_kernel()[0] == "ell"
+
+
+@pytest.mark.parametrize("case", ["sc_j1j2_bq_si", "bcc_pt"])
+def test_trajectory_does_not_depend_on_cluster_geometry(case):
+    """Every (CTAs per replica, threads per CTA) geometry the GPU can run gives
+    the same spins and rejected counts (same colour order and random stream);
+    only the FP32 grouping of the per-sweep sums may differ."""
+    inp = _cases()[case]
+    h = build_hamiltonian(inp)
+    rng = np.random.default_rng(8)
+    v = rng.normal(size=(len(inp.tems), h.n, 3))
+    s0 = v / np.linalg.norm(v, axis=2, keepdims=True)
+    outs = []
+    geoms = [(cs, nt) for cs in (1, 2, 4) for nt in (512, 256)]
+    for cs, nt in geoms:
+        with _engine(h, inp.tems, "cluster") as e:
+            try:
+                e.set_cluster_geometry(cs, nt)
+            except Exception:
+                continue          # not possible for this lattice / GPU
+            assert e.cluster_geometry() == (cs, nt)
+            e.set_spins(s0)
+            e.sweep(20, 11, seed=5)
+            outs.append(((cs, nt), e.get_spins(), e.rejected(), e.running_energy()))
+    assert len(outs) >= 2, [o[0] for o in outs]
+    for g, s, rej, en in outs[1:]:
+        assert np.array_equal(s, outs[0][1]), g
+        assert np.array_equal(rej, outs[0][2]), g
+        assert np.max(np.abs(en - outs[0][3])) <= 1e-6 * h.n * 40.0, g
