@@ -74,8 +74,11 @@ struct esp_handle {
     // tiled path (translation-invariant lattices with nearest-cell stencils)
     bool tile_ok = false;
     int tile_T = 0, tile_G = 0, tile_nt[3] = {0, 0, 0}, ntiles = 0;
+    bool tile_pipe = false;         // persistent cp.async-pipelined variant
     size_t tile_smem = 0;
     int4 *d_tile_offs = nullptr;
+    ClusterNbr *d_tile_cpl = nullptr;
+    int tile_maxst = 0, tile_nbd8[kMaxClusterAtoms] = {}, tile_nall8[kMaxClusterAtoms] = {};
     double *d_tile_part = nullptr;
     unsigned long long *d_tile_rej = nullptr;
     long long tile_pending = 0;
@@ -160,7 +163,7 @@ void free_tables(esp_handle *h)
     dfree(h->d_J); dfree(h->d_B); dfree(h->d_Dx); dfree(h->d_Dy); dfree(h->d_Dz); dfree(h->d_mag);
     dfree(h->d_si); dfree(h->d_fld); dfree(h->d_scratch); dfree(h->d_part); dfree(h->d_part_rej);
     dfree(h->d_stencil_blob); dfree(h->d_nbidx); dfree(h->d_lp_axis);
-    dfree(h->d_tile_offs); dfree(h->d_tile_part); dfree(h->d_tile_rej);
+    dfree(h->d_tile_offs); dfree(h->d_tile_cpl); dfree(h->d_tile_part); dfree(h->d_tile_rej);
     h->cluster_ok = false;
     h->tile_ok = false;
 }
@@ -275,9 +278,12 @@ int tile_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o
     TileArgs a;
     a.stencil = reinterpret_cast<const ClusterStencil *>(h->d_stencil_blob);
     a.offs = h->d_tile_offs;
-    a.maxst = h->cl_maxst;
-    for (int at = 0; at < kMaxClusterAtoms; ++at)
-        a.count[at] = at < h->na ? (int)h->prep.stencil[at].size() : 0;
+    a.cpl = h->d_tile_cpl;
+    a.maxst = h->tile_maxst;
+    for (int at = 0; at < kMaxClusterAtoms; ++at) {
+        a.nbd8[at] = h->tile_nbd8[at];
+        a.nall8[at] = h->tile_nall8[at];
+    }
     a.Lx = h->L[0]; a.Ly = h->L[1]; a.Lz = h->L[2]; a.na = h->na; a.N = h->N; a.R = h->R;
     a.T = h->tile_T; a.G = h->tile_G;
     a.ntx = h->tile_nt[0]; a.nty = h->tile_nt[1]; a.ntz = h->tile_nt[2];
@@ -292,7 +298,8 @@ int tile_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o
         a.sweep = (unsigned long long)(first + w - (h->capturing ? h->cap_base[0] : 0));
         for (int ph = 0; ph < 8; ++ph) {
             a.phase = ph;
-            CK(launch_tile(a, h->tile_smem, h->st));
+            if (h->tile_pipe) CK(launch_tile_p(a, h->tile_smem, h->num_sms, h->st));
+            else CK(launch_tile(a, h->tile_smem, h->st));
             h->launches++;
         }
         h->tile_pending++;
@@ -546,6 +553,7 @@ std::vector<ClusterGeom> cluster_candidates(const esp_handle *h)
 // has fewer than two CTAs per SM.  Shared memory stays within two CTAs per SM.
 struct TileGeom {
     int T, G;
+    bool pipe;
     double cost;
 };
 
@@ -559,23 +567,31 @@ std::vector<TileGeom> tile_candidates(const esp_handle *h)
         const int ntiles = (h->L[0] / T) * (h->L[1] / T) * (h->L[2] / T);
         for (int G : Gs) {
             if (h->R % G || 256 % G) continue;
-            const size_t smem = tile_smem_bytes(T, G, h->na, h->cl_maxst);
-            if (smem > 113 * 1024) continue;
             const double b = (double)(T + 2) / T;
-            double cost = 12.0 * (b * b * b + 1.0) / std::min(1.0, G / 8.0);
-            const double ctas = (double)(ntiles / 8) * (h->R / G);
-            if (ctas < 2.0 * h->num_sms) cost *= 2.0 * h->num_sms / ctas;
-            out.push_back({T, G, cost});
+            const double bytes = 12.0 * (b * b * b + 1.0) / std::min(1.0, G / 8.0);
+            const double items = (double)(ntiles / 8) * (h->R / G);
+            // pipelined persistent variant: the copies overlap the updates
+            if (tile_p_supported(T, G, h->na) && tile_p_smem_bytes(T, G, h->na, h->tile_maxst) <= 226 * 1024) {
+                double cost = 0.5 * bytes;
+                if (items < 4.0 * h->num_sms) cost *= 4.0 * h->num_sms / items;
+                out.push_back({T, G, true, cost});
+            }
+            if (tile_smem_bytes(T, G, h->na, h->tile_maxst) <= 113 * 1024) {
+                double cost = bytes;
+                if (items < 2.0 * h->num_sms) cost *= 2.0 * h->num_sms / items;
+                out.push_back({T, G, false, cost});
+            }
         }
     }
     std::stable_sort(out.begin(), out.end(), [](const TileGeom &a, const TileGeom &b) { return a.cost < b.cost; });
     return out;
 }
 
-int tile_geometry(esp_handle *h, int T, int G)
+int tile_geometry(esp_handle *h, int T, int G, bool pipe)
 {
-    const size_t smem = tile_smem_bytes(T, G, h->na, h->cl_maxst);
-    CK(tile_configure(smem));
+    const size_t smem = pipe ? tile_p_smem_bytes(T, G, h->na, h->tile_maxst) : tile_smem_bytes(T, G, h->na, h->tile_maxst);
+    if (pipe) CK(tile_p_configure(T, G, smem));
+    else CK(tile_configure(smem));
     CK(cudaStreamSynchronize(h->st));
     int rc = fold(h);
     if (rc) return rc;
@@ -588,7 +604,7 @@ int tile_geometry(esp_handle *h, int T, int G)
         CK(cudaMemsetAsync(h->d_tile_part, 0, sizeof(double) * 4 * (size_t)ntiles * h->R, h->st));
         CK(cudaMemsetAsync(h->d_tile_rej, 0, sizeof(unsigned long long) * (size_t)ntiles * h->R, h->st));
     }
-    h->tile_T = T; h->tile_G = G;
+    h->tile_T = T; h->tile_G = G; h->tile_pipe = pipe;
     for (int d = 0; d < 3; ++d) h->tile_nt[d] = nt[d];
     h->ntiles = ntiles;
     h->tile_smem = smem;
@@ -599,22 +615,48 @@ int tile_geometry(esp_handle *h, int T, int G)
 // Stencil offsets of the tiled path, if every entry stays within one cell.
 int tile_setup(esp_handle *h)
 {
-    const int maxst = h->cl_maxst;
-    std::vector<int4> offs((size_t)h->na * maxst, make_int4(0, 0, 0, 0));
+    // per atom: entries with biquadratic or DM couplings first, then
+    // exchange-only ones, each part padded to a multiple of 8 with the site
+    // itself and zero couplings (the kernels apply the B/D arithmetic to the
+    // first part only)
+    std::vector<std::vector<StencilEntry>> bd(h->na), jo(h->na);
+    int maxst = 8;
     for (int at = 0; at < h->na; ++at) {
-        const auto &lst = h->prep.stencil[at];
-        for (size_t e = 0; e < lst.size(); ++e) {
-            const StencilEntry &x = lst[e];
+        for (const StencilEntry &x : h->prep.stencil[at]) {
             if (std::abs(x.dx) > 1 || std::abs(x.dy) > 1 || std::abs(x.dz) > 1) return ESP_OK;
-            offs[(size_t)at * maxst + e] = make_int4(x.dx, x.dy, x.dz, x.b);
+            const bool rich = x.B != 0.f || x.Dx != 0.f || x.Dy != 0.f || x.Dz != 0.f;
+            (rich ? bd[at] : jo[at]).push_back(x);
         }
+        h->tile_nbd8[at] = ((int)bd[at].size() + 7) & ~7;
+        h->tile_nall8[at] = h->tile_nbd8[at] + (((int)jo[at].size() + 7) & ~7);
+        maxst = std::max(maxst, h->tile_nall8[at]);
     }
+    for (int at = h->na; at < kMaxClusterAtoms; ++at) h->tile_nbd8[at] = h->tile_nall8[at] = 0;
+    std::vector<int4> offs((size_t)h->na * maxst);
+    std::vector<ClusterNbr> cpl((size_t)h->na * maxst);
+    for (int at = 0; at < h->na; ++at) {
+        for (int e = 0; e < maxst; ++e) {
+            offs[(size_t)at * maxst + e] = make_int4(0, 0, 0, at);
+            ClusterNbr z{};
+            cpl[(size_t)at * maxst + e] = z;
+        }
+        auto put = [&](int e, const StencilEntry &x) {
+            offs[(size_t)at * maxst + e] = make_int4(x.dx, x.dy, x.dz, x.b);
+            ClusterNbr &c = cpl[(size_t)at * maxst + e];
+            c.J = x.J; c.B = x.B; c.Dx = x.Dx; c.Dy = x.Dy; c.Dz = x.Dz;
+        };
+        for (size_t e = 0; e < bd[at].size(); ++e) put((int)e, bd[at][e]);
+        for (size_t e = 0; e < jo[at].size(); ++e) put(h->tile_nbd8[at] + (int)e, jo[at][e]);
+    }
+    h->tile_maxst = maxst;
     CK(dalloc(&h->d_tile_offs, offs.size()));
+    CK(dalloc(&h->d_tile_cpl, cpl.size()));
     int rc = h2d(h, h->d_tile_offs, offs.data(), sizeof(int4) * offs.size());
     if (rc) return rc;
+    if ((rc = h2d(h, h->d_tile_cpl, cpl.data(), sizeof(ClusterNbr) * cpl.size()))) return rc;
     const std::vector<TileGeom> c = tile_candidates(h);
     if (c.empty()) return ESP_OK;
-    return tile_geometry(h, c[0].T, c[0].G);
+    return tile_geometry(h, c[0].T, c[0].G, c[0].pipe);
 }
 
 // Set up the cluster path for cs CTAs of nt threads: slab height, shared
@@ -1196,20 +1238,22 @@ int esp_set_sweep_kernel(esp_handle *h, int32_t kind)
     return ESP_OK;
 }
 
-int esp_set_tile_geometry(esp_handle *h, int32_t tile, int32_t replicas)
+int esp_set_tile_geometry(esp_handle *h, int32_t tile, int32_t replicas, int32_t pipelined)
 {
     if (!h) return ESP_EINVAL;
     for (const TileGeom &g : tile_candidates(h))
-        if (g.T == tile && g.G == replicas) return tile_geometry(h, tile, replicas);
+        if (g.T == tile && g.G == replicas && g.pipe == (pipelined != 0))
+            return tile_geometry(h, tile, replicas, g.pipe);
     h->err = "tile geometry not possible for this lattice";
     return ESP_EINVAL;
 }
 
-int esp_get_tile_geometry(const esp_handle *h, int32_t *tile, int32_t *replicas)
+int esp_get_tile_geometry(const esp_handle *h, int32_t *tile, int32_t *replicas, int32_t *pipelined)
 {
     if (!h || !tile || !replicas) return ESP_EINVAL;
     *tile = h->tile_ok ? h->tile_T : 0;
     *replicas = h->tile_ok ? h->tile_G : 0;
+    if (pipelined) *pipelined = h->tile_ok && h->tile_pipe ? 1 : 0;
     return ESP_OK;
 }
 
@@ -2088,17 +2132,18 @@ int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out)
             for (size_t k = 0; k < g.size() && k < 3; ++k) cands.push_back({2, g[k].cs, g[k].nt});
         }
         if (h->tile_ok) {
-            // kind 4: cs, nt carry the tile edge and the replicas per CTA
+            // kinds 4 / 5: cs, nt carry the tile edge and the replicas per CTA
+            // (5: the pipelined variant)
             const std::vector<TileGeom> g = tile_candidates(h);
-            for (size_t k = 0; k < g.size() && k < 2; ++k) cands.push_back({4, g[k].T, g[k].G});
+            for (size_t k = 0; k < g.size() && k < 3; ++k) cands.push_back({g[k].pipe ? 5 : 4, g[k].T, g[k].G});
         }
         double best = 1e300, best_cl = 1e300;
         Cand pick{1, 0, 0};
         for (const Cand &c : cands) {
             int rc = ESP_OK;
             if (c.kind == 2 && (rc = cluster_geometry(h, c.cs, c.nt))) return batch_fail(b, "cluster geometry", h);
-            if (c.kind == 4 && (rc = tile_geometry(h, c.cs, c.nt))) return batch_fail(b, "tile geometry", h);
-            if ((rc = esp_set_sweep_kernel(h, c.kind))) return batch_fail(b, "esp_set_sweep_kernel", h);
+            if (c.kind >= 4 && (rc = tile_geometry(h, c.cs, c.nt, c.kind == 5))) return batch_fail(b, "tile geometry", h);
+            if ((rc = esp_set_sweep_kernel(h, std::min(c.kind, 4)))) return batch_fail(b, "esp_set_sweep_kernel", h);
             esp_batch one;
             one.hs.assign(1, h);
             one.st = b->st;
@@ -2113,9 +2158,10 @@ int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out)
         if (out && out->cluster_us) out->cluster_us[i] = cands.size() > 1 ? best_cl : -1.0;
         int rc = ESP_OK;
         if (pick.kind == 2 && (rc = cluster_geometry(h, pick.cs, pick.nt))) return batch_fail(b, "cluster geometry", h);
-        if (pick.kind == 4 && (rc = tile_geometry(h, pick.cs, pick.nt))) return batch_fail(b, "tile geometry", h);
-        if ((rc = esp_set_sweep_kernel(h, pick.kind))) return batch_fail(b, "esp_set_sweep_kernel", h);
-        if (out && out->kernel) out->kernel[i] = pick.kind;
+        if (pick.kind >= 4 && (rc = tile_geometry(h, pick.cs, pick.nt, pick.kind == 5)))
+            return batch_fail(b, "tile geometry", h);
+        if ((rc = esp_set_sweep_kernel(h, std::min(pick.kind, 4)))) return batch_fail(b, "esp_set_sweep_kernel", h);
+        if (out && out->kernel) out->kernel[i] = std::min(pick.kind, 4);
         if (out && out->cluster_size) out->cluster_size[i] = h->cluster_ok ? h->csize : 0;
         if (out && out->cluster_threads) out->cluster_threads[i] = h->cluster_ok ? h->cthreads : 0;
     }

@@ -53,27 +53,22 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_sweep_tile(const TileArgs a
     double *red = reinterpret_cast<double *>(sx);                      // [4][kTileThreads], after the write-back
     unsigned long long *red_n = reinterpret_cast<unsigned long long *>(red + 4 * kTileThreads);
 
+    __shared__ int s_nbd8[kMaxClusterAtoms], s_nall8[kMaxClusterAtoms];
     {
-        // header, then the entries of class 8*at (every parity class of an
-        // atom has the same couplings)
         const int *src = reinterpret_cast<const int *>(a.stencil);
         int *dst = reinterpret_cast<int *>(st);
         for (int i = threadIdx.x; i < (int)(sizeof(ClusterStencil) / 4); i += blockDim.x) dst[i] = src[i];
-        const ClusterNbr *gn = reinterpret_cast<const ClusterNbr *>(a.stencil + 1);
+        // couplings and box-site offsets of entry e of atom at:
+        // (((dz*B + dy)*B + dx)*na + b) - at
         for (int i = threadIdx.x; i < na * maxst; i += blockDim.x) {
-            const int at = i / maxst, e = i % maxst;
-            nbt[i] = gn[(size_t)(8 * at) * maxst + e];
+            const int at = i / maxst;
+            nbt[i] = a.cpl[i];
+            const int4 d = a.offs[i];
+            toff[i] = ((d.z * B + d.y) * B + d.x) * na + d.w - at;
         }
-        // box-site offset of entry e of atom at: (((dz*B + dy)*B + dx)*na + b) - at; 0 (the
-        // site itself, zero couplings) for padding entries
-        for (int i = threadIdx.x; i < na * maxst; i += blockDim.x) {
-            const int at = i / maxst, e = i % maxst;
-            int o = 0;
-            if (e < a.count[at]) {
-                const int4 d = a.offs[i];
-                o = ((d.z * B + d.y) * B + d.x) * na + d.w - at;
-            }
-            toff[i] = o;
+        if (threadIdx.x < kMaxClusterAtoms) {
+            s_nbd8[threadIdx.x] = a.nbd8[threadIdx.x];
+            s_nall8[threadIdx.x] = a.nall8[threadIdx.x];
         }
     }
     // the box: tile + one cell of halo, periodic
@@ -113,10 +108,11 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_sweep_tile(const TileArgs a
             const float ox = sx[l], oy = sy[l], oz = sz[l];
             float gx = 0.f, gy = 0.f, gz = 0.f;
             float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
-            const int ne8 = (st->count[k] + 7) & ~7;
             const ClusterNbr *nb = nbt + at * maxst;
             const int *to = toff + at * maxst;
-            for (int e0 = 0; e0 < ne8; e0 += 8) {
+            const int nbd8 = s_nbd8[at], nall8 = s_nall8[at];
+            int e0 = 0;
+            for (; e0 < nbd8; e0 += 8) {
                 float tx_[8], ty_[8], tz_[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
@@ -140,6 +136,19 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_sweep_tile(const TileArgs a
                         gy += tz_[j] * dx - tx_[j] * dz;
                         gz += tx_[j] * dy - ty_[j] * dx;
                     }
+                }
+            }
+            for (; e0 < nall8; e0 += 8) {   // exchange only
+                float tx_[8], ty_[8], tz_[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int q = (bsite + to[e0 + j]) * G + g;
+                    tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
+                }
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const float J = nb[e0 + j].J;
+                    gx = fmaf(-J, tx_[j], gx); gy = fmaf(-J, ty_[j], gy); gz = fmaf(-J, tz_[j], gz);
                 }
             }
             if (a.has_si) {
@@ -211,6 +220,287 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_sweep_tile(const TileArgs a
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined variant: persistent CTAs of 512 threads, one per SM, loop over the
+// (tile, replica group) items of the launch's tile parity.  While item k is
+// updated in one shared-memory buffer, the box of item k+1 arrives in the
+// other by cp.async (16-byte chunks: the G replicas of a site are contiguous)
+// and the site-index lookups of item k+2 are in flight in registers.  Tile
+// edge T and group size G are compile-time constants.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+constexpr int kTilePThreads = 512;
+constexpr int kInvPerThread = 8;   // box sites per thread for the index prefetch (<= 4096 box sites)
+
+template <int T, int G>
+__global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArgs a)
+{
+    constexpr int NT = kTilePThreads, B = T + 2, H = T / 2, PC = H * H * H, CH = G / 4;
+    static_assert(G % 4 == 0 && NT % G == 0 && (T & 1) == 0, "tile shape");
+    const int na = a.na, maxst = a.maxst;
+    const int ngroups = a.R / G;
+    const int hx_t = a.ntx >> 1, hy_t = a.nty >> 1, hz_t = a.ntz >> 1;
+    const int W = hx_t * hy_t * hz_t * ngroups;
+    const int nbs = B * B * B * na;
+    const unsigned long long sweep = a.sweep + (a.ctr ? *a.ctr : 0ull);
+    const uint32_t sw_lo = (uint32_t)sweep, sw_hi = (uint32_t)(sweep >> 32);
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    ClusterStencil *st = reinterpret_cast<ClusterStencil *>(smem);
+    ClusterNbr *nbt = reinterpret_cast<ClusterNbr *>(st + 1);          // [na][maxst]
+    int *toff = reinterpret_cast<int *>(nbt + na * maxst);              // [na][maxst], padded to 4
+    int *inv_s = toff + ((na * maxst + 3) & ~3);                        // [2][nbs], padded to 4
+    float *buf = reinterpret_cast<float *>(inv_s + 2 * ((nbs + 3) & ~3));  // [2][3][nbs*G]
+    double *red = reinterpret_cast<double *>(buf + (size_t)6 * nbs * G);   // [NT/32][G][4]
+    unsigned long long *red_n = reinterpret_cast<unsigned long long *>(red + (NT / 32) * G * 4);
+
+    __shared__ int s_nbd8[kMaxClusterAtoms], s_nall8[kMaxClusterAtoms];
+    {
+        const int *src = reinterpret_cast<const int *>(a.stencil);
+        int *dst = reinterpret_cast<int *>(st);
+        for (int i = threadIdx.x; i < (int)(sizeof(ClusterStencil) / 4); i += NT) dst[i] = src[i];
+        // couplings, and offsets premultiplied by G: the spin of a neighbour is
+        // at (bsite*G + g) + toff
+        for (int i = threadIdx.x; i < na * maxst; i += NT) {
+            const int at = i / maxst;
+            nbt[i] = a.cpl[i];
+            const int4 d = a.offs[i];
+            toff[i] = (((d.z * B + d.y) * B + d.x) * na + d.w - at) * G;
+        }
+        if (threadIdx.x < kMaxClusterAtoms) {
+            s_nbd8[threadIdx.x] = a.nbd8[threadIdx.x];
+            s_nall8[threadIdx.x] = a.nall8[threadIdx.x];
+        }
+    }
+
+    // item -> tile origin and first replica
+    auto item_tile = [&](int w, int &x0, int &y0, int &z0, int &r0, int &tile) {
+        const int tp = w / ngroups;
+        r0 = (w % ngroups) * G;
+        const int tx = 2 * (tp % hx_t) + (a.phase & 1);
+        const int ty = 2 * ((tp / hx_t) % hy_t) + ((a.phase >> 1) & 1);
+        const int tz = 2 * (tp / (hx_t * hy_t)) + ((a.phase >> 2) & 1);
+        x0 = tx * T; y0 = ty * T; z0 = tz * T;
+        tile = (tz * a.nty + ty) * a.ntx + tx;
+    };
+    // reference-site index -> permuted index of the box sites of item w
+    auto load_inv = [&](int w, int (&regs)[kInvPerThread]) {
+        int x0, y0, z0, r0, tile;
+        item_tile(w, x0, y0, z0, r0, tile);
+#pragma unroll
+        for (int j = 0; j < kInvPerThread; ++j) {
+            const int i = threadIdx.x + j * NT;
+            int v = 0;
+            if (i < nbs) {
+                const int at = na == 1 ? 0 : i % na, cell = na == 1 ? i : i / na;
+                const int bx = cell % B, by = (cell / B) % B, bz = cell / (B * B);
+                int x = x0 - 1 + bx, y = y0 - 1 + by, z = z0 - 1 + bz;
+                x += (x < 0) ? a.Lx : (x >= a.Lx ? -a.Lx : 0);
+                y += (y < 0) ? a.Ly : (y >= a.Ly ? -a.Ly : 0);
+                z += (z < 0) ? a.Lz : (z >= a.Lz ? -a.Lz : 0);
+                v = __ldg(a.inv + ((z * a.Ly + y) * a.Lx + x) * na + at);
+            }
+            regs[j] = v;
+        }
+    };
+    auto store_inv = [&](int stage, const int (&regs)[kInvPerThread]) {
+#pragma unroll
+        for (int j = 0; j < kInvPerThread; ++j) {
+            const int i = threadIdx.x + j * NT;
+            if (i < nbs) inv_s[stage * ((nbs + 3) & ~3) + i] = regs[j];
+        }
+    };
+    // the box of item w into buffer `stage`, as 16-byte asynchronous copies
+    auto issue_box = [&](int w, int stage) {
+        int x0, y0, z0, r0, tile;
+        item_tile(w, x0, y0, z0, r0, tile);
+        const int *inv = inv_s + stage * ((nbs + 3) & ~3);
+        float *dst = buf + (size_t)stage * 3 * nbs * G;
+        for (int i = threadIdx.x; i < nbs * 3 * CH; i += NT) {
+            const int c = i % CH, rest = i / CH;
+            const int cp = rest % 3, bs = rest / 3;
+            const float *base = cp == 0 ? a.sx : (cp == 1 ? a.sy : a.sz);
+            const float *src = base + (size_t)inv[bs] * a.R + r0 + 4 * c;
+            cp_async16(dst + (size_t)cp * nbs * G + bs * G + 4 * c, src);
+        }
+        cp_async_commit();
+    };
+
+    int w = blockIdx.x;
+    if (w >= W) return;
+    int regs[kInvPerThread];
+    load_inv(w, regs);
+    store_inv(0, regs);
+    __syncthreads();
+    issue_box(w, 0);
+    const int w1 = w + gridDim.x;
+    if (w1 < W) {
+        load_inv(w1, regs);
+        store_inv(1, regs);
+    }
+    const int g = threadIdx.x % G;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = 0; w < W; ++k, w += gridDim.x) {
+        const int cur = k & 1, nxt = cur ^ 1;
+        const int wn = w + gridDim.x, wnn = wn + gridDim.x;
+        __syncthreads();   // inv_s[nxt] written, buffer nxt free
+        if (wn < W) issue_box(wn, nxt);
+        if (wnn < W) load_inv(wnn, regs);   // in flight during the update
+        if (wn < W) cp_async_wait<1>(); else cp_async_wait<0>();
+        __syncthreads();   // box of item w visible to every thread
+
+        int x0, y0, z0, r0, tile;
+        item_tile(w, x0, y0, z0, r0, tile);
+        float *sx = buf + (size_t)cur * 3 * nbs * G;
+        float *sy = sx + (size_t)nbs * G;
+        float *sz = sy + (size_t)nbs * G;
+        const int r = r0 + g;
+        const float beta = a.beta[a.temp_of[r]];
+        float accE = 0.f, accX = 0.f, accY = 0.f, accZ = 0.f;
+        unsigned int nrej = 0;
+        for (int c = 0; c < st->ncolour; ++c) {
+            const int c0 = st->colour_start[c];
+            const int items = (st->colour_start[c + 1] - c0) * PC * G;
+            for (int it = threadIdx.x; it < items; it += NT) {
+                const int si = it / G;
+                const int kcl = st->class_order[c0 + si / PC];
+                const int rem = si % PC;
+                const int hx = rem % H, hy = (rem / H) % H, hz = rem / (H * H);
+                const int at = kcl >> 3;
+                const int lx = 2 * hx + ((kcl >> 2) & 1), ly = 2 * hy + ((kcl >> 1) & 1), lz = 2 * hz + (kcl & 1);
+                const int bsite = (((lz + 1) * B + (ly + 1)) * B + (lx + 1)) * na + at;
+                const int l = bsite * G + g;
+                const float ox = sx[l], oy = sy[l], oz = sz[l];
+                float gx = 0.f, gy = 0.f, gz = 0.f;
+                float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
+                const ClusterNbr *nb = nbt + at * maxst;
+                const int *to = toff + at * maxst;
+                const int nbd8 = s_nbd8[at], nall8 = s_nall8[at];
+                int e0 = 0;
+                for (; e0 < nbd8; e0 += 8) {
+                    float tx_[8], ty_[8], tz_[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int q = l + to[e0 + j];
+                        tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
+                    }
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        // couplings as two 16-byte loads: (J, B, Dx, Dy), (Dz, ...)
+                        const float4 c0 = *reinterpret_cast<const float4 *>(nb + e0 + j);
+                        const float J = c0.x;
+                        gx = fmaf(-J, tx_[j], gx); gy = fmaf(-J, ty_[j], gy); gz = fmaf(-J, tz_[j], gz);
+                        if (a.has_b) {
+                            const float Bv = c0.y;
+                            const float bx = Bv * tx_[j], by = Bv * ty_[j], bz = Bv * tz_[j];
+                            qxx = fmaf(bx, tx_[j], qxx); qyy = fmaf(by, ty_[j], qyy); qzz = fmaf(bz, tz_[j], qzz);
+                            qxy = fmaf(bx, ty_[j], qxy); qxz = fmaf(bx, tz_[j], qxz); qyz = fmaf(by, tz_[j], qyz);
+                        }
+                        if (a.has_d) {
+                            const float dx = c0.z, dy = c0.w, dz = nb[e0 + j].Dz;
+                            gx += ty_[j] * dz - tz_[j] * dy;
+                            gy += tz_[j] * dx - tx_[j] * dz;
+                            gz += tx_[j] * dy - ty_[j] * dx;
+                        }
+                    }
+                }
+                for (; e0 < nall8; e0 += 8) {   // exchange only
+                    float tx_[8], ty_[8], tz_[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int q = l + to[e0 + j];
+                        tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
+                    }
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const float J = nb[e0 + j].J;
+                        gx = fmaf(-J, tx_[j], gx); gy = fmaf(-J, ty_[j], gy); gz = fmaf(-J, tz_[j], gz);
+                    }
+                }
+                if (a.has_si) {
+                    const float4 s = st->si[at];
+                    const float dx = s.w * s.x, dy = s.w * s.y, dz = s.w * s.z;
+                    qxx = fmaf(dx, s.x, qxx); qyy = fmaf(dy, s.y, qyy); qzz = fmaf(dz, s.z, qzz);
+                    qxy = fmaf(dx, s.y, qxy); qxz = fmaf(dx, s.z, qxz); qyz = fmaf(dy, s.z, qyz);
+                }
+                if (a.has_f) {
+                    const float4 f = st->fld[at];
+                    gx += f.x; gy += f.y; gz += f.z;
+                }
+                const int orig = (((z0 + lz) * a.Ly + (y0 + ly)) * a.Lx + (x0 + lx)) * na + at;
+                const Philox4 xr = philox4x32_10((uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
+                float nx, ny, nz;
+                trial_spin(a.mode, a.tilt, st->mag[at], ox, oy, oz, xr.x, xr.y, nx, ny, nz);
+                const float dx = nx - ox, dy = ny - oy, dz = nz - oz;
+                float de = gx * dx + gy * dy + gz * dz;
+                if (a.has_b || a.has_si) {
+                    const float px2 = nx + ox, py2 = ny + oy, pz2 = nz + oz;
+                    de += dx * (qxx * px2 + qxy * py2 + qxz * pz2)
+                        + dy * (qxy * px2 + qyy * py2 + qyz * pz2)
+                        + dz * (qxz * px2 + qyz * py2 + qzz * pz2);
+                }
+                bool acc = true;
+                if (de > 0.0f) acc = expf(-beta * de) >= u24f(xr.z);
+                if (acc) {
+                    sx[l] = nx; sy[l] = ny; sz[l] = nz;
+                    accE += de;
+                    accX += dx; accY += dy; accZ += dz;
+                } else {
+                    ++nrej;
+                }
+            }
+            __syncthreads();
+        }
+        // write the tile back (16-byte chunks), its sums to the tile's slots
+        {
+            const int *inv = inv_s + cur * ((nbs + 3) & ~3);
+            for (int i = threadIdx.x; i < T * T * T * na * 3 * CH; i += NT) {
+                const int c = i % CH, rest = i / CH;
+                const int cp = rest % 3, ts = rest / 3;
+                const int at = na == 1 ? 0 : ts % na, cell = na == 1 ? ts : ts / na;
+                const int lx = cell % T, ly = (cell / T) % T, lz = cell / (T * T);
+                const int bsite = (((lz + 1) * B + (ly + 1)) * B + (lx + 1)) * na + at;
+                const float4 v = *reinterpret_cast<const float4 *>(sx + (size_t)cp * nbs * G + bsite * G + 4 * c);
+                float *base = cp == 0 ? a.sx : (cp == 1 ? a.sy : a.sz);
+                *reinterpret_cast<float4 *>(base + (size_t)inv[bsite] * a.R + r0 + 4 * c) = v;
+            }
+        }
+        double v[4] = {(double)accE, (double)accX, (double)accY, (double)accZ};
+        unsigned long long nr = nrej;
+        for (int o = G; o < 32; o <<= 1) {
+            for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+            nr += __shfl_xor_sync(0xffffffffu, nr, o);
+        }
+        if (lane < G) {
+            for (int q = 0; q < 4; ++q) red[(warp * G + lane) * 4 + q] = v[q];
+            red_n[warp * G + lane] = nr;
+        }
+        __syncthreads();   // sums in place; nobody reads inv_s[cur] any more
+        if ((int)threadIdx.x < G) {
+            double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+            unsigned long long sn = 0;
+            for (int q = 0; q < NT / 32; ++q) {
+                const double *o = red + (q * G + threadIdx.x) * 4;
+                s0 += o[0]; s1 += o[1]; s2 += o[2]; s3 += o[3];
+                sn += red_n[q * G + threadIdx.x];
+            }
+            const size_t slot = (size_t)tile * a.R + r0 + threadIdx.x;
+            double *o = a.part + 4 * slot;
+            o[0] += s0; o[1] += s1; o[2] += s2; o[3] += s3;
+            a.part_rej[slot] += sn;
+        }
+        if (wnn < W) store_inv(cur, regs);
+    }
+}
+
 // e_run / m_run / rejected of every replica from the tiles' slots, in tile
 // order, and the slots cleared.  One block per replica.
 __global__ void __launch_bounds__(256) k_tile_fold(TileFoldArgs a)
@@ -266,6 +556,63 @@ cudaError_t launch_tile(const TileArgs &a, size_t smem, cudaStream_t st)
     const int tiles = (a.ntx / 2) * (a.nty / 2) * (a.ntz / 2);
     k_sweep_tile<<<tiles * (a.R / a.G), kTileThreads, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+size_t tile_p_smem_bytes(int T, int G, int na, int maxst)
+{
+    const size_t B = (size_t)T + 2, nbs = B * B * B * na;
+    return sizeof(ClusterStencil) + (size_t)na * maxst * sizeof(ClusterNbr) +
+           (size_t)((na * maxst + 3) & ~3) * sizeof(int) + 2 * ((nbs + 3) & ~(size_t)3) * sizeof(int) +
+           (size_t)6 * nbs * G * sizeof(float) + (size_t)(kTilePThreads / 32) * G * (4 * sizeof(double) + 8);
+}
+
+bool tile_p_supported(int T, int G, int na)
+{
+    const int B = T + 2;
+    if (B * B * B * na > kInvPerThread * kTilePThreads) return false;
+    return (T == 4 || T == 6 || T == 8) && (G == 4 || G == 8 || G == 16);
+}
+
+namespace {
+template <int T, int G>
+cudaError_t launch_p(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
+{
+    if (configure) return cudaFuncSetAttribute(k_sweep_tile_p<T, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_sweep_tile_p<T, G><<<blocks, kTilePThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int T>
+cudaError_t launch_pg(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
+{
+    if (a.G == 4) return launch_p<T, 4>(a, smem, blocks, st, configure);
+    if (a.G == 8) return launch_p<T, 8>(a, smem, blocks, st, configure);
+    if (a.G == 16) return launch_p<T, 16>(a, smem, blocks, st, configure);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pt(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
+{
+    if (a.T == 4) return launch_pg<4>(a, smem, blocks, st, configure);
+    if (a.T == 6) return launch_pg<6>(a, smem, blocks, st, configure);
+    if (a.T == 8) return launch_pg<8>(a, smem, blocks, st, configure);
+    return cudaErrorInvalidValue;
+}
+}  // namespace
+
+cudaError_t tile_p_configure(int T, int G, size_t smem)
+{
+    TileArgs a{};
+    a.T = T; a.G = G;
+    return launch_pt(a, smem, 0, nullptr, true);
+}
+
+cudaError_t launch_tile_p(const TileArgs &a, size_t smem, int num_sms, cudaStream_t st)
+{
+    if (!tile_p_supported(a.T, a.G, a.na) || a.R % a.G != 0) return cudaErrorInvalidValue;
+    const int items = (a.ntx / 2) * (a.nty / 2) * (a.ntz / 2) * (a.R / a.G);
+    const int blocks = items < num_sms ? items : num_sms;
+    return launch_pt(a, smem, blocks, st, false);
 }
 
 cudaError_t launch_tile_fold(const TileFoldArgs &a, cudaStream_t st)

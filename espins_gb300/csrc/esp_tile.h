@@ -11,9 +11,13 @@ namespace esp {
 
 struct TileArgs {
     const ClusterStencil *stencil;  // device copy of the cluster path's stencil (header + entries)
+    // per atom: entries with biquadratic or DM couplings first (nbd8 of them,
+    // padded to a multiple of 8), then exchange-only entries up to nall8;
+    // padding entries are the site itself with zero couplings
     const int4 *offs;               // [na][maxst]: (dx, dy, dz, target atom) in cells
+    const ClusterNbr *cpl;          // [na][maxst] couplings in the same order
     int maxst;
-    int count[kMaxClusterAtoms];    // entries of each atom's list
+    int nbd8[kMaxClusterAtoms], nall8[kMaxClusterAtoms];
     int Lx, Ly, Lz, na, N, R;
     int T, G;                       // tile edge (cells, even), replicas per CTA
     int ntx, nty, ntz;              // tiles per axis (even)
@@ -46,5 +50,10 @@ cudaError_t tile_configure(size_t smem);
 // one launch = the tiles of one parity (a.phase); eight make a sweep
 cudaError_t launch_tile(const TileArgs &a, size_t smem, cudaStream_t st);
 cudaError_t launch_tile_fold(const TileFoldArgs &a, cudaStream_t st);
+// pipelined persistent variant (T in {4, 6, 8}, G in {4, 8, 16}), one CTA per SM
+size_t tile_p_smem_bytes(int T, int G, int na, int maxst);
+bool tile_p_supported(int T, int G, int na);
+cudaError_t tile_p_configure(int T, int G, size_t smem);
+cudaError_t launch_tile_p(const TileArgs &a, size_t smem, int num_sms, cudaStream_t st);
 
 }  // namespace esp

@@ -153,8 +153,8 @@ def load(build_if_missing: bool = True):
     lib.esp_get_proposal.argtypes = [vp, P(C.c_int32)]
     lib.esp_set_pt_groups.argtypes = [vp, C.c_int32]
     lib.esp_set_cluster_geometry.argtypes = [vp, C.c_int32, C.c_int32]
-    lib.esp_set_tile_geometry.argtypes = [vp, C.c_int32, C.c_int32]
-    lib.esp_get_tile_geometry.argtypes = [vp, P(C.c_int32), P(C.c_int32)]
+    lib.esp_set_tile_geometry.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
+    lib.esp_get_tile_geometry.argtypes = [vp, P(C.c_int32), P(C.c_int32), P(C.c_int32)]
     lib.esp_get_cluster_geometry.argtypes = [vp, P(C.c_int32), P(C.c_int32)]
     lib.esp_batch_create.argtypes = [vp, C.c_int32, vp, P(vp)]
     lib.esp_batch_destroy.argtypes = [vp]
@@ -477,14 +477,14 @@ class Engine:
         self._check(self.lib.esp_get_cluster_geometry(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
-    def set_tile_geometry(self, tile: int, replicas: int) -> None:
-        self._check(self.lib.esp_set_tile_geometry(self.h, int(tile), int(replicas)))
+    def set_tile_geometry(self, tile: int, replicas: int, pipelined: bool = False) -> None:
+        self._check(self.lib.esp_set_tile_geometry(self.h, int(tile), int(replicas), int(bool(pipelined))))
 
     def tile_geometry(self):
-        """(tile edge in cells, replicas per CTA) of the tiled path, (0, 0) without one."""
-        a, b = C.c_int32(), C.c_int32()
-        self._check(self.lib.esp_get_tile_geometry(self.h, C.byref(a), C.byref(b)))
-        return a.value, b.value
+        """(tile edge in cells, replicas per CTA, pipelined) of the tiled path, (0, 0, False) without one."""
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(self.lib.esp_get_tile_geometry(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, bool(c.value)
 
     def set_pt_groups(self, group_size: int) -> None:
         """Replica exchange only inside consecutive groups of `group_size`

@@ -204,9 +204,12 @@ int esp_set_sweep_kernel(esp_handle *h, int32_t kind);
 int esp_set_cluster_geometry(esp_handle *h, int32_t cluster_size, int32_t threads);
 int esp_get_cluster_geometry(const esp_handle *h, int32_t *cluster_size, int32_t *threads);
 /* Geometry of the tiled sweep: tile edge in cells (even, 2 * tile dividing
- * every supercell edge) and replicas per CTA. */
-int esp_set_tile_geometry(esp_handle *h, int32_t tile, int32_t replicas);
-int esp_get_tile_geometry(const esp_handle *h, int32_t *tile, int32_t *replicas);
+ * every supercell edge), replicas per CTA, and the variant: 0 one CTA per
+ * tile, 1 persistent CTAs that copy the next tile asynchronously while
+ * updating the current one (tile 4, 6 or 8; 4, 8 or 16 replicas).  Both give
+ * the same trajectory. */
+int esp_set_tile_geometry(esp_handle *h, int32_t tile, int32_t replicas, int32_t pipelined);
+int esp_get_tile_geometry(const esp_handle *h, int32_t *tile, int32_t *replicas, int32_t *pipelined);
 /* The kernel in use (1 ELL, 2 cluster, 3 the learned-proposal sweep, 4
  * tiled) and the cluster size of the cluster path. */
 int esp_get_sweep_kernel(const esp_handle *h, int32_t *kind, int32_t *cluster_size);
