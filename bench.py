@@ -299,12 +299,14 @@ def learned_compare(a, rank, local):
         out[kind] = {
             "site_updates_per_s": ups,
             "independent_samples_per_s": float(np.sum(sweeps_per_s / (2.0 * tau))),
+            "per_slot_samples_per_s": (sweeps_per_s / (2.0 * tau)).tolist(),
             "tau_int_E": tau_e.tolist(), "tau_int_absM": tau_m.tolist(),
             "tau_int_binning_E": [analysis.binning_tau(ser[:, t, 0]) for t in range(R)],
             "acceptance": acc.tolist(), "kernel": eng.sweep_kernel()[0],
             "mean_E_per_site": (res["data"][:, 0] / N).tolist(), "mean_absM": res["data"][:, 3].tolist(),
         }
     eng.close()
+    gains = np.asarray(out["learned"]["per_slot_samples_per_s"]) / np.asarray(out["plain"]["per_slot_samples_per_s"])
     if rank == 0:
         line = {
             "metric": "independent samples/s", "value": out["learned"]["independent_samples_per_s"],
@@ -314,6 +316,11 @@ def learned_compare(a, rank, local):
             "plain": out["plain"], "learned": out["learned"],
             "ratio_independent_samples": out["learned"]["independent_samples_per_s"]
             / out["plain"]["independent_samples_per_s"],
+            # per temperature slot: learned / plain independent samples/s
+            "gain_per_slot": gains.tolist(),
+            "gain_geomean": float(np.exp(np.mean(np.log(gains)))),
+            "gain_min": float(gains.min()), "gain_max": float(gains.max()),
+            "slots_with_gain_ge_2": int((gains >= 2.0).sum()),
             "training": {"pairs": int(rows), "collect_s": t_collect, "steps": a.train_steps, "batch": 4096,
                          "seconds": t_train, "loss_first": float(np.mean(loss[:20])),
                          "loss_last": float(np.mean(loss[-50:]))},

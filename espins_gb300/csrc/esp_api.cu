@@ -15,6 +15,7 @@
 #include "esp_cluster.h"
 #include "esp_kernels.h"
 #include "esp_learned.h"
+#include "esp_lp_tc.h"
 #include "esp_tile.h"
 #include "esp_tables.h"
 #include "esp_errors.h"
@@ -100,6 +101,8 @@ struct esp_handle {
     // learned proposal: network (fp32 master + Adam moments + bf16 copies),
     // training set, mini-batch buffers
     int proposal = 0;               // 0 plain Metropolis, 1 learned
+    int lp_engine = 0;              // network on 0: mma.sync (warp tiles), 1: tcgen05 (128-row tiles)
+    int *d_tc_err = nullptr;        // set by a tensor-core completion wait that gave up
     bool lp_weights = false;
     int lp_grid = 0;
     float *d_lp_p = nullptr, *d_lp_g = nullptr, *d_lp_m = nullptr, *d_lp_v = nullptr;
@@ -188,6 +191,7 @@ void free_all(esp_handle *h)
     dfree(h->d_lp_w1); dfree(h->d_lp_w2); dfree(h->d_lp_w3);
     dfree(h->d_lp_x); dfree(h->d_lp_t); dfree(h->d_lp_loss);
     dfree(h->d_ctr);
+    dfree(h->d_tc_err);
 }
 
 SweepArgs sweep_args(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o)
@@ -337,6 +341,9 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
         a.ctr = h->d_ctr;
     }
     a.sweep_base = (unsigned long long)first;
+    a.fd_pc = make_fastdiv((uint32_t)((h->L[0] / 2) * (h->L[1] / 2) * (h->pz / 2)));
+    a.fd_hx = make_fastdiv((uint32_t)(h->L[0] / 2));
+    a.fd_hy = make_fastdiv((uint32_t)(h->L[1] / 2));
     a.key0 = (uint32_t)o->seed; a.key1 = (uint32_t)(o->seed >> 32);
     a.mode = o->mcarlo_mode ? 1 : 0; a.tilt = (float)o->tilt_angles_max;
     CK(launch_cluster(a, h->csize, h->cthreads, h->cluster_smem, h->st));
@@ -741,6 +748,7 @@ int esp_create(const esp_dims *dims, esp_handle **out)
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = lp_configure(h->device);
+    if (e == cudaSuccess) e = lp_tc_configure();
     if (e != cudaSuccess) {
         set_global_error("CUDA unavailable: %s", cudaGetErrorString(e));
         delete h;
@@ -1833,12 +1841,33 @@ int esp_lp_forward(esp_handle *h, const float *features, int64_t n, float *out)
     LpWeights w;
     w.w1 = h->d_lp_w1; w.w2 = h->d_lp_w2; w.w3 = h->d_lp_w3;
     w.b1 = h->d_lp_p + kPadB1; w.b2 = h->d_lp_p + kPadB2; w.b3 = h->d_lp_p + kPadB3;
-    if (e == cudaSuccess) e = launch_lp_forward(w, dx, (int)n, dout, h->st);
+    if (h->lp_engine == 1) {
+        if (e == cudaSuccess && !h->d_tc_err) e = dalloc(&h->d_tc_err, 1);
+        if (e == cudaSuccess) e = cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->st);
+        if (e == cudaSuccess) e = launch_lp_forward_tc(w, dx, (int)n, dout, h->d_tc_err, h->num_sms, h->st);
+    } else if (e == cudaSuccess) {
+        e = launch_lp_forward(w, dx, (int)n, dout, h->st);
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, sizeof(float) * n * kMlpOut, cudaMemcpyDeviceToHost, h->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     h->launches++;
     dfree(dx); dfree(dout);
     if (e != cudaSuccess) { h->err = std::string("esp_lp_forward: ") + cudaGetErrorString(e); return ESP_ECUDA; }
+    if (h->lp_engine == 1) {
+        int flag = 0;
+        int rc = d2h(h, &flag, h->d_tc_err, sizeof(int));
+        if (rc) return rc;
+        if (flag) { h->err = "esp_lp_forward: a tensor-core completion wait gave up"; return ESP_ETIMEOUT; }
+    }
+    return ESP_OK;
+}
+
+int esp_lp_set_engine(esp_handle *h, int32_t engine)
+{
+    if (!h || engine < 0 || engine > 1) return ESP_EINVAL;
+    int rc = fold(h);
+    if (rc) return rc;
+    h->lp_engine = engine;
     return ESP_OK;
 }
 

@@ -59,8 +59,10 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
         for (int i = threadIdx.x; i < a.nf; i += blockDim.x) hist[i] = 0u;
     }
     for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
-        const int k = l / per_class, rem = l % per_class;
-        const int hx = rem % Hx, hy = (rem / Hx) % Hy, hzl = rem / (Hx * Hy);
+        int k, rem, q1, hx, hy, hzl;
+        fdivmod(l, a.fd_pc, k, rem);
+        fdivmod(rem, a.fd_hx, q1, hx);
+        fdivmod(q1, a.fd_hy, hzl, hy);
         const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
         const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pz;
         const int orig = ((z * a.Ly + y) * a.Lx + x) * a.na + at;
@@ -91,10 +93,12 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                 const int c0 = st->colour_start[c];
                 const int items = (st->colour_start[c + 1] - c0) * per_class;
                 for (int it = threadIdx.x; it < items; it += blockDim.x) {
-                    const int k = st->class_order[c0 + it / per_class];
-                    const int rem = it % per_class;
+                    int ci, rem, q1, hx, hy, hzl;
+                    fdivmod(it, a.fd_pc, ci, rem);
+                    const int k = st->class_order[c0 + ci];
                     const int l = k * per_class + rem;
-                    const int hx = rem % Hx, hy = (rem / Hx) % Hy, hzl = rem / (Hx * Hy);
+                    fdivmod(rem, a.fd_hx, q1, hx);
+                    fdivmod(q1, a.fd_hy, hzl, hy);
                     const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pzb = k & 1;
                     const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pzb;
                     const float ox = sx[l], oy = sy[l], oz = sz[l];
@@ -304,8 +308,10 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
         }
     }
     for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
-        const int k = l / per_class, rem = l % per_class;
-        const int hx = rem % Hx, hy = (rem / Hx) % Hy, hzl = rem / (Hx * Hy);
+        int k, rem, q1, hx, hy, hzl;
+        fdivmod(l, a.fd_pc, k, rem);
+        fdivmod(rem, a.fd_hx, q1, hx);
+        fdivmod(q1, a.fd_hy, hzl, hy);
         const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
         const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pz;
         const int orig = ((z * a.Ly + y) * a.Lx + x) * a.na + at;

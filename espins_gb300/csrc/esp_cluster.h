@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "esp_device.cuh"
+
 namespace esp {
 
 constexpr int kClusterThreads = 512;
@@ -64,6 +66,8 @@ struct ClusterArgs {
     // device counters [sweep, swap, measurement, unit] added to sweep_base
     // and meas_base, or null
     const unsigned long long *ctr;
+    // divisions by per-class sites and half-cell extents
+    FastDiv fd_pc, fd_hx, fd_hy;
     uint32_t key0, key1;
     int mode;
     float tilt;

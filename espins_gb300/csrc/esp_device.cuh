@@ -91,6 +91,37 @@ __device__ __forceinline__ int pm_bin(float mx, float my, float mz, float m_min,
     return bin > nf ? nf : bin;
 }
 
+// Division by an invariant integer d >= 1 as a multiply-high, an add and a
+// shift (T. Granlund, P. Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994): with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (mulhi(n, m) + n) >> l for
+// 0 <= n < 2^31.
+struct FastDiv {
+    uint32_t d, m, s;
+};
+
+inline FastDiv make_fastdiv(uint32_t d)
+{
+    FastDiv f{d, 0u, 0u};
+    uint32_t l = 0;
+    while ((1ull << l) < d) ++l;
+    f.s = l;
+    f.m = (uint32_t)((((1ull << l) - d) << 32) / d + 1ull);
+    if (d == 1) f.m = 0u;
+    return f;
+}
+
+__host__ __device__ __forceinline__ int fdiv(int n, const FastDiv &f)
+{
+    return (int)((mulhi32((uint32_t)n, f.m) + (uint32_t)n) >> f.s);
+}
+
+__host__ __device__ __forceinline__ void fdivmod(int n, const FastDiv &f, int &q, int &r)
+{
+    q = fdiv(n, f);
+    r = n - q * (int)f.d;
+}
+
 // Arguments of the colour-class sweep over the merged ELL tables.
 struct SweepArgs {
     // tables, permuted site order (colour-major); entry k of site p at k*N+p

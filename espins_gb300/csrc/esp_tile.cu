@@ -237,6 +237,12 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// Shared-memory slot of box site b: within each block of 8 sites,
+// b = 8 blk + 2 a + p goes to slot 8 blk + a + 4 p, so sites two apart (one
+// colour class along x: the 4 sites one warp reads with 8 replicas each) land
+// in 4 distinct 8-bank groups.
+__device__ __forceinline__ int box_slot(int b) { return (b & ~7) | ((b >> 1) & 3) | ((b & 1) << 2); }
+
 constexpr int kTilePThreads = 512;
 constexpr int kInvPerThread = 8;   // box sites per thread for the index prefetch (<= 4096 box sites)
 
@@ -250,6 +256,7 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
     const int hx_t = a.ntx >> 1, hy_t = a.nty >> 1, hz_t = a.ntz >> 1;
     const int W = hx_t * hy_t * hz_t * ngroups;
     const int nbs = B * B * B * na;
+    const int nbs8 = (nbs + 7) & ~7;   // box sites rounded to whole slot blocks
     const unsigned long long sweep = a.sweep + (a.ctr ? *a.ctr : 0ull);
     const uint32_t sw_lo = (uint32_t)sweep, sw_hi = (uint32_t)(sweep >> 32);
 
@@ -258,8 +265,8 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
     ClusterNbr *nbt = reinterpret_cast<ClusterNbr *>(st + 1);          // [na][maxst]
     int *toff = reinterpret_cast<int *>(nbt + na * maxst);              // [na][maxst], padded to 4
     int *inv_s = toff + ((na * maxst + 3) & ~3);                        // [2][nbs], padded to 4
-    float *buf = reinterpret_cast<float *>(inv_s + 2 * ((nbs + 3) & ~3));  // [2][3][nbs*G]
-    double *red = reinterpret_cast<double *>(buf + (size_t)6 * nbs * G);   // [NT/32][G][4]
+    float *buf = reinterpret_cast<float *>(inv_s + 2 * ((nbs + 3) & ~3));  // [2][3][nbs8*G]
+    double *red = reinterpret_cast<double *>(buf + (size_t)6 * nbs8 * G);  // [NT/32][G][4]
     unsigned long long *red_n = reinterpret_cast<unsigned long long *>(red + (NT / 32) * G * 4);
 
     __shared__ int s_nbd8[kMaxClusterAtoms], s_nall8[kMaxClusterAtoms];
@@ -267,13 +274,12 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
         const int *src = reinterpret_cast<const int *>(a.stencil);
         int *dst = reinterpret_cast<int *>(st);
         for (int i = threadIdx.x; i < (int)(sizeof(ClusterStencil) / 4); i += NT) dst[i] = src[i];
-        // couplings, and offsets premultiplied by G: the spin of a neighbour is
-        // at (bsite*G + g) + toff
+        // couplings, and box-site offsets of the entries
         for (int i = threadIdx.x; i < na * maxst; i += NT) {
             const int at = i / maxst;
             nbt[i] = a.cpl[i];
             const int4 d = a.offs[i];
-            toff[i] = (((d.z * B + d.y) * B + d.x) * na + d.w - at) * G;
+            toff[i] = ((d.z * B + d.y) * B + d.x) * na + d.w - at;
         }
         if (threadIdx.x < kMaxClusterAtoms) {
             s_nbd8[threadIdx.x] = a.nbd8[threadIdx.x];
@@ -323,13 +329,13 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
         int x0, y0, z0, r0, tile;
         item_tile(w, x0, y0, z0, r0, tile);
         const int *inv = inv_s + stage * ((nbs + 3) & ~3);
-        float *dst = buf + (size_t)stage * 3 * nbs * G;
+        float *dst = buf + (size_t)stage * 3 * nbs8 * G;
         for (int i = threadIdx.x; i < nbs * 3 * CH; i += NT) {
             const int c = i % CH, rest = i / CH;
             const int cp = rest % 3, bs = rest / 3;
             const float *base = cp == 0 ? a.sx : (cp == 1 ? a.sy : a.sz);
             const float *src = base + (size_t)inv[bs] * a.R + r0 + 4 * c;
-            cp_async16(dst + (size_t)cp * nbs * G + bs * G + 4 * c, src);
+            cp_async16(dst + (size_t)cp * nbs8 * G + box_slot(bs) * G + 4 * c, src);
         }
         cp_async_commit();
     };
@@ -359,9 +365,9 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
 
         int x0, y0, z0, r0, tile;
         item_tile(w, x0, y0, z0, r0, tile);
-        float *sx = buf + (size_t)cur * 3 * nbs * G;
-        float *sy = sx + (size_t)nbs * G;
-        float *sz = sy + (size_t)nbs * G;
+        float *sx = buf + (size_t)cur * 3 * nbs8 * G;
+        float *sy = sx + (size_t)nbs8 * G;
+        float *sz = sy + (size_t)nbs8 * G;
         const int r = r0 + g;
         const float beta = a.beta[a.temp_of[r]];
         float accE = 0.f, accX = 0.f, accY = 0.f, accZ = 0.f;
@@ -377,7 +383,7 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
                 const int at = kcl >> 3;
                 const int lx = 2 * hx + ((kcl >> 2) & 1), ly = 2 * hy + ((kcl >> 1) & 1), lz = 2 * hz + (kcl & 1);
                 const int bsite = (((lz + 1) * B + (ly + 1)) * B + (lx + 1)) * na + at;
-                const int l = bsite * G + g;
+                const int l = box_slot(bsite) * G + g;
                 const float ox = sx[l], oy = sy[l], oz = sz[l];
                 float gx = 0.f, gy = 0.f, gz = 0.f;
                 float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
@@ -389,7 +395,7 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
                     float tx_[8], ty_[8], tz_[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        const int q = l + to[e0 + j];
+                        const int q = box_slot(bsite + to[e0 + j]) * G + g;
                         tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
                     }
 #pragma unroll
@@ -416,7 +422,7 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
                     float tx_[8], ty_[8], tz_[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        const int q = l + to[e0 + j];
+                        const int q = box_slot(bsite + to[e0 + j]) * G + g;
                         tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
                     }
 #pragma unroll
@@ -468,7 +474,7 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
                 const int at = na == 1 ? 0 : ts % na, cell = na == 1 ? ts : ts / na;
                 const int lx = cell % T, ly = (cell / T) % T, lz = cell / (T * T);
                 const int bsite = (((lz + 1) * B + (ly + 1)) * B + (lx + 1)) * na + at;
-                const float4 v = *reinterpret_cast<const float4 *>(sx + (size_t)cp * nbs * G + bsite * G + 4 * c);
+                const float4 v = *reinterpret_cast<const float4 *>(sx + (size_t)cp * nbs8 * G + box_slot(bsite) * G + 4 * c);
                 float *base = cp == 0 ? a.sx : (cp == 1 ? a.sy : a.sz);
                 *reinterpret_cast<float4 *>(base + (size_t)inv[bsite] * a.R + r0 + 4 * c) = v;
             }
@@ -560,10 +566,10 @@ cudaError_t launch_tile(const TileArgs &a, size_t smem, cudaStream_t st)
 
 size_t tile_p_smem_bytes(int T, int G, int na, int maxst)
 {
-    const size_t B = (size_t)T + 2, nbs = B * B * B * na;
+    const size_t B = (size_t)T + 2, nbs = B * B * B * na, nbs8 = (nbs + 7) & ~(size_t)7;
     return sizeof(ClusterStencil) + (size_t)na * maxst * sizeof(ClusterNbr) +
            (size_t)((na * maxst + 3) & ~3) * sizeof(int) + 2 * ((nbs + 3) & ~(size_t)3) * sizeof(int) +
-           (size_t)6 * nbs * G * sizeof(float) + (size_t)(kTilePThreads / 32) * G * (4 * sizeof(double) + 8);
+           (size_t)6 * nbs8 * G * sizeof(float) + (size_t)(kTilePThreads / 32) * G * (4 * sizeof(double) + 8);
 }
 
 bool tile_p_supported(int T, int G, int na)

@@ -307,6 +307,11 @@ int esp_lp_loss_grad(esp_handle *h, const float *features, const float *targets,
                      float *grad);
 /* Raw network outputs (n,20) of n feature rows by the sweep's fused forward pass. */
 int esp_lp_forward(esp_handle *h, const float *features, int64_t n, float *out);
+/* Tensor-core engine of the network in esp_lp_forward and the learned sweep:
+ * 0 warp-level mma.sync tiles of 32 trials (default), 1 tcgen05 MMAs on
+ * 128-trial tiles with tensor-memory accumulators.  ESP_ETIMEOUT if a
+ * completion wait gave up. */
+int esp_lp_set_engine(esp_handle *h, int32_t engine);
 /* 0: the reference's trial moves (default); 1: the learned proposal (needs
  * weights).  Applies to esp_sweep, esp_sweep_colour, esp_run and esp_advance. */
 int esp_set_proposal(esp_handle *h, int32_t kind);

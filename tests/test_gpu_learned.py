@@ -76,6 +76,25 @@ def test_fused_forward_matches_fp64_network():
     assert np.max(np.abs(got - want)) <= 2e-2 * scale, np.max(np.abs(got - want)) / scale
 
 
+def test_tcgen05_forward_matches_fp64_network_and_mma_path():
+    """The tcgen05 engine (128-row tiles, tensor-memory accumulators) against
+    the FP64 network and the mma.sync engine on the same rows."""
+    p = _weights(11)
+    rng = np.random.default_rng(12)
+    x = rng.normal(size=(1000, 12)).astype(np.float32)   # ragged: not a multiple of 128
+    with _small_engine() as e:
+        e.lp_set_weights(p)
+        ref = e.lp_forward(x)
+        e.lp_set_engine("tcgen05")
+        got = e.lp_forward(x)
+    want = O.lp_forward(_rounded(p), bf16(x))
+    scale = np.abs(want).max()
+    assert np.max(np.abs(got - want)) <= 2e-2 * scale, np.max(np.abs(got - want)) / scale
+    # both engines round the hidden activations to bf16 the same way; only the
+    # FP32 accumulation order differs
+    assert np.max(np.abs(got - ref)) <= 5e-3 * scale, np.max(np.abs(got - ref)) / scale
+
+
 def test_training_loss_and_gradient_match_fp64_network():
     p = _weights(3)
     rng = np.random.default_rng(4)
