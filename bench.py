@@ -64,6 +64,7 @@ def _args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--proposal", choices=["plain", "learned", "compare"], default="plain")
+    p.add_argument("--lp-engine", choices=["mma", "tcgen05"], default="tcgen05")
     p.add_argument("--train-pairs", type=int, default=10_000_000)
     p.add_argument("--train-steps", type=int, default=3000)
     p.add_argument("--measure-sweeps", type=int, default=20000)
@@ -265,6 +266,7 @@ def learned_compare(a, rank, local):
     t_collect = time.perf_counter() - t0
     start = eng.get_spins()
     eng.lp_init(seed=seed)
+    eng.lp_set_engine(a.lp_engine)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     loss = eng.lp_train(a.train_steps, batch=4096, lr=1e-3, seed=seed)
@@ -455,6 +457,7 @@ def main():
     if a.proposal == "learned":
         # an untrained network (the learned sampler's cost does not depend on its weights)
         eng.lp_init(seed=seed)
+        eng.lp_set_engine(a.lp_engine)
         eng.set_proposal("learned")
     _, ncol = eng.colouring()
     mode = 1 if inp.mcarlo_mode.startswith("const") else 0
@@ -517,7 +520,8 @@ def main():
         peak, peak_kind = _peaks("tensor")
         achieved = flop_per_launch / per_launch_s / 1e12
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                    "frac": achieved / peak, "traffic": None, "kernel": "k_sweep_lp",
+                    "frac": achieved / peak, "traffic": None,
+                    "kernel": "k_sweep_lp_tc" if a.lp_engine == "tcgen05" else "k_sweep_lp",
                     "flop_per_launch": flop_per_launch, "sweeps_timed": nsw, "launch_us": per_launch_s * 1e6,
                     "peak_source": peak_kind,
                     "hbm_equivalent_GBps": bytes_per_launch / per_launch_s / 1e9}
@@ -541,6 +545,7 @@ def main():
     eng2.set_temperatures(inp.tems)
     if a.proposal == "learned":
         eng2.lp_init(seed=seed)
+        eng2.lp_set_engine(a.lp_engine)
         eng2.set_proposal("learned")
     elif kernel == "cluster":
         eng2.set_cluster_geometry(*eng.cluster_geometry())

@@ -103,6 +103,11 @@ struct esp_handle {
     int proposal = 0;               // 0 plain Metropolis, 1 learned
     int lp_engine = 0;              // network on 0: mma.sync (warp tiles), 1: tcgen05 (128-row tiles)
     int *d_tc_err = nullptr;        // set by a tensor-core completion wait that gave up
+    // partial sums of the tcgen05 learned sweep (128-thread blocks)
+    int tc_grid = 0, tc_slots = 0;
+    double *d_tc_part = nullptr;
+    unsigned long long *d_tc_part_rej = nullptr;
+    long long tc_pending = 0;
     bool lp_weights = false;
     int lp_grid = 0;
     float *d_lp_p = nullptr, *d_lp_g = nullptr, *d_lp_m = nullptr, *d_lp_v = nullptr;
@@ -165,6 +170,7 @@ void free_tables(esp_handle *h)
     dfree(h->d_nnb); dfree(h->d_nbr); dfree(h->d_perm); dfree(h->d_inv);
     dfree(h->d_J); dfree(h->d_B); dfree(h->d_Dx); dfree(h->d_Dy); dfree(h->d_Dz); dfree(h->d_mag);
     dfree(h->d_si); dfree(h->d_fld); dfree(h->d_scratch); dfree(h->d_part); dfree(h->d_part_rej);
+    dfree(h->d_tc_part); dfree(h->d_tc_part_rej);
     dfree(h->d_stencil_blob); dfree(h->d_nbidx); dfree(h->d_lp_axis);
     dfree(h->d_tile_offs); dfree(h->d_tile_cpl); dfree(h->d_tile_part); dfree(h->d_tile_rej);
     h->cluster_ok = false;
@@ -239,6 +245,15 @@ int require(esp_handle *h, bool tables, bool temps)
 // magnetisations and rejected counters (k_fold), in block order.
 int fold(esp_handle *h)
 {
+    if (h->tc_pending > 0) {
+        FoldArgs f;
+        f.part = h->d_tc_part; f.part_rej = h->d_tc_part_rej; f.e_run = h->d_e_run; f.m_run = h->d_m_run;
+        f.rej = h->d_rej; f.temp_of = h->d_temp_of; f.R = h->R; f.nblocks = h->tc_grid; f.slots = h->tc_slots;
+        f.block_threads = 128; f.phase = h->pending_phase;
+        CK(launch_fold(f, h->st));
+        h->launches++;
+        h->tc_pending = 0;
+    }
     if (h->tile_pending > 0) {
         TileFoldArgs t;
         t.part = h->d_tile_part; t.part_rej = h->d_tile_rej; t.e_run = h->d_e_run; t.m_run = h->d_m_run;
@@ -380,6 +395,17 @@ int do_sweep_colour(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o
         la.w.w1 = h->d_lp_w1; la.w.w2 = h->d_lp_w2; la.w.w3 = h->d_lp_w3;
         la.w.b1 = h->d_lp_p + kPadB1; la.w.b2 = h->d_lp_p + kPadB2; la.w.b3 = h->d_lp_p + kPadB3;
         la.axis = h->hsi ? h->d_lp_axis : nullptr;
+        if (h->lp_engine == 1) {
+            if (!h->d_tc_err) {
+                CK(dalloc(&h->d_tc_err, 1));
+                CK(cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->st));
+            }
+            CK(launch_sweep_lp_tc(la, h->prep.has_b, h->prep.has_d, h->tc_grid, h->d_tc_part, h->d_tc_part_rej,
+                                  h->tc_slots, h->d_tc_err, h->st));
+            h->launches++;
+            h->tc_pending++;
+            return ESP_OK;
+        }
         CK(launch_sweep_lp(la, h->prep.has_b, h->prep.has_d, h->lp_grid, h->st));
     } else {
         CK(launch_sweep(a, h->prep.has_b, h->prep.has_d, h->sweep_grid, h->st));
@@ -749,6 +775,7 @@ int esp_create(const esp_dims *dims, esp_handle **out)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = lp_configure(h->device);
     if (e == cudaSuccess) e = lp_tc_configure();
+    if (e == cudaSuccess) e = lp_tc_sweep_configure();
     if (e != cudaSuccess) {
         set_global_error("CUDA unavailable: %s", cudaGetErrorString(e));
         delete h;
@@ -880,6 +907,14 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
         // the learned sweep's 512-thread blocks count as two 256-thread blocks
         h->lp_grid = lp_sweep_blocks((long long)maxc * h->R, h->R, h->num_sms);
         h->part_blocks = std::max(h->sweep_grid, 2 * h->lp_grid);
+        h->tc_grid = lp_tc_sweep_blocks((long long)maxc * h->R, h->R, h->num_sms);
+        h->tc_slots = std::min(h->R, 128);
+        const size_t tslot = (size_t)h->tc_grid * h->tc_slots;
+        CK(dalloc(&h->d_tc_part, 4 * tslot));
+        CK(dalloc(&h->d_tc_part_rej, tslot));
+        CK(cudaMemsetAsync(h->d_tc_part, 0, sizeof(double) * 4 * tslot, h->st));
+        CK(cudaMemsetAsync(h->d_tc_part_rej, 0, sizeof(unsigned long long) * tslot, h->st));
+        h->tc_pending = 0;
         const size_t nslot = (size_t)h->part_blocks * h->slots;
         CK(dalloc(&h->d_part, 4 * nslot));
         CK(dalloc(&h->d_part_rej, nslot));
@@ -1441,6 +1476,11 @@ int esp_collect(esp_handle *h, esp_results *res)
     if (!u.active) { h->err = "esp_begin has not been called"; return ESP_ESTATE; }
     if (!res) { h->err = "null results"; return ESP_EINVAL; }
     if (u.meas_done < 1) { h->err = "no measurement has been made (esp_advance)"; return ESP_ESTATE; }
+    if (h->d_tc_err) {
+        int flag = 0;
+        if ((rc = d2h(h, &flag, h->d_tc_err, sizeof(int)))) return rc;
+        if (flag) { h->err = "a tensor-core completion wait of the learned sweep gave up"; return ESP_ETIMEOUT; }
+    }
     const int R = h->R, N = h->N, nlev = u.nlev;
     const esp_schedule &s = u.s;
     const int64_t steps_mc = u.meas_done;

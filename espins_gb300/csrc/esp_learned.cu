@@ -16,6 +16,7 @@
 // non-symmetric proposal); the network and its training have no counterpart
 // in the reference.
 #include "esp_learned.h"
+#include "esp_lp_tc.cuh"
 
 namespace esp {
 
@@ -92,6 +93,49 @@ __device__ __forceinline__ void store_features(__nv_bfloat16 *row, const float *
     v1.x = pack_bf16(f[8], f[9]); v1.y = pack_bf16(f[10], f[11]); v1.z = 0u; v1.w = 0u;
     reinterpret_cast<uint4 *>(row)[0] = v0;
     reinterpret_cast<uint4 *>(row)[1] = v1;
+}
+
+// One learned Metropolis-Hastings trial of permuted site p in replica r from
+// the network outputs o: a vMF-mixture sample, both log-densities, the
+// energy change of the local form g.s + s^T Q s, the test
+// u < exp(-beta dE) q(old) / q(new), and the update.
+__device__ __forceinline__ void lp_trial(const SweepArgs &a, const LpFrame &fr, const float *o, int p, int r, int orig,
+                                         float mag, float beta, float gx, float gy, float gz, const float q[6],
+                                         uint32_t sw_lo, uint32_t sw_hi, float &accE, float &accX, float &accY,
+                                         float &accZ, unsigned int &nrej)
+{
+    VmfMix mix;
+    vmf_params(o, fr.kappa0, mix);
+    const size_t idx = (size_t)p * a.R + r;
+    const float ox = a.sx[idx], oy = a.sy[idx], oz = a.sz[idx];
+    const Philox4 x = philox4x32_10((uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
+    float ux, uy, uz;
+    vmf_sample(mix, u24f(x.x), u24f(x.y), u24f(x.z), ux, uy, uz);
+    const float nx = mag * (ux * fr.e[0][0] + uy * fr.e[1][0] + uz * fr.e[2][0]);
+    const float ny = mag * (ux * fr.e[0][1] + uy * fr.e[1][1] + uz * fr.e[2][1]);
+    const float nz = mag * (ux * fr.e[0][2] + uy * fr.e[1][2] + uz * fr.e[2][2]);
+    const float im = 1.f / mag;
+    const float lx = (ox * fr.e[0][0] + oy * fr.e[0][1] + oz * fr.e[0][2]) * im;
+    const float ly = (ox * fr.e[1][0] + oy * fr.e[1][1] + oz * fr.e[1][2]) * im;
+    const float lz = (ox * fr.e[2][0] + oy * fr.e[2][1] + oz * fr.e[2][2]) * im;
+    const float lq_new = vmf_logpdf(mix, ux, uy, uz);
+    const float lq_old = vmf_logpdf(mix, lx, ly, lz);
+    const float dx = nx - ox, dy = ny - oy, dz = nz - oz;
+    const float px = nx + ox, py = ny + oy, pz = nz + oz;
+    const float de = gx * dx + gy * dy + gz * dz
+                   + dx * (q[0] * px + q[3] * py + q[4] * pz)
+                   + dy * (q[3] * px + q[1] * py + q[5] * pz)
+                   + dz * (q[4] * px + q[5] * py + q[2] * pz);
+    // Metropolis-Hastings: accept with min(1, exp(-beta dE) q(old) / q(new))
+    const float lacc = -beta * de + lq_old - lq_new;
+    const bool acc = lacc >= 0.f || u24f(x.w) < expf(lacc);
+    if (acc) {
+        a.sx[idx] = nx; a.sy[idx] = ny; a.sz[idx] = nz;
+        accE += de;
+        accX += dx; accY += dy; accZ += dz;
+    } else {
+        ++nrej;
+    }
 }
 
 constexpr int kLpThreads = 512;
@@ -187,46 +231,98 @@ __global__ void __launch_bounds__(kLpThreads, 1) k_sweep_lp(const LpSweepArgs la
             for (int i = 0; i < kMlpOut; ++i) o[i] = orow[i];
         }
         __syncwarp();
-        if (act && mag > 0.f) {
-            VmfMix mix;
-            vmf_params(o, fr.kappa0, mix);
-            const size_t idx = (size_t)p * R + r;
-            const float ox = a.sx[idx], oy = a.sy[idx], oz = a.sz[idx];
-            const Philox4 x = philox4x32_10((uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
-            float ux, uy, uz;
-            vmf_sample(mix, u24f(x.x), u24f(x.y), u24f(x.z), ux, uy, uz);
-            const float nx = mag * (ux * fr.e[0][0] + uy * fr.e[1][0] + uz * fr.e[2][0]);
-            const float ny = mag * (ux * fr.e[0][1] + uy * fr.e[1][1] + uz * fr.e[2][1]);
-            const float nz = mag * (ux * fr.e[0][2] + uy * fr.e[1][2] + uz * fr.e[2][2]);
-            const float im = 1.f / mag;
-            const float lx = (ox * fr.e[0][0] + oy * fr.e[0][1] + oz * fr.e[0][2]) * im;
-            const float ly = (ox * fr.e[1][0] + oy * fr.e[1][1] + oz * fr.e[1][2]) * im;
-            const float lz = (ox * fr.e[2][0] + oy * fr.e[2][1] + oz * fr.e[2][2]) * im;
-            const float lq_new = vmf_logpdf(mix, ux, uy, uz);
-            const float lq_old = vmf_logpdf(mix, lx, ly, lz);
-            const float dx = nx - ox, dy = ny - oy, dz = nz - oz;
-            const float px = nx + ox, py = ny + oy, pz = nz + oz;
-            const float de = gx * dx + gy * dy + gz * dz
-                           + dx * (q[0] * px + q[3] * py + q[4] * pz)
-                           + dy * (q[3] * px + q[1] * py + q[5] * pz)
-                           + dz * (q[4] * px + q[5] * py + q[2] * pz);
-            // Metropolis-Hastings: accept with min(1, exp(-beta dE) q(old) / q(new))
-            const float lacc = -beta * de + lq_old - lq_new;
-            const bool acc = lacc >= 0.f || u24f(x.w) < expf(lacc);
-            if (acc) {
-                a.sx[idx] = nx; a.sy[idx] = ny; a.sz[idx] = nz;
-                accE += de;
-                accX += dx; accY += dy; accZ += dz;
-            } else {
-                ++nrej;
-            }
-        }
+        if (act && mag > 0.f)
+            lp_trial(a, fr, o, p, r, orig, mag, beta, gx, gy, gz, q, sw_lo, sw_hi, accE, accX, accY, accZ, nrej);
         pi += pstep;
     }
     __syncthreads();   // the warp buffers become the reduction scratch
     double *s_part = reinterpret_cast<double *>(bufs);
     unsigned int *s_rej = reinterpret_cast<unsigned int *>(s_part + 4 * kLpThreads);
     add_slots_512(accE, accX, accY, accZ, nrej, R, a.slots, a.part, a.part_rej, s_part, s_rej);
+}
+
+// ---------------------------------------------------------------------------
+// The same sweep with the network on tcgen05: CTAs of 128 threads, thread t
+// owns one trial and tensor-memory lane t; each pass evaluates the network on
+// the 128 current trials with three chains of MMAs (K = 16, 128, 128) into
+// tensor memory.  Partial sums go to slots of 128-thread blocks
+// (thread t of block b works on replica (b*128 + t) % R).
+// ---------------------------------------------------------------------------
+template <bool HB, bool HD>
+__global__ void __launch_bounds__(kTcRows) k_sweep_lp_tc(const LpSweepArgs la, double *part,
+                                                         unsigned long long *part_rej, int slots, int *err)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    TcSmem &s = *reinterpret_cast<TcSmem *>(smem);
+    const SweepArgs &a = la.s;
+    tc_stage_weights(la.w, s);
+    tc_setup(s);
+
+    const int R = a.R;
+    const long long nthreads = (long long)gridDim.x * blockDim.x;
+    const long long S = (nthreads / R) * R;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = (int)(tid % R);
+    const float beta = a.beta[a.temp_of[r]];
+    const int pstep = (int)(S / R);
+    float accE = 0.f, accX = 0.f, accY = 0.f, accZ = 0.f;
+    unsigned int nrej = 0;
+    uint32_t sw_lo, sw_hi;
+    sweep_index(a, sw_lo, sw_hi);
+    uint32_t phase = 0;
+    int pi = tid < S ? (int)(tid / R) : a.n_c;
+    while (__syncthreads_or(pi < a.n_c)) {
+        const bool act = pi < a.n_c;
+        const int p = a.off_c + (act ? pi : 0);
+        const int orig = __ldg(a.perm + p);
+        const float mag = __ldg(a.mag + p);
+        float gx = 0.f, gy = 0.f, gz = 0.f, q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float f[kMlpIn];
+        LpFrame fr;
+        if (act) {
+            site_terms<HB, HD>(a, p, r, orig, gx, gy, gz, q);
+            float ax, ay, az;
+            frame_axis(la.axis, orig, a.num_atoms, ax, ay, az);
+            lp_frame_features(beta, mag, gx, gy, gz, q, ax, ay, az, fr, f);
+        } else {
+            for (int i = 0; i < kMlpIn; ++i) f[i] = 0.f;
+            fr.kappa0 = 0.f;
+        }
+        tc_store_x_row(s, threadIdx.x, f);
+        float o[kMlpOut];
+        tc_forward(s, phase, o);
+        if (act && mag > 0.f)
+            lp_trial(a, fr, o, p, r, orig, mag, beta, gx, gy, gz, q, sw_lo, sw_hi, accE, accX, accY, accZ, nrej);
+        pi += pstep;
+    }
+    tc_teardown(s);
+    if (threadIdx.x == 0 && s.error) atomicExch(err, 1);
+    // the activation tile becomes the reduction scratch
+    __syncthreads();
+    double *sp = reinterpret_cast<double *>(s.h);
+    unsigned int *sr = reinterpret_cast<unsigned int *>(sp + 4 * kTcRows);
+    const int t = threadIdx.x;
+    const size_t slot = (size_t)blockIdx.x * slots + t;
+    if (R >= kTcRows) {
+        double *o = part + 4 * slot;
+        o[0] += (double)accE; o[1] += (double)accX; o[2] += (double)accY; o[3] += (double)accZ;
+        part_rej[slot] += (unsigned long long)nrej;
+        return;
+    }
+    sp[4 * t] = (double)accE; sp[4 * t + 1] = (double)accX; sp[4 * t + 2] = (double)accY; sp[4 * t + 3] = (double)accZ;
+    sr[t] = nrej;
+    __syncthreads();
+    if (t < R) {
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        unsigned long long nr = 0;
+        for (int u = t; u < kTcRows; u += R) {
+            a0 += sp[4 * u]; a1 += sp[4 * u + 1]; a2 += sp[4 * u + 2]; a3 += sp[4 * u + 3];
+            nr += sr[u];
+        }
+        double *o = part + 4 * slot;
+        o[0] += a0; o[1] += a1; o[2] += a2; o[3] += a3;
+        part_rej[slot] += nr;
+    }
 }
 
 // Training pairs of one colour class: item i = pi * R + r for i in [0, count).
@@ -507,6 +603,37 @@ cudaError_t lp_configure(int device)
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_lp<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e;
+}
+
+int lp_tc_sweep_blocks(long long max_items, int R, int num_sms)
+{
+    long long b = (max_items + kTcRows - 1) / kTcRows;
+    if (b > 2 * num_sms) b = 2 * num_sms;
+    const long long need = (R + kTcRows - 1) / kTcRows;
+    if (b < need) b = need;
+    return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t lp_tc_sweep_configure()
+{
+    const int bytes = (int)sizeof(TcSmem);
+    static_assert(sizeof(TcSmem) >= kTcRows * (4 * sizeof(double) + sizeof(unsigned int)), "scratch");
+    cudaError_t e = cudaFuncSetAttribute(k_sweep_lp_tc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_lp_tc<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_lp_tc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_lp_tc<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return e;
+}
+
+cudaError_t launch_sweep_lp_tc(const LpSweepArgs &a, bool hb, bool hd, int blocks, double *part,
+                               unsigned long long *part_rej, int slots, int *err, cudaStream_t st)
+{
+    const size_t sm = sizeof(TcSmem);
+    if (hb && hd) k_sweep_lp_tc<true, true><<<blocks, kTcRows, sm, st>>>(a, part, part_rej, slots, err);
+    else if (hb) k_sweep_lp_tc<true, false><<<blocks, kTcRows, sm, st>>>(a, part, part_rej, slots, err);
+    else if (hd) k_sweep_lp_tc<false, true><<<blocks, kTcRows, sm, st>>>(a, part, part_rej, slots, err);
+    else k_sweep_lp_tc<false, false><<<blocks, kTcRows, sm, st>>>(a, part, part_rej, slots, err);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_sweep_lp(const LpSweepArgs &a, bool hb, bool hd, int blocks, cudaStream_t st)

@@ -53,6 +53,12 @@ size_t lp_sweep_smem_bytes();
 int lp_sweep_blocks(long long max_items, int R, int num_sms);
 cudaError_t lp_configure(int device);
 cudaError_t launch_sweep_lp(const LpSweepArgs &a, bool hb, bool hd, int blocks, cudaStream_t st);
+// tcgen05 variant: 128-thread CTAs with their own partial slots [blocks][slots]
+// (slots = min(R, 128)); err is set when a tensor-core wait gave up
+int lp_tc_sweep_blocks(long long max_items, int R, int num_sms);
+cudaError_t lp_tc_sweep_configure();
+cudaError_t launch_sweep_lp_tc(const LpSweepArgs &a, bool hb, bool hd, int blocks, double *part,
+                               unsigned long long *part_rej, int slots, int *err, cudaStream_t st);
 cudaError_t launch_lp_collect(const LpCollectArgs &a, bool hb, bool hd, int max_blocks, cudaStream_t st);
 // C = op(A) op(B): ta -> A stored [K][M] (else [M][K]); tb -> B stored [K][N] (else [N][K])
 cudaError_t launch_gemm(const GemmArgs &g, bool ta, bool tb, cudaStream_t st);

@@ -155,13 +155,14 @@ def test_collected_pairs_match_oracle_features():
 COPIES = 4
 
 
-def _learned_copies(h, tems, warm, mc, weights, seed=2468):
+def _learned_copies(h, tems, warm, mc, weights, seed=2468, engine="mma"):
     rt = np.repeat(np.asarray(tems, dtype=float), COPIES)
     with Engine(h.n, h.num_atoms, h.supercell, len(rt)) as e:
         e.upload(h)
         e.set_temperatures(rt)
         e.init_spins("ferro")
         e.lp_set_weights(weights)
+        e.lp_set_engine(engine)
         e.set_proposal("learned")
         assert e.sweep_kernel()[0] == "learned"
         res = e.run(warm, mc, 1, pt=False, seed=seed, binning_level=LEVELS)
@@ -193,22 +194,24 @@ def _exact_energy_per_site(h, T):
     return float((e * w).sum() / w.sum())
 
 
+@pytest.mark.parametrize("engine", ["mma", "tcgen05"])
 @pytest.mark.parametrize("out_scale", [0.0, 0.3])
-def test_learned_sampler_is_exact_on_independent_sites(out_scale):
+def test_learned_sampler_is_exact_on_independent_sites(out_scale, engine):
     """Any network gives the exact single-site distribution: the zero network
     (the Heisenberg conditional, far from the true one because of the
     anisotropy) and a random one whose proposals point anywhere."""
     tems = [2.0, 6.0, 20.0]
     inp, h = _independent_sites(tems)
     warm, mc = 500, 20000
-    gd, gb, res = _learned_copies(h, tems, warm, mc, _weights(8, out_scale=out_scale))
+    gd, gb, res = _learned_copies(h, tems, warm, mc, _weights(8, out_scale=out_scale), engine=engine)
     for t, T in enumerate(tems):
         g, sg = _mean_sigma(gd[t], gb[t], h.n)
         want = _exact_energy_per_site(h, T)
         assert abs(g[0] - want) <= 3 * sg[0] + 1e-5 * abs(want), (T, g[0], want, sg[0])
 
 
-def test_learned_sampler_matches_reference_algorithm():
+@pytest.mark.parametrize("engine", ["mma", "tcgen05"])
+def test_learned_sampler_matches_reference_algorithm(engine):
     """An untrained network away from the prior on a frustrated lattice with
     biquadratic and single-ion terms: the exact Hastings ratio keeps the
     chain on the reference algorithm's stationary averages."""
@@ -216,7 +219,7 @@ def test_learned_sampler_matches_reference_algorithm():
     h = build_hamiltonian(inp)
     tems = inp.tems
     warm, mc = 2000, 30000
-    gd, gb, res = _learned_copies(h, tems, warm, mc, _weights(7, out_scale=0.03))
+    gd, gb, res = _learned_copies(h, tems, warm, mc, _weights(7, out_scale=0.03), engine=engine)
     od, ob = _oracle_chains(h, tems, warm, mc, 515)
     _check(h, tems, gd, gb, od, ob, "learned MH")
     e = res["energy"]
