@@ -396,10 +396,8 @@ int do_sweep_colour(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o
         la.w.b1 = h->d_lp_p + kPadB1; la.w.b2 = h->d_lp_p + kPadB2; la.w.b3 = h->d_lp_p + kPadB3;
         la.axis = h->hsi ? h->d_lp_axis : nullptr;
         if (h->lp_engine == 1) {
-            if (!h->d_tc_err) {
-                CK(dalloc(&h->d_tc_err, 1));
-                CK(cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->st));
-            }
+            // d_tc_err exists: esp_lp_set_engine allocates it (no allocation here,
+            // this may run inside a graph capture)
             CK(launch_sweep_lp_tc(la, h->prep.has_b, h->prep.has_d, h->tc_grid, h->d_tc_part, h->d_tc_part_rej,
                                   h->tc_slots, h->d_tc_err, h->st));
             h->launches++;
@@ -1882,7 +1880,6 @@ int esp_lp_forward(esp_handle *h, const float *features, int64_t n, float *out)
     w.w1 = h->d_lp_w1; w.w2 = h->d_lp_w2; w.w3 = h->d_lp_w3;
     w.b1 = h->d_lp_p + kPadB1; w.b2 = h->d_lp_p + kPadB2; w.b3 = h->d_lp_p + kPadB3;
     if (h->lp_engine == 1) {
-        if (e == cudaSuccess && !h->d_tc_err) e = dalloc(&h->d_tc_err, 1);
         if (e == cudaSuccess) e = cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->st);
         if (e == cudaSuccess) e = launch_lp_forward_tc(w, dx, (int)n, dout, h->d_tc_err, h->num_sms, h->st);
     } else if (e == cudaSuccess) {
@@ -1907,6 +1904,10 @@ int esp_lp_set_engine(esp_handle *h, int32_t engine)
     if (!h || engine < 0 || engine > 1) return ESP_EINVAL;
     int rc = fold(h);
     if (rc) return rc;
+    if (engine == 1 && !h->d_tc_err) {
+        CK(dalloc(&h->d_tc_err, 1));
+        CK(cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->st));
+    }
     h->lp_engine = engine;
     return ESP_OK;
 }
