@@ -95,6 +95,14 @@ struct esp_handle {
     int nlev_alloc = 0;
     unsigned long long *d_pm = nullptr;
     long long *d_swaps = nullptr;
+    // optional measurements (esp_set_observables): bit 0 order parameter,
+    // bit 1 staggered magnetisation
+    int obs = 0;
+    float4 *d_obs_atom = nullptr;           // [na]: axis (x, y, z), coefficient (w)
+    double *d_obs_rep = nullptr;            // [R replicas] sum s.a, then [R replicas][3] sum c s
+    double *d_obs_data = nullptr;           // [R slots][6]
+    double *d_obs_lsum = nullptr, *d_obs_bin = nullptr;   // [R slots][nlev_alloc][2]
+    unsigned long long *d_obs_pm = nullptr; // [R slots][2][nf]
     std::vector<double> tems;
     int nf = 2;
     double m_min = 0, m_max = 0;
@@ -177,6 +185,12 @@ void free_tables(esp_handle *h)
     h->tile_ok = false;
 }
 
+void free_obs(esp_handle *h)
+{
+    dfree(h->d_obs_atom); dfree(h->d_obs_rep); dfree(h->d_obs_data); dfree(h->d_obs_pm);
+    h->obs = 0;
+}
+
 void free_lp_batch(esp_handle *h)
 {
     dfree(h->d_lp_xb); dfree(h->d_lp_h1); dfree(h->d_lp_h2); dfree(h->d_lp_do); dfree(h->d_lp_dz2);
@@ -191,6 +205,8 @@ void free_all(esp_handle *h)
     dfree(h->d_temp_of); dfree(h->d_repl_at); dfree(h->d_beta); dfree(h->d_inv_t);
     dfree(h->d_e_run); dfree(h->d_m_run); dfree(h->d_rej); dfree(h->d_tmp_e); dfree(h->d_tmp_m);
     dfree(h->d_data); dfree(h->d_lsum); dfree(h->d_bin); dfree(h->d_levels); dfree(h->d_pm); dfree(h->d_swaps);
+    dfree(h->d_obs_lsum); dfree(h->d_obs_bin);
+    free_obs(h);
     dfree(h->d_series);
     free_lp_batch(h);
     dfree(h->d_lp_p); dfree(h->d_lp_g); dfree(h->d_lp_m); dfree(h->d_lp_v);
@@ -361,6 +377,9 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     a.fd_hy = make_fastdiv((uint32_t)(h->L[1] / 2));
     a.key0 = (uint32_t)o->seed; a.key1 = (uint32_t)(o->seed >> 32);
     a.mode = o->mcarlo_mode ? 1 : 0; a.tilt = (float)o->tilt_angles_max;
+    a.obs = measure ? h->obs : 0;
+    a.obs_atom = h->d_obs_atom; a.obs_data = h->d_obs_data; a.obs_lsum = h->d_obs_lsum; a.obs_bin = h->d_obs_bin;
+    a.obs_pm = h->d_obs_pm;
     CK(launch_cluster(a, h->csize, h->cthreads, h->cluster_smem, h->st));
     h->launches++;
     return ESP_OK;
@@ -496,17 +515,29 @@ int measure(esp_handle *h, long long step, int nlev, bool pt_quirk, long long &c
         m.step -= h->cap_base[2];
         m.ctr = h->d_ctr + 2;
     }
+    m.obs = h->obs;
+    m.obs_rep = h->d_obs_rep; m.obs_data = h->d_obs_data; m.obs_lsum = h->d_obs_lsum; m.obs_bin = h->d_obs_bin;
+    if (h->obs) {
+        // orderparam_get / staggered_get sums of every replica (the energy
+        // scratch is free between energy evaluations)
+        ObsArgs oa;
+        oa.sx = h->d_sx; oa.sy = h->d_sy; oa.sz = h->d_sz; oa.perm = h->d_perm; oa.atom = h->d_obs_atom;
+        oa.scratch = h->d_scratch; oa.N = h->N; oa.R = h->R; oa.num_atoms = h->na;
+        CK(launch_obs(oa, h->d_obs_rep, h->d_obs_rep + h->R, h->e_blocks, h->st));
+        h->launches += 2;
+    }
     CK(launch_measure(m, h->st));
     h->launches++;
-    if (h->na == 1) {
-        // one atom per cell: |sum_cell s| = |m| for every cell, so every cell
-        // lands in the top bin of Pm_get's grid; count it without a pass.
-        const_hits++;
-    } else {
+    // one atom per cell: |sum_cell s| = |m| for every cell, so every cell
+    // lands in the top bin of Pm_get's grid; count it without a pass.
+    if (h->na == 1) const_hits++;
+    if (h->na > 1 || h->obs) {
         PmArgs p;
         p.sx = h->d_sx; p.sy = h->d_sy; p.sz = h->d_sz; p.inv = h->d_inv; p.temp_of = h->d_temp_of;
         p.counts = h->d_pm; p.R = h->R; p.ncell = h->N / h->na; p.num_atoms = h->na; p.nf = h->nf;
         p.use_shared = 0; p.m_min = h->m_min; p.m_max = h->m_max;
+        p.count_m = h->na > 1 ? 1 : 0;
+        p.obs = h->obs; p.obs_atom = h->d_obs_atom; p.obs_counts = h->d_obs_pm;
         CK(launch_pm(p, h->max_blocks, h->st));
         h->launches++;
     }
@@ -516,9 +547,11 @@ int measure(esp_handle *h, long long step, int nlev, bool pt_quirk, long long &c
 int ensure_levels(esp_handle *h, int nlev, const int32_t *levels)
 {
     if (nlev > h->nlev_alloc) {
-        dfree(h->d_lsum); dfree(h->d_bin); dfree(h->d_levels);
+        dfree(h->d_lsum); dfree(h->d_bin); dfree(h->d_levels); dfree(h->d_obs_lsum); dfree(h->d_obs_bin);
         CK(dalloc(&h->d_lsum, (size_t)h->R * nlev * 2));
         CK(dalloc(&h->d_bin, (size_t)h->R * nlev * 2));
+        CK(dalloc(&h->d_obs_lsum, (size_t)h->R * nlev * 2));
+        CK(dalloc(&h->d_obs_bin, (size_t)h->R * nlev * 2));
         CK(dalloc(&h->d_levels, (size_t)nlev));
         h->nlev_alloc = nlev;
     }
@@ -526,6 +559,8 @@ int ensure_levels(esp_handle *h, int nlev, const int32_t *levels)
         CK(cudaMemcpyAsync(h->d_levels, levels, sizeof(int32_t) * nlev, cudaMemcpyHostToDevice, h->st));
         CK(cudaMemsetAsync(h->d_lsum, 0, sizeof(double) * h->R * nlev * 2, h->st));
         CK(cudaMemsetAsync(h->d_bin, 0, sizeof(double) * h->R * nlev * 2, h->st));
+        CK(cudaMemsetAsync(h->d_obs_lsum, 0, sizeof(double) * h->R * nlev * 2, h->st));
+        CK(cudaMemsetAsync(h->d_obs_bin, 0, sizeof(double) * h->R * nlev * 2, h->st));
     }
     return ESP_OK;
 }
@@ -565,7 +600,7 @@ std::vector<ClusterGeom> cluster_candidates(const esp_handle *h)
     for (int nt : nts)
         for (int cs = 1; cs <= 16; ++cs) {
             if (h->L[2] % (2 * cs) != 0) continue;
-            const size_t smem = cluster_smem_bytes(h->N / cs, h->nf, h->cl_sbytes);
+            const size_t smem = cluster_smem_bytes(h->N / cs, h->nf, h->obs ? 3 : 1, h->cl_sbytes);
             if (smem > 226 * 1024) continue;
             const int active = cluster_max_active(cs, nt, smem, h->R);
             if (active <= 0) continue;
@@ -696,7 +731,7 @@ int cluster_geometry(esp_handle *h, int cs, int nt)
 {
     const int maxst = h->cl_maxst;
     const int pz = h->L[2] / cs, n_local = h->N / cs;
-    const size_t smem = cluster_smem_bytes(n_local, h->nf, h->cl_sbytes);
+    const size_t smem = cluster_smem_bytes(n_local, h->nf, h->obs ? 3 : 1, h->cl_sbytes);
     CK(cluster_configure(smem, cs, nt));
     const int Lx = h->L[0], Ly = h->L[1], Lz = h->L[2], Hx = Lx / 2, Hy = Ly / 2, Hzl = pz / 2;
     const int per_class = Hx * Hy * Hzl;
@@ -854,6 +889,7 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
     if (rc) { h->err = err; return rc == 2 ? ESP_ECOLOR : ESP_EINVAL; }
     CK(cudaStreamSynchronize(h->st));
     free_tables(h);
+    free_obs(h);
     h->have_tables = false;
     const size_t M = (size_t)prep.maxnb * h->N;
     CK(dalloc(&h->d_nnb, h->N));
@@ -1367,6 +1403,10 @@ int esp_begin(esp_handle *h, const esp_schedule *s)
     u.nlev = nlev;
     CK(cudaMemsetAsync(h->d_data, 0, sizeof(double) * 6 * R, h->st));
     CK(cudaMemsetAsync(h->d_pm, 0, sizeof(unsigned long long) * R * h->nf, h->st));
+    if (h->obs) {
+        CK(cudaMemsetAsync(h->d_obs_data, 0, sizeof(double) * 6 * R, h->st));
+        CK(cudaMemsetAsync(h->d_obs_pm, 0, sizeof(unsigned long long) * 2 * R * h->nf, h->st));
+    }
     CK(cudaMemsetAsync(h->d_rej, 0, sizeof(unsigned long long) * 2 * R, h->st));
     CK(cudaMemsetAsync(h->d_swaps, 0, sizeof(long long) * 2 * R, h->st));
     esp_sweep_opts o;
@@ -1543,6 +1583,115 @@ int esp_collect(esp_handle *h, esp_results *res)
             if ((rc = get_repl_at(h, ra))) return rc;
             for (int t = 0; t < R; ++t) res->map[t] = ra[t] + 1;
         }
+    }
+    return ESP_OK;
+}
+
+int esp_set_observables(esp_handle *h, int32_t flags, const double *orderparam_axes, const int32_t *staggered_coeff)
+{
+    if (!h) return ESP_EINVAL;
+    if (!h->have_tables) { h->err = "upload the tables before choosing the optional measurements"; return ESP_ESTATE; }
+    if (flags & ~(ESP_OBS_ORDER_PARAMETER | ESP_OBS_STAGGERED)) { h->err = "unknown measurement flag"; return ESP_EINVAL; }
+    if ((flags & ESP_OBS_ORDER_PARAMETER) && !orderparam_axes) { h->err = "order-parameter axes missing"; return ESP_EINVAL; }
+    if ((flags & ESP_OBS_STAGGERED) && !staggered_coeff) { h->err = "staggered coefficients missing"; return ESP_EINVAL; }
+    std::vector<float4> atom((size_t)h->na);
+    for (int at = 0; at < h->na; ++at) {
+        float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (flags & ESP_OBS_ORDER_PARAMETER) {
+            const double *ax = orderparam_axes + 3 * at;
+            if (!std::isfinite(ax[0]) || !std::isfinite(ax[1]) || !std::isfinite(ax[2])) {
+                h->err = "order-parameter axes must be finite";
+                return ESP_EINVAL;
+            }
+            w.x = (float)ax[0]; w.y = (float)ax[1]; w.z = (float)ax[2];
+        }
+        if (flags & ESP_OBS_STAGGERED) {
+            if (staggered_coeff[at] != 1 && staggered_coeff[at] != -1) {
+                h->err = "staggered_m_coeff must be +1 or -1";
+                return ESP_EINVAL;
+            }
+            w.w = (float)staggered_coeff[at];
+        }
+        atom[at] = w;
+    }
+    int rc = fold(h);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->st));
+    free_obs(h);
+    if (flags) {
+        CK(dalloc(&h->d_obs_atom, (size_t)h->na));
+        CK(dalloc(&h->d_obs_rep, (size_t)h->R * 4));
+        CK(dalloc(&h->d_obs_data, (size_t)h->R * 6));
+        CK(dalloc(&h->d_obs_pm, (size_t)h->R * 2 * h->nf));
+        if ((rc = h2d(h, h->d_obs_atom, atom.data(), sizeof(float4) * atom.size()))) return rc;
+        CK(cudaMemsetAsync(h->d_obs_data, 0, sizeof(double) * 6 * h->R, h->st));
+        CK(cudaMemsetAsync(h->d_obs_pm, 0, sizeof(unsigned long long) * 2 * h->R * h->nf, h->st));
+        CK(cudaMemsetAsync(h->d_obs_rep, 0, sizeof(double) * 4 * h->R, h->st));
+    }
+    h->obs = flags;
+    // the cluster kernel keeps two more histograms in shared memory: keep the
+    // geometry if it still fits, else take the best one that does
+    if (h->cluster_ok) {
+        const std::vector<ClusterGeom> c = cluster_candidates(h);
+        bool same = false;
+        for (const ClusterGeom &g : c) same = same || (g.cs == h->csize && g.nt == h->cthreads);
+        if (same) rc = cluster_geometry(h, h->csize, h->cthreads);
+        else if (!c.empty()) rc = cluster_geometry(h, c[0].cs, c[0].nt);
+        else h->cluster_ok = false;
+        if (rc) return rc;
+    }
+    CK(cudaStreamSynchronize(h->st));
+    return ESP_OK;
+}
+
+int esp_collect_observables(esp_handle *h, esp_obs_results *res)
+{
+    int rc = require(h, true, true);
+    if (rc) return rc;
+    RunState &u = h->run;
+    if (!u.active) { h->err = "esp_begin has not been called"; return ESP_ESTATE; }
+    if (!res) { h->err = "null results"; return ESP_EINVAL; }
+    if (!h->obs) { h->err = "no optional measurement was chosen (esp_set_observables)"; return ESP_ESTATE; }
+    if (u.meas_done < 1) { h->err = "no measurement has been made (esp_advance)"; return ESP_ESTATE; }
+    if ((rc = fold(h))) return rc;
+    const int R = h->R, N = h->N, nlev = u.nlev, nf = h->nf;
+    const int64_t steps_mc = u.meas_done;
+    const double norm = 1.0 / (double)steps_mc;
+    std::vector<double> data((size_t)R * 6);
+    if ((rc = d2h(h, data.data(), h->d_obs_data, sizeof(double) * data.size()))) return rc;
+    // mcarlo.F90:713-715 / pt.F90:995-1000
+    if (res->data)
+        for (size_t i = 0; i < data.size(); ++i) res->data[i] = data[i] * norm;
+    if (res->pm_op || res->pm_sm) {
+        std::vector<unsigned long long> cnt((size_t)R * 2 * nf);
+        if ((rc = d2h(h, cnt.data(), h->d_obs_pm, sizeof(unsigned long long) * cnt.size()))) return rc;
+        const double ncell = (double)(N / h->na);
+        for (int t = 0; t < R; ++t)
+            for (int f = 0; f < nf; ++f) {
+                const size_t o = (size_t)t * nf + f;
+                if (res->pm_op) res->pm_op[o] = (double)cnt[((size_t)t * 2) * nf + f] * (1.0 / 0.01) * norm / ncell;
+                if (res->pm_sm) res->pm_sm[o] = (double)cnt[((size_t)t * 2 + 1) * nf + f] * (1.0 / 0.01) * norm / ncell;
+            }
+    }
+    if (res->binning && nlev > 0) {
+        std::vector<double> ls((size_t)R * nlev * 2), bn((size_t)R * nlev * 2);
+        if ((rc = d2h(h, ls.data(), h->d_obs_lsum, sizeof(double) * ls.size()))) return rc;
+        if ((rc = d2h(h, bn.data(), h->d_obs_bin, sizeof(double) * bn.size()))) return rc;
+        // mcarlo.F90:640-656 / pt.F90:918-936 for the |OP| and |SM| rows
+        for (int t = 0; t < R; ++t)
+            for (int l = 0; l < nlev; ++l) {
+                const double blk = (double)(1LL << u.levels[l]);
+                const double m_l = (double)(steps_mc / (1LL << u.levels[l]));
+                for (int c = 0; c < 2; ++c) {
+                    const size_t k = ((size_t)t * nlev + l) * 2 + c;
+                    const double tot = data[6 * t + 3 * c];
+                    double v = (tot - ls[k]) / blk / m_l;
+                    double b = bn[k] / m_l;
+                    b = (b - v * v) / (m_l - 1.0);
+                    if (u.s.pt) b = b / (double)N;
+                    res->binning[k] = b;
+                }
+            }
     }
     return ESP_OK;
 }

@@ -40,13 +40,15 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
     const unsigned long long sweep_base = a.sweep_base + (a.ctr ? a.ctr[0] : 0ull);
     const long long meas_base = a.meas_base + (a.ctr ? (long long)a.ctr[2] : 0ll);
 
-    // shared memory: stencil copy | P(M) histogram | reduction scratch | spins
-    // (stencil_words is a multiple of 4, so every part stays 16-byte aligned)
+    // shared memory: stencil copy | histograms P(M) [, P(OP), P(SM)] |
+    // reduction scratch | spins (stencil_words is a multiple of 4, so every
+    // part stays 16-byte aligned)
     extern __shared__ __align__(16) unsigned char smem[];
     ClusterStencil *st = reinterpret_cast<ClusterStencil *>(smem);
     const ClusterNbr *nbt = reinterpret_cast<const ClusterNbr *>(st + 1);
     unsigned int *hist = reinterpret_cast<unsigned int *>(smem) + a.stencil_words;
-    double *red = reinterpret_cast<double *>(hist + ((a.nf + 3) & ~3));
+    const int nhist = a.obs ? 3 : 1;
+    double *red = reinterpret_cast<double *>(hist + ((nhist * a.nf + 3) & ~3));
     float *sx = reinterpret_cast<float *>(red + 136);
     float *sy = sx + n_local;
     float *sz = sy + n_local;
@@ -56,7 +58,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
         const int *src = reinterpret_cast<const int *>(a.stencil);
         int *dst = reinterpret_cast<int *>(st);
         for (int i = threadIdx.x; i < a.stencil_words; i += blockDim.x) dst[i] = src[i];
-        for (int i = threadIdx.x; i < a.nf; i += blockDim.x) hist[i] = 0u;
+        for (int i = threadIdx.x; i < nhist * a.nf; i += blockDim.x) hist[i] = 0u;
     }
     for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
         int k, rem, q1, hx, hy, hzl;
@@ -181,52 +183,82 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
             accE += (double)fE; accX += (double)fX; accY += (double)fY; accZ += (double)fZ;
         }
         if (!a.measure) continue;
-        // ---- measurement: cluster-wide sums of dE and dM -------------------
+        // ---- measurement: cluster-wide sums of dE and dM (and, with the
+        // optional measurements, of s.a and c s over the slab) ---------------
         {
-            double v[4] = {accE, accX, accY, accZ};
+            double v[8] = {accE, accX, accY, accZ, 0.0, 0.0, 0.0, 0.0};
             accE = accX = accY = accZ = 0.0;
-            for (int c = 0; c < 4; ++c)
+            if (a.obs) {
+                // FP32 per thread (a few sites each), FP64 from here on
+                float op = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
+                for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
+                    int k, rem;
+                    fdivmod(l, a.fd_pc, k, rem);
+                    obs_add(sx[l], sy[l], sz[l], __ldg(a.obs_atom + (k >> 3)), op, qx, qy, qz);
+                }
+                v[4] = (double)op; v[5] = (double)qx; v[6] = (double)qy; v[7] = (double)qz;
+            }
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
                 for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
             const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-            if (lane == 0)
-                for (int c = 0; c < 4; ++c) red[4 * warp + c] = v[c];
+            if (lane == 0) {
+#pragma unroll
+                for (int c = 0; c < 8; ++c) red[8 * warp + c] = v[c];
+            }
             __syncthreads();
             if (threadIdx.x == 0) {
-                double t4[4] = {0, 0, 0, 0};
-                for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-                    for (int c = 0; c < 4; ++c) t4[c] += red[4 * w + c];
-                for (int c = 0; c < 4; ++c) red[128 + c] = t4[c];  // this CTA's total
+                double t8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) t8[c] += red[8 * w + c];
+                }
+#pragma unroll
+                for (int c = 0; c < 8; ++c) red[128 + c] = t8[c];  // this CTA's total
             }
-            // P(M) of this CTA's cells
-            if (a.na > 1) {
+            // P(M) [P(OP), P(SM)] of this CTA's cells
+            if (a.na > 1 || a.obs) {
                 const int ncells_local = Hx * Hy * Hzl * 8;  // cells of the slab
                 const int cl_end = (ncells_local + 31) & ~31;   // whole warps take part in the vote
                 for (int cl = threadIdx.x; cl < cl_end; cl += blockDim.x) {
-                    int bin = -1;
+                    int bin = -1, bin_op = -1, bin_sm = -1;
                     if (cl < ncells_local) {
                         const int x = cl % a.Lx, y = (cl / a.Lx) % a.Ly, zl = cl / (a.Lx * a.Ly);
                         const int z = z0 + zl;
-                        float mx = 0.f, my = 0.f, mz = 0.f;
+                        float mx = 0.f, my = 0.f, mz = 0.f, op = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
                         for (int at = 0; at < a.na; ++at) {
                             const int k = (at << 3) | ((x & 1) << 2) | ((y & 1) << 1) | (z & 1);
                             const int l = k * per_class + (((zl >> 1) * Hy + (y >> 1)) * Hx + (x >> 1));
-                            mx += sx[l]; my += sy[l]; mz += sz[l];
+                            const float ox = sx[l], oy = sy[l], oz = sz[l];
+                            mx += ox; my += oy; mz += oz;
+                            if (a.obs) obs_add(ox, oy, oz, __ldg(a.obs_atom + at), op, qx, qy, qz);
                         }
-                        bin = pm_bin(mx, my, mz, (float)a.m_min, pm_scale, a.nf);
+                        if (a.na > 1) bin = pm_bin(mx, my, mz, (float)a.m_min, pm_scale, a.nf);
+                        if (a.obs & 1) bin_op = pm_bin_value(op, (float)a.m_min, pm_scale, a.nf);
+                        if (a.obs & 2) bin_sm = pm_bin(qx, qy, qz, (float)a.m_min, pm_scale, a.nf);
                     }
                     // lanes with the same bin add once (low temperatures put
                     // almost every cell in one bin)
                     const unsigned int peers = __match_any_sync(0xffffffffu, bin);
                     if (bin > 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
                         atomicAdd(hist + (bin - 1), (unsigned)__popc(peers));
+                    if (a.obs) {
+                        const unsigned int po = __match_any_sync(0xffffffffu, bin_op);
+                        if (bin_op > 0 && (int)(threadIdx.x & 31) == __ffs(po) - 1)
+                            atomicAdd(hist + a.nf + (bin_op - 1), (unsigned)__popc(po));
+                        const unsigned int ps = __match_any_sync(0xffffffffu, bin_sm);
+                        if (bin_sm > 0 && (int)(threadIdx.x & 31) == __ffs(ps) - 1)
+                            atomicAdd(hist + 2 * a.nf + (bin_sm - 1), (unsigned)__popc(ps));
+                    }
                 }
             }
             cluster.sync();
             if (rank == 0 && threadIdx.x == 0) {
-                double d4[4] = {0, 0, 0, 0};
+                double d4[8] = {0, 0, 0, 0, 0, 0, 0, 0};
                 for (int q = 0; q < csize; ++q) {
                     const double *pr = cluster.map_shared_rank(red, q);
-                    for (int c = 0; c < 4; ++c) d4[c] += pr[128 + c];
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) d4[c] += pr[128 + c];
                 }
                 e_run += d4[0];
                 m_run[0] += d4[1]; m_run[1] += d4[2]; m_run[2] += d4[3];
@@ -244,11 +276,31 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                     double *o = a.series + (((step - 1) % a.series_cap) * a.R + temp) * 2;
                     o[0] = e; o[1] = am;
                 }
+                // orderparam_get / staggered_get (mcarlo.F90:553-568)
+                double aop = 0.0, asm_ = 0.0;
+                if (a.obs) {
+                    double *od = a.obs_data + 6 * temp;
+                    if (a.obs & 1) {
+                        const double op = d4[4] / (double)a.N;
+                        const double o2 = op * op;
+                        aop = sqrt(o2);
+                        od[0] += aop; od[1] += o2; od[2] += o2 * o2;
+                    }
+                    if (a.obs & 2) {
+                        const double qx = d4[5] / (double)a.N, qy = d4[6] / (double)a.N, qz = d4[7] / (double)a.N;
+                        const double q2 = qx * qx + qy * qy + qz * qz;
+                        asm_ = sqrt(q2);
+                        od[3] += asm_; od[4] += q2; od[5] += q2 * q2;
+                    }
+                }
                 for (int lv = 0; lv < a.nlev; ++lv) {
                     double *ls = a.lsum + ((size_t)temp * a.nlev + lv) * 2;
                     double *bn = a.binning + ((size_t)temp * a.nlev + lv) * 2;
+                    double *ols = a.obs ? a.obs_lsum + ((size_t)temp * a.nlev + lv) * 2 : nullptr;
+                    double *obn = a.obs ? a.obs_bin + ((size_t)temp * a.nlev + lv) * 2 : nullptr;
                     ls[0] += e * rn_inv;
                     ls[1] += am;
+                    if (ols) { ols[0] += aop; ols[1] += asm_; }
                     const long long blk = 1LL << a.levels[lv];
                     if ((step & (blk - 1)) == 0) {
                         // 1/2^n is exact, so the product equals the division
@@ -257,6 +309,11 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                             const double v2 = ls[c] * inv_div;
                             bn[c] += v2 * v2;
                             ls[c] = 0.0;
+                            if (ols) {
+                                const double w2 = ols[c] * inv_div;
+                                obn[c] += w2 * w2;
+                                ols[c] = 0.0;
+                            }
                         }
                     }
                 }
@@ -291,6 +348,9 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
         if (a.na > 1)
             for (int i = threadIdx.x; i < a.nf; i += blockDim.x)
                 if (hist[i]) atomicAdd(a.pm_counts + (size_t)temp * a.nf + i, (unsigned long long)hist[i]);
+        if (a.obs)
+            for (int i = threadIdx.x; i < 2 * a.nf; i += blockDim.x)
+                if (hist[a.nf + i]) atomicAdd(a.obs_pm + (size_t)temp * 2 * a.nf + i, (unsigned long long)hist[a.nf + i]);
         cluster.sync();
         if (rank == 0 && threadIdx.x == 0) {
             double d4[4] = {0, 0, 0, 0};
@@ -322,9 +382,9 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
     cluster.sync();
 }
 
-size_t cluster_smem_bytes(int n_local, int nf, size_t stencil_bytes)
+size_t cluster_smem_bytes(int n_local, int nf, int nhist, size_t stencil_bytes)
 {
-    return ((stencil_bytes + 15) & ~(size_t)15) + (size_t)((nf + 3) & ~3) * sizeof(unsigned int) +
+    return ((stencil_bytes + 15) & ~(size_t)15) + (size_t)((nhist * nf + 3) & ~3) * sizeof(unsigned int) +
            (size_t)136 * sizeof(double) + (size_t)3 * n_local * sizeof(float);
 }
 

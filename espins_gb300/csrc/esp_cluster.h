@@ -71,9 +71,17 @@ struct ClusterArgs {
     uint32_t key0, key1;
     int mode;
     float tilt;
+    // optional measurements (mcarlo.F90:553-578): bit 0 order parameter,
+    // bit 1 staggered magnetisation
+    int obs;
+    const float4 *obs_atom;         // [na]: axis (x, y, z), staggered coefficient (w)
+    double *obs_data;               // [R slots][6]
+    double *obs_lsum, *obs_bin;     // [R slots][nlev][2]
+    unsigned long long *obs_pm;     // [R slots][2][nf]
 };
 
-size_t cluster_smem_bytes(int n_local, int nf, size_t stencil_bytes);
+// nhist: P(M) histogram only (1) or P(M), P(OP), P(SM) (3)
+size_t cluster_smem_bytes(int n_local, int nf, int nhist, size_t stencil_bytes);
 // nt: threads per CTA, 256 or 512
 cudaError_t cluster_configure(size_t smem, int csize, int nt);
 // Clusters of csize CTAs of nt threads with `smem` bytes each that fit on the GPU at once.

@@ -79,16 +79,33 @@ __device__ __forceinline__ void trial_spin(int mode, float tilt, float mag, floa
     }
 }
 
-// Bin of a unit cell's |sum of spins| on the P(M) grid of Pm_get
-// (get_quant.F90:425-493): max(nint((|m| - m_min) / (m_max - m_min) * (nf-1)) + 1, 1),
-// clamped to nf; FP32 (an edge flip needs |m| within ~1e-7 of a bin edge).
-// scale = (nf - 1) / (m_max - m_min).  Returns the 1-based bin.
-__device__ __forceinline__ int pm_bin(float mx, float my, float mz, float m_min, float scale, int nf)
+// Bin of a unit cell's value m on the P(M) grid of Pm_get
+// (get_quant.F90:425-493): max(nint((m - m_min) / (m_max - m_min) * (nf-1)) + 1, 1),
+// clamped to nf; FP32 (an edge flip needs m within ~1e-7 of a bin edge).
+// scale = (nf - 1) / (m_max - m_min).  Returns the 1-based bin.  m is |sum s|
+// for P(M) and P(SM), the signed sum of s.a for P(OP).
+// Adds one spin's s.a to op and c s to (qx, qy, qz), w = (a, c), with
+// explicitly rounded fused multiply-adds: every kernel that measures the order
+// parameter or the staggered magnetisation gets the same bits for a cell.
+__device__ __forceinline__ void obs_add(float ox, float oy, float oz, float4 w, float &op, float &qx, float &qy,
+                                        float &qz)
 {
-    const float m = sqrtf(mx * mx + my * my + mz * mz);
+    op = __fmaf_rn(oz, w.z, __fmaf_rn(oy, w.y, __fmaf_rn(ox, w.x, op)));
+    qx = __fmaf_rn(w.w, ox, qx);
+    qy = __fmaf_rn(w.w, oy, qy);
+    qz = __fmaf_rn(w.w, oz, qz);
+}
+
+__device__ __forceinline__ int pm_bin_value(float m, float m_min, float scale, int nf)
+{
     int bin = (int)floorf((m - m_min) * scale + 0.5f) + 1;  // nint of a non-negative value
     bin = bin < 1 ? 1 : bin;
     return bin > nf ? nf : bin;
+}
+
+__device__ __forceinline__ int pm_bin(float mx, float my, float mz, float m_min, float scale, int nf)
+{
+    return pm_bin_value(sqrtf(mx * mx + my * my + mz * mz), m_min, scale, nf);
 }
 
 // Division by an invariant integer d >= 1 as a multiply-high, an add and a

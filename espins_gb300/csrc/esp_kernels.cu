@@ -6,6 +6,8 @@
 //                    replica: per-block partials into scratch ...
 //   k_energy_reduce  ... reduced in a fixed order (deterministic FP64)
 //   k_local_terms    the per-site linear/quadratic coefficients (parity checks)
+//   k_obs_part       orderparam_get / staggered_get sums (get_quant.F90:366-422),
+//                    reduced by k_energy_reduce
 //   k_measure        per-measurement accumulators and binning
 //                    (mcarlo.F90:536-590, pt.F90:789-849)
 //   k_pm_hist        Pm_get (get_quant.F90:425-493) as an integer histogram
@@ -217,6 +219,28 @@ struct EnergyArgs {
     int32_t N, R, num_atoms;
 };
 
+// Per-replica sums of the four values in s_acc[t] of this block's threads
+// (the replica of thread t is (blockIdx.x * blockDim.x + t) % R, threads at or
+// past S hold nothing), in a fixed order, to scratch[block][R][4].
+__device__ void store_block_replica_sums(double (*s_acc)[4], long long S, int R, double *scratch)
+{
+    const int t = threadIdx.x;
+    const int base = (int)(((long long)blockIdx.x * blockDim.x) % R);
+    for (int rr = t; rr < R; rr += blockDim.x) {
+        // first thread of this block holding replica rr
+        int u0 = rr - base;
+        if (u0 < 0) u0 += R;
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        for (int u = u0; u < (int)blockDim.x; u += R) {
+            const long long g = (long long)blockIdx.x * blockDim.x + u;
+            if (g >= S) break;
+            a0 += s_acc[u][0]; a1 += s_acc[u][1]; a2 += s_acc[u][2]; a3 += s_acc[u][3];
+        }
+        double *o = scratch + ((size_t)blockIdx.x * R + rr) * 4;
+        o[0] = a0; o[1] = a1; o[2] = a2; o[3] = a3;
+    }
+}
+
 template <bool HB, bool HD>
 __global__ void __launch_bounds__(256) k_energy_part(const EnergyArgs a)
 {
@@ -266,21 +290,36 @@ __global__ void __launch_bounds__(256) k_energy_part(const EnergyArgs a)
     const int t = threadIdx.x;
     s_acc[t][0] = e; s_acc[t][1] = mx; s_acc[t][2] = my; s_acc[t][3] = mz;
     __syncthreads();
-    // replica of thread t is (blockIdx.x*blockDim.x + t) % R
-    const int base = (int)(((long long)blockIdx.x * blockDim.x) % R);
-    for (int rr = t; rr < R; rr += blockDim.x) {
-        // first thread of this block holding replica rr
-        int u0 = rr - base;
-        if (u0 < 0) u0 += R;
-        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-        for (int u = u0; u < (int)blockDim.x; u += R) {
-            const long long g = (long long)blockIdx.x * blockDim.x + u;
-            if (g >= S) break;
-            a0 += s_acc[u][0]; a1 += s_acc[u][1]; a2 += s_acc[u][2]; a3 += s_acc[u][3];
+    store_block_replica_sums(s_acc, S, R, a.scratch);
+}
+
+// Stage 1 of the order-parameter / staggered sums: per (site, replica) the
+// FP32 products s.a and c s, summed per thread and block in FP64 like the
+// energy.
+__global__ void __launch_bounds__(256) k_obs_part(const ObsArgs a)
+{
+    __shared__ double s_acc[256][4];
+    const int R = a.R;
+    const long long nthreads = (long long)gridDim.x * blockDim.x;
+    const long long S = (nthreads / R) * R;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double op = 0, qx = 0, qy = 0, qz = 0;
+    if (tid < S) {
+        const int r = (int)(tid % R);
+        const int pstep = (int)(S / R);
+        for (int p = (int)(tid / R); p < a.N; p += pstep) {
+            const size_t idx = (size_t)p * R + r;
+            const float ox = a.sx[idx], oy = a.sy[idx], oz = a.sz[idx];
+            const float4 w = __ldg(a.atom + a.perm[p] % a.num_atoms);
+            float fo = 0.f, fx = 0.f, fy = 0.f, fz = 0.f;
+            obs_add(ox, oy, oz, w, fo, fx, fy, fz);
+            op += (double)fo; qx += (double)fx; qy += (double)fy; qz += (double)fz;
         }
-        double *o = a.scratch + ((size_t)blockIdx.x * R + rr) * 4;
-        o[0] = a0; o[1] = a1; o[2] = a2; o[3] = a3;
     }
+    const int t = threadIdx.x;
+    s_acc[t][0] = op; s_acc[t][1] = qx; s_acc[t][2] = qy; s_acc[t][3] = qz;
+    __syncthreads();
+    store_block_replica_sums(s_acc, S, R, a.scratch);
 }
 
 // Stage 2: out_e[r] = sum over blocks, out_m[r][3] likewise.  One block per
@@ -381,12 +420,33 @@ __global__ void k_measure(MeasureArgs a)
         double *o = a.series + (((a.step - 1) % a.series_cap) * a.R + t) * 2;
         o[0] = e; o[1] = am;
     }
+    // orderparam_get / staggered_get of this replica (mcarlo.F90:553-568)
+    double aop = 0.0, asm_ = 0.0;
+    if (a.obs) {
+        double *od = a.obs_data + 6 * t;
+        const double *q = a.obs_rep + a.R + 3 * r;
+        if (a.obs & 1) {
+            const double op = a.obs_rep[r] / (double)a.N;
+            const double o2 = op * op;
+            aop = sqrt(o2);
+            od[0] += aop; od[1] += o2; od[2] += o2 * o2;
+        }
+        if (a.obs & 2) {
+            const double qx = q[0] / (double)a.N, qy = q[1] / (double)a.N, qz = q[2] / (double)a.N;
+            const double q2 = qx * qx + qy * qy + qz * qz;
+            asm_ = sqrt(q2);
+            od[3] += asm_; od[4] += q2; od[5] += q2 * q2;
+        }
+    }
     if (a.nlev > 0) {
         double *ls = a.lsum + (size_t)t * a.nlev * 2;
         double *bn = a.binning + (size_t)t * a.nlev * 2;
+        double *ols = a.obs ? a.obs_lsum + (size_t)t * a.nlev * 2 : nullptr;
+        double *obn = a.obs ? a.obs_bin + (size_t)t * a.nlev * 2 : nullptr;
         for (int l = 0; l < a.nlev; ++l) {
             ls[2 * l] += e / (double)a.N;
             ls[2 * l + 1] += am;
+            if (ols) { ols[2 * l] += aop; ols[2 * l + 1] += asm_; }
             const long long blk = 1LL << a.levels[l];
             if (a.step % blk == 0) {
                 const double div = a.pt_quirk ? (double)(1LL << (l + 1)) : (double)blk;
@@ -394,6 +454,11 @@ __global__ void k_measure(MeasureArgs a)
                     const double v = ls[2 * l + c] / div;
                     bn[2 * l + c] += v * v;
                     ls[2 * l + c] = 0.0;
+                    if (ols) {
+                        const double w = ols[2 * l + c] / div;
+                        obn[2 * l + c] += w * w;
+                        ols[2 * l + c] = 0.0;
+                    }
                 }
             }
         }
@@ -409,31 +474,40 @@ __global__ void k_measure(MeasureArgs a)
 __global__ void __launch_bounds__(256) k_pm_hist(PmArgs a)
 {
     // block (x, y): a chunk of cells x the replica tile [y*rt, y*rt + nrt)
+    // per replica of the tile: histograms [nh][nf], P(M) then P(OP), P(SM)
     extern __shared__ unsigned int s_hist[];
     const int R = a.R, nf = a.nf;
+    const int nh = a.obs ? 3 : 1;
     const int r0 = blockIdx.y * a.rt;
     const int nrt = min(a.rt, R - r0);
-    for (int i = threadIdx.x; i < nrt * nf; i += blockDim.x) s_hist[i] = 0u;
+    for (int i = threadIdx.x; i < nrt * nh * nf; i += blockDim.x) s_hist[i] = 0u;
     __syncthreads();
+    const float m_min = (float)a.m_min, scale = (float)((double)(nf - 1) / (a.m_max - a.m_min));
     const long long total = (long long)a.ncell * nrt;
     for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
          it += (long long)gridDim.x * blockDim.x) {
         const int cell = (int)(it / nrt), rr = (int)(it % nrt), r = r0 + rr;
-        float mx = 0.f, my = 0.f, mz = 0.f;
+        float mx = 0.f, my = 0.f, mz = 0.f, op = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
         for (int at = 0; at < a.num_atoms; ++at) {
             const int p = __ldg(a.inv + cell * a.num_atoms + at);
             const size_t idx = (size_t)p * R + r;
-            mx += a.sx[idx]; my += a.sy[idx]; mz += a.sz[idx];
+            const float sx = a.sx[idx], sy = a.sy[idx], sz = a.sz[idx];
+            mx += sx; my += sy; mz += sz;
+            if (a.obs) obs_add(sx, sy, sz, __ldg(a.obs_atom + at), op, qx, qy, qz);
         }
-        const int bin = pm_bin(mx, my, mz, (float)a.m_min, (float)((double)(nf - 1) / (a.m_max - a.m_min)), nf);
-        atomicAdd(s_hist + rr * nf + (bin - 1), 1u);
+        unsigned int *hr = s_hist + (size_t)rr * nh * nf;
+        if (a.count_m) atomicAdd(hr + (pm_bin(mx, my, mz, m_min, scale, nf) - 1), 1u);
+        if (a.obs & 1) atomicAdd(hr + nf + (pm_bin_value(op, m_min, scale, nf) - 1), 1u);
+        if (a.obs & 2) atomicAdd(hr + 2 * nf + (pm_bin(qx, qy, qz, m_min, scale, nf) - 1), 1u);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nrt * nf; i += blockDim.x) {
+    for (int i = threadIdx.x; i < nrt * nh * nf; i += blockDim.x) {
         const unsigned int c = s_hist[i];
         if (c) {
-            const int t = a.temp_of[r0 + i / nf];
-            atomicAdd(a.counts + (size_t)t * nf + (i % nf), (unsigned long long)c);
+            const int rr = i / (nh * nf), k = (i / nf) % nh, f = i % nf;
+            const int t = a.temp_of[r0 + rr];
+            if (k == 0) atomicAdd(a.counts + (size_t)t * nf + f, (unsigned long long)c);
+            else atomicAdd(a.obs_counts + ((size_t)t * 2 + (k - 1)) * nf + f, (unsigned long long)c);
         }
     }
 }
@@ -567,6 +641,15 @@ cudaError_t launch_energy(const EnergyArgsHost &h, double *out_e, double *out_m,
     return cudaGetLastError();
 }
 
+cudaError_t launch_obs(const ObsArgs &a, double *out_op, double *out_sm, int blocks, cudaStream_t st)
+{
+    k_obs_part<<<blocks, 256, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_energy_reduce<<<a.R, 256, 0, st>>>(a.scratch, blocks, a.R, out_op, out_sm);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_local_terms(const EnergyArgsHost &h, float *g, float *q, cudaStream_t st)
 {
     EnergyArgs a;
@@ -591,9 +674,10 @@ cudaError_t launch_measure(const MeasureArgs &a, cudaStream_t st)
 cudaError_t launch_pm(const PmArgs &a0, int max_blocks, cudaStream_t st)
 {
     PmArgs a = a0;
-    // replica tile: its [rt][nf] histogram fits in 96 KB of shared memory
+    // replica tile: its [rt][nh][nf] histograms fit in 96 KB of shared memory
     const size_t cap = 96 * 1024;
-    a.rt = (int)(cap / ((size_t)a.nf * sizeof(unsigned int)));
+    const int nh = a.obs ? 3 : 1;
+    a.rt = (int)(cap / ((size_t)nh * a.nf * sizeof(unsigned int)));
     if (a.rt < 1) return cudaErrorInvalidValue;
     if (a.rt > a.R) a.rt = a.R;
     a.use_shared = 1;
@@ -612,7 +696,7 @@ cudaError_t launch_pm(const PmArgs &a0, int max_blocks, cudaStream_t st)
     // global atomic per non-empty bin, so fewer blocks means less contention
     const int cap_blocks = max_blocks / 8 / tiles > 0 ? max_blocks / 8 / tiles : 1;
     int bx = grid_for((long long)a.ncell * a.rt, 256, cap_blocks);
-    const size_t smem = (size_t)a.rt * a.nf * sizeof(unsigned int);
+    const size_t smem = (size_t)a.rt * nh * a.nf * sizeof(unsigned int);
     k_pm_hist<<<dim3(bx, tiles), 256, smem, st>>>(a);
     return cudaGetLastError();
 }

@@ -37,6 +37,23 @@ struct MeasureArgs {
     double *series;           // [cap][R][2]: (E, |m|) per measurement, or null
     long long series_cap;
     const unsigned long long *ctr;   // device measurement counter added to step, or null
+    // optional measurements, mcarlo.F90:553-568: bit 0 order parameter, bit 1
+    // staggered magnetisation
+    int32_t obs;
+    const double *obs_rep;    // [R replicas] sum_i s_i.a_i, then [R replicas][3] sum_i c_i s_i
+    double *obs_data;         // [R][6]: |OP|, OP^2, OP^4, |SM|, SM^2, SM^4 sums
+    double *obs_lsum, *obs_bin;   // [R][nlev][2]: |OP|, |SM| binning
+};
+
+// Sums over the sites of every replica of s.a (order-parameter axis a of the
+// site's atom) and c s (staggered coefficient c), for orderparam_get /
+// staggered_get (get_quant.F90:366-422).
+struct ObsArgs {
+    const float *sx, *sy, *sz;
+    const int32_t *perm;      // permuted index -> reference site
+    const float4 *atom;       // [num_atoms]: axis (x, y, z), coefficient (w)
+    double *scratch;          // [blocks][R][4]
+    int32_t N, R, num_atoms;
 };
 
 struct PmArgs {
@@ -46,6 +63,10 @@ struct PmArgs {
     unsigned long long *counts;  // [R slots][nf]
     int32_t R, ncell, num_atoms, nf, use_shared, rt;
     double m_min, m_max;
+    int32_t count_m;          // bin |sum s| (P(M)) into counts
+    int32_t obs;              // bit 0: P(OP), bit 1: P(SM) into obs_counts
+    const float4 *obs_atom;   // [num_atoms]: axis (x, y, z), coefficient (w)
+    unsigned long long *obs_counts;  // [R slots][2][nf]
 };
 
 struct PtSwapArgs {
@@ -68,6 +89,9 @@ int energy_blocks(int N, int R, int max_blocks);
 cudaError_t launch_energy(const EnergyArgsHost &h, double *out_e, double *out_m, int blocks, cudaStream_t st);
 cudaError_t launch_local_terms(const EnergyArgsHost &h, float *g, float *q, cudaStream_t st);
 cudaError_t launch_measure(const MeasureArgs &a, cudaStream_t st);
+// out_op[r] = sum_i s_i.a_i, out_sm[3r..3r+2] = sum_i c_i s_i; scratch holds
+// blocks x R x 4 doubles (the energy scratch serves)
+cudaError_t launch_obs(const ObsArgs &a, double *out_op, double *out_sm, int blocks, cudaStream_t st);
 cudaError_t launch_pm(const PmArgs &a, int max_blocks, cudaStream_t st);
 cudaError_t launch_pt_swap(const PtSwapArgs &a, cudaStream_t st);
 // ctr[i] += d[i] for the four run counters

@@ -31,7 +31,10 @@ EXPORTED = [
     "esp_set_pt_groups", "esp_set_cluster_geometry", "esp_get_cluster_geometry",
     "esp_set_tile_geometry", "esp_get_tile_geometry", "esp_batch_create", "esp_batch_destroy", "esp_batch_last_error",
     "esp_batch_set_units_per_graph", "esp_batch_advance", "esp_batch_tune",
+    "esp_set_observables", "esp_collect_observables",
 ]
+
+OBS_ORDER_PARAMETER, OBS_STAGGERED = 1, 2
 
 LP_NUM_PARAMS = 20756
 LP_IN, LP_OUT = 12, 20
@@ -79,6 +82,10 @@ class Results(C.Structure):
     _fields_ = [("rejected", C.c_void_p), ("steps_tot", C.c_void_p), ("energy", C.c_void_p),
                 ("data", C.c_void_p), ("pm", C.c_void_p), ("binning", C.c_void_p),
                 ("num_swaps", C.c_void_p), ("map", C.c_void_p), ("steps_mc_eff", C.c_int64)]
+
+
+class ObsResults(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("pm_op", C.c_void_p), ("pm_sm", C.c_void_p), ("binning", C.c_void_p)]
 
 
 class EnergyArgs(C.Structure):
@@ -258,6 +265,7 @@ class Engine:
             t.field_axis = arr(ham.field_axis, np.float64)
             t.field_val = arr(ham.field_val, np.float64)
         self._check(self.lib.esp_upload_tables(self.h, C.byref(t)))
+        self._obs = 0   # new tables clear the optional measurements
 
     def set_temperatures(self, tems) -> None:
         t = np.ascontiguousarray(tems, dtype=np.float64)
@@ -336,7 +344,41 @@ class Engine:
         out["steps_mc_eff"] = r.steps_mc_eff
         if nlev == 0:
             out["binning"] = None
+        self._collect_obs(out, nlev)
         return out
+
+    def set_observables(self, order_axes=None, staggered_coeff=None) -> None:
+        """Measure the order parameter (order_axes: (num_atoms, 3) unit vectors)
+        and / or the staggered magnetisation (staggered_coeff: num_atoms of +1/-1)
+        with every measurement; None for both switches them off."""
+        flags = (OBS_ORDER_PARAMETER if order_axes is not None else 0) | \
+                (OBS_STAGGERED if staggered_coeff is not None else 0)
+        ax = np.ascontiguousarray(order_axes, dtype=np.float64).reshape(-1) if order_axes is not None else None
+        cf = np.ascontiguousarray(staggered_coeff, dtype=np.int32).reshape(-1) if staggered_coeff is not None else None
+        if ax is not None and ax.size != 3 * self.na:
+            raise ValueError("order_axes must hold num_atoms x 3 values")
+        if cf is not None and cf.size != self.na:
+            raise ValueError("staggered_coeff must hold num_atoms values")
+        self._check(self.lib.esp_set_observables(self.h, flags, _p(ax) if ax is not None else None,
+                                                 _p(cf) if cf is not None else None))
+        self._obs = flags
+
+    def _collect_obs(self, out: dict, nlev: int) -> None:
+        if not getattr(self, "_obs", 0):
+            return
+        R, nf = self.R, self.num_freq()
+        o = {"obs_data": np.zeros((R, 6)), "pm_op": np.zeros((R, nf)), "pm_sm": np.zeros((R, nf)),
+             "obs_binning": np.zeros((R, max(nlev, 1), 2))}
+        r = ObsResults()
+        r.data, r.pm_op, r.pm_sm, r.binning = (_p(o[k]) for k in ("obs_data", "pm_op", "pm_sm", "obs_binning"))
+        self._check(self.lib.esp_collect_observables(self.h, C.byref(r)))
+        if not self._obs & OBS_ORDER_PARAMETER:
+            o["pm_op"] = None
+        if not self._obs & OBS_STAGGERED:
+            o["pm_sm"] = None
+        if nlev == 0:
+            o["obs_binning"] = None
+        out.update(o)
 
     def run(self, steps_warmup: int, steps_mc: int, steps_measure: int, pt: bool = False,
             pt_steps_swap: int = 1, mode: int = 0, tilt: float = 0.125, seed: int = 1,
@@ -350,6 +392,7 @@ class Engine:
         out["steps_mc_eff"] = r.steps_mc_eff
         if nlev == 0:
             out["binning"] = None
+        self._collect_obs(out, nlev)
         return out
 
     # -- observables --------------------------------------------------------------

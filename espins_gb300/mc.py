@@ -13,9 +13,11 @@ files.  Differences from the reference, by design:
   MT19937 stream per MPI rank;
 * sites are updated colour class by colour class instead of in typewriter
   order.
-Optional measurements outside the hot path (order parameter, staggered
-magnetisation, spin correlations, structure factor, energy series) are
-rejected with an error naming the keyword.
+The order parameter and the staggered magnetisation (order_parameter,
+staggered_m) are measured on the GPU with every measurement and written to
+_op.dat / _staggered.dat and the extra _pm.dat / _binerror.dat columns.  The
+other optional measurements (spin correlations, structure factor, energy
+series) are rejected with an error naming the keyword.
 """
 from __future__ import annotations
 
@@ -30,8 +32,7 @@ from .lib import Engine
 from .mcin import McInput, McinError
 from .tables import Hamiltonian, build_hamiltonian
 
-UNSUPPORTED = [("lorderparam", "order_parameter"), ("lstaggered", "staggered_m"),
-               ("lspincorr", "spin_correlation"), ("lsfactor", "sfactor"), ("energy_write", "energy_write")]
+UNSUPPORTED = [("lspincorr", "spin_correlation"), ("lsfactor", "sfactor"), ("energy_write", "energy_write")]
 
 
 @dataclass
@@ -63,6 +64,9 @@ def run(inp: McInput, seed: Optional[int] = None, outdir: Optional[str] = None,
     mode = 1 if inp.mcarlo_mode.startswith("const") else 0
     with engine_factory(ham.n, ham.num_atoms, ham.supercell, R, inp.boundary_open) as e:
         e.upload(ham)
+        if inp.lorderparam or inp.lstaggered:
+            e.set_observables(order_axes=inp.orderparam_axes_cart if inp.lorderparam else None,
+                              staggered_coeff=inp.staggered_coeff if inp.lstaggered else None)
         e.set_temperatures(tems)
         if inp.initial_sconfig.startswith("file"):
             path = os.path.join(outdir or ".", inp.seedname + "_sconfig.dat")
@@ -85,10 +89,18 @@ def write_outputs(inp: McInput, r: RunResult, outdir: str) -> None:
     base = os.path.join(outdir, inp.seedname or "espins")
     n = r.ham.n
     m_max = float(np.abs(inp.mag_cell).sum())
-    W.write_mc_dat(base + "_mc.dat", r.tems, r.res["data"], n)
-    W.write_pm_dat(base + "_pm.dat", r.tems, r.res["pm"], -m_max, m_max)
+    res = r.res
+    op, sm = bool(inp.lorderparam), bool(inp.lstaggered)
+    W.write_mc_dat(base + "_mc.dat", r.tems, res["data"], n)
+    W.write_pm_dat(base + "_pm.dat", r.tems, res["pm"], -m_max, m_max,
+                   pm_op=res.get("pm_op") if op else None, pm_sm=res.get("pm_sm") if sm else None, pt=inp.pt)
     W.write_sconfig(base + "_sconfig.dat", inp.supercell_size, r.tems, r.spins)
-    if inp.lbinerror and r.res["binning"] is not None:
-        W.write_binerror(base + "_binerror.dat", r.tems, r.res["binning"], inp.binning_level, n, inp.pt)
+    if op:
+        W.write_obs_dat(base + "_op.dat", "op", r.tems, res["obs_data"], n)
+    if sm:
+        W.write_obs_dat(base + "_staggered.dat", "staggered", r.tems, res["obs_data"], n)
+    if inp.lbinerror and res["binning"] is not None:
+        W.write_binerror(base + "_binerror.dat", r.tems, res["binning"], inp.binning_level, n, inp.pt,
+                         obs_binning=res.get("obs_binning"), op=op, sm=sm)
     with open(base + ".mcout", "w") as fh:
         fh.write(W.mcout_block(r.tems, r.res, n, inp.pt))

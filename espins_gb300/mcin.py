@@ -579,9 +579,14 @@ def parse_mcin(text: str, seedname: str = "", num_nodes: int = 1) -> McInput:
     inp.lstaggered = L.logical("staggered_m", False)
     if inp.lstaggered and inp.num_atoms == 1:
         inp.lstaggered = False
+    # staggered_m_coeff (parameters.F90:450-463): +1 by default, only +1/-1,
+    # reordered with the atoms (matmul with convert_matrix_atoms)
     coeff = L.vector("staggered_m_coeff", inp.num_atoms, _fint)
-    if coeff is not None:
-        inp.staggered_coeff = np.array([coeff[c] for c in convert])
+    if inp.lstaggered and coeff is not None and any(abs(int(c)) != 1 for c in coeff):
+        raise McinError("Error: staggered_m_coeff must be +1 or -1")
+    if coeff is None:
+        coeff = [1] * inp.num_atoms
+    inp.staggered_coeff = np.array([int(coeff[c]) for c in convert])
     inp.lorderparam = L.logical("order_parameter", False)
     for k in ("order_parameter_axes_frac", "order_parameter_axes_cart"):
         ax = _parse_axes(L, k, inp, with_param=False)

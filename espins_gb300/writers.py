@@ -9,6 +9,12 @@ src/pt.F90:1040-1085:
 * ``seed_binerror.dat`` '#T=' line, rows (2x,I8,8x,E15.8,3x,E15.8)
 * ``seed.mcout``        the MONTECARLO summary block of mcarlo.F90:736-753 /
                         pt.F90:1000-1010 (format 124)
+* ``seed_op.dat``, ``seed_staggered.dat``
+                        headers of mcarlo.F90:144-162, rows format 126:
+                        (3x,f9.4,5x,E15.8,6x,E15.8,7x,E15.8,5x) (:772-782)
+With the order parameter or the staggered magnetisation switched on, _pm.dat
+gains the P(OP) / P(SM) columns and _binerror.dat their error columns
+(mcarlo.F90:174-215 and :784-818, pt.F90:159-200 and :1050-1073).
 """
 from __future__ import annotations
 
@@ -87,20 +93,150 @@ def mc_dat_row(T: float, row: np.ndarray, n: int) -> str:
     return fortran_f(T, 9, 4) + "".join("  " + fortran_e(v) for v in vals)
 
 
-def write_pm_dat(path: str, tems, pm: np.ndarray, m_min: float, m_max: float) -> None:
+# Header lines of _pm.dat and _binerror.dat by (order parameter, staggered,
+# parallel tempering): mcarlo.F90:174-215, pt.F90:159-200.
+_PM_HEAD = {
+    (True, True, False): [
+        '#------------------------------------- MONTECARLO -------------------------------------------#',
+        '#       M or OP                 P(M)                     P(OP)               P(Staggered_m)  #',
+        '#--------------------------------------------------------------------------------------------#',
+    ],
+    (True, False, False): [
+        '#-------------------------- MONTECARLO -------------------------------#',
+        '#       M or OP                 P(M)                     P(OP)        #',
+        '#---------------------------------------------------------------------#',
+    ],
+    (False, True, False): [
+        '#-------------------------- MONTECARLO -----------------------------#',
+        '# M or Staggered                P(M)                P(Staggered_m)  #',
+        '#-------------------------------------------------------------------#',
+    ],
+    (False, False, False): [
+        '#----------------- MONTECARLO -------------------#',
+        '#        M                      P(M)             #',
+        '#------------------------------------------------#',
+    ],
+    (True, True, True): [
+        '#-------------------------------------- MONTECARLO ------------------------------------------#',
+        '#       M or OP                 P(M)                     P(OP)               P(Staggered_m)  #',
+        '#--------------------------------------------------------------------------------------------#',
+    ],
+    (True, False, True): [
+        '#---------------------------- MONTECARLO -----------------------------#',
+        '#       M or OP                 P(M)                     P(OP)        #',
+        '#---------------------------------------------------------------------#',
+    ],
+    (False, True, True): [
+        '#--------------------------- MONTECARLO-----------------------------#',
+        '# M or Staggered                P(M)                P(Staggered_m)  #',
+        '#-------------------------------------------------------------------#',
+    ],
+    (False, False, True): [
+        '#----------------- MONTECARLO -------------------#',
+        '#        M                      P(M)             #',
+        '#------------------------------------------------#',
+    ],
+}
+
+_BIN_HEAD = {
+    (True, True, False): [
+        '#------------------------------------ MONTECARLO ------------------------------------------#',
+        '#  Binning_level     Error(E)          Error(M)        Error(OP)       Error(Staggered_m)  #',
+        '#------------------------------------------------------ ------------------------------------#',
+    ],
+    (True, False, False): [
+        '#------------------------- MONTECARLO -------------------------------#',
+        '#  Binning_level     Error(E)          Error(M)         Error(OP)    #',
+        '#--------------------------------------------------------------------#',
+    ],
+    (False, True, False): [
+        '#----------------------------- MONTECARLO -------------------------------#',
+        '#  Binning_level     Error(E)          Error(M)      Error(Staggered_m)  #',
+        '#------------------------------------------------------------------------#',
+    ],
+    (False, False, False): [
+        '#------------------- MONTECARLO -----------------#',
+        '#  Block_length      Error(E)          Error(M)  #',
+        '#------------------------------------------------#',
+    ],
+    (True, True, True): [
+        '#------------------------------------- MONTECARLO -----------------------------------------#',
+        '#  Binning_level     Error(E)          Error(M)        Error(OP)       Error(Staggered_m)  #',
+        '#------------------------------------------------------------------------------------------#',
+    ],
+    (True, False, True): [
+        '#--------------------------- MONTECARLO -----------------------------#',
+        '#  Binning_level     Error(E)          Error(M)         Error(OP)    #',
+        '#--------------------------------------------------------------------#',
+    ],
+    (False, True, True): [
+        '#----------------------------- MONTECARLO -------------------------------#',
+        '#  Binning_level     Error(E)          Error(M)      Error(Staggered_m)  #',
+        '#------------------------------------------------------------------------#',
+    ],
+    (False, False, True): [
+        '#------------------- MONTECARLO -----------------#',
+        '#  Block_length      Error(E)          Error(M)  #',
+        '#------------------------------------------------#',
+    ],
+}
+
+
+def write_pm_dat(path: str, tems, pm: np.ndarray, m_min: float, m_max: float, pm_op=None, pm_sm=None,
+                 pt: bool = False) -> None:
+    """pm: (R, nf) P(M); pm_op / pm_sm: (R, nf) P(OP) / P(SM) columns or None."""
     nf = pm.shape[1]
     dm = (m_max - m_min) / (nf - 1)
     m_array = [m_min + i * dm for i in range(nf)]
+    cols = [c for c in (pm_op, pm_sm) if c is not None]
     d, t = _date()
     with open(path, "w") as fh:
         fh.write(f" #written on {d} at {t} \n")
-        fh.write(" #----------------- MONTECARLO -------------------#\n")
-        fh.write(" #        M                      P(M)             #\n")
-        fh.write(" #------------------------------------------------#\n")
-        for T, row in zip(tems, pm):
+        for ln in _PM_HEAD[(pm_op is not None, pm_sm is not None, bool(pt))]:
+            fh.write(" " + ln + "\n")
+        for k, (T, row) in enumerate(zip(tems, pm)):
             fh.write(" #T=  " + fortran_f(T, 9, 4) + "\n")
-            for m, p in zip(m_array, row):
-                fh.write("  " + fortran_e(m) + " " * 10 + fortran_e(p) + "\n")
+            for f, (m, p) in enumerate(zip(m_array, row)):
+                fh.write("  " + fortran_e(m) + " " * 10 + fortran_e(p)
+                         + "".join(" " * 10 + fortran_e(c[k][f]) for c in cols) + "\n")
+
+
+def obs_row(T: float, row3, n: int) -> str:
+    """Format 126 row of _op.dat / _staggered.dat from <|x|>, <x^2>, <x^4>
+    (x = OP or SM): T, <|x|>, beta (<x^2> - <|x|>^2) N, 1 - <x^4> / (3 <x^2>^2)."""
+    beta = 1.0 / T
+    a, a2, a4 = row3
+    sus = beta * (a2 - a ** 2) * n
+    U = 1.0 - (1.0 / 3.0) * (a4 / a2 ** 2)
+    return format126(T, a, sus, U)
+
+
+def format126(T: float, v1: float, v2: float, v3: float) -> str:
+    """mcarlo.F90 format 126: (3x,f9.4,5x,E15.8,6x,E15.8,7x,E15.8,5x); the
+    trailing 5x writes nothing (position editing at the end of a record)."""
+    return ("   " + fortran_f(T, 9, 4) + " " * 5 + fortran_e(v1) + " " * 6 + fortran_e(v2)
+            + " " * 7 + fortran_e(v3))
+
+
+def write_obs_dat(path: str, kind: str, tems, obs_data: np.ndarray, n: int) -> None:
+    """kind 'op' (_op.dat, obs_data[:, 0:3]) or 'staggered' (_staggered.dat, [:, 3:6])."""
+    d, t = _date()
+    if kind == "op":
+        head = [" #------------------------------- MONTECARLO -----------------------------------#",
+                " #    Temp              OP                 Sus_OP                 U_OP          #",
+                " #------------------------------------------------------------------------------#"]
+        c0 = 0
+    else:
+        head = [" #------------------------------- MONTECARLO --------------------------------#",
+                " #    Temp         Staggered_m          Sus_Staggered_m       U_Staggered_m  #",
+                " #---------------------------------------------------------------------------#"]
+        c0 = 3
+    with open(path, "w") as fh:
+        fh.write(f" #written on {d} at {t} \n")
+        for ln in head:
+            fh.write(ln + "\n")
+        for T, row in zip(tems, obs_data):
+            fh.write(obs_row(T, row[c0:c0 + 3], n) + "\n")
 
 
 def write_sconfig(path: str, supercell, tems, spins: np.ndarray) -> None:
@@ -140,16 +276,27 @@ def read_sconfig(path: str, n: int, tems) -> np.ndarray:
     return out
 
 
-def write_binerror(path: str, tems, binning: np.ndarray, levels, n: int, pt: bool) -> None:
+def write_binerror(path: str, tems, binning: np.ndarray, levels, n: int, pt: bool, obs_binning=None,
+                   op: bool = False, sm: bool = False) -> None:
+    """binning: (R, nlev, 2) E/N and |m| rows; obs_binning: (R, nlev, 2) |OP|
+    and SM rows, of which the op / sm ones are written."""
+    ncol = 2 + int(op) + int(sm)
     with open(path, "w") as fh:
-        fh.write(" #------------------- MONTECARLO -----------------#\n")
-        fh.write(" #  Block_length      Error(E)          Error(M)  #\n")
-        fh.write(" #------------------------------------------------#\n")
-        for T, b in zip(tems, binning):
+        for ln in _BIN_HEAD[(op, sm, bool(pt))]:
+            fh.write(" " + ln + "\n")
+        for k, (T, b) in enumerate(zip(tems, binning)):
             fh.write(" #T=  " + (fortran_f(T, 6, 2) if pt else fortran_f(T, 9, 4)) + "\n")
-            for lv, row in zip(levels, b):
+            for l, (lv, row) in enumerate(zip(levels, b)):
+                row = list(row)
+                if op:
+                    row.append(obs_binning[k][l][0])
+                if sm:
+                    row.append(obs_binning[k][l][1])
+                row = np.asarray(row)
                 vals = np.sqrt(np.maximum(row, 0.0)) if pt else np.sqrt(np.maximum(row / n, 0.0))
-                fh.write(f"  {int(lv):8d}        " + fortran_e(vals[0]) + "   " + fortran_e(vals[1]) + "\n")
+                # mcarlo.F90 writes the level as I3 when both extra rows are on
+                lvs = f"{int(lv):3d}" if (ncol == 4 and not pt) else f"{int(lv):8d}"
+                fh.write(f"  {lvs}        " + "   ".join(fortran_e(v) for v in vals[:ncol]) + "\n")
 
 
 def mcout_block(tems, res: dict, n: int, pt: bool) -> str:

@@ -178,6 +178,34 @@ int esp_energy(esp_handle *h, double *energy_out);
 int esp_running_energy(esp_handle *h, double *energy_out);
 /* Running magnetisation sum_i s_i per temperature slot, [R][3]. */
 int esp_running_magnetization(esp_handle *h, double *m_out);
+/* ---- optional measurements ------------------------------------------- */
+/* The order parameter and the staggered magnetisation of mcarlo.F90:553-578 /
+ * pt.F90:808-838 (orderparam_get, staggered_get and the pdf_order /
+ * pdf_staggered parts of Pm_get, get_quant.F90:366-493), measured with every
+ * measurement of esp_advance / esp_run when chosen here:
+ *   OP = sum_i s_i . a_type(i) / N   (a: orderparam_axes_cart, unit vectors)
+ *   SM = |sum_i c_type(i) s_i| / N   (c: staggered_coeff, +1 or -1)
+ * Call after esp_upload_tables (new tables clear the choice) and before
+ * esp_begin; flags 0 switches both off.  orderparam_axes: [num_atoms][3]
+ * (NULL unless ESP_OBS_ORDER_PARAMETER), staggered_coeff: [num_atoms] (NULL
+ * unless ESP_OBS_STAGGERED). */
+#define ESP_OBS_ORDER_PARAMETER 1
+#define ESP_OBS_STAGGERED 2
+int esp_set_observables(esp_handle *h, int32_t flags, const double *orderparam_axes,
+                        const int32_t *staggered_coeff);
+
+/* Caller-allocated; NULL members are skipped.  Normalised as the reference
+ * normalises local_data columns 7-12, local_pm rows 2-3 and local_binning rows
+ * 3-4 before writing _op.dat, _staggered.dat, _pm.dat and _binerror.dat
+ * (mcarlo.F90:713-781, pt.F90:995-1048). */
+typedef struct {
+    double *data;               /* [R][6]: <|OP|>,<OP^2>,<OP^4>,<SM>,<SM^2>,<SM^4> */
+    double *pm_op;              /* [R][nf]: P(OP) */
+    double *pm_sm;              /* [R][nf]: P(SM) */
+    double *binning;            /* [R][nl][2]: binning variances of |OP| and SM */
+} esp_obs_results;
+int esp_collect_observables(esp_handle *h, esp_obs_results *res);
+
 /* Local terms of every site: energy of site i as a function of its spin s is
  * g_i.s + s^T Q_i s;  g: (3,N,R), q: (6,N,R) as xx,yy,zz,xy,xz,yz.
  * The exchange local field of delta_energy_get is -g without the Zeeman part. */

@@ -17,6 +17,8 @@
  *   metropolis              src/get_quant.F90:52-182
  *   magnetization_get       src/get_quant.F90:340-363
  *   Pm_get                  src/get_quant.F90:425-493
+ *   orderparam_get          src/get_quant.F90:396-422
+ *   staggered_get           src/get_quant.F90:366-392
  *   mcarlo (one T chain)    src/mcarlo.F90:463-659 (+ grid :432-456)
  *   pt_mcarlo / pt_swap     src/pt.F90:504-942, :1235-1288
  *
@@ -375,6 +377,126 @@ void or_pm(const or_ham *h, const double *s, int num_freq, double *pdf)
     }
 }
 
+/* orderparam_get (get_quant.F90:396-422): (sum_j s_j . a_type(j) / N)^2.
+ * The reference's atom type of 1-based site j is mod(j, num_atoms) (0 read as
+ * num_atoms), which is atom j % num_atoms of the cell for 0-based j. */
+double or_orderparam2(const or_ham *h, const double *axes, const double *s)
+{
+    double op = 0.0, rn = (double)h->n;
+    for (int j = 0; j < h->n; ++j)
+        op = op + dot3(s + 3 * j, axes + 3 * (j % h->num_atoms)) / rn;
+    return op * op;
+}
+
+/* staggered_get (get_quant.F90:366-392): |sum_j c_type(j) s_j / N|^2. */
+double or_staggered2(const or_ham *h, const double *coeff, const double *s)
+{
+    double m[3] = {0, 0, 0}, rn = (double)h->n;
+    for (int j = 0; j < h->n; ++j) {
+        double c = coeff[j % h->num_atoms];
+        for (int x = 0; x < 3; ++x) m[x] = m[x] + s[3 * j + x] * c / rn;
+    }
+    return dot3(m, m);
+}
+
+static inline void pm_hit(double v, double m_min, double m_max, int num_freq, double *pdf)
+{
+    long p = lround(((v - m_min) / (m_max - m_min)) * (double)(num_freq - 1)) + 1;
+    if (p < 1) p = 1;
+    if (p > num_freq) p = num_freq;   /* the reference does not guard the top */
+    pdf[p - 1] = pdf[p - 1] + 1.0 / 0.01;
+}
+
+/* Pm_get (get_quant.F90:425-493), the pdf_order and pdf_staggered parts: per
+ * unit cell the signed sum of s.a (order parameter) and |sum c s| (staggered
+ * magnetisation), binned on the P(M) grid.  Either output may be NULL. */
+void or_pm_obs(const or_ham *h, const double *s, int num_freq, const double *axes,
+               const double *coeff, double *pdf_op, double *pdf_st)
+{
+    double m_max = 0.0;
+    for (int i = 0; i < h->num_atoms; ++i) m_max = m_max + fabs(h->mag[i]);
+    double m_min = -m_max;
+    for (int j = 0; j < h->n; j += h->num_atoms) {
+        if (pdf_op) {
+            double op = 0.0;
+            for (int i = 0; i < h->num_atoms; ++i) op = op + dot3(s + 3 * (j + i), axes + 3 * i);
+            pm_hit(op, m_min, m_max, num_freq, pdf_op);
+        }
+        if (pdf_st) {
+            double m[3] = {0, 0, 0};
+            for (int i = 0; i < h->num_atoms; ++i)
+                for (int x = 0; x < 3; ++x) m[x] = m[x] + s[3 * (j + i) + x] * coeff[i];
+            pm_hit(sqrt(dot3(m, m)), m_min, m_max, num_freq, pdf_st);
+        }
+    }
+}
+
+/* The optional measurements of one temperature slot after a measurement
+ * (mcarlo.F90:553-578, pt.F90:808-838): sums of |x|, x^2, x^4 with x^2 the
+ * squared order parameter (data[0..2]) and staggered magnetisation
+ * (data[3..5]); binning partial sums ls[nlev][2]; P(OP) and P(SM). */
+typedef struct {
+    const double *op_axes;  /* orderparam_axes_cart(3,num_atoms), unit vectors, or NULL */
+    const double *st_coeff; /* staggered_coeff(num_atoms) (+1/-1), or NULL */
+    double *data;           /* [R][6], caller-zeroed */
+    double *pm_op, *pm_st;  /* [R][num_freq] or NULL, caller-zeroed */
+    double *binning;        /* [R][nlev][2] or NULL, caller-zeroed: binning variances of |OP| and |SM| */
+} or_obs;
+
+static void obs_measure(const or_ham *h, const or_obs *ob, int t, const double *s, int nf,
+                        int nlev, double *ls)
+{
+    double *d = ob->data + 6 * (size_t)t;
+    if (ob->op_axes) {
+        double o2 = or_orderparam2(h, ob->op_axes, s);
+        d[0] = d[0] + sqrt(o2); d[1] = d[1] + o2; d[2] = d[2] + o2 * o2;
+        if (ls) for (int l = 0; l < nlev; ++l) ls[2 * l] = ls[2 * l] + sqrt(o2);
+    }
+    if (ob->st_coeff) {
+        double m2 = or_staggered2(h, ob->st_coeff, s);
+        d[3] = d[3] + sqrt(m2); d[4] = d[4] + m2; d[5] = d[5] + m2 * m2;
+        if (ls) for (int l = 0; l < nlev; ++l) ls[2 * l + 1] = ls[2 * l + 1] + sqrt(m2);
+    }
+    if ((ob->pm_op && ob->op_axes) || (ob->pm_st && ob->st_coeff))
+        or_pm_obs(h, s, nf, ob->op_axes,  ob->st_coeff,
+                  ob->pm_op && ob->op_axes ? ob->pm_op + (size_t)nf * t : NULL,
+                  ob->pm_st && ob->st_coeff ? ob->pm_st + (size_t)nf * t : NULL);
+}
+
+/* A completed binning block of level l: divide, square into the variance sum. */
+static void obs_block(const or_obs *ob, int t, int nlev, int l, double div, double *ls)
+{
+    double *bn = ob->binning + ((size_t)t * nlev + l) * 2;
+    for (int c = 0; c < 2; ++c) {
+        ls[2 * l + c] = ls[2 * l + c] / div;
+        bn[c] = bn[c] + ls[2 * l + c] * ls[2 * l + c];
+        ls[2 * l + c] = 0.0;
+    }
+}
+
+/* mcarlo.F90:635-656 for the |OP| and |SM| rows (pt: pt.F90:914-936, with
+ * the extra 1/N). */
+static void obs_finish(const or_obs *ob, int t, int nlev, const int32_t *levels, int64_t steps_mc,
+                       double *ls, int n_div)
+{
+    const double *d = ob->data + 6 * (size_t)t;
+    for (int l = 0; l < nlev; ++l) {
+        double *bn = ob->binning + ((size_t)t * nlev + l) * 2;
+        ls[2 * l] = d[0] - ls[2 * l];
+        ls[2 * l + 1] = d[3] - ls[2 * l + 1];
+        int64_t blk = (int64_t)1 << levels[l];
+        int64_t m_l = steps_mc / blk;
+        for (int c = 0; c < 2; ++c) {
+            double v = ls[2 * l + c] / (double)blk;
+            v = v / (double)m_l;
+            double b = bn[c] / (double)m_l;
+            b = (b - v * v) / (double)(m_l - 1);
+            if (n_div > 0) b = b / (double)n_div;
+            bn[c] = b;
+        }
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Plain Metropolis for one temperature (mcarlo.F90:496-659).                */
 /* ------------------------------------------------------------------------ */
@@ -393,6 +515,7 @@ typedef struct {
     double data[6];         /* E, E2, E4, M, M2, M4 (sums, not normalised) */
     double *pm;             /* [num_freq] caller-allocated, accumulated */
     double *binning;        /* [2*nlev] caller-allocated: local_binning(1:2,l) */
+    const or_obs *obs;      /* order parameter / staggered magnetisation, or NULL (R = 1) */
 } or_mc_result;
 
 void or_mcarlo_run(const or_ham *h, const or_mc_opts *o, or_mt *st, double beta,
@@ -402,6 +525,8 @@ void or_mcarlo_run(const or_ham *h, const or_mc_opts *o, or_mt *st, double beta,
     const int nlev = o->num_binning_level;
     int nf = or_num_freq(h);
     double *lsum = (double *)calloc((size_t)(2 * (nlev > 0 ? nlev : 1)), sizeof(double));
+    double *lso = (double *)calloc((size_t)(2 * (nlev > 0 ? nlev : 1)), sizeof(double));
+    const or_obs *ob = res->obs;
     memset(res->data, 0, sizeof(res->data));
     res->rejected[0] = res->rejected[1] = 0;
     res->steps_tot[0] = res->steps_tot[1] = 0;
@@ -434,6 +559,7 @@ void or_mcarlo_run(const or_ham *h, const or_mc_opts *o, or_mt *st, double beta,
                 lsum[2 * l + 1] = lsum[2 * l + 1] + sqrt(m2);
             }
         }
+        if (ob) obs_measure(h, ob, 0, s, nf, nlev, res->binning && ob->binning ? lso : NULL);
         if (res->pm) or_pm(h, s, nf, res->pm);
         if (res->binning) {
             for (int l = 0; l < nlev; ++l) {
@@ -444,6 +570,7 @@ void or_mcarlo_run(const or_ham *h, const or_mc_opts *o, or_mt *st, double beta,
                         res->binning[2 * l + c] = res->binning[2 * l + c] + lsum[2 * l + c] * lsum[2 * l + c];
                         lsum[2 * l + c] = 0.0;
                     }
+                    if (ob && ob->binning) obs_block(ob, 0, nlev, l, (double)blk, lso);
                 }
             }
         }
@@ -461,10 +588,12 @@ void or_mcarlo_run(const or_ham *h, const or_mc_opts *o, or_mt *st, double beta,
                 res->binning[2 * l + c] = (b - v * v) / (double)(m_l - 1);
             }
         }
+        if (ob && ob->binning) obs_finish(ob, 0, nlev, o->binning_level, o->steps_mc, lso, 0);
     }
     res->energy[1] = e;
     res->energy[2] = or_energy(h, s);
     free(lsum);
+    free(lso);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -486,6 +615,7 @@ typedef struct {
     double *data;           /* [6*R] sums */
     double *pm;             /* [R*num_freq] */
     double *binning;        /* [R*2*nlev] */
+    const or_obs *obs;      /* order parameter / staggered magnetisation, or NULL */
     int64_t steps_mc_eff;   /* steps_mc after rounding to pt_steps_swap */
     int64_t steps_tot_main; /* per-slot updates in the main phase */
 } or_pt_result;
@@ -531,6 +661,8 @@ void or_pt_run(const or_ham *h, const or_pt_opts *o, or_mt *st, int R,
     double *tmp = (double *)malloc(sizeof(double) * 3 * (size_t)n);
     double *e2 = (double *)calloc((size_t)R, sizeof(double));
     double *lsum = (double *)calloc((size_t)R * 2 * (nlev > 0 ? nlev : 1), sizeof(double));
+    double *lso = (double *)calloc((size_t)R * 2 * (nlev > 0 ? nlev : 1), sizeof(double));
+    const or_obs *ob = res->obs;
     int64_t pss = o->pt_steps_swap;
     int64_t sw = ceil_div_real(o->steps_warmup, 2);
     int64_t nsw_warm = ceil_div_real(sw, pss);
@@ -590,6 +722,7 @@ void or_pt_run(const or_ham *h, const or_pt_opts *o, or_mt *st, int R,
                 d[0] = d[0] + e; d[1] = d[1] + ee; d[2] = d[2] + ee * ee;
                 double m2 = or_magnetization2(h, s);
                 d[3] = d[3] + sqrt(m2); d[4] = d[4] + m2; d[5] = d[5] + m2 * m2;
+                if (ob) obs_measure(h, ob, t, s, nf, nlev, res->binning && ob->binning ? lso + (size_t)2 * nlev * t : NULL);
                 if (res->binning) {
                     double *ls = lsum + (size_t)2 * nlev * t;
                     double *bn = res->binning + (size_t)2 * nlev * t;
@@ -607,6 +740,7 @@ void or_pt_run(const or_ham *h, const or_pt_opts *o, or_mt *st, int R,
                                 bn[2 * l + c] = bn[2 * l + c] + ls[2 * l + c] * ls[2 * l + c];
                                 ls[2 * l + c] = 0.0;
                             }
+                            if (ob && ob->binning) obs_block(ob, t, nlev, l, div, lso + (size_t)2 * nlev * t);
                         }
                     }
                 }
@@ -635,13 +769,14 @@ void or_pt_run(const or_ham *h, const or_pt_opts *o, or_mt *st, int R,
                     bn[2 * l + c] = b / (double)n;
                 }
             }
+            if (ob && ob->binning) obs_finish(ob, t, nlev, o->binning_level, steps_mc, lso + (size_t)2 * nlev * t, n);
         }
     }
     for (int t = 0; t < R; ++t) {
         res->energy[3 * t + 1] = e2[t];
         res->energy[3 * t + 2] = or_energy(h, spins + (size_t)3 * n * t);
     }
-    free(tmp); free(e2); free(lsum);
+    free(tmp); free(e2); free(lsum); free(lso);
 }
 
 /* ------------------------------------------------------------------------ */

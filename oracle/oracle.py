@@ -58,10 +58,15 @@ class OrMcOpts(C.Structure):
                 ("num_binning_level", C.c_int32), ("binning_level", C.c_void_p)]
 
 
+class OrObs(C.Structure):
+    _fields_ = [("op_axes", C.c_void_p), ("st_coeff", C.c_void_p), ("data", C.c_void_p),
+                ("pm_op", C.c_void_p), ("pm_st", C.c_void_p), ("binning", C.c_void_p)]
+
+
 class OrMcResult(C.Structure):
     _fields_ = [("rejected", C.c_int64 * 2), ("steps_tot", C.c_int64 * 2),
                 ("energy", C.c_double * 3), ("data", C.c_double * 6),
-                ("pm", C.c_void_p), ("binning", C.c_void_p)]
+                ("pm", C.c_void_p), ("binning", C.c_void_p), ("obs", C.c_void_p)]
 
 
 class OrPtOpts(C.Structure):
@@ -73,7 +78,8 @@ class OrPtOpts(C.Structure):
 class OrPtResult(C.Structure):
     _fields_ = [("rejected", C.c_void_p), ("num_swaps", C.c_void_p), ("map", C.c_void_p),
                 ("energy", C.c_void_p), ("data", C.c_void_p), ("pm", C.c_void_p),
-                ("binning", C.c_void_p), ("steps_mc_eff", C.c_int64), ("steps_tot_main", C.c_int64)]
+                ("binning", C.c_void_p), ("obs", C.c_void_p), ("steps_mc_eff", C.c_int64),
+                ("steps_tot_main", C.c_int64)]
 
 
 def _declare(L):
@@ -107,6 +113,11 @@ def _declare(L):
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                C.c_void_p, C.c_void_p, C.c_void_p, P(C.c_int32)]
     L.or_build_ell.restype = C.c_int
+    L.or_orderparam2.argtypes = [P(OrHam), C.c_void_p, C.c_void_p]
+    L.or_orderparam2.restype = C.c_double
+    L.or_staggered2.argtypes = [P(OrHam), C.c_void_p, C.c_void_p]
+    L.or_staggered2.restype = C.c_double
+    L.or_pm_obs.argtypes = [P(OrHam), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.or_lp_num_params.restype = C.c_int
     L.or_lp_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     L.or_lp_loss_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
@@ -208,6 +219,50 @@ class Ham:
     def num_freq(self) -> int:
         return lib().or_num_freq(self.ref)
 
+    def orderparam2(self, axes, spins) -> float:
+        a = np.ascontiguousarray(axes, dtype=np.float64)
+        s = np.ascontiguousarray(spins, dtype=np.float64)
+        return lib().or_orderparam2(self.ref, _ptr(a), _ptr(s))
+
+    def staggered2(self, coeff, spins) -> float:
+        c = np.ascontiguousarray(coeff, dtype=np.float64)
+        s = np.ascontiguousarray(spins, dtype=np.float64)
+        return lib().or_staggered2(self.ref, _ptr(c), _ptr(s))
+
+    def pm_obs(self, spins, axes=None, coeff=None):
+        """P(OP) and P(SM) hits of one configuration (Pm_get's optional parts)."""
+        nf = self.num_freq()
+        s = np.ascontiguousarray(spins, dtype=np.float64)
+        a = np.ascontiguousarray(axes, dtype=np.float64) if axes is not None else None
+        c = np.ascontiguousarray(coeff, dtype=np.float64) if coeff is not None else None
+        po = np.zeros(nf) if a is not None else None
+        ps = np.zeros(nf) if c is not None else None
+        lib().or_pm_obs(self.ref, _ptr(s), nf, _ptr(a) if a is not None else None,
+                        _ptr(c) if c is not None else None,
+                        _ptr(po) if po is not None else None, _ptr(ps) if ps is not None else None)
+        return po, ps
+
+    def _obs(self, R, nlev, op_axes, st_coeff, want_pm):
+        """An or_obs for R slots, or (None, None) when neither measurement is on."""
+        if op_axes is None and st_coeff is None:
+            return None, None
+        nf = self.num_freq()
+        out = {"obs_data": np.zeros((R, 6)),
+               "pm_op": np.zeros((R, nf)) if want_pm and op_axes is not None else None,
+               "pm_st": np.zeros((R, nf)) if want_pm and st_coeff is not None else None,
+               "obs_binning": np.zeros((R, nlev, 2)) if nlev else None}
+        ob = OrObs()
+        if op_axes is not None:
+            ob.op_axes = self._arr(np.asarray(op_axes).reshape(-1), np.float64)
+        if st_coeff is not None:
+            ob.st_coeff = self._arr(np.asarray(st_coeff).reshape(-1), np.float64)
+        ob.data = _ptr(out["obs_data"])
+        ob.pm_op = _ptr(out["pm_op"]) if out["pm_op"] is not None else None
+        ob.pm_st = _ptr(out["pm_st"]) if out["pm_st"] is not None else None
+        ob.binning = _ptr(out["obs_binning"]) if nlev else None
+        self._keep.append(ob)
+        return ob, out
+
     def pm(self, spins, pdf=None):
         nf = self.num_freq()
         if pdf is None:
@@ -226,7 +281,11 @@ class Ham:
 
     def mcarlo(self, mt: MT, beta: float, spins: np.ndarray, steps_warmup: int, steps_mc: int,
                steps_measure: int, mode: int = 0, tilt: float = 0.125, binning_level=None,
-               want_pm: bool = True):
+               want_pm: bool = True, op_axes=None, st_coeff=None):
+        """One temperature chain.  op_axes (num_atoms, 3) unit vectors and
+        st_coeff (num_atoms,) switch on the order parameter and the staggered
+        magnetisation; their sums, P(OP)/P(SM) hits and binning variances come
+        back as obs_data (1, 6), pm_op / pm_st (1, nf) and obs_binning."""
         o = OrMcOpts()
         o.steps_warmup, o.steps_mc, o.steps_measure = steps_warmup, steps_mc, steps_measure
         o.mode, o.tilt = mode, tilt
@@ -238,16 +297,21 @@ class Ham:
         bn = np.zeros(2 * bl.size) if bl.size else None
         res.pm = _ptr(pm) if pm is not None else None
         res.binning = _ptr(bn) if bn is not None else None
+        ob, obs = self._obs(1, bl.size, op_axes, st_coeff, want_pm)
+        res.obs = C.addressof(ob) if ob is not None else None
         lib().or_mcarlo_run(self.ref, C.byref(o), C.byref(mt.st), beta, _ptr(spins), C.byref(res))
-        return {
+        out = {
             "rejected": list(res.rejected), "steps_tot": list(res.steps_tot),
             "energy": list(res.energy), "data": np.array(res.data[:]),
             "pm": pm, "binning": bn.reshape(-1, 2) if bn is not None else None,
         }
+        if obs is not None:
+            out.update(obs)
+        return out
 
     def pt(self, mt: MT, tems, spins: np.ndarray, steps_warmup: int, steps_mc: int,
            steps_measure: int, pt_steps_swap: int, mode: int = 0, tilt: float = 0.125,
-           binning_level=None, want_pm: bool = True):
+           binning_level=None, want_pm: bool = True, op_axes=None, st_coeff=None):
         tems = np.ascontiguousarray(tems, dtype=np.float64)
         R = tems.size
         o = OrPtOpts()
@@ -268,6 +332,10 @@ class Ham:
         res.map = _ptr(out["map"]); res.energy = _ptr(out["energy"]); res.data = _ptr(out["data"])
         res.pm = _ptr(out["pm"]) if want_pm else None
         res.binning = _ptr(out["binning"]) if bl.size else None
+        ob, obs = self._obs(R, bl.size, op_axes, st_coeff, want_pm)
+        res.obs = C.addressof(ob) if ob is not None else None
+        if obs is not None:
+            out.update(obs)
         lib().or_pt_run(self.ref, C.byref(o), C.byref(mt.st), R, _ptr(tems), _ptr(spins), C.byref(res))
         out["steps_mc_eff"] = res.steps_mc_eff
         out["steps_tot_main"] = res.steps_tot_main

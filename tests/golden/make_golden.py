@@ -8,7 +8,11 @@ outputs as text and writes small fixtures next to itself:
 * ``<name>_golden.json``                seeds, per-temperature accept/reject
                                         counts and the energy triple of the
                                         ``.mcout`` (mcarlo.F90:736-753 format),
-                                        and the ``_mc.dat`` rows
+                                        and the ``_mc.dat`` rows; the
+                                        ``_op.dat`` / ``_staggered.dat`` rows
+                                        when the example wrote them; the
+                                        ``_pm.dat`` columns of the temperatures
+                                        listed in PM_TEMPS
 * ``<name>_sconfig.npz``                final spins per temperature
                                         (``_sconfig.dat``, 6 decimals)
 
@@ -33,6 +37,26 @@ EXAMPLES = {
     "ex02_cubic_pt": ("examples/example02/reference", "cubic", 4),
     "ex04_bmno_mc": ("examples/example04/reference/mc_with_uniform_temperatures", "bmno", 0),
 }
+
+# temperatures whose _pm.dat block is kept (the ones the seed-exact replays reach)
+PM_TEMPS = {"ex03_fef3": [11.1111], "ex01_cubic": [], "ex05_snwo": [], "ex02_cubic_pt": [], "ex04_bmno_mc": []}
+
+
+def parse_pm_dat(text: str, keep):
+    """{T: rows} of a _pm.dat file for the temperatures in keep."""
+    out, cur = {}, None
+    for ln in text.splitlines():
+        s = ln.strip()
+        if s.startswith("#T="):
+            t = float(s[3:])
+            cur = [] if any(abs(t - k) < 1e-4 for k in keep) else None
+            if cur is not None:
+                out["%.4f" % t] = cur
+            continue
+        if not s or s.startswith("#") or cur is None:
+            continue
+        cur.append([float(x) for x in s.split()])
+    return out
 
 
 def parse_mcout(text: str) -> dict:
@@ -106,6 +130,19 @@ def main(ref_root: str) -> None:
         if os.path.exists(mcdat):
             with open(mcdat) as fh:
                 gold["mc_dat"] = parse_mc_dat(fh.read())
+        for kind in ("op", "staggered"):
+            f = os.path.join(base, seed + "_" + kind + ".dat")
+            if os.path.exists(f):
+                with open(f) as fh:
+                    text = fh.read()
+                gold[kind + "_dat"] = parse_mc_dat(text)
+                # a few rows verbatim, for the writer's format check
+                gold[kind + "_dat_lines"] = [ln for ln in text.splitlines() if ln.strip()
+                                             and not ln.strip().startswith("#")][:3]
+        pmf = os.path.join(base, seed + "_pm.dat")
+        if PM_TEMPS.get(name) and os.path.exists(pmf):
+            with open(pmf) as fh:
+                gold["pm_dat"] = parse_pm_dat(fh.read(), PM_TEMPS[name])
         scf = os.path.join(base, seed + "_sconfig.dat")
         if keep != 0 and os.path.exists(scf):
             with open(scf) as fh:

@@ -5,7 +5,9 @@ The reference has no unit tests; its example runs are the known answers:
   so the first temperature of a rank (ferro start, typewriter order) can be
   replayed update by update and must give the printed accept/reject counts,
   the energy triple and the ``_mc.dat`` row, and the final spins of the
-  ``_sconfig.dat`` file (mcarlo.F90:496-733);
+  ``_sconfig.dat`` file (mcarlo.F90:496-733); where the example measured the
+  order parameter, also its ``_op.dat`` row and the P(M) / P(OP) columns of
+  ``_pm.dat`` (orderparam_get, Pm_get: get_quant.F90:396-493);
 * energy fixtures: the final spins of every temperature and the printed
   "Final Energy by direct calculations" (energy_get, get_quant.F90:186-261);
 * MT19937 (mtprng.f90) against numpy's MT19937 for non-negative seeds, and
@@ -100,7 +102,12 @@ def test_energy_of_reference_final_configurations(golden_dir, name):
         assert abs(e - ref) <= 2e-6 * abs(ref) + 1e-3, (T, e, ref)
 
 
-def _replay(golden_dir, name, rank, check_mcdat=True):
+def _e8(x):
+    """x as Fortran's E15.8 prints it (8 significant digits)."""
+    return float("%.7E" % x)
+
+
+def _replay(golden_dir, name, rank, check_mcdat=True, check_obs=False):
     inp, g = _load(golden_dir, name)
     h = build_hamiltonian(inp)
     H = O.Ham(h)
@@ -110,8 +117,9 @@ def _replay(golden_dir, name, rank, check_mcdat=True):
     s = np.zeros((h.n, 3))
     s[:, 2] = h.mag                     # initial_sconfig = ferro
     mt = O.MT(g["seeds"][rank])
+    obs = {"op_axes": inp.orderparam_axes_cart} if check_obs else {}
     r = H.mcarlo(mt, 1.0 / T, s, inp.steps_warmup, inp.steps_mc, inp.steps_measure,
-                 binning_level=[1, 2, 3, 4, 5])
+                 binning_level=[1, 2, 3, 4, 5], **obs)
     row = g["rows"][t_index]
     assert abs(row["T"] - T) < 1e-4
     assert r["steps_tot"] == [row["warmup"][0], row["mc"][0]]
@@ -133,6 +141,26 @@ def _replay(golden_dir, name, rank, check_mcdat=True):
         for a, b in zip(got[1:], ref[1:]):
             # Fortran E15.8 keeps 8 significant digits
             assert float("%.7E" % a) == pytest.approx(b, rel=1e-12, abs=1e-300)
+    if check_obs:
+        N = h.n
+        beta = 1.0 / T
+        normalize = 1.0 / inp.steps_mc
+        d = r["obs_data"][0] * normalize
+        sus = beta * (d[1] - d[0] ** 2) * N
+        U = 1.0 - (1.0 / 3.0) * (d[2] / d[1] ** 2)
+        ref = g["op_dat"][t_index]
+        assert abs(ref[0] - T) < 1e-4
+        for a, b in zip([d[0], sus, U], ref[1:]):
+            assert _e8(a) == pytest.approx(b, rel=1e-12, abs=1e-300)
+        # _pm.dat: global_pm * normalize / num_supercell (mcarlo.F90:713-715)
+        rows = np.array(g["pm_dat"]["%.4f" % T])
+        ncell = N // h.num_atoms
+        pm = r["pm"] * normalize / ncell
+        pop = r["pm_op"][0] * normalize / ncell
+        assert rows.shape == (pm.size, 3)
+        for f in range(pm.size):
+            assert _e8(pm[f]) == pytest.approx(rows[f, 1], rel=1e-12, abs=1e-300), f
+            assert _e8(pop[f]) == pytest.approx(rows[f, 2], rel=1e-12, abs=1e-300), f
     return r
 
 
@@ -149,4 +177,4 @@ def test_seed_exact_replay_ex05_biquadratic_singleion(golden_dir):
 
 
 def test_seed_exact_replay_ex03_biquadratic_dm(golden_dir):
-    _replay(golden_dir, "ex03_fef3", rank=1, check_mcdat=True)
+    _replay(golden_dir, "ex03_fef3", rank=1, check_mcdat=True, check_obs=True)
