@@ -103,6 +103,13 @@ struct esp_handle {
     double *d_obs_data = nullptr;           // [R slots][6]
     double *d_obs_lsum = nullptr, *d_obs_bin = nullptr;   // [R slots][nlev_alloc][2]
     unsigned long long *d_obs_pm = nullptr; // [R slots][2][nf]
+    // spin correlations (esp_set_spin_correlation): B bins = shells x
+    // species x species, per-site entry lists grouped by bin
+    int sc_B = 0, sc_S = 0, sc_nsp = 0, sc_blocks = 0;
+    int32_t *d_sc_off = nullptr, *d_sc_nb = nullptr;
+    float *d_sc_w = nullptr;
+    double *d_sc_scratch = nullptr, *d_sc_out = nullptr, *d_sc_acc = nullptr;
+    std::vector<double> mag_host;   // mag_moments_matrix, reference order
     std::vector<double> tems;
     int nf = 2;
     double m_min = 0, m_max = 0;
@@ -191,6 +198,13 @@ void free_obs(esp_handle *h)
     h->obs = 0;
 }
 
+void free_sc(esp_handle *h)
+{
+    dfree(h->d_sc_off); dfree(h->d_sc_nb); dfree(h->d_sc_w);
+    dfree(h->d_sc_scratch); dfree(h->d_sc_out); dfree(h->d_sc_acc);
+    h->sc_B = h->sc_S = h->sc_nsp = 0;
+}
+
 void free_lp_batch(esp_handle *h)
 {
     dfree(h->d_lp_xb); dfree(h->d_lp_h1); dfree(h->d_lp_h2); dfree(h->d_lp_do); dfree(h->d_lp_dz2);
@@ -207,6 +221,7 @@ void free_all(esp_handle *h)
     dfree(h->d_data); dfree(h->d_lsum); dfree(h->d_bin); dfree(h->d_levels); dfree(h->d_pm); dfree(h->d_swaps);
     dfree(h->d_obs_lsum); dfree(h->d_obs_bin);
     free_obs(h);
+    free_sc(h);
     dfree(h->d_series);
     free_lp_batch(h);
     dfree(h->d_lp_p); dfree(h->d_lp_g); dfree(h->d_lp_m); dfree(h->d_lp_v);
@@ -501,6 +516,19 @@ int by_slot(esp_handle *h, const double *d_by_rep, int width, double *out)
     return ESP_OK;
 }
 
+// One spincorr_get measurement of every replica, accumulated per slot.
+int spincorr_measure(esp_handle *h)
+{
+    ScArgs a;
+    a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz;
+    a.off = h->d_sc_off; a.nb = h->d_sc_nb; a.w = h->d_sc_w;
+    a.scratch = h->d_sc_scratch; a.out = h->d_sc_out; a.acc = h->d_sc_acc; a.repl_at = h->d_repl_at;
+    a.N = h->N; a.R = h->R; a.B = h->sc_B;
+    CK(launch_spincorr(a, h->sc_blocks, h->st));
+    h->launches += 3;
+    return ESP_OK;
+}
+
 int measure(esp_handle *h, long long step, int nlev, bool pt_quirk, long long &const_hits)
 {
     int rc = fold(h);
@@ -528,6 +556,10 @@ int measure(esp_handle *h, long long step, int nlev, bool pt_quirk, long long &c
     }
     CK(launch_measure(m, h->st));
     h->launches++;
+    if (h->sc_B) {
+        int rc = spincorr_measure(h);
+        if (rc) return rc;
+    }
     // one atom per cell: |sum_cell s| = |m| for every cell, so every cell
     // lands in the top bin of Pm_get's grid; count it without a pass.
     if (h->na == 1) const_hits++;
@@ -890,7 +922,9 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
     CK(cudaStreamSynchronize(h->st));
     free_tables(h);
     free_obs(h);
+    free_sc(h);
     h->have_tables = false;
+    h->mag_host.assign(t->mag, t->mag + h->N);
     const size_t M = (size_t)prep.maxnb * h->N;
     CK(dalloc(&h->d_nnb, h->N));
     CK(dalloc(&h->d_nbr, M));
@@ -1407,6 +1441,7 @@ int esp_begin(esp_handle *h, const esp_schedule *s)
         CK(cudaMemsetAsync(h->d_obs_data, 0, sizeof(double) * 6 * R, h->st));
         CK(cudaMemsetAsync(h->d_obs_pm, 0, sizeof(unsigned long long) * 2 * R * h->nf, h->st));
     }
+    if (h->sc_B) CK(cudaMemsetAsync(h->d_sc_acc, 0, sizeof(double) * 3 * (size_t)R * h->sc_B, h->st));
     CK(cudaMemsetAsync(h->d_rej, 0, sizeof(unsigned long long) * 2 * R, h->st));
     CK(cudaMemsetAsync(h->d_swaps, 0, sizeof(long long) * 2 * R, h->st));
     esp_sweep_opts o;
@@ -1458,26 +1493,34 @@ int esp_advance(esp_handle *h, int64_t n)
     esp_sweep_opts o;
     o.mcarlo_mode = s.mcarlo_mode; o.tilt_angles_max = s.tilt_angles_max; o.seed = s.seed; o.phase = 1;
     if (use_cluster(h)) {
+        // spin correlations are measured by their own kernels after every
+        // measurement, so each launch then runs one measurement unit
+        const int64_t chunk = h->sc_B ? 1 : kChunk;
         if (!s.pt) {
             // independent temperatures: many measurement units per launch
-            for (int64_t done = 0; done < n; done += kChunk) {
-                const int64_t k = std::min(kChunk, n - done);
+            for (int64_t done = 0; done < n; done += chunk) {
+                const int64_t k = std::min(chunk, n - done);
                 if ((rc = cluster_run(h, k, (int)s.steps_measure, h->next_sweep, 1, u.meas_done, &o, 1, u.nlev, false)))
                     return rc;
                 h->next_sweep += k * s.steps_measure;
                 u.meas_done += k;
                 if (h->na == 1) u.const_hits += k;
+                if (h->sc_B && (rc = spincorr_measure(h))) return rc;
             }
             u.units_done += n;
         } else {
             for (int64_t k = 0; k < n; ++k) {
                 const int64_t l = ++u.units_done;
-                if ((rc = cluster_run(h, s.pt_steps_swap, (int)s.steps_measure, h->next_sweep, 1, u.meas_done, &o, 1,
-                                      u.nlev, true)))
-                    return rc;
-                h->next_sweep += s.pt_steps_swap * s.steps_measure;
-                u.meas_done += s.pt_steps_swap;
-                if (h->na == 1) u.const_hits += s.pt_steps_swap;
+                for (int64_t done = 0; done < s.pt_steps_swap; done += chunk) {
+                    const int64_t m = std::min(chunk, s.pt_steps_swap - done);
+                    if ((rc = cluster_run(h, m, (int)s.steps_measure, h->next_sweep, 1, u.meas_done, &o, 1, u.nlev,
+                                          true)))
+                        return rc;
+                    h->next_sweep += m * s.steps_measure;
+                    u.meas_done += m;
+                    if (h->na == 1) u.const_hits += m;
+                    if (h->sc_B && (rc = spincorr_measure(h))) return rc;
+                }
                 if ((rc = pt_swap_launch(h, (int)((l + 1) % 2) + 1, h->next_swap++, s.seed, l))) return rc;
             }
         }
@@ -1693,6 +1736,109 @@ int esp_collect_observables(esp_handle *h, esp_obs_results *res)
                 }
             }
     }
+    return ESP_OK;
+}
+
+int esp_set_spin_correlation(esp_handle *h, int32_t num_shells, int32_t num_species, int32_t nbors_max,
+                             const int32_t *kind_atoms, const int32_t *shell_num_nbors, const int32_t *shell_nbors,
+                             const int32_t *shell_num_nbors_kind)
+{
+    if (!h) return ESP_EINVAL;
+    if (!h->have_tables) { h->err = "upload the tables before the spin-correlation shells"; return ESP_ESTATE; }
+    if (num_shells < 0 || num_species < 1 || nbors_max < 0) { h->err = "invalid shell dimensions"; return ESP_EINVAL; }
+    if (num_shells > 0 && (!kind_atoms || !shell_num_nbors || (nbors_max > 0 && !shell_nbors) || !shell_num_nbors_kind)) {
+        h->err = "shell tables missing";
+        return ESP_EINVAL;
+    }
+    const int N = h->N, S = num_shells, nsp = num_species;
+    const long long B = (long long)S * nsp * nsp;
+    if (B > 4096) { h->err = "more than 4096 spin-correlation bins (shells x species^2)"; return ESP_EINVAL; }
+    // per permuted site: entries (neighbour, weight) grouped by bin
+    // (shell, species of the site, species of the neighbour), each group in
+    // the order of shell_nbors_matrix
+    std::vector<std::vector<std::pair<int, std::pair<int, float>>>> lists;
+    if (S > 0) {
+        for (int i = 0; i < N; ++i)
+            if (kind_atoms[i] < 1 || kind_atoms[i] > nsp) { h->err = "kind_atoms out of range"; return ESP_EINVAL; }
+        lists.resize(N);
+        for (int p = 0; p < N; ++p) {
+            const int i = h->prep.perm[p];
+            const int a = kind_atoms[i] - 1;
+            auto &lst = lists[p];
+            for (int sh = 0; sh < S; ++sh) {
+                const int nn = shell_num_nbors[(size_t)i * S + sh];
+                if (nn < 0 || nn > nbors_max) { h->err = "shell_num_nbors_matrix out of range"; return ESP_EINVAL; }
+                for (int k = 0; k < nn; ++k) {
+                    const int j = shell_nbors[((size_t)k * N + i) * S + sh] - 1;
+                    if (j < 0 || j >= N) { h->err = "shell_nbors_matrix out of range"; return ESP_EINVAL; }
+                    const int b = kind_atoms[j] - 1;
+                    const int c = shell_num_nbors_kind[((size_t)b * nsp + a) * S + sh];
+                    const int bin = (sh * nsp + a) * nsp + b;
+                    // get_quant.F90:525-530: 1 / (shell_num_nbors_kind m_i m_j)
+                    const double den = (double)c * h->mag_host[i] * h->mag_host[j];
+                    lst.push_back({bin, {h->prep.inv[j], (float)(1.0 / den)}});
+                }
+            }
+            std::stable_sort(lst.begin(), lst.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+        }
+    }
+    int rc = fold(h);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->st));
+    free_sc(h);
+    if (S == 0) return ESP_OK;
+    size_t maxe = 1;
+    for (const auto &l : lists) maxe = std::max(maxe, l.size());
+    std::vector<int32_t> off((size_t)(B + 1) * N), nb(maxe * N, 0);
+    std::vector<float> w(maxe * N, 0.f);
+    for (int p = 0; p < N; ++p) {
+        const auto &l = lists[p];
+        size_t e = 0;
+        for (long long b = 0; b <= B; ++b) {
+            while (e < l.size() && l[e].first < b) ++e;
+            off[(size_t)b * N + p] = (int32_t)e;
+        }
+        for (size_t q = 0; q < l.size(); ++q) {
+            nb[q * N + p] = l[q].second.first;
+            w[q * N + p] = l[q].second.second;
+        }
+    }
+    const int npass = (int)((B + 1) / 2);
+    h->sc_blocks = std::max(1, std::min(h->e_blocks, 4 * h->num_sms));
+    if (h->sc_blocks * 256LL < h->R) h->sc_blocks = (h->R + 255) / 256;
+    CK(dalloc(&h->d_sc_off, off.size()));
+    CK(dalloc(&h->d_sc_nb, nb.size()));
+    CK(dalloc(&h->d_sc_w, w.size()));
+    CK(dalloc(&h->d_sc_scratch, (size_t)npass * h->sc_blocks * h->R * 4));
+    CK(dalloc(&h->d_sc_out, (size_t)npass * h->R * 4));
+    CK(dalloc(&h->d_sc_acc, (size_t)h->R * B * 3));
+    if ((rc = h2d(h, h->d_sc_off, off.data(), sizeof(int32_t) * off.size()))) return rc;
+    if ((rc = h2d(h, h->d_sc_nb, nb.data(), sizeof(int32_t) * nb.size()))) return rc;
+    if ((rc = h2d(h, h->d_sc_w, w.data(), sizeof(float) * w.size()))) return rc;
+    CK(cudaMemsetAsync(h->d_sc_acc, 0, sizeof(double) * 3 * (size_t)h->R * B, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->sc_B = (int)B; h->sc_S = S; h->sc_nsp = nsp;
+    return ESP_OK;
+}
+
+int esp_collect_spin_correlation(esp_handle *h, double *spincorr, double *spincorr_abs, double *spincorr_tot_abs)
+{
+    int rc = require(h, true, true);
+    if (rc) return rc;
+    RunState &u = h->run;
+    if (!u.active) { h->err = "esp_begin has not been called"; return ESP_ESTATE; }
+    if (!h->sc_B) { h->err = "no spin-correlation shells were set (esp_set_spin_correlation)"; return ESP_ESTATE; }
+    if (u.meas_done < 1) { h->err = "no measurement has been made (esp_advance)"; return ESP_ESTATE; }
+    if ((rc = fold(h))) return rc;
+    const size_t B = (size_t)h->sc_B, R = (size_t)h->R;
+    std::vector<double> acc(R * B * 3);
+    if ((rc = d2h(h, acc.data(), h->d_sc_acc, sizeof(double) * acc.size()))) return rc;
+    // global_spincorr * normalize / N (mcarlo.F90:717-723, pt.F90:1003-1009)
+    const double normalize = 1.0 / (double)u.meas_done;
+    double *outs[3] = {spincorr, spincorr_abs, spincorr_tot_abs};
+    for (int c = 0; c < 3; ++c)
+        if (outs[c])
+            for (size_t k = 0; k < R * B; ++k) outs[c][k] = acc[k * 3 + c] * normalize / (double)h->N;
     return ESP_OK;
 }
 

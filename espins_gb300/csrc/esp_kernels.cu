@@ -8,6 +8,8 @@
 //   k_local_terms    the per-site linear/quadratic coefficients (parity checks)
 //   k_obs_part       orderparam_get / staggered_get sums (get_quant.F90:366-422),
 //                    reduced by k_energy_reduce
+//   k_sc_part        spincorr_get (get_quant.F90:495-540) bin sums per
+//                    replica, reduced by k_sc_reduce, accumulated by k_sc_finish
 //   k_measure        per-measurement accumulators and binning
 //                    (mcarlo.F90:536-590, pt.F90:789-849)
 //   k_pm_hist        Pm_get (get_quant.F90:425-493) as an integer histogram
@@ -349,6 +351,91 @@ __global__ void __launch_bounds__(256) k_energy_reduce(const double *scratch, in
 }
 
 // ---------------------------------------------------------------------------
+// spincorr_get: bins in pairs per pass; per item (site, replica) FP32 sums over
+// the bin's entries, FP64 per thread and block (like the energy).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_sc_part(const ScArgs a)
+{
+    __shared__ double s_acc[256][4];
+    const int R = a.R, N = a.N;
+    const long long nthreads = (long long)gridDim.x * blockDim.x;
+    const long long S = (nthreads / R) * R;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int npass = (a.B + 1) / 2;
+    for (int pass = 0; pass < npass; ++pass) {
+        double v[4] = {0, 0, 0, 0};
+        if (tid < S) {
+            const int r = (int)(tid % R);
+            const int pstep = (int)(S / R);
+            for (int p = (int)(tid / R); p < N; p += pstep) {
+                const size_t idx = (size_t)p * R + r;
+                const float ox = a.sx[idx], oy = a.sy[idx], oz = a.sz[idx];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int b = 2 * pass + q;
+                    if (b < a.B) {
+                        const int e0 = a.off[(size_t)b * N + p], e1 = a.off[(size_t)(b + 1) * N + p];
+                        float sum = 0.f, sabs = 0.f;
+                        for (int e = e0; e < e1; ++e) {
+                            const size_t ee = (size_t)e * N + p;
+                            const size_t iq = (size_t)a.nb[ee] * R + r;
+                            const float d = ox * a.sx[iq] + oy * a.sy[iq] + oz * a.sz[iq];
+                            const float wd = a.w[ee] * d;
+                            sum += wd;
+                            sabs += fabsf(wd);
+                        }
+                        v[2 * q] += (double)sum;
+                        v[2 * q + 1] += (double)sabs;
+                    }
+                }
+            }
+        }
+        const int t = threadIdx.x;
+        s_acc[t][0] = v[0]; s_acc[t][1] = v[1]; s_acc[t][2] = v[2]; s_acc[t][3] = v[3];
+        __syncthreads();
+        store_block_replica_sums(s_acc, S, R, a.scratch + (size_t)pass * gridDim.x * R * 4);
+        __syncthreads();
+    }
+}
+
+// Block (r, pass): fixed-order sum of the blocks' partials of replica r.
+__global__ void __launch_bounds__(256) k_sc_reduce(const double *scratch, int nblocks, int R, double *out)
+{
+    __shared__ double s_v[4][256];
+    const int r = blockIdx.x, pass = blockIdx.y, t = threadIdx.x;
+    const double *base = scratch + (size_t)pass * nblocks * R * 4;
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    for (int b = t; b < nblocks; b += blockDim.x) {
+        const double *o = base + ((size_t)b * R + r) * 4;
+        a0 += o[0]; a1 += o[1]; a2 += o[2]; a3 += o[3];
+    }
+    s_v[0][t] = a0; s_v[1][t] = a1; s_v[2][t] = a2; s_v[3][t] = a3;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w)
+            for (int c = 0; c < 4; ++c) s_v[c][t] += s_v[c][t + w];
+        __syncthreads();
+    }
+    if (t < 4) out[((size_t)pass * R + r) * 4 + t] = s_v[t][0];
+}
+
+// Per temperature slot: spincorr += S_b, spincorr_abs += A_b, tot_abs += |S_b|
+// (get_quant.F90:535-537).
+__global__ void k_sc_finish(const ScArgs a)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.R) return;
+    const int r = a.repl_at[t];
+    for (int b = 0; b < a.B; ++b) {
+        const double *o = a.out + ((size_t)(b >> 1) * a.R + r) * 4 + 2 * (b & 1);
+        double *acc = a.acc + ((size_t)t * a.B + b) * 3;
+        acc[0] += o[0];
+        acc[1] += o[1];
+        acc[2] += fabs(o[0]);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Local terms g_i (3) and Q_i (6) of every (site, replica), FP32.
 // ---------------------------------------------------------------------------
 template <bool HB, bool HD>
@@ -647,6 +734,18 @@ cudaError_t launch_obs(const ObsArgs &a, double *out_op, double *out_sm, int blo
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_energy_reduce<<<a.R, 256, 0, st>>>(a.scratch, blocks, a.R, out_op, out_sm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spincorr(const ScArgs &a, int blocks, cudaStream_t st)
+{
+    if (a.B <= 0) return cudaSuccess;
+    k_sc_part<<<blocks, 256, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_sc_reduce<<<dim3(a.R, (a.B + 1) / 2), 256, 0, st>>>(a.scratch, blocks, a.R, a.out);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_sc_finish<<<(a.R + 127) / 128, 128, 0, st>>>(a);
     return cudaGetLastError();
 }
 

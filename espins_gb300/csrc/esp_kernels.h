@@ -56,6 +56,23 @@ struct ObsArgs {
     int32_t N, R, num_atoms;
 };
 
+// spincorr_get (get_quant.F90:495-540) per replica: for every bin b = (shell,
+// species of the site, species of the neighbour) the sums over sites p of
+// sum_{e in bin b} w_e (s_p . s_nb[e]) and of its magnitudes, with
+// w = 1 / (shell_num_nbors_kind m_i m_j).  Entries of site p for bin b are
+// off[b][p] .. off[b+1][p]-1 of the site-fastest lists nb / w.
+struct ScArgs {
+    const float *sx, *sy, *sz;
+    const int32_t *off;       // [B+1][N]
+    const int32_t *nb;        // [maxe][N], permuted neighbour index
+    const float *w;           // [maxe][N]
+    double *scratch;          // [npass][blocks][R][4], npass = ceil(B/2)
+    double *out;              // [npass][R replicas][4]: bins 2k, 2k+1 (sum, sum |.|)
+    double *acc;              // [R slots][B][3]: += sum, sum |.|, |sum|
+    const int32_t *repl_at;
+    int32_t N, R, B;
+};
+
 struct PmArgs {
     const float *sx, *sy, *sz;
     const int32_t *inv;       // reference site -> permuted index
@@ -93,6 +110,8 @@ cudaError_t launch_measure(const MeasureArgs &a, cudaStream_t st);
 // blocks x R x 4 doubles (the energy scratch serves)
 cudaError_t launch_obs(const ObsArgs &a, double *out_op, double *out_sm, int blocks, cudaStream_t st);
 cudaError_t launch_pm(const PmArgs &a, int max_blocks, cudaStream_t st);
+// one spincorr_get measurement of every replica, accumulated per slot
+cudaError_t launch_spincorr(const ScArgs &a, int blocks, cudaStream_t st);
 cudaError_t launch_pt_swap(const PtSwapArgs &a, cudaStream_t st);
 // ctr[i] += d[i] for the four run counters
 cudaError_t launch_bump(unsigned long long *ctr, const unsigned long long d[4], cudaStream_t st);

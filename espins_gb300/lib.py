@@ -31,7 +31,7 @@ EXPORTED = [
     "esp_set_pt_groups", "esp_set_cluster_geometry", "esp_get_cluster_geometry",
     "esp_set_tile_geometry", "esp_get_tile_geometry", "esp_batch_create", "esp_batch_destroy", "esp_batch_last_error",
     "esp_batch_set_units_per_graph", "esp_batch_advance", "esp_batch_tune",
-    "esp_set_observables", "esp_collect_observables",
+    "esp_set_observables", "esp_collect_observables", "esp_set_spin_correlation", "esp_collect_spin_correlation",
 ]
 
 OBS_ORDER_PARAMETER, OBS_STAGGERED = 1, 2
@@ -266,6 +266,7 @@ class Engine:
             t.field_val = arr(ham.field_val, np.float64)
         self._check(self.lib.esp_upload_tables(self.h, C.byref(t)))
         self._obs = 0   # new tables clear the optional measurements
+        self._sc = None
 
     def set_temperatures(self, tems) -> None:
         t = np.ascontiguousarray(tems, dtype=np.float64)
@@ -363,7 +364,29 @@ class Engine:
                                                  _p(cf) if cf is not None else None))
         self._obs = flags
 
+    def set_spin_correlation(self, shells) -> None:
+        """Measure spincorr_get with every measurement over the neighbour shells
+        of espins_gb300.tables.build_shells (None switches it off)."""
+        if shells is None:
+            self._check(self.lib.esp_set_spin_correlation(self.h, 0, 1, 0, None, None, None, None))
+            self._sc = None
+            return
+        S, nsp = int(shells.nn.shape[0]), int(shells.count.shape[1])
+        maxk = int(shells.nb.shape[1])
+        # the reference's Fortran arrays: column-major, 1-based
+        kind = np.ascontiguousarray(shells.kind + 1, dtype=np.int32)
+        nn = np.asfortranarray(shells.nn.astype(np.int32))                                # (S, N)
+        nb = np.asfortranarray(np.transpose(shells.nb, (0, 2, 1)).astype(np.int32) + 1)  # (S, N, maxk)
+        cnt = np.asfortranarray(shells.count.astype(np.int32))                            # (S, nsp, nsp)
+        self._check(self.lib.esp_set_spin_correlation(self.h, S, nsp, maxk, _p(kind), _p(nn), _p(nb), _p(cnt)))
+        self._sc = (S, nsp)
+
     def _collect_obs(self, out: dict, nlev: int) -> None:
+        if getattr(self, "_sc", None):
+            S, nsp = self._sc
+            sc = [np.zeros((self.R, S, nsp, nsp)) for _ in range(3)]
+            self._check(self.lib.esp_collect_spin_correlation(self.h, _p(sc[0]), _p(sc[1]), _p(sc[2])))
+            out["spincorr"], out["spincorr_abs"], out["spincorr_tot"] = sc
         if not getattr(self, "_obs", 0):
             return
         R, nf = self.R, self.num_freq()

@@ -13,11 +13,12 @@ files.  Differences from the reference, by design:
   MT19937 stream per MPI rank;
 * sites are updated colour class by colour class instead of in typewriter
   order.
-The order parameter and the staggered magnetisation (order_parameter,
-staggered_m) are measured on the GPU with every measurement and written to
-_op.dat / _staggered.dat and the extra _pm.dat / _binerror.dat columns.  The
-other optional measurements (spin correlations, structure factor, energy
-series) are rejected with an error naming the keyword.
+The order parameter, the staggered magnetisation and the spin correlations
+(order_parameter, staggered_m, spin_correlation) are measured on the GPU with
+every measurement and written to _op.dat / _staggered.dat / _spincorr.dat and
+the extra _pm.dat / _binerror.dat columns.  The other optional measurements
+(structure factor, energy series) are rejected with an error naming the
+keyword.
 """
 from __future__ import annotations
 
@@ -30,9 +31,9 @@ import numpy as np
 from . import writers as W
 from .lib import Engine
 from .mcin import McInput, McinError
-from .tables import Hamiltonian, build_hamiltonian
+from .tables import Hamiltonian, build_hamiltonian, build_shells
 
-UNSUPPORTED = [("lspincorr", "spin_correlation"), ("lsfactor", "sfactor"), ("energy_write", "energy_write")]
+UNSUPPORTED = [("lsfactor", "sfactor"), ("energy_write", "energy_write")]
 
 
 @dataclass
@@ -67,6 +68,8 @@ def run(inp: McInput, seed: Optional[int] = None, outdir: Optional[str] = None,
         if inp.lorderparam or inp.lstaggered:
             e.set_observables(order_axes=inp.orderparam_axes_cart if inp.lorderparam else None,
                               staggered_coeff=inp.staggered_coeff if inp.lstaggered else None)
+        if inp.lspincorr:
+            e.set_spin_correlation(build_shells(inp))
         e.set_temperatures(tems)
         if inp.initial_sconfig.startswith("file"):
             path = os.path.join(outdir or ".", inp.seedname + "_sconfig.dat")
@@ -99,6 +102,9 @@ def write_outputs(inp: McInput, r: RunResult, outdir: str) -> None:
         W.write_obs_dat(base + "_op.dat", "op", r.tems, res["obs_data"], n)
     if sm:
         W.write_obs_dat(base + "_staggered.dat", "staggered", r.tems, res["obs_data"], n)
+    if inp.lspincorr:
+        W.write_spincorr(base + "_spincorr.dat", r.tems, res["spincorr"], res["spincorr_abs"], res["spincorr_tot"],
+                         inp.atoms_symbol)
     if inp.lbinerror and res["binning"] is not None:
         W.write_binerror(base + "_binerror.dat", r.tems, res["binning"], inp.binning_level, n, inp.pt,
                          obs_binning=res.get("obs_binning"), op=op, sm=sm)

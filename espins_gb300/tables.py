@@ -71,18 +71,15 @@ def _find_atom(pos: np.ndarray, atoms_frac: np.ndarray) -> np.ndarray:
     return out
 
 
-def expand_pairs(num_atoms: int, atoms_frac: np.ndarray, mag_cell: np.ndarray,
-                 supercell, open_boundary: bool, f1: np.ndarray, f2: np.ndarray,
-                 values: np.ndarray, what: str = "Jij") -> EllTable:
-    """Expand pair rows over the supercell and compact into ELL.
-
-    ``values`` has shape (npairs,) for J/B or (npairs, 3) for D (already in K).
-    """
+def _expand_sites(num_atoms: int, atoms_frac: np.ndarray, supercell, open_boundary: bool,
+                  f1: np.ndarray, f2: np.ndarray, what: str):
+    """First and second site of every (cell, pair row), in the visiting order
+    of the reference loops (cell outer, pair inner), with the open-boundary
+    keep mask and the pair row of each entry."""
     L = np.asarray(supercell, dtype=np.int64)
     ncell = int(L[0] * L[1] * L[2])
     n = ncell * num_atoms
     npairs = f1.shape[0]
-    vec = values.ndim == 2
     cells = np.arange(ncell, dtype=np.int64)
     lmn = np.stack([cells % L[0], (cells // L[0]) % L[1], cells // (L[0] * L[1])], axis=1).astype(float)
 
@@ -110,12 +107,19 @@ def expand_pairs(num_atoms: int, atoms_frac: np.ndarray, mag_cell: np.ndarray,
         i1_all[:, p] = c1 * num_atoms + at1
         i2_all[:, p] = np.where(keep, c2 * num_atoms + np.maximum(at2, 0), 0)
         keep_all[:, p] = keep
-
     # visiting order of the reference loops: cell outer, pair inner
-    i1f = i1_all.reshape(-1)
-    i2f = i2_all.reshape(-1)
-    kf = keep_all.reshape(-1)
-    pidx = np.tile(np.arange(npairs), ncell)
+    return i1_all.reshape(-1), i2_all.reshape(-1), keep_all.reshape(-1), np.tile(np.arange(npairs), ncell), n
+
+
+def expand_pairs(num_atoms: int, atoms_frac: np.ndarray, mag_cell: np.ndarray,
+                 supercell, open_boundary: bool, f1: np.ndarray, f2: np.ndarray,
+                 values: np.ndarray, what: str = "Jij") -> EllTable:
+    """Expand pair rows over the supercell and compact into ELL.
+
+    ``values`` has shape (npairs,) for J/B or (npairs, 3) for D (already in K).
+    """
+    vec = values.ndim == 2
+    i1f, i2f, kf, pidx, n = _expand_sites(num_atoms, atoms_frac, supercell, open_boundary, f1, f2, what)
     mm = np.abs(mag_cell[i1f % num_atoms] * mag_cell[i2f % num_atoms])
     if vec:
         v = values[pidx] / mm[:, None]
@@ -141,6 +145,71 @@ def expand_pairs(num_atoms: int, atoms_frac: np.ndarray, mag_cell: np.ndarray,
         val = np.zeros((maxnb, n), dtype=np.float64)
         val[k, i1s] = vs
     return EllTable(nn=nn, nb=nb, val=val)
+
+
+@dataclass
+class ShellTables:
+    """Neighbour shells of spincorr_get (jij.F90:449-503), 0-based.
+
+    kind[i]            species of site i (kind_atoms)
+    nn[s, i]           neighbours of site i in shell s+1 (shell_num_nbors_matrix)
+    nb[s, k, i]        k-th such neighbour, in the order of the Jij rows
+                       (shell_nbors_matrix)
+    count[s, a, b]     shell_num_nbors_kind(s+1, a+1, b+1): the shell-(s+1)
+                       neighbours of species a around the LAST site of
+                       species b, as jij.F90:478-479 leaves it
+    """
+    kind: np.ndarray
+    nn: np.ndarray
+    nb: np.ndarray
+    count: np.ndarray
+    num_species: int
+
+    @property
+    def num_shells(self) -> int:
+        return int(self.nn.shape[0])
+
+
+def build_shells(inp: McInput) -> ShellTables:
+    """shell_neighbors_get over the expanded Jij rows: every (cell, row) entry
+    whose row carries shell sh > 0 and whose second site exists (open
+    boundaries drop it) lists the second site under shell sh of the first."""
+    j = inp.jij
+    if j.shell is None:
+        raise McinError("spin_correlation needs a shell (sh=) on every Jij_parameters row")
+    S = int(np.max(j.shell))
+    n = inp.num_total_atoms
+    nsp = len(inp.atoms_symbol)
+    kind = np.tile(np.asarray(inp.atom_species, dtype=np.int32), inp.num_supercell)
+    i1f, i2f, kf, pidx, _ = _expand_sites(inp.num_atoms, inp.atoms_frac, inp.supercell_size,
+                                          inp.boundary_open, j.f1, j.f2, "Jij")
+    sh = np.asarray(j.shell, dtype=np.int64)[pidx]
+    sel = kf & (sh > 0)
+    order = np.argsort(i1f, kind="stable")          # per first site, in row order
+    order = order[sel[order]]
+    i1s, i2s, ss = i1f[order], i2f[order], sh[order] - 1
+    nn = np.zeros((S, n), dtype=np.int32)
+    np.add.at(nn, (ss, i1s), 1)
+    maxk = int(nn.max()) if nn.size else 0
+    nb = np.zeros((S, max(maxk, 1), n), dtype=np.int32)
+    # position of every entry within its (shell, site) list
+    key = ss * n + i1s
+    o2 = np.argsort(key, kind="stable")
+    ks = key[o2]
+    first = np.searchsorted(ks, ks, side="left")
+    pos = np.empty_like(o2)
+    pos[o2] = np.arange(o2.size) - first
+    nb[ss, pos, i1s] = i2s
+    count = np.zeros((S, nsp, nsp), dtype=np.int32)
+    for b in range(nsp):
+        sites = np.nonzero(kind == b)[0]
+        if sites.size == 0:
+            continue
+        last = sites[-1]
+        for s_ in range(S):
+            nbrs = nb[s_, :nn[s_, last], last]
+            count[s_, :, b] = np.bincount(kind[nbrs], minlength=nsp)
+    return ShellTables(kind=kind, nn=nn, nb=nb, count=count, num_species=nsp)
 
 
 def check_symmetric(t: EllTable, antisym: bool, what: str) -> None:

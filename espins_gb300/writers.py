@@ -12,6 +12,9 @@ src/pt.F90:1040-1085:
 * ``seed_op.dat``, ``seed_staggered.dat``
                         headers of mcarlo.F90:144-162, rows format 126:
                         (3x,f9.4,5x,E15.8,6x,E15.8,7x,E15.8,5x) (:772-782)
+* ``seed_spincorr.dat`` header of mcarlo.F90:131-141, rows
+                        (f9.4,1x,I5,6x,a3,4x,i3,6x,a3,4x,i3,8x,f12.9,10x,f12.9,12x,f12.9)
+                        per temperature, shell and species pair (:760-770)
 With the order parameter or the staggered magnetisation switched on, _pm.dat
 gains the P(OP) / P(SM) columns and _binerror.dat their error columns
 (mcarlo.F90:174-215 and :784-818, pt.F90:159-200 and :1050-1073).
@@ -274,6 +277,39 @@ def read_sconfig(path: str, n: int, tems) -> np.ndarray:
             raise ValueError("All components of an spin in block are zero")
         out[k] = blk / np.sqrt((blk * blk).sum(axis=1, keepdims=True))
     return out
+
+
+def spincorr_row(T: float, shell: int, sym1: str, t1: int, sym2: str, t2: int, v1: float, v2: float,
+                 v3: float) -> str:
+    """(f9.4,1x,I5,6x,a3,4x,i3,6x,a3,4x,i3,8x,f12.9,10x,f12.9,12x,f12.9)."""
+    def a3(x):
+        return (x + "   ")[:3]
+    return (fortran_f(T, 9, 4) + " " + f"{shell:5d}" + " " * 6 + a3(sym1) + " " * 4 + f"{t1:3d}" + " " * 6
+            + a3(sym2) + " " * 4 + f"{t2:3d}" + " " * 8 + fortran_f(v1, 12, 9) + " " * 10 + fortran_f(v2, 12, 9)
+            + " " * 12 + fortran_f(v3, 12, 9))
+
+
+def write_spincorr(path: str, tems, sc: np.ndarray, sc_abs: np.ndarray, sc_tot: np.ndarray, symbols) -> None:
+    """sc, sc_abs, sc_tot: (R, shells, species, species), normalised.  The
+    species symbols print with a capital first letter (param_uppercase,
+    parameters.F90:1047-1070)."""
+    symbols = [x[:1].upper() + x[1:] for x in symbols]
+    d, t = _date()
+    with open(path, "w") as fh:
+        fh.write(f" #written on {d} at {t} \n")
+        fh.write(" #---------------------------------------------------- MONTECARLO "
+                 "----------------------------------------------------#\n")
+        fh.write(" #  Temp    Shell   Atom1   Type1   Atom2   Type2   "
+                 "<\\sum_{ij} Si.Sj/N>   <\\sum_{ij}|Si.Sj|/N>   <|\\sum_{ij}Si.Sj|/N> #\n")
+        fh.write(" #----------------------------------------------------------------"
+                 "----------------------------------------------------#\n")
+        for k, T in enumerate(tems):
+            S, nsp = sc.shape[1], sc.shape[2]
+            for l in range(S):
+                for a in range(nsp):
+                    for b in range(nsp):
+                        fh.write(spincorr_row(T, l + 1, symbols[a], a + 1, symbols[b], b + 1, sc[k, l, a, b],
+                                              sc_abs[k, l, a, b], sc_tot[k, l, a, b]) + "\n")
 
 
 def write_binerror(path: str, tems, binning: np.ndarray, levels, n: int, pt: bool, obs_binning=None,

@@ -206,6 +206,27 @@ typedef struct {
 } esp_obs_results;
 int esp_collect_observables(esp_handle *h, esp_obs_results *res);
 
+/* Spin correlations of spincorr_get (get_quant.F90:495-540), measured with
+ * every measurement when shells are set: per shell s and species pair (a, b)
+ *   S   = sum_i sum_{j in shell s of i} s_i.s_j / (n_s(a, b) m_i m_j)
+ *   A   = the same sum of |s_i.s_j| / (...)
+ * with a = kind(i), b = kind(j), n_s(a, b) = shell_num_nbors_kind(s, a, b);
+ * S, A and |S| are summed over measurements.  The tables are the reference's
+ * Fortran arrays (column-major, 1-based indices):
+ *   kind_atoms(N), shell_num_nbors_matrix(num_shells, N),
+ *   shell_nbors_matrix(num_shells, N, nbors_max),
+ *   shell_num_nbors_kind(num_shells, num_species, num_species)
+ * (jij.F90:449-503).  At most 4096 bins (num_shells x num_species^2).  Call
+ * after esp_upload_tables (new tables clear them) and before esp_begin;
+ * num_shells 0 switches them off. */
+int esp_set_spin_correlation(esp_handle *h, int32_t num_shells, int32_t num_species, int32_t nbors_max,
+                             const int32_t *kind_atoms, const int32_t *shell_num_nbors,
+                             const int32_t *shell_nbors, const int32_t *shell_num_nbors_kind);
+/* [R][num_shells][num_species][num_species] each (C order: species of the
+ * neighbour fastest), normalised as _spincorr.dat prints them: sums / (number
+ * of measurements x N).  NULL outputs are skipped. */
+int esp_collect_spin_correlation(esp_handle *h, double *spincorr, double *spincorr_abs, double *spincorr_tot_abs);
+
 /* Local terms of every site: energy of site i as a function of its spin s is
  * g_i.s + s^T Q_i s;  g: (3,N,R), q: (6,N,R) as xx,yy,zz,xy,xz,yz.
  * The exchange local field of delta_energy_get is -g without the Zeeman part. */

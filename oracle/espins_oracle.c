@@ -19,6 +19,7 @@
  *   Pm_get                  src/get_quant.F90:425-493
  *   orderparam_get          src/get_quant.F90:396-422
  *   staggered_get           src/get_quant.F90:366-392
+ *   spincorr_get            src/get_quant.F90:495-540 (shells: jij.F90:449-503)
  *   mcarlo (one T chain)    src/mcarlo.F90:463-659 (+ grid :432-456)
  *   pt_mcarlo / pt_swap     src/pt.F90:504-942, :1235-1288
  *
@@ -431,6 +432,48 @@ void or_pm_obs(const or_ham *h, const double *s, int num_freq, const double *axe
     }
 }
 
+/* Neighbour shells of spincorr_get (jij.F90:449-503), 0-based. */
+typedef struct {
+    int32_t num_shells, num_species, maxk;
+    const int32_t *kind;    /* [n]: species of the site (kind_atoms - 1) */
+    const int32_t *nn;      /* [S][n]: shell_num_nbors_matrix */
+    const int32_t *nb;      /* [S][maxk][n]: shell_nbors_matrix, 0-based */
+    const int32_t *count;   /* [S][nsp][nsp]: shell_num_nbors_kind(s, a, b) */
+} or_shells;
+
+/* spincorr_get (get_quant.F90:495-540): per shell and species pair (a, b)
+ * of (site, neighbour) the sums of s_i.s_j and |s_i.s_j| over
+ * shell_num_nbors_kind(s, a, b) m_i m_j; adds the signed sum to sc, its
+ * magnitude to sc_tot and the sum of magnitudes to sc_abs ([S][nsp][nsp]). */
+void or_spincorr(const or_ham *h, const or_shells *sh, const double *s, double *sc, double *sc_abs,
+                 double *sc_tot)
+{
+    const int S = sh->num_shells, nsp = sh->num_species, n = h->n;
+    double *tmp = (double *)calloc((size_t)2 * nsp * nsp, sizeof(double));
+    double *tabs = tmp + (size_t)nsp * nsp;
+    for (int is = 0; is < S; ++is) {
+        memset(tmp, 0, sizeof(double) * 2 * (size_t)nsp * nsp);
+        for (int i = 0; i < n; ++i) {
+            int a = sh->kind[i];
+            int cnt = sh->nn[(size_t)is * n + i];
+            for (int k = 0; k < cnt; ++k) {
+                int j = sh->nb[((size_t)is * sh->maxk + k) * n + i];
+                int b = sh->kind[j];
+                double d = dot3(s + 3 * i, s + 3 * j);
+                double den = (double)sh->count[((size_t)is * nsp + a) * nsp + b] * h->mag[i] * h->mag[j];
+                tmp[a * nsp + b] = tmp[a * nsp + b] + d / den;
+                tabs[a * nsp + b] = tabs[a * nsp + b] + fabs(d) / den;
+            }
+        }
+        for (int q = 0; q < nsp * nsp; ++q) {
+            sc[(size_t)is * nsp * nsp + q] = sc[(size_t)is * nsp * nsp + q] + tmp[q];
+            sc_tot[(size_t)is * nsp * nsp + q] = sc_tot[(size_t)is * nsp * nsp + q] + fabs(tmp[q]);
+            sc_abs[(size_t)is * nsp * nsp + q] = sc_abs[(size_t)is * nsp * nsp + q] + tabs[q];
+        }
+    }
+    free(tmp);
+}
+
 /* The optional measurements of one temperature slot after a measurement
  * (mcarlo.F90:553-578, pt.F90:808-838): sums of |x|, x^2, x^4 with x^2 the
  * squared order parameter (data[0..2]) and staggered magnetisation
@@ -441,6 +484,8 @@ typedef struct {
     double *data;           /* [R][6], caller-zeroed */
     double *pm_op, *pm_st;  /* [R][num_freq] or NULL, caller-zeroed */
     double *binning;        /* [R][nlev][2] or NULL, caller-zeroed: binning variances of |OP| and |SM| */
+    const or_shells *shells;            /* spin correlations, or NULL */
+    double *sc, *sc_abs, *sc_tot;       /* [R][S][nsp][nsp], caller-zeroed */
 } or_obs;
 
 static void obs_measure(const or_ham *h, const or_obs *ob, int t, const double *s, int nf,
@@ -456,6 +501,10 @@ static void obs_measure(const or_ham *h, const or_obs *ob, int t, const double *
         double m2 = or_staggered2(h, ob->st_coeff, s);
         d[3] = d[3] + sqrt(m2); d[4] = d[4] + m2; d[5] = d[5] + m2 * m2;
         if (ls) for (int l = 0; l < nlev; ++l) ls[2 * l + 1] = ls[2 * l + 1] + sqrt(m2);
+    }
+    if (ob->shells) {
+        size_t B = (size_t)ob->shells->num_shells * ob->shells->num_species * ob->shells->num_species;
+        or_spincorr(h, ob->shells, s, ob->sc + B * t, ob->sc_abs + B * t, ob->sc_tot + B * t);
     }
     if ((ob->pm_op && ob->op_axes) || (ob->pm_st && ob->st_coeff))
         or_pm_obs(h, s, nf, ob->op_axes,  ob->st_coeff,

@@ -58,9 +58,15 @@ class OrMcOpts(C.Structure):
                 ("num_binning_level", C.c_int32), ("binning_level", C.c_void_p)]
 
 
+class OrShells(C.Structure):
+    _fields_ = [("num_shells", C.c_int32), ("num_species", C.c_int32), ("maxk", C.c_int32),
+                ("kind", C.c_void_p), ("nn", C.c_void_p), ("nb", C.c_void_p), ("count", C.c_void_p)]
+
+
 class OrObs(C.Structure):
     _fields_ = [("op_axes", C.c_void_p), ("st_coeff", C.c_void_p), ("data", C.c_void_p),
-                ("pm_op", C.c_void_p), ("pm_st", C.c_void_p), ("binning", C.c_void_p)]
+                ("pm_op", C.c_void_p), ("pm_st", C.c_void_p), ("binning", C.c_void_p),
+                ("shells", C.c_void_p), ("sc", C.c_void_p), ("sc_abs", C.c_void_p), ("sc_tot", C.c_void_p)]
 
 
 class OrMcResult(C.Structure):
@@ -118,6 +124,7 @@ def _declare(L):
     L.or_staggered2.argtypes = [P(OrHam), C.c_void_p, C.c_void_p]
     L.or_staggered2.restype = C.c_double
     L.or_pm_obs.argtypes = [P(OrHam), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.or_spincorr.argtypes = [P(OrHam), P(OrShells), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.or_lp_num_params.restype = C.c_int
     L.or_lp_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     L.or_lp_loss_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
@@ -242,9 +249,29 @@ class Ham:
                         _ptr(po) if po is not None else None, _ptr(ps) if ps is not None else None)
         return po, ps
 
-    def _obs(self, R, nlev, op_axes, st_coeff, want_pm):
-        """An or_obs for R slots, or (None, None) when neither measurement is on."""
-        if op_axes is None and st_coeff is None:
+    def _shells(self, sh):
+        """An or_shells view of a ShellTables-like object (kind, nn, nb, count)."""
+        o = OrShells()
+        o.num_shells, o.num_species, o.maxk = int(sh.nn.shape[0]), int(sh.count.shape[1]), int(sh.nb.shape[1])
+        o.kind = self._arr(sh.kind, np.int32)
+        o.nn = self._arr(sh.nn, np.int32)
+        o.nb = self._arr(sh.nb, np.int32)
+        o.count = self._arr(sh.count, np.int32)
+        self._keep.append(o)
+        return o
+
+    def spincorr(self, shells, spins):
+        """One spincorr_get call: (sum, sum of |.|, |sum|) per shell and species pair."""
+        o = self._shells(shells)
+        B = (o.num_shells, o.num_species, o.num_species)
+        out = [np.zeros(B) for _ in range(3)]
+        s = np.ascontiguousarray(spins, dtype=np.float64)
+        lib().or_spincorr(self.ref, C.byref(o), _ptr(s), _ptr(out[0]), _ptr(out[1]), _ptr(out[2]))
+        return out[0], out[1], out[2]
+
+    def _obs(self, R, nlev, op_axes, st_coeff, want_pm, shells=None):
+        """An or_obs for R slots, or (None, None) when no optional measurement is on."""
+        if op_axes is None and st_coeff is None and shells is None:
             return None, None
         nf = self.num_freq()
         out = {"obs_data": np.zeros((R, 6)),
@@ -260,6 +287,13 @@ class Ham:
         ob.pm_op = _ptr(out["pm_op"]) if out["pm_op"] is not None else None
         ob.pm_st = _ptr(out["pm_st"]) if out["pm_st"] is not None else None
         ob.binning = _ptr(out["obs_binning"]) if nlev else None
+        if shells is not None:
+            sh = self._shells(shells)
+            B = (R, sh.num_shells, sh.num_species, sh.num_species)
+            for k in ("spincorr", "spincorr_abs", "spincorr_tot"):
+                out[k] = np.zeros(B)
+            ob.shells = C.addressof(sh)
+            ob.sc, ob.sc_abs, ob.sc_tot = (_ptr(out[k]) for k in ("spincorr", "spincorr_abs", "spincorr_tot"))
         self._keep.append(ob)
         return ob, out
 
@@ -281,11 +315,13 @@ class Ham:
 
     def mcarlo(self, mt: MT, beta: float, spins: np.ndarray, steps_warmup: int, steps_mc: int,
                steps_measure: int, mode: int = 0, tilt: float = 0.125, binning_level=None,
-               want_pm: bool = True, op_axes=None, st_coeff=None):
+               want_pm: bool = True, op_axes=None, st_coeff=None, shells=None):
         """One temperature chain.  op_axes (num_atoms, 3) unit vectors and
         st_coeff (num_atoms,) switch on the order parameter and the staggered
         magnetisation; their sums, P(OP)/P(SM) hits and binning variances come
-        back as obs_data (1, 6), pm_op / pm_st (1, nf) and obs_binning."""
+        back as obs_data (1, 6), pm_op / pm_st (1, nf) and obs_binning;
+        shells (espins_gb300.tables.ShellTables) switches on the spin
+        correlations: spincorr / spincorr_abs / spincorr_tot (1, S, nsp, nsp) sums."""
         o = OrMcOpts()
         o.steps_warmup, o.steps_mc, o.steps_measure = steps_warmup, steps_mc, steps_measure
         o.mode, o.tilt = mode, tilt
@@ -297,7 +333,7 @@ class Ham:
         bn = np.zeros(2 * bl.size) if bl.size else None
         res.pm = _ptr(pm) if pm is not None else None
         res.binning = _ptr(bn) if bn is not None else None
-        ob, obs = self._obs(1, bl.size, op_axes, st_coeff, want_pm)
+        ob, obs = self._obs(1, bl.size, op_axes, st_coeff, want_pm, shells)
         res.obs = C.addressof(ob) if ob is not None else None
         lib().or_mcarlo_run(self.ref, C.byref(o), C.byref(mt.st), beta, _ptr(spins), C.byref(res))
         out = {
@@ -311,7 +347,7 @@ class Ham:
 
     def pt(self, mt: MT, tems, spins: np.ndarray, steps_warmup: int, steps_mc: int,
            steps_measure: int, pt_steps_swap: int, mode: int = 0, tilt: float = 0.125,
-           binning_level=None, want_pm: bool = True, op_axes=None, st_coeff=None):
+           binning_level=None, want_pm: bool = True, op_axes=None, st_coeff=None, shells=None):
         tems = np.ascontiguousarray(tems, dtype=np.float64)
         R = tems.size
         o = OrPtOpts()
@@ -332,7 +368,7 @@ class Ham:
         res.map = _ptr(out["map"]); res.energy = _ptr(out["energy"]); res.data = _ptr(out["data"])
         res.pm = _ptr(out["pm"]) if want_pm else None
         res.binning = _ptr(out["binning"]) if bl.size else None
-        ob, obs = self._obs(R, bl.size, op_axes, st_coeff, want_pm)
+        ob, obs = self._obs(R, bl.size, op_axes, st_coeff, want_pm, shells)
         res.obs = C.addressof(ob) if ob is not None else None
         if obs is not None:
             out.update(obs)

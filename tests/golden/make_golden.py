@@ -12,7 +12,8 @@ outputs as text and writes small fixtures next to itself:
                                         ``_op.dat`` / ``_staggered.dat`` rows
                                         when the example wrote them; the
                                         ``_pm.dat`` columns of the temperatures
-                                        listed in PM_TEMPS
+                                        listed in PM_TEMPS; the _spincorr.dat
+                                        rows of the temperatures in SC_TEMPS
 * ``<name>_sconfig.npz``                final spins per temperature
                                         (``_sconfig.dat``, 6 decimals)
 
@@ -40,6 +41,23 @@ EXAMPLES = {
 
 # temperatures whose _pm.dat block is kept (the ones the seed-exact replays reach)
 PM_TEMPS = {"ex03_fef3": [11.1111], "ex01_cubic": [], "ex05_snwo": [], "ex02_cubic_pt": [], "ex04_bmno_mc": []}
+
+# temperatures whose _spincorr.dat rows are kept
+SC_TEMPS = {"ex05_snwo": [4.0]}
+
+
+def parse_spincorr(text: str, keep):
+    """Rows (T, shell, type1, type2, sum, sum_abs, tot_abs) at the kept temperatures."""
+    rows, lines = [], []
+    for ln in text.splitlines():
+        s = ln.split()
+        if not s or s[0].startswith("#"):
+            continue
+        t = float(s[0])
+        if any(abs(t - k) < 1e-4 for k in keep):
+            rows.append([t, int(s[1]), int(s[3]), int(s[5])] + [float(x) for x in s[6:9]])
+            lines.append(ln)
+    return rows, lines
 
 
 def parse_pm_dat(text: str, keep):
@@ -139,6 +157,10 @@ def main(ref_root: str) -> None:
                 # a few rows verbatim, for the writer's format check
                 gold[kind + "_dat_lines"] = [ln for ln in text.splitlines() if ln.strip()
                                              and not ln.strip().startswith("#")][:3]
+        scf_ = os.path.join(base, seed + "_spincorr.dat")
+        if SC_TEMPS.get(name) and os.path.exists(scf_):
+            with open(scf_) as fh:
+                gold["spincorr_dat"], gold["spincorr_dat_lines"] = parse_spincorr(fh.read(), SC_TEMPS[name])
         pmf = os.path.join(base, seed + "_pm.dat")
         if PM_TEMPS.get(name) and os.path.exists(pmf):
             with open(pmf) as fh:

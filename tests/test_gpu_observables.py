@@ -1,6 +1,7 @@
-"""The order parameter and the staggered magnetisation measured on the GPU
-(orderparam_get, staggered_get and Pm_get's pdf_order / pdf_staggered,
-get_quant.F90:366-493, accumulated as mcarlo.F90:553-590 / pt.F90:808-849):
+"""The order parameter, the staggered magnetisation and the spin correlations
+measured on the GPU (orderparam_get, staggered_get, Pm_get's pdf_order /
+pdf_staggered and spincorr_get, get_quant.F90:366-540, accumulated as
+mcarlo.F90:545-590 / pt.F90:798-849):
 
 * every sweep kernel's measurements equal the oracle's evaluation of the same
   spins, measurement by measurement (accumulators, binning, P(OP), P(SM));
@@ -9,7 +10,10 @@ get_quant.F90:366-493, accumulated as mcarlo.F90:553-590 / pt.F90:808-849):
 * staggered coefficients of +1 reproduce the magnetisation columns;
 * the stationary averages of <|OP|> and <SM> agree with the oracle's
   typewriter chains (the reference's algorithm) within 3 sigma;
-* the host driver writes _op.dat, _staggered.dat and the extra columns.
+* the spin correlations equal the oracle's spincorr_get of the same spins,
+  measurement by measurement, for every sweep kernel;
+* the host driver writes _op.dat, _staggered.dat, _spincorr.dat and the extra
+  columns.
 """
 import os
 
@@ -19,9 +23,9 @@ import pytest
 import oracle as O
 from espins_gb300 import mc
 from espins_gb300.lib import Engine
-from espins_gb300.tables import build_hamiltonian
+from espins_gb300.tables import build_hamiltonian, build_shells
 from helpers import example
-from test_observables_cpu import _bcc_afm
+from test_observables_cpu import _bcc_afm, _bcc_shells
 
 pytestmark = pytest.mark.gpu
 
@@ -201,3 +205,65 @@ def test_host_driver_writes_order_parameter_files(tmp_path):
     # the file's OP column is the collected <|OP|>
     op = [float(x[1]) for x in [l.split() for l in open(base + "_op.dat") if not l.lstrip().startswith("#")]]
     assert np.allclose(op, r.res["obs_data"][:, 0], rtol=1e-7)
+
+
+@pytest.mark.parametrize("kernel", ["ell", "cluster", "tile"])
+def test_spin_correlations_equal_the_oracle_on_the_gpu_spins(kernel):
+    tems = (2.0, 5.0, 12.0, 40.0)
+    inp = _bcc_shells(L=4, tems=tems)
+    h = build_hamiltonian(inp)
+    sh = build_shells(inp)
+    H = O.Ham(h)
+    R, K = len(tems), 24
+    acc = np.zeros((3, R, 2, 2, 2))
+    with Engine(h.n, h.num_atoms, h.supercell, R) as e:
+        e.upload(h)
+        e.set_spin_correlation(sh)
+        e.set_temperatures(tems)
+        e.set_sweep_kernel(kernel)
+        assert e.sweep_kernel()[0] == kernel
+        e.init_spins("rand", seed=2)
+        e.begin(e.schedule(10, K, 1, seed=5))
+        for _ in range(K):
+            e.advance(1)
+            S = e.get_spins()
+            for t in range(R):
+                sc, sa, st = H.spincorr(sh, S[t].reshape(-1))
+                acc[0, t] += sc; acc[1, t] += sa; acc[2, t] += st
+        r = e.collect()
+    for k, name in enumerate(("spincorr", "spincorr_abs", "spincorr_tot")):
+        want = acc[k] / K / h.n
+        assert np.allclose(r[name], want, rtol=1e-5, atol=1e-7), name
+
+
+@pytest.mark.parametrize("pt", [False, True])
+def test_cluster_kernel_spin_correlations_match_ell(pt):
+    inp = _bcc_shells(L=8, tems=tuple(np.geomspace(3.0, 30.0, 6)))
+    h = build_hamiltonian(inp)
+    sh = build_shells(inp)
+    res = {}
+    for kernel in ("ell", "cluster"):
+        with Engine(h.n, h.num_atoms, h.supercell, len(inp.tems)) as e:
+            e.upload(h)
+            e.set_spin_correlation(sh)
+            e.set_temperatures(inp.tems)
+            e.set_sweep_kernel(kernel)
+            e.init_spins("ferro")
+            res[kernel] = e.run(20, 60, 2, pt=pt, pt_steps_swap=4, seed=13)
+    a, b = res["ell"], res["cluster"]
+    assert np.array_equal(a["rejected"], b["rejected"])
+    for name in ("spincorr", "spincorr_abs", "spincorr_tot"):
+        assert np.allclose(a[name], b[name], rtol=1e-5, atol=1e-7), name
+
+
+def test_host_driver_writes_spin_correlation_file(tmp_path):
+    inp, g = example("ex05_snwo")
+    inp.steps_warmup, inp.steps_mc, inp.steps_measure = 50, 100, 1
+    mc.run(inp, seed=3, outdir=str(tmp_path))
+    rows = [l.split() for l in open(os.path.join(str(tmp_path), inp.seedname + "_spincorr.dat"))
+            if l.strip() and not l.lstrip().startswith("#")]
+    assert len(rows) == 4 * len(inp.tems)
+    assert rows[0][2] == "Ni" and rows[3][1] == "4"
+    # at the lowest temperature shells 3 and 4 are antiferromagnetic, as in
+    # the reference's file
+    assert float(rows[2][6]) < -0.5 and float(rows[3][6]) < -0.5

@@ -1,13 +1,18 @@
-"""The order parameter and the staggered magnetisation on the CPU side:
+"""The order parameter, the staggered magnetisation and the spin correlations
+on the CPU side:
 
 * the oracle's orderparam_get / staggered_get / Pm_get restatement against
   identities that hold for any configuration (all staggered coefficients +1
   give the magnetisation; axes along z give m_z), and over a whole chain
   (the staggered columns of a run with +1 coefficients equal its |m| columns);
-* the writers' format 126 against rows of the reference's own _op.dat;
+* the writers' format 126 and the _spincorr.dat row format against rows of
+  the reference's own files;
+* the neighbour shells of spincorr_get (jij.F90:449-503) and the oracle's
+  spincorr_get on ordered states;
 * the input parser's staggered_m_coeff rules (parameters.F90:450-463).
 The oracle's order parameter is pinned to the reference's ex03 _op.dat row and
-P(OP) column by the seed-exact replay in test_oracle_golden.py.
+P(OP) column, and its spin correlations to the ex05 _spincorr.dat rows, by the
+seed-exact replays in test_oracle_golden.py.
 """
 import numpy as np
 import pytest
@@ -15,7 +20,7 @@ import pytest
 import oracle as O
 from espins_gb300 import writers as W
 from espins_gb300.mcin import McinError, parse_mcin
-from espins_gb300.tables import build_hamiltonian
+from espins_gb300.tables import build_hamiltonian, build_shells
 from helpers import NN, example, sc_mcin
 
 
@@ -36,6 +41,27 @@ def _bcc_afm(L=4, tems=(6.0,), extra=""):
     lines.append("end jij_parameters")
     lines += [l for l in extra.splitlines() if l.strip()]
     return parse_mcin("\n".join(lines) + "\n", seedname="bcc")
+
+
+def _bcc_shells(L=4, tems=(6.0,), j1=-0.002, j2=0.0003):
+    """bcc as a two-species simple-cubic cell (Fe at the corner, Co at the
+    centre) with spin-correlation shells: sh=1 the 8 Fe-Co neighbours, sh=2 the
+    6 same-species neighbours."""
+    lines = ["begin unit_cell_cart", "1 0 0", "0 1 0", "0 0 1", "end unit_cell_cart",
+             "begin atoms_frac", "Fe 0 0 0 1.0", "Co 0.5 0.5 0.5 1.0", "end atoms_frac",
+             f"supercell_size = {L} {L} {L}", "tems_mode = man", f"tems_num = {len(tems)}",
+             "tems = " + " ".join(repr(float(t)) for t in tems),
+             "steps_warmup = 10", "steps_mc = 100", "steps_measure = 1", "spin_correlation = .true.",
+             "begin jij_parameters"]
+    for c in ((0, 0, 0), (0.5, 0.5, 0.5)):
+        for dx in (0.5, -0.5):
+            for dy in (0.5, -0.5):
+                for dz in (0.5, -0.5):
+                    lines.append(f"f1={c[0]},{c[1]},{c[2]}:f2={c[0] + dx},{c[1] + dy},{c[2] + dz}:jij={j1}:sh=1")
+        for o in NN:
+            lines.append(f"f1={c[0]},{c[1]},{c[2]}:f2={c[0] + o[0]},{c[1] + o[1]},{c[2] + o[2]}:jij={j2}:sh=2")
+    lines.append("end jij_parameters")
+    return parse_mcin("\n".join(lines) + "\n", seedname="bccsc")
 
 
 def _random_spins(h, seed):
@@ -124,3 +150,43 @@ def test_staggered_coefficients_default_and_validation():
     # one atom per cell: staggered_m is switched off
     one = sc_mcin(4, [(1e-3, NN)], [5.0], extra="staggered_m = .true.")
     assert not one.lstaggered
+
+
+def test_spincorr_row_format_reproduces_reference_rows():
+    _, g = example("ex05_snwo")
+    for row, line in zip(g["spincorr_dat"], g["spincorr_dat_lines"]):
+        assert W.spincorr_row(row[0], row[1], "Ni", row[2], "Ni", row[3], *row[4:]) == line
+
+
+def test_shell_tables():
+    inp, _ = example("ex05_snwo")
+    t = build_shells(inp)
+    assert t.num_shells == 4 and t.num_species == 1
+    assert [int(x) for x in t.nn[:, 0]] == [4, 8, 4, 2]
+    assert np.all(t.nn == t.nn[:, :1])
+    # periodic shells are symmetric: j in shell s of i <=> i in shell s of j
+    for s_ in range(t.num_shells):
+        pairs = {(i, int(t.nb[s_, k, i])) for i in range(t.kind.size) for k in range(t.nn[s_, i])}
+        assert all((j, i) in pairs for i, j in pairs)
+    b = build_shells(_bcc_shells())
+    assert b.num_species == 2
+    assert [int(x) for x in b.nn[:, 0]] == [8, 6]
+    # shell_num_nbors_kind(s, a, b): species-a neighbours around the last site of species b
+    assert b.count[0].tolist() == [[0, 8], [8, 0]] and b.count[1].tolist() == [[6, 0], [0, 6]]
+
+
+def test_oracle_spincorr_on_ordered_states():
+    inp = _bcc_shells()
+    h = build_hamiltonian(inp)
+    H = O.Ham(h)
+    sh = build_shells(inp)
+    ferro = np.zeros((h.n, 3)); ferro[:, 2] = 1.0
+    sc, sa, st = H.spincorr(sh, ferro.reshape(-1))
+    # every existing (shell, species pair) bin sums to its number of sites
+    want = np.zeros((2, 2, 2))
+    want[0, 0, 1] = want[0, 1, 0] = want[1, 0, 0] = want[1, 1, 1] = h.n // 2
+    assert np.allclose(sc, want) and np.allclose(sa, want) and np.allclose(st, want)
+    neel = ferro.copy(); neel[1::2, 2] = -1.0      # Co antiparallel to Fe
+    sc, sa, st = H.spincorr(sh, neel.reshape(-1))
+    assert np.allclose(sc[0], -want[0]) and np.allclose(sc[1], want[1])
+    assert np.allclose(sa, want) and np.allclose(st, want)

@@ -7,7 +7,9 @@ The reference has no unit tests; its example runs are the known answers:
   the energy triple and the ``_mc.dat`` row, and the final spins of the
   ``_sconfig.dat`` file (mcarlo.F90:496-733); where the example measured the
   order parameter, also its ``_op.dat`` row and the P(M) / P(OP) columns of
-  ``_pm.dat`` (orderparam_get, Pm_get: get_quant.F90:396-493);
+  ``_pm.dat`` (orderparam_get, Pm_get: get_quant.F90:396-493); where it
+  measured spin correlations, its ``_spincorr.dat`` rows (spincorr_get,
+  get_quant.F90:495-540, over the shells of jij.F90:449-503);
 * energy fixtures: the final spins of every temperature and the printed
   "Final Energy by direct calculations" (energy_get, get_quant.F90:186-261);
 * MT19937 (mtprng.f90) against numpy's MT19937 for non-negative seeds, and
@@ -21,7 +23,7 @@ import pytest
 
 import oracle as O
 from espins_gb300.mcin import K_B, read_mcin
-from espins_gb300.tables import build_hamiltonian
+from espins_gb300.tables import build_hamiltonian, build_shells
 
 
 def _load(golden_dir, name, nodes=4):
@@ -107,7 +109,7 @@ def _e8(x):
     return float("%.7E" % x)
 
 
-def _replay(golden_dir, name, rank, check_mcdat=True, check_obs=False):
+def _replay(golden_dir, name, rank, check_mcdat=True, check_obs=False, check_spincorr=False):
     inp, g = _load(golden_dir, name)
     h = build_hamiltonian(inp)
     H = O.Ham(h)
@@ -118,6 +120,8 @@ def _replay(golden_dir, name, rank, check_mcdat=True, check_obs=False):
     s[:, 2] = h.mag                     # initial_sconfig = ferro
     mt = O.MT(g["seeds"][rank])
     obs = {"op_axes": inp.orderparam_axes_cart} if check_obs else {}
+    if check_spincorr:
+        obs["shells"] = build_shells(inp)
     r = H.mcarlo(mt, 1.0 / T, s, inp.steps_warmup, inp.steps_mc, inp.steps_measure,
                  binning_level=[1, 2, 3, 4, 5], **obs)
     row = g["rows"][t_index]
@@ -161,6 +165,16 @@ def _replay(golden_dir, name, rank, check_mcdat=True, check_obs=False):
         for f in range(pm.size):
             assert _e8(pm[f]) == pytest.approx(rows[f, 1], rel=1e-12, abs=1e-300), f
             assert _e8(pop[f]) == pytest.approx(rows[f, 2], rel=1e-12, abs=1e-300), f
+    if check_spincorr:
+        # global_spincorr * normalize / N (mcarlo.F90:717-723), printed f12.9
+        normalize = 1.0 / inp.steps_mc
+        got = {k: r[k][0] * normalize / h.n for k in ("spincorr", "spincorr_abs", "spincorr_tot")}
+        rows = [x for x in g["spincorr_dat"] if abs(x[0] - T) < 1e-4]
+        assert len(rows) == got["spincorr"].size
+        for x in rows:
+            sh, a, b = x[1] - 1, x[2] - 1, x[3] - 1
+            for k, want in zip(("spincorr", "spincorr_abs", "spincorr_tot"), x[4:7]):
+                assert float("%.9f" % got[k][sh, a, b]) == pytest.approx(want, abs=1e-15), (k, x)
     return r
 
 
@@ -173,7 +187,7 @@ def test_seed_exact_replay_ex01_positive_seed(golden_dir):
 
 
 def test_seed_exact_replay_ex05_biquadratic_singleion(golden_dir):
-    _replay(golden_dir, "ex05_snwo", rank=0, check_mcdat=True)
+    _replay(golden_dir, "ex05_snwo", rank=0, check_mcdat=True, check_spincorr=True)
 
 
 def test_seed_exact_replay_ex03_biquadratic_dm(golden_dir):
