@@ -16,8 +16,10 @@ files.  Differences from the reference, by design:
 The order parameter, the staggered magnetisation and the spin correlations
 (order_parameter, staggered_m, spin_correlation) are measured on the GPU with
 every measurement and written to _op.dat / _staggered.dat / _spincorr.dat and
-the extra _pm.dat / _binerror.dat columns.  The other optional measurements
-(structure factor, energy series) are rejected with an error naming the
+the extra _pm.dat / _binerror.dat columns.  With energy_write the running
+energy of every measurement is recorded on the device and written to the
+_energy-T###.dat files in chunks of the measurements that fit the device
+series buffer.  The structure factor is rejected with an error naming the
 keyword.
 """
 from __future__ import annotations
@@ -33,7 +35,10 @@ from .lib import Engine
 from .mcin import McInput, McinError
 from .tables import Hamiltonian, build_hamiltonian, build_shells
 
-UNSUPPORTED = [("lsfactor", "sfactor"), ("energy_write", "energy_write")]
+UNSUPPORTED = [("lsfactor", "sfactor")]
+
+# bytes of device memory the energy series may hold at once
+SERIES_BYTES = 1 << 28
 
 
 @dataclass
@@ -77,14 +82,44 @@ def run(inp: McInput, seed: Optional[int] = None, outdir: Optional[str] = None,
             e.set_spins(s)
         else:
             e.init_spins("rand" if inp.initial_sconfig.startswith("rand") else "ferro", seed)
-        res = e.run(inp.steps_warmup, inp.steps_mc, inp.steps_measure, pt=inp.pt,
-                    pt_steps_swap=inp.pt_steps_swap, mode=mode, tilt=inp.tilt_angles_max, seed=seed,
-                    binning_level=inp.binning_level if inp.lbinerror else None)
+        kw = dict(pt=inp.pt, pt_steps_swap=inp.pt_steps_swap, mode=mode, tilt=inp.tilt_angles_max, seed=seed,
+                  binning_level=inp.binning_level if inp.lbinerror else None)
+        if inp.energy_write and write and outdir is not None:
+            res = _run_with_series(e, inp, outdir, tems, ham.n, kw)
+        else:
+            res = e.run(inp.steps_warmup, inp.steps_mc, inp.steps_measure, **kw)
         spins = e.get_spins()
     out = RunResult(tems=tems, res=res, spins=spins, ham=ham, seed=seed)
     if write and outdir is not None:
         write_outputs(inp, out, outdir)
     return out
+
+
+def _run_with_series(e: Engine, inp: McInput, outdir: str, tems, n: int, kw) -> dict:
+    """esp_begin / esp_advance / esp_collect with the energy series read back
+    after every chunk of measurement units (open_E_unit, write_E: the
+    reference writes every energy_num_print measurements; the content of the
+    files does not depend on the chunking)."""
+    R = len(tems)
+    per_unit = inp.pt_steps_swap if inp.pt else 1
+    units = -(-inp.steps_mc // per_unit) if inp.pt else inp.steps_mc
+    nsteps = units * per_unit
+    chunk = max(1, min(units, SERIES_BYTES // (16 * R * per_unit)))
+    e.set_series(chunk * per_unit)
+    os.makedirs(outdir, exist_ok=True)
+    series = W.EnergySeries(os.path.join(outdir, inp.seedname or "espins"), tems, nsteps, n)
+    try:
+        e.begin(e.schedule(inp.steps_warmup, inp.steps_mc, inp.steps_measure, **kw))
+        done = 0
+        while done < units:
+            k = min(chunk, units - done)
+            e.advance(k)
+            done += k
+            series.append(e.series()[-k * per_unit:, :, 0])
+        return e.collect()
+    finally:
+        series.close()
+        e.set_series(0)
 
 
 def write_outputs(inp: McInput, r: RunResult, outdir: str) -> None:

@@ -15,6 +15,10 @@ src/pt.F90:1040-1085:
 * ``seed_spincorr.dat`` header of mcarlo.F90:131-141, rows
                         (f9.4,1x,I5,6x,a3,4x,i3,6x,a3,4x,i3,8x,f12.9,10x,f12.9,12x,f12.9)
                         per temperature, shell and species pair (:760-770)
+* ``seed_energy-T###.dat`` one file per temperature (energy_write): date line,
+                        '(3x,a,f9.4)' '# T = ', '(3x,i16)' the number of
+                        measurements, then '(I14,4x,1E16.8)' measurement index
+                        and running E/N (get_quant.F90:1130-1191)
 With the order parameter or the staggered magnetisation switched on, _pm.dat
 gains the P(OP) / P(SM) columns and _binerror.dat their error columns
 (mcarlo.F90:174-215 and :784-818, pt.F90:159-200 and :1050-1073).
@@ -23,6 +27,7 @@ from __future__ import annotations
 
 import datetime
 import math
+import os
 from typing import Sequence
 
 import numpy as np
@@ -310,6 +315,42 @@ def write_spincorr(path: str, tems, sc: np.ndarray, sc_abs: np.ndarray, sc_tot: 
                     for b in range(nsp):
                         fh.write(spincorr_row(T, l + 1, symbols[a], a + 1, symbols[b], b + 1, sc[k, l, a, b],
                                               sc_abs[k, l, a, b], sc_tot[k, l, a, b]) + "\n")
+
+
+def energy_series_name(seedname: str, n: int) -> str:
+    """seed_energy-T###.dat of the n-th temperature (1-based, three digits)."""
+    return f"{seedname}_energy-T{n // 100 % 10}{n // 10 % 10}{n % 10}.dat"
+
+
+class EnergySeries:
+    """The energy series files of open_E_unit / write_E / close_E_unit: rows
+    are appended in measurement order as the run produces them."""
+
+    def __init__(self, base: str, tems, nsteps: int, n: int):
+        self.n = n
+        self.count = 0
+        d, t = _date()
+        folder, seed = os.path.split(base)
+        self.fh = []
+        for k, T in enumerate(tems, start=1):
+            fh = open(os.path.join(folder, energy_series_name(seed, k)), "w")
+            fh.write(f" #written on {d} at {t} \n")
+            fh.write("   # T = " + fortran_f(T, 9, 4) + "\n")
+            fh.write("   " + f"{int(nsteps):16d}" + "\n")
+            self.fh.append(fh)
+
+    def append(self, energies: np.ndarray) -> None:
+        """energies: (measurements, R) running energies, oldest first."""
+        m = energies.shape[0]
+        for t, fh in enumerate(self.fh):
+            fh.write("".join(f"{self.count + i + 1:14d}    " + fortran_e(energies[i, t] / self.n, 16, 8) + "\n"
+                             for i in range(m)))
+        self.count += m
+
+    def close(self) -> None:
+        for fh in self.fh:
+            fh.close()
+        self.fh = []
 
 
 def write_binerror(path: str, tems, binning: np.ndarray, levels, n: int, pt: bool, obs_binning=None,

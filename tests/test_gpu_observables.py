@@ -12,8 +12,9 @@ mcarlo.F90:545-590 / pt.F90:798-849):
   typewriter chains (the reference's algorithm) within 3 sigma;
 * the spin correlations equal the oracle's spincorr_get of the same spins,
   measurement by measurement, for every sweep kernel;
-* the host driver writes _op.dat, _staggered.dat, _spincorr.dat and the extra
-  columns.
+* the host driver writes _op.dat, _staggered.dat, _spincorr.dat, the extra
+  columns and the energy series files (whose rows do not depend on how the
+  run is chunked, and whose last row is the final running energy).
 """
 import os
 
@@ -267,3 +268,25 @@ def test_host_driver_writes_spin_correlation_file(tmp_path):
     # at the lowest temperature shells 3 and 4 are antiferromagnetic, as in
     # the reference's file
     assert float(rows[2][6]) < -0.5 and float(rows[3][6]) < -0.5
+
+
+@pytest.mark.parametrize("pt", [False, True])
+def test_energy_series_files(tmp_path, monkeypatch, pt):
+    inp = _bcc_afm(L=4, tems=(3.0, 6.0, 12.0, 24.0))
+    inp.steps_warmup, inp.steps_mc, inp.steps_measure = 20, 47, 1
+    inp.pt, inp.pt_steps_swap = pt, 5
+    inp.energy_write = True
+    texts = []
+    for budget, sub in ((1 << 28, "a"), (16 * 4 * 5 * 3, "b")):    # one chunk / chunks of 3 units
+        monkeypatch.setattr(mc, "SERIES_BYTES", budget)
+        r = mc.run(inp, seed=11, outdir=str(tmp_path / sub))
+        texts.append([open(os.path.join(str(tmp_path / sub), "bcc_energy-T%03d.dat" % (t + 1))).read().splitlines()[1:]
+                      for t in range(4)])
+        nsteps = 50 if pt else 47
+        for t in range(4):
+            rows = texts[-1][t][2:]
+            assert int(texts[-1][t][1]) == nsteps and len(rows) == nsteps
+            assert [int(x.split()[0]) for x in rows] == list(range(1, nsteps + 1))
+            # the last row is the final running energy per site
+            assert float(rows[-1].split()[1]) == pytest.approx(r.res["energy"][t, 1] / r.ham.n, rel=1e-7)
+    assert texts[0] == texts[1]

@@ -190,3 +190,22 @@ def test_oracle_spincorr_on_ordered_states():
     sc, sa, st = H.spincorr(sh, neel.reshape(-1))
     assert np.allclose(sc[0], -want[0]) and np.allclose(sc[1], want[1])
     assert np.allclose(sa, want) and np.allclose(st, want)
+
+
+def test_energy_series_files_format(tmp_path):
+    """open_E_unit / write_E layout: name seed_energy-T###.dat, '# T =' line,
+    the number of measurements, rows (I14,4x,E16.8) of E/N in order."""
+    assert W.energy_series_name("fef3", 7) == "fef3_energy-T007.dat"
+    assert W.energy_series_name("fef3", 123) == "fef3_energy-T123.dat"
+    s = W.EnergySeries(str(tmp_path / "x"), [5.0, 12.5], 5, 4)
+    s.append(np.array([[-4.0, 2.0], [-8.0, 6.0]]))
+    s.append(np.array([[-2.0, 0.4]] * 3))
+    s.close()
+    lines = open(tmp_path / "x_energy-T002.dat").read().splitlines()
+    assert lines[1] == "   # T =   12.5000"
+    assert lines[2] == "   " + " " * 15 + "5"
+    assert lines[3] == "             1      0.50000000E+00"
+    assert lines[4] == "             2      0.15000000E+01"
+    assert len(lines) == 8 and lines[7].startswith("             5")
+    first = open(tmp_path / "x_energy-T001.dat").read().splitlines()
+    assert first[3] == "             1     -0.10000000E+01"
