@@ -110,6 +110,15 @@ struct esp_handle {
     float *d_sc_w = nullptr;
     double *d_sc_scratch = nullptr, *d_sc_out = nullptr, *d_sc_acc = nullptr;
     std::vector<double> mag_host;   // mag_moments_matrix, reference order
+    // structure factor (esp_set_structure_factor)
+    int sf_nq = 0, sf_every = 1;
+    double sf_p[3] = {1.0, 0.0, 0.0}, sf_pnorm = 1.0;
+    int4 *d_sf_n = nullptr;
+    float4 *d_sf_f = nullptr, *d_sf_qf = nullptr, *d_sf_qc = nullptr;
+    uint4 *d_sf_qfix = nullptr;
+    float *d_sf_fq = nullptr;
+    double *d_sf_acc = nullptr;
+    unsigned long long *d_sf_count = nullptr;
     std::vector<double> tems;
     int nf = 2;
     double m_min = 0, m_max = 0;
@@ -198,6 +207,13 @@ void free_obs(esp_handle *h)
     h->obs = 0;
 }
 
+void free_sf(esp_handle *h)
+{
+    dfree(h->d_sf_n); dfree(h->d_sf_f); dfree(h->d_sf_qf); dfree(h->d_sf_qc); dfree(h->d_sf_qfix);
+    dfree(h->d_sf_fq); dfree(h->d_sf_acc); dfree(h->d_sf_count);
+    h->sf_nq = 0;
+}
+
 void free_sc(esp_handle *h)
 {
     dfree(h->d_sc_off); dfree(h->d_sc_nb); dfree(h->d_sc_w);
@@ -222,6 +238,7 @@ void free_all(esp_handle *h)
     dfree(h->d_obs_lsum); dfree(h->d_obs_bin);
     free_obs(h);
     free_sc(h);
+    free_sf(h);
     dfree(h->d_series);
     free_lp_batch(h);
     dfree(h->d_lp_p); dfree(h->d_lp_g); dfree(h->d_lp_m); dfree(h->d_lp_v);
@@ -529,6 +546,39 @@ int spincorr_measure(esp_handle *h)
     return ESP_OK;
 }
 
+// The structure factor after measurement `step` (1-based) when step is a
+// multiple of sfactor_steps_measure; inside a graph capture the kernels test
+// the step against the device measurement counter instead.
+int sfactor_measure(esp_handle *h, long long step)
+{
+    SfArgs a;
+    a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz; a.inv = h->d_inv;
+    a.site_n = h->d_sf_n; a.site_f = h->d_sf_f; a.q_fix = h->d_sf_qfix; a.q_frac = h->d_sf_qf; a.q_cart = h->d_sf_qc;
+    a.fq = h->d_sf_fq; a.acc = h->d_sf_acc; a.count = h->d_sf_count; a.repl_at = h->d_repl_at;
+    a.px = h->sf_p[0]; a.py = h->sf_p[1]; a.pz = h->sf_p[2]; a.pnorm = h->sf_pnorm;
+    a.N = h->N; a.R = h->R; a.nq = h->sf_nq; a.every = h->sf_every;
+    a.step = step; a.ctr = nullptr;
+    if (h->capturing) {
+        a.step -= h->cap_base[2];
+        a.ctr = h->d_ctr + 2;
+    } else if (step % h->sf_every != 0) {
+        return ESP_OK;
+    }
+    CK(launch_sfactor(a, h->st));
+    h->launches += 2;
+    return ESP_OK;
+}
+
+// Measurements made by their own kernels after measurement `step`: spin
+// correlations and the structure factor.
+int extra_measure(esp_handle *h, long long step)
+{
+    int rc = ESP_OK;
+    if (h->sc_B && (rc = spincorr_measure(h))) return rc;
+    if (h->sf_nq && (rc = sfactor_measure(h, step))) return rc;
+    return rc;
+}
+
 int measure(esp_handle *h, long long step, int nlev, bool pt_quirk, long long &const_hits)
 {
     int rc = fold(h);
@@ -556,8 +606,8 @@ int measure(esp_handle *h, long long step, int nlev, bool pt_quirk, long long &c
     }
     CK(launch_measure(m, h->st));
     h->launches++;
-    if (h->sc_B) {
-        int rc = spincorr_measure(h);
+    {
+        int rc = extra_measure(h, step);
         if (rc) return rc;
     }
     // one atom per cell: |sum_cell s| = |m| for every cell, so every cell
@@ -923,6 +973,7 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
     free_tables(h);
     free_obs(h);
     free_sc(h);
+    free_sf(h);
     h->have_tables = false;
     h->mag_host.assign(t->mag, t->mag + h->N);
     const size_t M = (size_t)prep.maxnb * h->N;
@@ -1442,6 +1493,10 @@ int esp_begin(esp_handle *h, const esp_schedule *s)
         CK(cudaMemsetAsync(h->d_obs_pm, 0, sizeof(unsigned long long) * 2 * R * h->nf, h->st));
     }
     if (h->sc_B) CK(cudaMemsetAsync(h->d_sc_acc, 0, sizeof(double) * 3 * (size_t)R * h->sc_B, h->st));
+    if (h->sf_nq) {
+        CK(cudaMemsetAsync(h->d_sf_acc, 0, sizeof(double) * 3 * (size_t)R * h->sf_nq, h->st));
+        CK(cudaMemsetAsync(h->d_sf_count, 0, sizeof(unsigned long long), h->st));
+    }
     CK(cudaMemsetAsync(h->d_rej, 0, sizeof(unsigned long long) * 2 * R, h->st));
     CK(cudaMemsetAsync(h->d_swaps, 0, sizeof(long long) * 2 * R, h->st));
     esp_sweep_opts o;
@@ -1493,9 +1548,10 @@ int esp_advance(esp_handle *h, int64_t n)
     esp_sweep_opts o;
     o.mcarlo_mode = s.mcarlo_mode; o.tilt_angles_max = s.tilt_angles_max; o.seed = s.seed; o.phase = 1;
     if (use_cluster(h)) {
-        // spin correlations are measured by their own kernels after every
-        // measurement, so each launch then runs one measurement unit
-        const int64_t chunk = h->sc_B ? 1 : kChunk;
+        // spin correlations and the structure factor are measured by their
+        // own kernels after a measurement, so each launch then runs one
+        // measurement unit
+        const int64_t chunk = (h->sc_B || h->sf_nq) ? 1 : kChunk;
         if (!s.pt) {
             // independent temperatures: many measurement units per launch
             for (int64_t done = 0; done < n; done += chunk) {
@@ -1505,7 +1561,7 @@ int esp_advance(esp_handle *h, int64_t n)
                 h->next_sweep += k * s.steps_measure;
                 u.meas_done += k;
                 if (h->na == 1) u.const_hits += k;
-                if (h->sc_B && (rc = spincorr_measure(h))) return rc;
+                if ((h->sc_B || h->sf_nq) && (rc = extra_measure(h, u.meas_done))) return rc;
             }
             u.units_done += n;
         } else {
@@ -1519,7 +1575,7 @@ int esp_advance(esp_handle *h, int64_t n)
                     h->next_sweep += m * s.steps_measure;
                     u.meas_done += m;
                     if (h->na == 1) u.const_hits += m;
-                    if (h->sc_B && (rc = spincorr_measure(h))) return rc;
+                    if ((h->sc_B || h->sf_nq) && (rc = extra_measure(h, u.meas_done))) return rc;
                 }
                 if ((rc = pt_swap_launch(h, (int)((l + 1) % 2) + 1, h->next_swap++, s.seed, l))) return rc;
             }
@@ -1839,6 +1895,118 @@ int esp_collect_spin_correlation(esp_handle *h, double *spincorr, double *spinco
     for (int c = 0; c < 3; ++c)
         if (outs[c])
             for (size_t k = 0; k < R * B; ++k) outs[c][k] = acc[k * 3 + c] * normalize / (double)h->N;
+    return ESP_OK;
+}
+
+int esp_set_structure_factor(esp_handle *h, int32_t nq, const double *qpts, const double *polar,
+                             int32_t steps_measure, const double *real_lattice, const double *pos)
+{
+    if (!h) return ESP_EINVAL;
+    if (!h->have_tables) { h->err = "upload the tables before the structure factor"; return ESP_ESTATE; }
+    if (nq < 0 || (nq > 0 && (!qpts || !polar || !real_lattice || !pos || steps_measure < 1))) {
+        h->err = "invalid structure-factor arguments";
+        return ESP_EINVAL;
+    }
+    if ((long long)nq * h->R > (1LL << 31) / 8) { h->err = "too many q-points x replicas"; return ESP_EINVAL; }
+    const int N = h->N;
+    std::vector<int4> sn;
+    std::vector<float4> sf_f, qf, qc;
+    std::vector<uint4> qfix;
+    double pnorm = 1.0;
+    if (nq > 0) {
+        // a_j = real_lattice(j, :), Fortran column-major
+        double A[3][3];
+        for (int j = 0; j < 3; ++j)
+            for (int i = 0; i < 3; ++i) A[j][i] = real_lattice[j + 3 * i];
+        // pos = sum_j u_j a_j: u = M pos with M the inverse of the transpose of A
+        const double det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) -
+                           A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+                           A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+        if (!(std::fabs(det) > 1e-12)) { h->err = "singular real_lattice"; return ESP_EINVAL; }
+        double M[3][3];   // M[j][i]: u_j = sum_i M[j][i] pos_i, rows of the reciprocal lattice / 2 pi
+        M[0][0] = (A[1][1] * A[2][2] - A[1][2] * A[2][1]) / det;
+        M[0][1] = (A[1][2] * A[2][0] - A[1][0] * A[2][2]) / det;
+        M[0][2] = (A[1][0] * A[2][1] - A[1][1] * A[2][0]) / det;
+        M[1][0] = (A[2][1] * A[0][2] - A[2][2] * A[0][1]) / det;
+        M[1][1] = (A[2][2] * A[0][0] - A[2][0] * A[0][2]) / det;
+        M[1][2] = (A[2][0] * A[0][1] - A[2][1] * A[0][0]) / det;
+        M[2][0] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) / det;
+        M[2][1] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) / det;
+        M[2][2] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) / det;
+        sn.resize(N); sf_f.resize(N);
+        for (int i = 0; i < N; ++i) {
+            double u[3], n[3];
+            for (int j = 0; j < 3; ++j) {
+                u[j] = M[j][0] * pos[3 * i] + M[j][1] * pos[3 * i + 1] + M[j][2] * pos[3 * i + 2];
+                n[j] = std::floor(u[j]);
+                if (std::fabs(n[j]) > 1e9) { h->err = "site position too far from the origin"; return ESP_EINVAL; }
+            }
+            sn[i] = make_int4((int)n[0], (int)n[1], (int)n[2], 0);
+            sf_f[i] = make_float4((float)(u[0] - n[0]), (float)(u[1] - n[1]), (float)(u[2] - n[2]), 0.f);
+        }
+        qf.resize(nq); qc.resize(nq); qfix.resize(nq);
+        const double two32 = 4294967296.0, twopi = 6.283185307179586476925286766559;
+        for (int k = 0; k < nq; ++k) {
+            const double *q = qpts + 3 * k;
+            double f[3];
+            uint32_t fx[3];
+            for (int j = 0; j < 3; ++j) {
+                f[j] = (q[0] * A[j][0] + q[1] * A[j][1] + q[2] * A[j][2]) / twopi;
+                const double fr = f[j] - std::floor(f[j]);
+                fx[j] = (uint32_t)(unsigned long long)std::llround(fr * two32);
+            }
+            qfix[k] = make_uint4(fx[0], fx[1], fx[2], 0u);
+            qf[k] = make_float4((float)f[0], (float)f[1], (float)f[2], 0.f);
+            const bool zero = q[0] == 0.0 && q[1] == 0.0 && q[2] == 0.0;
+            qc[k] = make_float4((float)q[0], (float)q[1], (float)q[2], zero ? 1.f : 0.f);
+        }
+        pnorm = std::sqrt(polar[0] * polar[0] + polar[1] * polar[1] + polar[2] * polar[2]);
+        if (!(pnorm > 0.0)) { h->err = "sfactor_polar must not be zero"; return ESP_EINVAL; }
+    }
+    int rc = fold(h);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->st));
+    free_sf(h);
+    if (nq == 0) return ESP_OK;
+    CK(dalloc(&h->d_sf_n, (size_t)N));
+    CK(dalloc(&h->d_sf_f, (size_t)N));
+    CK(dalloc(&h->d_sf_qfix, (size_t)nq));
+    CK(dalloc(&h->d_sf_qf, (size_t)nq));
+    CK(dalloc(&h->d_sf_qc, (size_t)nq));
+    CK(dalloc(&h->d_sf_fq, (size_t)nq * h->R * 6));
+    CK(dalloc(&h->d_sf_acc, (size_t)nq * h->R * 3));
+    CK(dalloc(&h->d_sf_count, 1));
+    if ((rc = h2d(h, h->d_sf_n, sn.data(), sizeof(int4) * N))) return rc;
+    if ((rc = h2d(h, h->d_sf_f, sf_f.data(), sizeof(float4) * N))) return rc;
+    if ((rc = h2d(h, h->d_sf_qfix, qfix.data(), sizeof(uint4) * nq))) return rc;
+    if ((rc = h2d(h, h->d_sf_qf, qf.data(), sizeof(float4) * nq))) return rc;
+    if ((rc = h2d(h, h->d_sf_qc, qc.data(), sizeof(float4) * nq))) return rc;
+    CK(cudaMemsetAsync(h->d_sf_acc, 0, sizeof(double) * 3 * (size_t)nq * h->R, h->st));
+    CK(cudaMemsetAsync(h->d_sf_count, 0, sizeof(unsigned long long), h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->sf_nq = nq; h->sf_every = steps_measure;
+    for (int c = 0; c < 3; ++c) h->sf_p[c] = polar[c];
+    h->sf_pnorm = pnorm;
+    return ESP_OK;
+}
+
+int esp_collect_structure_factor(esp_handle *h, double *sf, int64_t *num_measured)
+{
+    int rc = require(h, true, true);
+    if (rc) return rc;
+    RunState &u = h->run;
+    if (!u.active) { h->err = "esp_begin has not been called"; return ESP_ESTATE; }
+    if (!h->sf_nq) { h->err = "no structure factor was set (esp_set_structure_factor)"; return ESP_ESTATE; }
+    if ((rc = fold(h))) return rc;
+    unsigned long long cnt = 0;
+    if ((rc = d2h(h, &cnt, h->d_sf_count, sizeof(cnt)))) return rc;
+    if (num_measured) *num_measured = (int64_t)cnt;
+    if (sf) {
+        const size_t n = (size_t)h->R * h->sf_nq * 3;
+        if ((rc = d2h(h, sf, h->d_sf_acc, sizeof(double) * n))) return rc;
+        // global_sfactor_matrix / N / num_sfsteps_tot (mcarlo.F90:821-822)
+        for (size_t k = 0; k < n; ++k) sf[k] = cnt ? sf[k] / (double)h->N / (double)cnt : 0.0;
+    }
     return ESP_OK;
 }
 

@@ -10,6 +10,8 @@
 //                    reduced by k_energy_reduce
 //   k_sc_part        spincorr_get (get_quant.F90:495-540) bin sums per
 //                    replica, reduced by k_sc_reduce, accumulated by k_sc_finish
+//   k_sf_part        mcarlo_structure_factor (get_quant.F90:649-717): F(q) per
+//                    replica; k_sf_finish projects and accumulates per slot
 //   k_measure        per-measurement accumulators and binning
 //                    (mcarlo.F90:536-590, pt.F90:789-849)
 //   k_pm_hist        Pm_get (get_quant.F90:425-493) as an integer histogram
@@ -436,6 +438,100 @@ __global__ void k_sc_finish(const ScArgs a)
 }
 
 // ---------------------------------------------------------------------------
+// Structure factor.  Block: 64 q-points x 4 replicas (thread = one pair);
+// the block walks all sites in tiles of 64, staging the tile's phases
+// e^{i q.r} (shared by the replicas) and spins (shared by the q-points) in
+// shared memory.  FP32 sums; the phase is exact to 2^-24 of a turn.
+// ---------------------------------------------------------------------------
+constexpr int kSfQ = 64, kSfR = 4, kSfTile = 64;
+
+__device__ __forceinline__ long long sf_step(const SfArgs &a)
+{
+    return a.step + (a.ctr ? (long long)*a.ctr : 0ll);
+}
+
+__global__ void __launch_bounds__(kSfQ * kSfR) k_sf_part(const SfArgs a)
+{
+    if (sf_step(a) % a.every != 0) return;
+    __shared__ float2 s_ph[kSfTile][kSfQ];
+    __shared__ float s_sp[kSfTile][kSfR][3];
+    const int qi = threadIdx.x % kSfQ, rr = threadIdx.x / kSfQ;
+    const int q = blockIdx.x * kSfQ + qi, r = blockIdx.y * kSfR + rr;
+    float fxr = 0.f, fxi = 0.f, fyr = 0.f, fyi = 0.f, fzr = 0.f, fzi = 0.f;
+    for (int i0 = 0; i0 < a.N; i0 += kSfTile) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < kSfTile * kSfQ; k += blockDim.x) {
+            const int j = k / kSfQ, qq = k % kSfQ;
+            const int i = i0 + j, qg = blockIdx.x * kSfQ + qq;
+            float c = 0.f, sn = 0.f;
+            if (i < a.N && qg < a.nq) {
+                const int4 n = __ldg(a.site_n + i);
+                const float4 f = __ldg(a.site_f + i);
+                const uint4 qfix = __ldg(a.q_fix + qg);
+                const float4 qf = __ldg(a.q_frac + qg);
+                // whole cells: exact modulo one turn in 32-bit fixed point
+                const uint32_t t = qfix.x * (uint32_t)n.x + qfix.y * (uint32_t)n.y + qfix.z * (uint32_t)n.z;
+                const float tw = (float)(int32_t)t * 2.3283064365386963e-10f;   // [-1/2, 1/2) turn
+                float tf = qf.x * f.x + qf.y * f.y + qf.z * f.z;
+                tf -= rintf(tf);
+                sincospif(2.f * (tw + tf), &sn, &c);
+            }
+            s_ph[j][qq] = make_float2(c, sn);
+        }
+        for (int k = threadIdx.x; k < kSfTile * kSfR; k += blockDim.x) {
+            const int j = k / kSfR, rq = k % kSfR;
+            const int i = i0 + j, rg = blockIdx.y * kSfR + rq;
+            float x = 0.f, y = 0.f, z = 0.f;
+            if (i < a.N && rg < a.R) {
+                const size_t idx = (size_t)__ldg(a.inv + i) * a.R + rg;
+                x = a.sx[idx]; y = a.sy[idx]; z = a.sz[idx];
+            }
+            s_sp[j][rq][0] = x; s_sp[j][rq][1] = y; s_sp[j][rq][2] = z;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int j = 0; j < kSfTile; ++j) {
+            const float2 ph = s_ph[j][qi];
+            const float x = s_sp[j][rr][0], y = s_sp[j][rr][1], z = s_sp[j][rr][2];
+            fxr = fmaf(x, ph.x, fxr); fxi = fmaf(x, ph.y, fxi);
+            fyr = fmaf(y, ph.x, fyr); fyi = fmaf(y, ph.y, fyi);
+            fzr = fmaf(z, ph.x, fzr); fzi = fmaf(z, ph.y, fzi);
+        }
+    }
+    if (q < a.nq && r < a.R) {
+        float *o = a.fq + ((size_t)r * a.nq + q) * 6;
+        o[0] = fxr; o[1] = fxi; o[2] = fyr; o[3] = fyi; o[4] = fzr; o[5] = fzi;
+    }
+}
+
+// Per (q, slot): F_perp = F - q (q.F) / q.q, NSF = Re(p.F_perp) / |p|
+// (get_quant.F90:693-710), accumulated in FP64.
+__global__ void k_sf_finish(const SfArgs a)
+{
+    if (sf_step(a) % a.every != 0) return;
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) *a.count += 1;
+    if (k >= (long long)a.nq * a.R) return;
+    const int q = (int)(k % a.nq), t = (int)(k / a.nq);
+    const float4 qc = __ldg(a.q_cart + q);
+    if (qc.w != 0.f) return;
+    const float *f = a.fq + ((size_t)a.repl_at[t] * a.nq + q) * 6;
+    const double qx = qc.x, qy = qc.y, qz = qc.z;
+    const double qq = qx * qx + qy * qy + qz * qz;
+    const double dre = (f[0] * qx + f[2] * qy + f[4] * qz) / qq;
+    const double dim = (f[1] * qx + f[3] * qy + f[5] * qz) / qq;
+    const double xr = f[0] - dre * qx, xi = f[1] - dim * qx;
+    const double yr = f[2] - dre * qy, yi = f[3] - dim * qy;
+    const double zr = f[4] - dre * qz, zi = f[5] - dim * qz;
+    const double f2 = xr * xr + xi * xi + yr * yr + yi * yi + zr * zr + zi * zi;
+    const double nsf = (a.px * xr + a.py * yr + a.pz * zr) / a.pnorm;
+    double *o = a.acc + ((size_t)t * a.nq + q) * 3;
+    o[0] += f2;
+    o[1] += f2 - nsf * nsf;
+    o[2] += nsf * nsf;
+}
+
+// ---------------------------------------------------------------------------
 // Local terms g_i (3) and Q_i (6) of every (site, replica), FP32.
 // ---------------------------------------------------------------------------
 template <bool HB, bool HD>
@@ -746,6 +842,17 @@ cudaError_t launch_spincorr(const ScArgs &a, int blocks, cudaStream_t st)
     k_sc_reduce<<<dim3(a.R, (a.B + 1) / 2), 256, 0, st>>>(a.scratch, blocks, a.R, a.out);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_sc_finish<<<(a.R + 127) / 128, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sfactor(const SfArgs &a, cudaStream_t st)
+{
+    if (a.nq <= 0) return cudaSuccess;
+    k_sf_part<<<dim3((a.nq + kSfQ - 1) / kSfQ, (a.R + kSfR - 1) / kSfR), kSfQ * kSfR, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const long long n = (long long)a.nq * a.R;
+    k_sf_finish<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -73,6 +73,28 @@ struct ScArgs {
     int32_t N, R, B;
 };
 
+// mcarlo_structure_factor (get_quant.F90:649-717): F(q) = sum_i s_i e^{i q.r_i}
+// per replica, q.r_i / 2 pi = nq . n_i + qf . f_i with n_i the site's integer
+// lattice coordinates (phase in 32-bit fixed point, exact modulo one turn)
+// and f_i its fractional remainder.
+struct SfArgs {
+    const float *sx, *sy, *sz;
+    const int32_t *inv;       // reference site -> permuted index
+    const int4 *site_n;       // [N]: integer lattice coordinates of the site
+    const float4 *site_f;     // [N]: fractional remainder
+    const uint4 *q_fix;       // [nq]: frac(qf_j) * 2^32, j = 1..3
+    const float4 *q_frac;     // [nq]: qf_j (q in reciprocal-lattice units)
+    const float4 *q_cart;     // [nq]: q (x, y, z), w = 1 if q is exactly zero
+    float *fq;                // [R replicas][nq][6]: Re/Im of F_x, F_y, F_z
+    double *acc;              // [R slots][nq][3]: += |F_perp|^2, |F_perp|^2 - NSF^2, NSF^2
+    unsigned long long *count;   // number of structure-factor measurements
+    const int32_t *repl_at;
+    double px, py, pz, pnorm;    // sfactor_polar and its length
+    int32_t N, R, nq, every;     // measure when step % every == 0
+    long long step;              // 1-based measurement index (relative under capture)
+    const unsigned long long *ctr;   // device measurement counter added to step, or null
+};
+
 struct PmArgs {
     const float *sx, *sy, *sz;
     const int32_t *inv;       // reference site -> permuted index
@@ -112,6 +134,8 @@ cudaError_t launch_obs(const ObsArgs &a, double *out_op, double *out_sm, int blo
 cudaError_t launch_pm(const PmArgs &a, int max_blocks, cudaStream_t st);
 // one spincorr_get measurement of every replica, accumulated per slot
 cudaError_t launch_spincorr(const ScArgs &a, int blocks, cudaStream_t st);
+// one structure-factor measurement of every replica if step % every == 0
+cudaError_t launch_sfactor(const SfArgs &a, cudaStream_t st);
 cudaError_t launch_pt_swap(const PtSwapArgs &a, cudaStream_t st);
 // ctr[i] += d[i] for the four run counters
 cudaError_t launch_bump(unsigned long long *ctr, const unsigned long long d[4], cudaStream_t st);

@@ -32,6 +32,7 @@ EXPORTED = [
     "esp_set_tile_geometry", "esp_get_tile_geometry", "esp_batch_create", "esp_batch_destroy", "esp_batch_last_error",
     "esp_batch_set_units_per_graph", "esp_batch_advance", "esp_batch_tune",
     "esp_set_observables", "esp_collect_observables", "esp_set_spin_correlation", "esp_collect_spin_correlation",
+    "esp_set_structure_factor", "esp_collect_structure_factor",
 ]
 
 OBS_ORDER_PARAMETER, OBS_STAGGERED = 1, 2
@@ -267,6 +268,7 @@ class Engine:
         self._check(self.lib.esp_upload_tables(self.h, C.byref(t)))
         self._obs = 0   # new tables clear the optional measurements
         self._sc = None
+        self._sf = 0
 
     def set_temperatures(self, tems) -> None:
         t = np.ascontiguousarray(tems, dtype=np.float64)
@@ -381,7 +383,29 @@ class Engine:
         self._check(self.lib.esp_set_spin_correlation(self.h, S, nsp, maxk, _p(kind), _p(nn), _p(nb), _p(cnt)))
         self._sc = (S, nsp)
 
+    def set_structure_factor(self, qpts, polar, steps_measure: int, real_lattice, positions) -> None:
+        """Measure mcarlo_structure_factor every steps_measure measurements at the
+        cartesian q-points qpts (nq, 3); real_lattice rows are a_j, positions
+        (N, 3) the cartesian site positions (espins_gb300.tables).  qpts None
+        switches it off."""
+        if qpts is None:
+            self._check(self.lib.esp_set_structure_factor(self.h, 0, None, None, 1, None, None))
+            self._sf = 0
+            return
+        q = np.ascontiguousarray(qpts, dtype=np.float64).reshape(-1, 3)
+        p = np.ascontiguousarray(polar, dtype=np.float64).reshape(3)
+        rl = np.asfortranarray(np.asarray(real_lattice, dtype=np.float64))        # real_lattice(j, :) = a_j
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)    # atoms_supercell_pos_cart(3, N)
+        self._check(self.lib.esp_set_structure_factor(self.h, q.shape[0], _p(q), _p(p), int(steps_measure),
+                                                      _p(rl), _p(pos)))
+        self._sf = q.shape[0]
+
     def _collect_obs(self, out: dict, nlev: int) -> None:
+        if getattr(self, "_sf", 0):
+            sf = np.zeros((self.R, self._sf, 3))
+            n = C.c_int64()
+            self._check(self.lib.esp_collect_structure_factor(self.h, _p(sf), C.byref(n)))
+            out["sfactor"], out["sfactor_count"] = sf, n.value
         if getattr(self, "_sc", None):
             S, nsp = self._sc
             sc = [np.zeros((self.R, S, nsp, nsp)) for _ in range(3)]

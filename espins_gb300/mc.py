@@ -19,8 +19,9 @@ every measurement and written to _op.dat / _staggered.dat / _spincorr.dat and
 the extra _pm.dat / _binerror.dat columns.  With energy_write the running
 energy of every measurement is recorded on the device and written to the
 _energy-T###.dat files in chunks of the measurements that fit the device
-series buffer.  The structure factor is rejected with an error naming the
-keyword.
+series buffer.  With sfactor the structure factor is measured every
+sfactor_steps_measure measurements and written to _sf-T###.dat (the plotting
+scripts _sf.py / _sf.gnu that the reference writes beside them are not).
 """
 from __future__ import annotations
 
@@ -33,9 +34,9 @@ import numpy as np
 from . import writers as W
 from .lib import Engine
 from .mcin import McInput, McinError
-from .tables import Hamiltonian, build_hamiltonian, build_shells
+from .tables import Hamiltonian, build_hamiltonian, build_shells, sfactor_qpoints, site_positions
 
-UNSUPPORTED = [("lsfactor", "sfactor")]
+UNSUPPORTED = []
 
 # bytes of device memory the energy series may hold at once
 SERIES_BYTES = 1 << 28
@@ -75,6 +76,9 @@ def run(inp: McInput, seed: Optional[int] = None, outdir: Optional[str] = None,
                               staggered_coeff=inp.staggered_coeff if inp.lstaggered else None)
         if inp.lspincorr:
             e.set_spin_correlation(build_shells(inp))
+        if inp.lsfactor:
+            e.set_structure_factor(sfactor_qpoints(inp), inp.sfactor_polar, inp.sfactor_steps_measure,
+                                   inp.real_lattice, site_positions(inp))
         e.set_temperatures(tems)
         if inp.initial_sconfig.startswith("file"):
             path = os.path.join(outdir or ".", inp.seedname + "_sconfig.dat")
@@ -137,6 +141,10 @@ def write_outputs(inp: McInput, r: RunResult, outdir: str) -> None:
         W.write_obs_dat(base + "_op.dat", "op", r.tems, res["obs_data"], n)
     if sm:
         W.write_obs_dat(base + "_staggered.dat", "staggered", r.tems, res["obs_data"], n)
+    if inp.lsfactor:
+        W.write_sfactor(base, r.tems, res["sfactor"],
+                        W.sfactor_plane_coords(inp.sfactor_corner, inp.sfactor_q1, inp.sfactor_q2,
+                                               inp.sfactor_2dqmesh), inp.lsfactor_polar)
     if inp.lspincorr:
         W.write_spincorr(base + "_spincorr.dat", r.tems, res["spincorr"], res["spincorr_abs"], res["spincorr_tot"],
                          inp.atoms_symbol)

@@ -124,6 +124,13 @@ class McInput:
     energy_write: bool = False
     energy_num_print: int = 1000
     lsfactor: bool = False
+    lsfactor_polar: bool = False
+    sfactor_polar: Optional[np.ndarray] = None      # cartesian (1/length)
+    sfactor_corner: Optional[np.ndarray] = None
+    sfactor_q1: Optional[np.ndarray] = None
+    sfactor_q2: Optional[np.ndarray] = None
+    sfactor_steps_measure: int = 100
+    sfactor_2dqmesh: Optional[list] = None
     spin_glass: bool = False
     # Hamiltonian
     have_biquad: bool = False
@@ -607,11 +614,25 @@ def parse_mcin(text: str, seedname: str = "", num_nodes: int = 1) -> McInput:
     inp.energy_num_print = L.integer("energy_num_print", 1000)
     if inp.energy_num_print < 1:
         raise McinError("energy_num_print must be greater than zero")
+    # structure factor (parameters.F90:543-592): fractional vectors converted
+    # to cartesian with the reciprocal lattice (rows b_j, 2 pi included)
     inp.lsfactor = L.logical("sfactor", False)
-    for k in ("sfactor_polar", "sfactor_corner", "sfactor_q1", "sfactor_q2"):
-        L.vector(k, 3, _fnum)
-    L.integer("sfactor_steps_measure", 100)
-    L.vector("sfactor_2dqmesh", 2, _fint)
+    defaults = {"sfactor_polar": [1.0, 0.0, 0.0], "sfactor_corner": [0.0, 0.0, 0.0],
+                "sfactor_q1": [1.0, 0.0, 0.0], "sfactor_q2": [0.0, 0.0, 1.0]}
+    for k, d in defaults.items():
+        v = L.vector(k, 3, _fnum)
+        if k == "sfactor_polar":
+            inp.lsfactor_polar = v is not None
+        setattr(inp, k, np.asarray(v if v is not None else d, dtype=float) @ inp.recip_lattice)
+    if np.linalg.norm(np.cross(inp.sfactor_q1, inp.sfactor_q2)) < 1e-8:
+        raise McinError("Error: Vectors sfactor_q1 and sfactor_q2 not linearly independent")
+    inp.sfactor_steps_measure = L.integer("sfactor_steps_measure", 100)
+    if inp.lsfactor and (inp.sfactor_steps_measure < 1 or inp.sfactor_steps_measure > inp.steps_mc):
+        raise McinError("Error: sfactor_steps_measure must be greater than zero and less than steps_mc.")
+    mesh = L.vector("sfactor_2dqmesh", 2, _fint)
+    inp.sfactor_2dqmesh = [int(x) for x in mesh] if mesh is not None else [50, 50]
+    if inp.lsfactor and any(x < 1 for x in inp.sfactor_2dqmesh):
+        raise McinError("Error: sfactor_2dqmesh must be greater than zero")
 
     inp.pt = L.logical("pt", False)
     if inp.pt and inp.tems_num <= 1:

@@ -212,6 +212,30 @@ def build_shells(inp: McInput) -> ShellTables:
     return ShellTables(kind=kind, nn=nn, nb=nb, count=count, num_species=nsp)
 
 
+def site_positions(inp: McInput) -> np.ndarray:
+    """Cartesian position of every site (mcarlo_get_atoms_pos,
+    get_quant.F90:600-646): atom fractional position plus its cell's integer
+    offset, cells x-fastest, atoms species-major."""
+    L = np.asarray(inp.supercell_size, dtype=np.int64)
+    ncell = int(L.prod())
+    cells = np.arange(ncell)
+    lmn = np.stack([cells % L[0], (cells // L[0]) % L[1], cells // (L[0] * L[1])], axis=1).astype(float)
+    frac = (lmn[:, None, :] + np.asarray(inp.atoms_frac, dtype=float)[None, :, :]).reshape(-1, 3)
+    return frac @ inp.real_lattice
+
+
+def sfactor_qpoints(inp: McInput) -> np.ndarray:
+    """The q-points of mcarlo_structure_factor (get_quant.F90:670-685), in
+    loop_xy order: corner + (i/m1) q1 + (j/m2) q2 for i = 0..m1 (slow),
+    j = 0..m2 (fast); cartesian, 1/length."""
+    m1, m2 = inp.sfactor_2dqmesh
+    out = np.empty(((m1 + 1) * (m2 + 1), 3))
+    for xy in range(out.shape[0]):
+        lx, ly = xy // (m2 + 1), xy % (m2 + 1)
+        out[xy] = inp.sfactor_corner + (lx / float(m1)) * inp.sfactor_q1 + (ly / float(m2)) * inp.sfactor_q2
+    return out
+
+
 def check_symmetric(t: EllTable, antisym: bool, what: str) -> None:
     """The periodic-boundary symmetry checks of jij.F90:323-371 / dij.F90:285."""
     n = t.nn.shape[0]

@@ -19,6 +19,9 @@ src/pt.F90:1040-1085:
                         '(3x,a,f9.4)' '# T = ', '(3x,i16)' the number of
                         measurements, then '(I14,4x,1E16.8)' measurement index
                         and running E/N (get_quant.F90:1130-1191)
+* ``seed_sf-T###.dat``  structure factor per temperature: rows (3x,E15.8) x 3
+                        (qpt_x, qpt_y, S) or x 5 with sfactor_polar (S, S - NSF,
+                        NSF) in the plane coordinates of get_quant.F90:720-822
 With the order parameter or the staggered magnetisation switched on, _pm.dat
 gains the P(OP) / P(SM) columns and _binerror.dat their error columns
 (mcarlo.F90:174-215 and :784-818, pt.F90:159-200 and :1050-1073).
@@ -351,6 +354,40 @@ class EnergySeries:
         for fh in self.fh:
             fh.close()
         self.fh = []
+
+
+def sfactor_plane_coords(corner, q1v, q2v, mesh):
+    """(qpt_x, qpt_y) of every q-point in loop_xy order, in the orthogonal
+    frame of the (q1, q2) plane (mcarlo_structure_factor_write_mc,
+    get_quant.F90:745-813)."""
+    from .mcin import _recip_lattice
+    q1v, q2v, corner = (np.asarray(v, dtype=float) for v in (q1v, q2v, corner))
+    z = np.cross(q1v, q2v)
+    y = np.cross(z, q1v)
+    q1mod, q2mod, ymod = (math.sqrt(float(v @ v)) for v in (q1v, q2v, y))
+    qvec = np.array([q1v, q2v, z / math.sqrt(float(z @ z))])
+    avec, _ = _recip_lattice(qvec)
+    cosyq2 = float(y @ q2v) / (ymod * q2mod)
+    cosq1q2 = float(q1v @ q2v) / (q1mod * q2mod)
+    m1, m2 = mesh
+    out = []
+    for xy in range((m1 + 1) * (m2 + 1)):
+        lx, ly = xy // (m2 + 1), xy % (m2 + 1)
+        a = lx / float(m1) + float(corner @ avec[0]) / (2.0 * math.pi)
+        b = ly / float(m2) + float(corner @ avec[1]) / (2.0 * math.pi)
+        out.append((a * q1mod + b * q2mod * cosq1q2, b * q2mod * cosyq2))
+    return out
+
+
+def write_sfactor(base: str, tems, sf: np.ndarray, coords, polar: bool) -> None:
+    """One seed_sf-T###.dat per temperature; sf (R, nq, 3) normalised."""
+    folder, seed = os.path.split(base)
+    for k, _ in enumerate(tems, start=1):
+        name = os.path.join(folder, f"{seed}_sf-T{k // 100 % 10}{k // 10 % 10}{k % 10}.dat")
+        with open(name, "w") as fh:
+            for (x, y), v in zip(coords, sf[k - 1]):
+                vals = [x, y] + (list(v) if polar else [v[0]])
+                fh.write("".join("   " + fortran_e(u) for u in vals) + "\n")
 
 
 def write_binerror(path: str, tems, binning: np.ndarray, levels, n: int, pt: bool, obs_binning=None,

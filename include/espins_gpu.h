@@ -227,6 +227,24 @@ int esp_set_spin_correlation(esp_handle *h, int32_t num_shells, int32_t num_spec
  * of measurements x N).  NULL outputs are skipped. */
 int esp_collect_spin_correlation(esp_handle *h, double *spincorr, double *spincorr_abs, double *spincorr_tot_abs);
 
+/* Structure factor of mcarlo_structure_factor (get_quant.F90:649-717),
+ * measured after every measurement whose 1-based index is a multiple of
+ * steps_measure (sfactor_steps_measure): per q-point the transverse
+ * F(q) = sum_i (s_i - (s_i.q) q / q.q) e^{i q.r_i}, NSF = Re(p.F(q)) / |p|,
+ * accumulating |F|^2, |F|^2 - NSF^2 and NSF^2.  qpts: [nq][3] cartesian
+ * q-points (1/length, 2 pi included, the loop_xy order of the reference);
+ * polar: sfactor_polar (cartesian); real_lattice(3,3) and
+ * atoms_supercell_pos_cart(3,N) as the reference holds them (Fortran order,
+ * a_j = real_lattice(j,:)).  The phase q.r is evaluated as whole lattice
+ * translations in 32-bit fixed point plus an FP32 remainder, the sums in FP32.
+ * Call after esp_upload_tables (new tables clear it) and before esp_begin;
+ * nq 0 switches it off. */
+int esp_set_structure_factor(esp_handle *h, int32_t nq, const double *qpts, const double *polar,
+                             int32_t steps_measure, const double *real_lattice, const double *pos);
+/* sf: [R][nq][3] divided by N and by the number of structure-factor
+ * measurements (mcarlo.F90:821-822), which goes to *num_measured. */
+int esp_collect_structure_factor(esp_handle *h, double *sf, int64_t *num_measured);
+
 /* Local terms of every site: energy of site i as a function of its spin s is
  * g_i.s + s^T Q_i s;  g: (3,N,R), q: (6,N,R) as xx,yy,zz,xy,xz,yz.
  * The exchange local field of delta_energy_get is -g without the Zeeman part. */

@@ -20,6 +20,7 @@
  *   orderparam_get          src/get_quant.F90:396-422
  *   staggered_get           src/get_quant.F90:366-392
  *   spincorr_get            src/get_quant.F90:495-540 (shells: jij.F90:449-503)
+ *   mcarlo_structure_factor src/get_quant.F90:649-717
  *   mcarlo (one T chain)    src/mcarlo.F90:463-659 (+ grid :432-456)
  *   pt_mcarlo / pt_swap     src/pt.F90:504-942, :1235-1288
  *
@@ -472,6 +473,42 @@ void or_spincorr(const or_ham *h, const or_shells *sh, const double *s, double *
         }
     }
     free(tmp);
+}
+
+/* mcarlo_structure_factor (get_quant.F90:649-717) for one configuration:
+ * for every q-point (cartesian, nq of them) the transverse sum
+ * F(q) = sum_i (s_i - (s_i.q) q / q.q) exp(i q.r_i) and NSF, the REAL part of
+ * sum_i p.(s_i - (s_i.q) q / q.q) exp(i q.r_i) / |p| (the reference stores it
+ * in a real variable); adds |F|^2, |F|^2 - NSF^2 and NSF^2 to sf[3*iq + 0..2].
+ * A q-point with all three components zero adds nothing. */
+void or_structure_factor(const or_ham *h, const double *pos, int nq, const double *qpts, const double *polar,
+                         const double *s, double *sf)
+{
+    const double pnorm = sqrt(dot3(polar, polar));
+    for (int iq = 0; iq < nq; ++iq) {
+        const double *q = qpts + 3 * iq;
+        if (q[0] == 0.0 && q[1] == 0.0 && q[2] == 0.0) continue;
+        const double qq = dot3(q, q);
+        double fre[3] = {0, 0, 0}, fim[3] = {0, 0, 0};
+        double nsf = 0.0;
+        for (int i = 0; i < h->n; ++i) {
+            const double qr = dot3(pos + 3 * i, q);
+            const double c = cos(qr), sn = sin(qr);
+            const double mq = dot3(s + 3 * i, q) / qq;
+            double v[3];
+            for (int x = 0; x < 3; ++x) {
+                v[x] = s[3 * i + x] - mq * q[x];
+                fre[x] = fre[x] + v[x] * c;
+                fim[x] = fim[x] + v[x] * sn;
+            }
+            nsf = nsf + dot3(polar, v) * c / pnorm;
+        }
+        const double f2 = fre[0] * fre[0] + fim[0] * fim[0] + fre[1] * fre[1] + fim[1] * fim[1]
+                        + fre[2] * fre[2] + fim[2] * fim[2];
+        sf[3 * iq] = sf[3 * iq] + f2;
+        sf[3 * iq + 1] = sf[3 * iq + 1] + f2 - nsf * nsf;
+        sf[3 * iq + 2] = sf[3 * iq + 2] + nsf * nsf;
+    }
 }
 
 /* The optional measurements of one temperature slot after a measurement

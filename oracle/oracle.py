@@ -125,6 +125,8 @@ def _declare(L):
     L.or_staggered2.restype = C.c_double
     L.or_pm_obs.argtypes = [P(OrHam), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.or_spincorr.argtypes = [P(OrHam), P(OrShells), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.or_structure_factor.argtypes = [P(OrHam), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p]
     L.or_lp_num_params.restype = C.c_int
     L.or_lp_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     L.or_lp_loss_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
@@ -296,6 +298,17 @@ class Ham:
             ob.sc, ob.sc_abs, ob.sc_tot = (_ptr(out[k]) for k in ("spincorr", "spincorr_abs", "spincorr_tot"))
         self._keep.append(ob)
         return ob, out
+
+    def structure_factor(self, pos, qpts, polar, spins, sf=None):
+        """mcarlo_structure_factor of one configuration, added to sf (nq, 3)."""
+        q = np.ascontiguousarray(qpts, dtype=np.float64)
+        if sf is None:
+            sf = np.zeros((q.shape[0], 3))
+        r = np.ascontiguousarray(pos, dtype=np.float64)
+        p = np.ascontiguousarray(polar, dtype=np.float64)
+        s = np.ascontiguousarray(spins, dtype=np.float64)
+        lib().or_structure_factor(self.ref, _ptr(r), q.shape[0], _ptr(q), _ptr(p), _ptr(s), _ptr(sf))
+        return sf
 
     def pm(self, spins, pdf=None):
         nf = self.num_freq()

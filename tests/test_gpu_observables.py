@@ -12,6 +12,8 @@ mcarlo.F90:545-590 / pt.F90:798-849):
   typewriter chains (the reference's algorithm) within 3 sigma;
 * the spin correlations equal the oracle's spincorr_get of the same spins,
   measurement by measurement, for every sweep kernel;
+* the structure factor equals the oracle's mcarlo_structure_factor of the
+  same spins on every measurement that is a multiple of its cadence;
 * the host driver writes _op.dat, _staggered.dat, _spincorr.dat, the extra
   columns and the energy series files (whose rows do not depend on how the
   run is chunked, and whose last row is the final running energy).
@@ -24,7 +26,7 @@ import pytest
 import oracle as O
 from espins_gb300 import mc
 from espins_gb300.lib import Engine
-from espins_gb300.tables import build_hamiltonian, build_shells
+from espins_gb300.tables import build_hamiltonian, build_shells, sfactor_qpoints, site_positions
 from helpers import example
 from test_observables_cpu import _bcc_afm, _bcc_shells
 
@@ -290,3 +292,49 @@ def test_energy_series_files(tmp_path, monkeypatch, pt):
             # the last row is the final running energy per site
             assert float(rows[-1].split()[1]) == pytest.approx(r.res["energy"][t, 1] / r.ham.n, rel=1e-7)
     assert texts[0] == texts[1]
+
+
+@pytest.mark.parametrize("kernel", ["ell", "cluster", "tile"])
+def test_structure_factor_equals_the_oracle_on_the_gpu_spins(kernel):
+    tems = (2.0, 6.0, 15.0, 40.0, 3.0)
+    inp = _bcc_afm(L=4, tems=tems,
+                   extra="sfactor = .true.\nsfactor_2dqmesh = 6 5\nsfactor_steps_measure = 3\n"
+                         "sfactor_corner = -0.5 0 0.25\nsfactor_q1 = 2 2 0\nsfactor_q2 = 0 0 1.5\n"
+                         "sfactor_polar = 0 1 1")
+    h = build_hamiltonian(inp)
+    H = O.Ham(h)
+    q = sfactor_qpoints(inp)
+    pos = site_positions(inp)
+    R, K, every = len(tems), 13, 3
+    want = np.zeros((R, q.shape[0], 3))
+    with Engine(h.n, h.num_atoms, h.supercell, R) as e:
+        e.upload(h)
+        e.set_structure_factor(q, inp.sfactor_polar, every, inp.real_lattice, pos)
+        e.set_temperatures(tems)
+        e.set_sweep_kernel(kernel)
+        assert e.sweep_kernel()[0] == kernel
+        e.init_spins("rand", seed=8)
+        e.begin(e.schedule(10, K, 1, seed=6))
+        for k in range(1, K + 1):
+            e.advance(1)
+            if k % every == 0:
+                S = e.get_spins()
+                for t in range(R):
+                    H.structure_factor(pos, q, inp.sfactor_polar, S[t].reshape(-1), want[t])
+        r = e.collect()
+    assert r["sfactor_count"] == K // every
+    want /= h.n * (K // every)
+    scale = want[..., 0].max()
+    assert np.allclose(r["sfactor"], want, rtol=1e-4, atol=2e-5 * scale)
+
+
+def test_host_driver_writes_structure_factor_files(tmp_path):
+    inp = _bcc_afm(L=4, tems=(2.0, 30.0), extra="sfactor = .true.\nsfactor_2dqmesh = 4 4\nsfactor_steps_measure = 5")
+    inp.steps_warmup, inp.steps_mc = 200, 100
+    r = mc.run(inp, seed=2, outdir=str(tmp_path))
+    rows = [l.split() for l in open(os.path.join(str(tmp_path), "bcc_sf-T001.dat"))]
+    assert len(rows) == 25 and all(len(x) == 3 for x in rows)
+    assert r.res["sfactor_count"] == 20
+    # the antiferromagnetic Bragg peak at q = 2 pi (1, 0, 0) lies in the
+    # default (h0l) plane: ordered at 2 K, not at 30 K
+    assert r.res["sfactor"][0, :, 0].max() > r.res["sfactor"][1, :, 0].max()

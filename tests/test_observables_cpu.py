@@ -209,3 +209,52 @@ def test_energy_series_files_format(tmp_path):
     assert len(lines) == 8 and lines[7].startswith("             5")
     first = open(tmp_path / "x_energy-T001.dat").read().splitlines()
     assert first[3] == "             1     -0.10000000E+01"
+
+
+def test_oracle_structure_factor_identities():
+    """mcarlo_structure_factor on a ferromagnet along z: at a reciprocal lattice
+    vector G along x every site adds in phase, F = N z (transverse to G), so
+    S = N^2 and NSF = N (polarisation along z) or 0 (along x); q = 0 adds
+    nothing; and the restatement equals a direct numpy evaluation."""
+    from espins_gb300.tables import site_positions
+    inp = sc_mcin(4, [(1e-3, NN)], [5.0])
+    h = build_hamiltonian(inp)
+    H = O.Ham(h)
+    pos = site_positions(inp)
+    ferro = np.zeros((h.n, 3)); ferro[:, 2] = 1.0
+    G = 2 * np.pi * np.array([[1.0, 0, 0], [0, 0, 0], [0.37, 0.1, 0.0]])
+    sz = H.structure_factor(pos, G, [0.0, 0.0, 1.0], ferro.reshape(-1))
+    sx = H.structure_factor(pos, G, [1.0, 0.0, 0.0], ferro.reshape(-1))
+    N = h.n
+    assert np.allclose(sz[0], [N * N, 0.0, N * N]) and np.allclose(sx[0], [N * N, N * N, 0.0])
+    assert np.all(sz[1] == 0.0)
+    rng = np.random.default_rng(4)
+    s = rng.normal(size=(N, 3)); s /= np.linalg.norm(s, axis=1, keepdims=True)
+    p = np.array([0.3, -0.2, 0.9])
+    got = H.structure_factor(pos, G, p, s.reshape(-1))
+    for k, q in enumerate(G):
+        if not q.any():
+            continue
+        ph = np.exp(1j * pos @ q)
+        perp = s - np.outer(s @ q, q) / (q @ q)
+        F = (perp * ph[:, None]).sum(axis=0)
+        nsf = float(np.real(((perp @ p) * ph).sum())) / np.linalg.norm(p)
+        f2 = float(np.sum(np.abs(F) ** 2))
+        assert np.allclose(got[k], [f2, f2 - nsf ** 2, nsf ** 2], rtol=1e-10, atol=1e-9)
+
+
+def test_sfactor_input_and_plane_coordinates():
+    from espins_gb300.tables import sfactor_qpoints
+    inp = sc_mcin(4, [(1e-3, NN)], [5.0], extra="sfactor = .true.\nsfactor_2dqmesh = 4 2\nsfactor_steps_measure = 10\n"
+                                               "sfactor_q1 = 1 1 0\nsfactor_q2 = 0 0 2\nsfactor_polar = 0 0 1")
+    assert inp.lsfactor and inp.lsfactor_polar and inp.sfactor_steps_measure == 10
+    q = sfactor_qpoints(inp)
+    assert q.shape == (15, 3)
+    assert np.allclose(q[1], 2 * np.pi * np.array([0, 0, 1.0]))        # i = 0, j = 1 of 2
+    assert np.allclose(q[3], 2 * np.pi * np.array([0.25, 0.25, 0.0]))  # i = 1, j = 0
+    xy = W.sfactor_plane_coords(inp.sfactor_corner, inp.sfactor_q1, inp.sfactor_q2, inp.sfactor_2dqmesh)
+    # q1 and q2 orthogonal: x along q1 (|q1| = 2 pi sqrt 2), y along q2 (|q2| = 4 pi)
+    assert np.allclose(xy[3], (0.25 * 2 * np.pi * np.sqrt(2), 0.0))
+    assert np.allclose(xy[1], (0.0, 0.5 * 4 * np.pi))
+    with pytest.raises(McinError):
+        sc_mcin(4, [(1e-3, NN)], [5.0], extra="sfactor = .true.\nsfactor_q1 = 1 0 0\nsfactor_q2 = 2 0 0")
