@@ -15,6 +15,7 @@
 // stencil lists in the merged-list order), so both kernels produce the same
 // trajectory.  Waits are cluster barriers only (hardware, no spinning).
 #include <cooperative_groups.h>
+#include <type_traits>
 
 #include "esp_cluster.h"
 #include "esp_device.cuh"
@@ -109,26 +110,38 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                     // neighbour k of site l: (owner rank << 24) | local index, from the
                     // precomputed table shared by every replica's cluster; lists are
                     // padded to multiples of 8 with zero-coupling self entries
-                    const int ne8 = (st->count[k] + 7) & ~7;
+                    const int cnt_k = st->count[k];
                     const ClusterNbr *nb = nbt + k * st->maxst;
                     const uint32_t *tab = a.nbidx + (size_t)rank * st->maxst * n_local + l;
-                    for (int e0 = 0; e0 < ne8; e0 += 8) {
-                        uint32_t id[8];
+                    // a batch of NB neighbours: read from this CTA's shared
+                    // memory when every lane of the warp finds all of them
+                    // here (warps cover slab planes, so this is the common
+                    // case), else through the cluster window
+                    auto batch = [&](auto nbc, int e0) {
+                        constexpr int NB = decltype(nbc)::value;
+                        uint32_t id[NB];
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) id[j] = __ldg(tab + (size_t)(e0 + j) * n_local);
-                        float tx[8], ty[8], tz[8];
+                        for (int j = 0; j < NB; ++j) id[j] = __ldg(tab + (size_t)(e0 + j) * n_local);
+                        float tx[NB], ty[NB], tz[NB];
+                        bool loc = true;
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            const int rn = (int)(id[j] >> 24), ln = (int)(id[j] & 0xffffffu);
-                            if (rn == rank) {
+                        for (int j = 0; j < NB; ++j) loc = loc && (int)(id[j] >> 24) == rank;
+                        if (__all_sync(__activemask(), loc)) {
+#pragma unroll
+                            for (int j = 0; j < NB; ++j) {
+                                const int ln = (int)(id[j] & 0xffffffu);
                                 tx[j] = sx[ln]; ty[j] = sy[ln]; tz[j] = sz[ln];
-                            } else {
+                            }
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < NB; ++j) {
+                                const int rn = (int)(id[j] >> 24), ln = (int)(id[j] & 0xffffffu);
                                 const float *px_ = cluster.map_shared_rank(sx, rn);
                                 tx[j] = px_[ln]; ty[j] = px_[ln + n_local]; tz[j] = px_[ln + 2 * n_local];
                             }
                         }
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
+                        for (int j = 0; j < NB; ++j) {
                             const ClusterNbr &se = nb[e0 + j];
                             const float J = se.J;
                             gx = fmaf(-J, tx[j], gx); gy = fmaf(-J, ty[j], gy); gz = fmaf(-J, tz[j], gz);
@@ -145,6 +158,19 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                                 gz += tx[j] * dy - ty[j] * dx;
                             }
                         }
+                    };
+                    int e0 = 0;
+                    for (; e0 + 8 <= cnt_k; e0 += 8) batch(std::integral_constant<int, 8>{}, e0);
+                    // the last partial batch at its exact size (no padding work)
+                    switch (cnt_k - e0) {
+                    case 1: batch(std::integral_constant<int, 1>{}, e0); break;
+                    case 2: batch(std::integral_constant<int, 2>{}, e0); break;
+                    case 3: batch(std::integral_constant<int, 3>{}, e0); break;
+                    case 4: batch(std::integral_constant<int, 4>{}, e0); break;
+                    case 5: batch(std::integral_constant<int, 5>{}, e0); break;
+                    case 6: batch(std::integral_constant<int, 6>{}, e0); break;
+                    case 7: batch(std::integral_constant<int, 7>{}, e0); break;
+                    default: break;
                     }
                     if (a.has_si) {
                         const float4 s = st->si[at];
