@@ -242,21 +242,25 @@ __global__ void __launch_bounds__(kLpThreads, 1) k_sweep_lp(const LpSweepArgs la
 }
 
 // ---------------------------------------------------------------------------
-// The same sweep with the network on tcgen05: CTAs of 128 threads, thread t
-// owns one trial and tensor-memory lane t; each pass evaluates the network on
-// the 128 current trials with three chains of MMAs (K = 16, 128, 128) into
-// tensor memory.  Partial sums go to slots of 128-thread blocks
-// (thread t of block b works on replica (b*128 + t) % R).
+// The same sweep with the network on tcgen05: CTAs of kTcGroups groups of 128
+// threads (one CTA per SM, the weights staged once); thread t of a group owns
+// one trial and tensor-memory lane t, and each group evaluates the network on
+// its 128 current trials with three chains of MMAs (K = 16, 128, 128) into its
+// own 128 tensor-memory columns, independently of the other groups, so one
+// group's gathers overlap another's MMAs.  Partial sums go to slots of
+// 128-thread virtual blocks (thread t of virtual block b = CTA * kTcGroups +
+// group works on replica (b*128 + t) % R).
 // ---------------------------------------------------------------------------
-template <bool HB, bool HD>
-__global__ void __launch_bounds__(kTcRows) k_sweep_lp_tc(const LpSweepArgs la, double *part,
-                                                         unsigned long long *part_rej, int slots, int *err)
+template <int NG, bool HB, bool HD>
+__global__ void __launch_bounds__(kTcRows * NG, 1) k_sweep_lp_tc(const LpSweepArgs la, double *part,
+                                                                 unsigned long long *part_rej, int slots, int *err)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    TcSmem &s = *reinterpret_cast<TcSmem *>(smem);
+    TcSmemG<NG> &s = *reinterpret_cast<TcSmemG<NG> *>(smem);
     const SweepArgs &a = la.s;
     tc_stage_weights(la.w, s);
     tc_setup(s);
+    const int g = threadIdx.x / kTcRows, lane = threadIdx.x % kTcRows;
 
     const int R = a.R;
     const long long nthreads = (long long)gridDim.x * blockDim.x;
@@ -271,7 +275,7 @@ __global__ void __launch_bounds__(kTcRows) k_sweep_lp_tc(const LpSweepArgs la, d
     sweep_index(a, sw_lo, sw_hi);
     uint32_t phase = 0;
     int pi = tid < S ? (int)(tid / R) : a.n_c;
-    while (__syncthreads_or(pi < a.n_c)) {
+    while (group_any<NG>(g, pi < a.n_c)) {
         const bool act = pi < a.n_c;
         const int p = a.off_c + (act ? pi : 0);
         const int orig = __ldg(a.perm + p);
@@ -288,21 +292,21 @@ __global__ void __launch_bounds__(kTcRows) k_sweep_lp_tc(const LpSweepArgs la, d
             for (int i = 0; i < kMlpIn; ++i) f[i] = 0.f;
             fr.kappa0 = 0.f;
         }
-        tc_store_x_row(s, threadIdx.x, f);
+        tc_store_x_row(s.t[g], lane, f);
         float o[kMlpOut];
-        tc_forward(s, phase, o);
+        tc_forward(s, g, phase, o);
         if (act && mag > 0.f)
             lp_trial(a, fr, o, p, r, orig, mag, beta, gx, gy, gz, q, sw_lo, sw_hi, accE, accX, accY, accZ, nrej);
         pi += pstep;
     }
     tc_teardown(s);
     if (threadIdx.x == 0 && s.error) atomicExch(err, 1);
-    // the activation tile becomes the reduction scratch
+    // the group's activation tile becomes its reduction scratch
     __syncthreads();
-    double *sp = reinterpret_cast<double *>(s.h);
+    double *sp = reinterpret_cast<double *>(s.t[g].h);
     unsigned int *sr = reinterpret_cast<unsigned int *>(sp + 4 * kTcRows);
-    const int t = threadIdx.x;
-    const size_t slot = (size_t)blockIdx.x * slots + t;
+    const int t = lane;
+    const size_t slot = ((size_t)blockIdx.x * NG + g) * slots + t;
     if (R >= kTcRows) {
         double *o = part + 4 * slot;
         o[0] += (double)accE; o[1] += (double)accX; o[2] += (double)accY; o[3] += (double)accZ;
@@ -311,7 +315,7 @@ __global__ void __launch_bounds__(kTcRows) k_sweep_lp_tc(const LpSweepArgs la, d
     }
     sp[4 * t] = (double)accE; sp[4 * t + 1] = (double)accX; sp[4 * t + 2] = (double)accY; sp[4 * t + 3] = (double)accZ;
     sr[t] = nrej;
-    __syncthreads();
+    group_sync<NG>(g);
     if (t < R) {
         double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
         unsigned long long nr = 0;
@@ -605,34 +609,46 @@ cudaError_t lp_configure(int device)
     return e;
 }
 
+// Virtual 128-thread blocks of the tcgen05 sweep: a multiple of kTcGroups, at
+// most one CTA (kTcGroups groups) per SM.
 int lp_tc_sweep_blocks(long long max_items, int R, int num_sms)
 {
     long long b = (max_items + kTcRows - 1) / kTcRows;
-    if (b > 2 * num_sms) b = 2 * num_sms;
+    if (b > (long long)kTcGroups * num_sms) b = (long long)kTcGroups * num_sms;
     const long long need = (R + kTcRows - 1) / kTcRows;
     if (b < need) b = need;
-    return (int)(b < 1 ? 1 : b);
+    if (b < 1) b = 1;
+    return (int)((b + kTcGroups - 1) / kTcGroups * kTcGroups);
 }
 
 cudaError_t lp_tc_sweep_configure()
 {
-    const int bytes = (int)sizeof(TcSmem);
-    static_assert(sizeof(TcSmem) >= kTcRows * (4 * sizeof(double) + sizeof(unsigned int)), "scratch");
-    cudaError_t e = cudaFuncSetAttribute(k_sweep_lp_tc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_lp_tc<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_lp_tc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_lp_tc<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    using Sm = TcSmemG<kTcGroups>;
+    const int bytes = (int)sizeof(Sm);
+    static_assert(sizeof(TcTile) >= kTcRows * (4 * sizeof(double) + sizeof(unsigned int)), "scratch");
+    static_assert(sizeof(Sm) <= 227 * 1024, "shared memory");
+    cudaError_t e = cudaFuncSetAttribute(k_sweep_lp_tc<kTcGroups, false, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_sweep_lp_tc<kTcGroups, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_sweep_lp_tc<kTcGroups, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_sweep_lp_tc<kTcGroups, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e;
 }
 
+// `blocks` counts virtual 128-thread blocks (a multiple of kTcGroups).
 cudaError_t launch_sweep_lp_tc(const LpSweepArgs &a, bool hb, bool hd, int blocks, double *part,
                                unsigned long long *part_rej, int slots, int *err, cudaStream_t st)
 {
-    const size_t sm = sizeof(TcSmem);
-    if (hb && hd) k_sweep_lp_tc<true, true><<<blocks, kTcRows, sm, st>>>(a, part, part_rej, slots, err);
-    else if (hb) k_sweep_lp_tc<true, false><<<blocks, kTcRows, sm, st>>>(a, part, part_rej, slots, err);
-    else if (hd) k_sweep_lp_tc<false, true><<<blocks, kTcRows, sm, st>>>(a, part, part_rej, slots, err);
-    else k_sweep_lp_tc<false, false><<<blocks, kTcRows, sm, st>>>(a, part, part_rej, slots, err);
+    if (blocks % kTcGroups) return cudaErrorInvalidValue;
+    const size_t sm = sizeof(TcSmemG<kTcGroups>);
+    const int grid = blocks / kTcGroups, nt = kTcRows * kTcGroups;
+    if (hb && hd) k_sweep_lp_tc<kTcGroups, true, true><<<grid, nt, sm, st>>>(a, part, part_rej, slots, err);
+    else if (hb) k_sweep_lp_tc<kTcGroups, true, false><<<grid, nt, sm, st>>>(a, part, part_rej, slots, err);
+    else if (hd) k_sweep_lp_tc<kTcGroups, false, true><<<grid, nt, sm, st>>>(a, part, part_rej, slots, err);
+    else k_sweep_lp_tc<kTcGroups, false, false><<<grid, nt, sm, st>>>(a, part, part_rej, slots, err);
     return cudaGetLastError();
 }
 

@@ -29,11 +29,11 @@ __global__ void __launch_bounds__(kTcRows) k_lp_forward_tc(const LpWeights w, co
             v0 = reinterpret_cast<const uint4 *>(x + (size_t)i * kMlpInPad)[0];
             v1 = reinterpret_cast<const uint4 *>(x + (size_t)i * kMlpInPad)[1];
         }
-        unsigned char *xb = reinterpret_cast<unsigned char *>(s.x);
+        unsigned char *xb = reinterpret_cast<unsigned char *>(s.t[0].x);
         *reinterpret_cast<uint4 *>(xb + kmajor_offset(t, 0, kMlpInPad)) = v0;
         *reinterpret_cast<uint4 *>(xb + kmajor_offset(t, 8, kMlpInPad)) = v1;
         float o[kMlpOut];
-        tc_forward(s, phase, o);
+        tc_forward(s, 0, phase, o);
         if (i < n)
             for (int k = 0; k < kMlpOut; ++k) out[(size_t)i * kMlpOut + k] = o[k];
     }

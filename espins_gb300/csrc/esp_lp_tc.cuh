@@ -1,8 +1,11 @@
 // The learned proposal's MLP (12 -> 128 -> 128 -> 20, ReLU) on the tcgen05
-// tensor cores for 128 rows at a time: one CTA of 128 threads, thread t owns
-// row t (its tensor-memory lane).  Operands in shared memory in the K-major
-// no-swizzle layout of esp_tc.cuh, accumulators in 128 tensor-memory columns,
-// one thread issues the MMAs and an mbarrier signals their completion.
+// tensor cores for tiles of 128 rows: a group of 128 threads (a warpgroup)
+// owns one tile, thread t of the group owns row t (its tensor-memory lane).
+// A CTA holds NG groups that share one copy of the weights and work on their
+// tiles independently (named barrier 1 + g per group); group g accumulates in
+// tensor-memory columns [128 g, 128 g + 128).  Operands in shared memory in
+// the K-major no-swizzle layout of esp_tc.cuh, one thread per group issues
+// the MMAs and an mbarrier per group signals their completion.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -12,23 +15,54 @@
 namespace esp {
 
 constexpr int kTcRows = 128;
-constexpr uint32_t kTcCols = 128;           // tensor-memory columns per CTA
+constexpr uint32_t kTcCols = 128;           // tensor-memory columns per group
+constexpr int kTcGroups = 4;                // groups (tiles in flight) per CTA of the sweep
 constexpr uint32_t kTcWaitLimit = 1u << 24; // mbarrier polls before giving up
 
-struct TcSmem {
+// One group's tile: features X, hidden activations H, completion barrier.
+struct alignas(128) TcTile {
+    __nv_bfloat16 x[kTcRows * kMlpInPad];      // [128][16]
+    __nv_bfloat16 h[kTcRows * kMlpHid];        // [128][128]
+    unsigned long long bar;
+};
+
+template <int NG>
+struct TcSmemG {
     __nv_bfloat16 w1[kMlpHid * kMlpInPad];     // [128][16] K-major
     __nv_bfloat16 w2[kMlpHid * kMlpHid];       // [128][128]
     __nv_bfloat16 w3[kMlpOutPad * kMlpHid];    // [32][128]
-    __nv_bfloat16 x[kTcRows * kMlpInPad];      // [128][16]
-    __nv_bfloat16 h[kTcRows * kMlpHid];        // [128][128]
     float b1[kMlpHid], b2[kMlpHid], b3[kMlpOutPad];
-    unsigned long long bar;
+    TcTile t[NG];
     uint32_t tmem;
     int error;
 };
+using TcSmem = TcSmemG<1>;
+
+// Barrier of group g's 128 threads (the whole CTA when there is one group).
+template <int NG>
+__device__ __forceinline__ void group_sync(int g)
+{
+    if (NG == 1) __syncthreads();
+    else asm volatile("bar.sync %0, 128;\n" ::"r"(g + 1) : "memory");
+}
+
+// OR of v over group g's 128 threads, with that group's barrier.
+template <int NG>
+__device__ __forceinline__ bool group_any(int g, bool v)
+{
+    if (NG == 1) return __syncthreads_or(v) != 0;
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, 128, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(g + 1)
+        : "memory");
+    return r != 0;
+}
 
 // Row-major global weights ([out][in]) to the K-major operand layout.
-__device__ __forceinline__ void tc_stage_weights(const LpWeights &w, TcSmem &s)
+template <int NG>
+__device__ __forceinline__ void tc_stage_weights(const LpWeights &w, TcSmemG<NG> &s)
 {
     auto stage = [&](const __nv_bfloat16 *src, __nv_bfloat16 *dst, int rows, int K) {
         const int chunks = rows * (K / 8);
@@ -45,32 +79,37 @@ __device__ __forceinline__ void tc_stage_weights(const LpWeights &w, TcSmem &s)
     for (int i = threadIdx.x; i < kMlpOutPad; i += blockDim.x) s.b3[i] = __ldg(w.b3 + i);
 }
 
-// Set-up by the whole CTA: mbarrier, 128 tensor-memory columns (warp 0).
-__device__ __forceinline__ void tc_setup(TcSmem &s)
+// Set-up by the whole CTA: one mbarrier per group, 128 tensor-memory columns
+// per group (warp 0).
+template <int NG>
+__device__ __forceinline__ void tc_setup(TcSmemG<NG> &s)
 {
     if (threadIdx.x == 0) {
-        mbar_init(smem_u32(&s.bar), 1);
+        for (int g = 0; g < NG; ++g) mbar_init(smem_u32(&s.t[g].bar), 1);
         s.error = 0;
     }
     if (threadIdx.x < 32) {
-        tmem_alloc(smem_u32(&s.tmem), kTcCols);
+        tmem_alloc(smem_u32(&s.tmem), kTcCols * NG);
         tmem_relinquish();
     }
+    // every thread's weight writes -> the tensor cores of every group
+    fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
 }
 
-__device__ __forceinline__ void tc_teardown(TcSmem &s)
+template <int NG>
+__device__ __forceinline__ void tc_teardown(TcSmemG<NG> &s)
 {
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (threadIdx.x < 32) tmem_dealloc(s.tmem, kTcCols);
+    if (threadIdx.x < 32) tmem_dealloc(s.tmem, kTcCols * NG);
 }
 
 // Thread t's 12 features as row t of the X operand (zero padding to 16).
-__device__ __forceinline__ void tc_store_x_row(TcSmem &s, int t, const float *f)
+__device__ __forceinline__ void tc_store_x_row(TcTile &s, int t, const float *f)
 {
     uint4 v0, v1;
     v0.x = pack_bf16(f[0], f[1]); v0.y = pack_bf16(f[2], f[3]); v0.z = pack_bf16(f[4], f[5]); v0.w = pack_bf16(f[6], f[7]);
@@ -80,36 +119,47 @@ __device__ __forceinline__ void tc_store_x_row(TcSmem &s, int t, const float *f)
     *reinterpret_cast<uint4 *>(b + kmajor_offset(t, 8, kMlpInPad)) = v1;
 }
 
-// Issue (thread 0) the MMAs of one layer, commit, and wait (every thread).
-// Returns false when the wait gave up.
-__device__ __forceinline__ bool tc_layer(TcSmem &s, const __nv_bfloat16 *a, int K, const __nv_bfloat16 *b, int N,
-                                         uint32_t &phase)
+// Issue (the group's thread 0) the MMAs of one layer of group g, commit, and
+// wait (every thread of the group).  Returns false when the wait gave up.
+template <int NG>
+__device__ __forceinline__ bool tc_layer(TcSmemG<NG> &s, int g, const __nv_bfloat16 *a, int K,
+                                         const __nv_bfloat16 *b, int N, uint32_t &phase)
 {
     fence_async_smem();     // this thread's operand writes -> tensor cores
     tc_fence_before();
-    __syncthreads();
+    group_sync<NG>(g);
     tc_fence_after();
-    if (threadIdx.x == 0) {
+    if ((threadIdx.x & (kTcRows - 1)) == 0) {
         const uint32_t idesc = idesc_bf16_f32(kTcRows, N);
         const uint32_t sbo = (uint32_t)(K / 8) * 128u;
         const uint32_t a0 = smem_u32(a), b0 = smem_u32(b);
+        const uint32_t d = s.tmem + kTcCols * (uint32_t)g;
         for (int kk = 0; kk < K / 16; ++kk)
-            tc_mma(s.tmem, smem_desc(a0 + 256u * kk, 128u, sbo), smem_desc(b0 + 256u * kk, 128u, sbo), idesc, kk > 0);
-        tc_commit(smem_u32(&s.bar));
+            tc_mma(d, smem_desc(a0 + 256u * kk, 128u, sbo), smem_desc(b0 + 256u * kk, 128u, sbo), idesc, kk > 0);
+        tc_commit(smem_u32(&s.t[g].bar));
     }
-    const bool ok = mbar_wait(smem_u32(&s.bar), phase, kTcWaitLimit);
+    const bool ok = mbar_wait(smem_u32(&s.t[g].bar), phase, kTcWaitLimit);
     phase ^= 1u;
     tc_fence_after();
     if (!ok) s.error = 1;
     return ok;
 }
 
-// Hidden-layer epilogue: relu(D + bias) of this thread's row to H.
-__device__ __forceinline__ void tc_hidden_epilogue(TcSmem &s, const float *bias)
+// This thread's tensor-memory lane in group g's columns.
+template <int NG>
+__device__ __forceinline__ uint32_t tc_lane_base(const TcSmemG<NG> &s, int g)
 {
-    const int t = threadIdx.x;
-    const uint32_t lane_base = s.tmem + ((uint32_t)(t & ~31) << 16);
-    unsigned char *hb = reinterpret_cast<unsigned char *>(s.h);
+    const int t = threadIdx.x & (kTcRows - 1);
+    return s.tmem + kTcCols * (uint32_t)g + ((uint32_t)(t & ~31) << 16);
+}
+
+// Hidden-layer epilogue: relu(D + bias) of this thread's row to group g's H.
+template <int NG>
+__device__ __forceinline__ void tc_hidden_epilogue(TcSmemG<NG> &s, int g, const float *bias)
+{
+    const int t = threadIdx.x & (kTcRows - 1);
+    const uint32_t lane_base = tc_lane_base(s, g);
+    unsigned char *hb = reinterpret_cast<unsigned char *>(s.t[g].h);
 #pragma unroll 1
     for (int c0 = 0; c0 < kMlpHid; c0 += 16) {
         float v[16];
@@ -127,16 +177,19 @@ __device__ __forceinline__ void tc_hidden_epilogue(TcSmem &s, const float *bias)
     }
 }
 
-// The whole network for the 128 rows of s.x; thread t gets row t's 20
-// outputs.  Returns false if a wait gave up (s.error is then set).
-__device__ __forceinline__ bool tc_forward(TcSmem &s, uint32_t &phase, float *o)
+// The whole network for the 128 rows of group g's X; thread t of the group
+// gets row t's 20 outputs.  Returns false if a wait gave up (s.error is then
+// set).
+template <int NG>
+__device__ __forceinline__ bool tc_forward(TcSmemG<NG> &s, int g, uint32_t &phase, float *o)
 {
-    bool ok = tc_layer(s, s.x, kMlpInPad, s.w1, kMlpHid, phase);
-    tc_hidden_epilogue(s, s.b1);
-    ok = tc_layer(s, s.h, kMlpHid, s.w2, kMlpHid, phase) && ok;
-    tc_hidden_epilogue(s, s.b2);
-    ok = tc_layer(s, s.h, kMlpHid, s.w3, kMlpOutPad, phase) && ok;
-    const uint32_t lane_base = s.tmem + ((uint32_t)(threadIdx.x & ~31) << 16);
+    TcTile &tl = s.t[g];
+    bool ok = tc_layer(s, g, tl.x, kMlpInPad, s.w1, kMlpHid, phase);
+    tc_hidden_epilogue(s, g, s.b1);
+    ok = tc_layer(s, g, tl.h, kMlpHid, s.w2, kMlpHid, phase) && ok;
+    tc_hidden_epilogue(s, g, s.b2);
+    ok = tc_layer(s, g, tl.h, kMlpHid, s.w3, kMlpOutPad, phase) && ok;
+    const uint32_t lane_base = tc_lane_base(s, g);
     float v[16];
     tmem_ld16(lane_base, v);
 #pragma unroll
