@@ -80,7 +80,6 @@ struct esp_handle {
     int4 *d_tile_offs = nullptr;
     ClusterNbr *d_tile_cpl = nullptr;
     int tile_maxst = 0, tile_nbd8[kMaxClusterAtoms] = {}, tile_nall8[kMaxClusterAtoms] = {};
-    int tile_nbd[kMaxClusterAtoms] = {}, tile_njo[kMaxClusterAtoms] = {};
     double *d_tile_part = nullptr;
     unsigned long long *d_tile_rej = nullptr;
     long long tile_pending = 0;
@@ -351,8 +350,6 @@ int tile_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o
     for (int at = 0; at < kMaxClusterAtoms; ++at) {
         a.nbd8[at] = h->tile_nbd8[at];
         a.nall8[at] = h->tile_nall8[at];
-        a.nbd[at] = h->tile_nbd[at];
-        a.njo[at] = h->tile_njo[at];
     }
     a.Lx = h->L[0]; a.Ly = h->L[1]; a.Lz = h->L[2]; a.na = h->na; a.N = h->N; a.R = h->R;
     a.T = h->tile_T; a.G = h->tile_G;
@@ -778,14 +775,11 @@ int tile_setup(esp_handle *h)
             const bool rich = x.B != 0.f || x.Dx != 0.f || x.Dy != 0.f || x.Dz != 0.f;
             (rich ? bd[at] : jo[at]).push_back(x);
         }
-        h->tile_nbd[at] = (int)bd[at].size();
-        h->tile_njo[at] = (int)jo[at].size();
         h->tile_nbd8[at] = ((int)bd[at].size() + 7) & ~7;
         h->tile_nall8[at] = h->tile_nbd8[at] + (((int)jo[at].size() + 7) & ~7);
         maxst = std::max(maxst, h->tile_nall8[at]);
     }
-    for (int at = h->na; at < kMaxClusterAtoms; ++at)
-        h->tile_nbd8[at] = h->tile_nall8[at] = h->tile_nbd[at] = h->tile_njo[at] = 0;
+    for (int at = h->na; at < kMaxClusterAtoms; ++at) h->tile_nbd8[at] = h->tile_nall8[at] = 0;
     std::vector<int4> offs((size_t)h->na * maxst);
     std::vector<ClusterNbr> cpl((size_t)h->na * maxst);
     for (int at = 0; at < h->na; ++at) {

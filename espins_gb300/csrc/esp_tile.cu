@@ -17,8 +17,6 @@
 // G replicas of a site are contiguous (element (p, r) at p*R + r).
 #include "esp_tile.h"
 
-#include <type_traits>
-
 namespace esp {
 
 namespace {
@@ -271,8 +269,7 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
     double *red = reinterpret_cast<double *>(buf + (size_t)6 * nbs8 * G);  // [NT/32][G][4]
     unsigned long long *red_n = reinterpret_cast<unsigned long long *>(red + (NT / 32) * G * 4);
 
-    __shared__ int s_nbd8[kMaxClusterAtoms], s_nall8[kMaxClusterAtoms], s_nbd[kMaxClusterAtoms],
-        s_njo[kMaxClusterAtoms];
+    __shared__ int s_nbd8[kMaxClusterAtoms], s_nall8[kMaxClusterAtoms];
     {
         const int *src = reinterpret_cast<const int *>(a.stencil);
         int *dst = reinterpret_cast<int *>(st);
@@ -287,8 +284,6 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
         if (threadIdx.x < kMaxClusterAtoms) {
             s_nbd8[threadIdx.x] = a.nbd8[threadIdx.x];
             s_nall8[threadIdx.x] = a.nall8[threadIdx.x];
-            s_nbd[threadIdx.x] = a.nbd[threadIdx.x];
-            s_njo[threadIdx.x] = a.njo[threadIdx.x];
         }
     }
 
@@ -394,61 +389,48 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
                 float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
                 const ClusterNbr *nb = nbt + at * maxst;
                 const int *to = toff + at * maxst;
-                const int nbd8 = s_nbd8[at], nbd = s_nbd[at], njo = s_njo[at];
-                // NB entries from e0: spins of the box, couplings of the atom;
-                // RICH: the entries with biquadratic / DM parts
-                auto batch = [&](auto nbc, auto richc, int e0) {
-                    constexpr int NB = decltype(nbc)::value;
-                    constexpr bool RICH = decltype(richc)::value;
-                    float tx_[NB], ty_[NB], tz_[NB];
+                const int nbd8 = s_nbd8[at], nall8 = s_nall8[at];
+                int e0 = 0;
+                for (; e0 < nbd8; e0 += 8) {
+                    float tx_[8], ty_[8], tz_[8];
 #pragma unroll
-                    for (int j = 0; j < NB; ++j) {
+                    for (int j = 0; j < 8; ++j) {
                         const int q = box_slot(bsite + to[e0 + j]) * G + g;
                         tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
                     }
 #pragma unroll
-                    for (int j = 0; j < NB; ++j) {
-                        if (RICH) {
-                            // couplings as two 16-byte loads: (J, B, Dx, Dy), (Dz, ...)
-                            const float4 c0 = *reinterpret_cast<const float4 *>(nb + e0 + j);
-                            const float J = c0.x;
-                            gx = fmaf(-J, tx_[j], gx); gy = fmaf(-J, ty_[j], gy); gz = fmaf(-J, tz_[j], gz);
-                            if (a.has_b) {
-                                const float Bv = c0.y;
-                                const float bx = Bv * tx_[j], by = Bv * ty_[j], bz = Bv * tz_[j];
-                                qxx = fmaf(bx, tx_[j], qxx); qyy = fmaf(by, ty_[j], qyy); qzz = fmaf(bz, tz_[j], qzz);
-                                qxy = fmaf(bx, ty_[j], qxy); qxz = fmaf(bx, tz_[j], qxz); qyz = fmaf(by, tz_[j], qyz);
-                            }
-                            if (a.has_d) {
-                                const float dx = c0.z, dy = c0.w, dz = nb[e0 + j].Dz;
-                                gx += ty_[j] * dz - tz_[j] * dy;
-                                gy += tz_[j] * dx - tx_[j] * dz;
-                                gz += tx_[j] * dy - ty_[j] * dx;
-                            }
-                        } else {
-                            const float J = nb[e0 + j].J;
-                            gx = fmaf(-J, tx_[j], gx); gy = fmaf(-J, ty_[j], gy); gz = fmaf(-J, tz_[j], gz);
+                    for (int j = 0; j < 8; ++j) {
+                        // couplings as two 16-byte loads: (J, B, Dx, Dy), (Dz, ...)
+                        const float4 c0 = *reinterpret_cast<const float4 *>(nb + e0 + j);
+                        const float J = c0.x;
+                        gx = fmaf(-J, tx_[j], gx); gy = fmaf(-J, ty_[j], gy); gz = fmaf(-J, tz_[j], gz);
+                        if (a.has_b) {
+                            const float Bv = c0.y;
+                            const float bx = Bv * tx_[j], by = Bv * ty_[j], bz = Bv * tz_[j];
+                            qxx = fmaf(bx, tx_[j], qxx); qyy = fmaf(by, ty_[j], qyy); qzz = fmaf(bz, tz_[j], qzz);
+                            qxy = fmaf(bx, ty_[j], qxy); qxz = fmaf(bx, tz_[j], qxz); qyz = fmaf(by, tz_[j], qyz);
+                        }
+                        if (a.has_d) {
+                            const float dx = c0.z, dy = c0.w, dz = nb[e0 + j].Dz;
+                            gx += ty_[j] * dz - tz_[j] * dy;
+                            gy += tz_[j] * dx - tx_[j] * dz;
+                            gz += tx_[j] * dy - ty_[j] * dx;
                         }
                     }
-                };
-                // entries [e0, e0 + n) in batches of 8 and one batch of the
-                // remainder at its exact size (the padding is not touched)
-                auto part = [&](auto richc, int e0, int n) {
-                    int e = 0;
-                    for (; e + 8 <= n; e += 8) batch(std::integral_constant<int, 8>{}, richc, e0 + e);
-                    switch (n - e) {
-                    case 1: batch(std::integral_constant<int, 1>{}, richc, e0 + e); break;
-                    case 2: batch(std::integral_constant<int, 2>{}, richc, e0 + e); break;
-                    case 3: batch(std::integral_constant<int, 3>{}, richc, e0 + e); break;
-                    case 4: batch(std::integral_constant<int, 4>{}, richc, e0 + e); break;
-                    case 5: batch(std::integral_constant<int, 5>{}, richc, e0 + e); break;
-                    case 6: batch(std::integral_constant<int, 6>{}, richc, e0 + e); break;
-                    case 7: batch(std::integral_constant<int, 7>{}, richc, e0 + e); break;
-                    default: break;
+                }
+                for (; e0 < nall8; e0 += 8) {   // exchange only
+                    float tx_[8], ty_[8], tz_[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int q = box_slot(bsite + to[e0 + j]) * G + g;
+                        tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
                     }
-                };
-                part(std::true_type{}, 0, nbd);
-                part(std::false_type{}, nbd8, njo);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const float J = nb[e0 + j].J;
+                        gx = fmaf(-J, tx_[j], gx); gy = fmaf(-J, ty_[j], gy); gz = fmaf(-J, tz_[j], gz);
+                    }
+                }
                 if (a.has_si) {
                     const float4 s = st->si[at];
                     const float dx = s.w * s.x, dy = s.w * s.y, dz = s.w * s.z;

@@ -18,8 +18,6 @@ struct TileArgs {
     const ClusterNbr *cpl;          // [na][maxst] couplings in the same order
     int maxst;
     int nbd8[kMaxClusterAtoms], nall8[kMaxClusterAtoms];
-    // entries actually listed per atom (the rest of each part is padding)
-    int nbd[kMaxClusterAtoms], njo[kMaxClusterAtoms];
     int Lx, Ly, Lz, na, N, R;
     int T, G;                       // tile edge (cells, even), replicas per CTA
     int ntx, nty, ntz;              // tiles per axis (even)
