@@ -110,6 +110,11 @@ struct esp_handle {
     float *d_sc_w = nullptr;
     double *d_sc_scratch = nullptr, *d_sc_out = nullptr, *d_sc_acc = nullptr;
     std::vector<double> mag_host;   // mag_moments_matrix, reference order
+    // staging of spin_matrix blocks for esp_set_spins / esp_get_spins, and a
+    // pinned host copy that esp_get_spins reads back through (a copy straight
+    // into the caller's pages would fault them in inside the transfer)
+    double *d_stage = nullptr, *h_stage = nullptr;
+    int stage_slots = 0;
     // structure factor (esp_set_structure_factor)
     int sf_nq = 0, sf_every = 1;
     double sf_p[3] = {1.0, 0.0, 0.0}, sf_pnorm = 1.0;
@@ -239,6 +244,10 @@ void free_all(esp_handle *h)
     free_obs(h);
     free_sc(h);
     free_sf(h);
+    dfree(h->d_stage);
+    if (h->h_stage) cudaFreeHost(h->h_stage);
+    h->h_stage = nullptr;
+    h->stage_slots = 0;
     dfree(h->d_series);
     free_lp_batch(h);
     dfree(h->d_lp_p); dfree(h->d_lp_g); dfree(h->d_lp_m); dfree(h->d_lp_v);
@@ -1135,26 +1144,35 @@ int esp_set_temperatures(esp_handle *h, const double *tems)
     return identity_labels(h);
 }
 
+// Device staging for spin_matrix blocks of whole temperature slots, at most
+// 256 MiB (one slot at least).
+int ensure_stage(esp_handle *h)
+{
+    if (h->d_stage) return ESP_OK;
+    const size_t per_slot = sizeof(double) * 3 * (size_t)h->N;
+    int slots = (int)std::max<size_t>(1, ((size_t)256 << 20) / per_slot);
+    slots = std::min(slots, h->R);
+    CK(dalloc(&h->d_stage, (size_t)3 * h->N * slots));
+    CK(cudaMallocHost((void **)&h->h_stage, sizeof(double) * 3 * (size_t)h->N * slots));
+    h->stage_slots = slots;
+    return ESP_OK;
+}
+
 int esp_set_spins(esp_handle *h, const double *spins)
 {
     int rc = require(h, true, false);
     if (rc) return rc;
     if (!spins) { h->err = "null spins"; return ESP_EINVAL; }
-    std::vector<int32_t> ra;
-    if ((rc = get_repl_at(h, ra))) return rc;
-    const size_t NR = (size_t)h->N * h->R;
-    std::vector<float> x(NR), y(NR), z(NR);
-    for (int t = 0; t < h->R; ++t) {
-        const int r = ra[t];
-        for (int i = 0; i < h->N; ++i) {
-            const size_t o = (size_t)h->prep.inv[i] * h->R + r;
-            const double *s = spins + 3 * ((size_t)t * h->N + i);
-            x[o] = (float)s[0]; y[o] = (float)s[1]; z[o] = (float)s[2];
-        }
+    if ((rc = ensure_stage(h))) return rc;
+    // blocks of slots: copy the FP64 block, then scatter it into the permuted
+    // FP32 state on the device
+    for (int t0 = 0; t0 < h->R; t0 += h->stage_slots) {
+        const int nt = std::min(h->stage_slots, h->R - t0);
+        CK(cudaMemcpyAsync(h->d_stage, spins + (size_t)3 * h->N * t0, sizeof(double) * 3 * (size_t)h->N * nt,
+                           cudaMemcpyHostToDevice, h->st));
+        CK(launch_spins_in(h->d_stage, h->d_inv, h->d_repl_at, h->d_sx, h->d_sy, h->d_sz, h->N, h->R, t0, nt, h->st));
+        h->launches++;
     }
-    if ((rc = h2d(h, h->d_sx, x.data(), sizeof(float) * NR))) return rc;
-    if ((rc = h2d(h, h->d_sy, y.data(), sizeof(float) * NR))) return rc;
-    if ((rc = h2d(h, h->d_sz, z.data(), sizeof(float) * NR))) return rc;
     if ((rc = reset_running(h))) return rc;
     CK(cudaStreamSynchronize(h->st));
     return ESP_OK;
@@ -1176,21 +1194,16 @@ int esp_get_spins(esp_handle *h, double *spins)
 {
     int rc = require(h, true, false);
     if (rc) return rc;
-    std::vector<int32_t> ra;
-    if ((rc = get_repl_at(h, ra))) return rc;
-    const size_t NR = (size_t)h->N * h->R;
-    std::vector<float> x(NR), y(NR), z(NR);
-    CK(cudaMemcpyAsync(x.data(), h->d_sx, sizeof(float) * NR, cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(y.data(), h->d_sy, sizeof(float) * NR, cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(z.data(), h->d_sz, sizeof(float) * NR, cudaMemcpyDeviceToHost, h->st));
-    CK(cudaStreamSynchronize(h->st));
-    for (int t = 0; t < h->R; ++t) {
-        const int r = ra[t];
-        for (int i = 0; i < h->N; ++i) {
-            const size_t o = (size_t)h->prep.inv[i] * h->R + r;
-            double *s = spins + 3 * ((size_t)t * h->N + i);
-            s[0] = x[o]; s[1] = y[o]; s[2] = z[o];
-        }
+    if (!spins) { h->err = "null spins"; return ESP_EINVAL; }
+    if ((rc = ensure_stage(h))) return rc;
+    for (int t0 = 0; t0 < h->R; t0 += h->stage_slots) {
+        const int nt = std::min(h->stage_slots, h->R - t0);
+        const size_t bytes = sizeof(double) * 3 * (size_t)h->N * nt;
+        CK(launch_spins_out(h->d_stage, h->d_inv, h->d_repl_at, h->d_sx, h->d_sy, h->d_sz, h->N, h->R, t0, nt, h->st));
+        h->launches++;
+        CK(cudaMemcpyAsync(h->h_stage, h->d_stage, bytes, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        std::memcpy(spins + (size_t)3 * h->N * t0, h->h_stage, bytes);
     }
     return ESP_OK;
 }

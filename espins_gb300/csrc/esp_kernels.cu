@@ -17,6 +17,7 @@
 //   k_pm_hist        Pm_get (get_quant.F90:425-493) as an integer histogram
 //   k_pt_swap        pt_swap (pt.F90:1235-1288) on temperature labels
 //   k_init_spins     ferro / rand start configurations (mcarlo.F90:271-293)
+//   k_spins_in/out   spin_matrix(3,N,slots) <-> the permuted FP32 SoA state
 //
 // Layout: spins are FP32 SoA (sx, sy, sz), element (p, r) at p*R + r, with p
 // the colour-major permuted site index and r the replica.  Consecutive threads
@@ -742,6 +743,40 @@ __global__ void k_pt_swap(PtSwapArgs a)
 // theta = pi*u1, phi = 2 pi*u2 (mcarlo.F90:279-293), one configuration for
 // all replicas as pt.F90:448-459 does.
 // ---------------------------------------------------------------------------
+// spin_matrix(3, N, t0 .. t0+nt-1) in FP64 (reference site order, slot t
+// holding replica repl_at[t]) -> the FP32 state, and back.  One thread per
+// (slot, site, component) of the staged block, reading or writing it
+// contiguously.
+__global__ void k_spins_in(const double *stage, const int32_t *inv, const int32_t *repl_at, float *sx, float *sy,
+                           float *sz, int N, int R, int t0, int nt)
+{
+    const long long total = 3LL * N * nt;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(k % 3);
+        const long long ti = k / 3;
+        const int i = (int)(ti % N), t = t0 + (int)(ti / N);
+        const size_t o = (size_t)inv[i] * R + repl_at[t];
+        float *dst = c == 0 ? sx : (c == 1 ? sy : sz);
+        dst[o] = (float)stage[k];
+    }
+}
+
+__global__ void k_spins_out(double *stage, const int32_t *inv, const int32_t *repl_at, const float *sx,
+                            const float *sy, const float *sz, int N, int R, int t0, int nt)
+{
+    const long long total = 3LL * N * nt;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(k % 3);
+        const long long ti = k / 3;
+        const int i = (int)(ti % N), t = t0 + (int)(ti / N);
+        const size_t o = (size_t)inv[i] * R + repl_at[t];
+        const float *src = c == 0 ? sx : (c == 1 ? sy : sz);
+        stage[k] = (double)src[o];
+    }
+}
+
 __global__ void k_init_spins(const int32_t *perm, const float *mag, float *sx, float *sy, float *sz,
                              int N, int R, int kind, uint32_t k0, uint32_t k1)
 {
@@ -924,6 +959,22 @@ __global__ void k_bump(unsigned long long *ctr, unsigned long long d0, unsigned 
 cudaError_t launch_bump(unsigned long long *ctr, const unsigned long long d[4], cudaStream_t st)
 {
     k_bump<<<1, 1, 0, st>>>(ctr, d[0], d[1], d[2], d[3]);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spins_in(const double *stage, const int32_t *inv, const int32_t *repl_at, float *sx, float *sy,
+                            float *sz, int N, int R, int t0, int nt, cudaStream_t st)
+{
+    const int blocks = grid_for(3LL * N * nt, 256, 4096);
+    k_spins_in<<<blocks, 256, 0, st>>>(stage, inv, repl_at, sx, sy, sz, N, R, t0, nt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spins_out(double *stage, const int32_t *inv, const int32_t *repl_at, const float *sx,
+                             const float *sy, const float *sz, int N, int R, int t0, int nt, cudaStream_t st)
+{
+    const int blocks = grid_for(3LL * N * nt, 256, 4096);
+    k_spins_out<<<blocks, 256, 0, st>>>(stage, inv, repl_at, sx, sy, sz, N, R, t0, nt);
     return cudaGetLastError();
 }
 

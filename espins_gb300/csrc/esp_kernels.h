@@ -139,6 +139,11 @@ cudaError_t launch_sfactor(const SfArgs &a, cudaStream_t st);
 cudaError_t launch_pt_swap(const PtSwapArgs &a, cudaStream_t st);
 // ctr[i] += d[i] for the four run counters
 cudaError_t launch_bump(unsigned long long *ctr, const unsigned long long d[4], cudaStream_t st);
+// spin_matrix(3, N, slots t0 .. t0+nt-1) staged on the device <-> the state
+cudaError_t launch_spins_in(const double *stage, const int32_t *inv, const int32_t *repl_at, float *sx, float *sy,
+                            float *sz, int N, int R, int t0, int nt, cudaStream_t st);
+cudaError_t launch_spins_out(double *stage, const int32_t *inv, const int32_t *repl_at, const float *sx,
+                             const float *sy, const float *sz, int N, int R, int t0, int nt, cudaStream_t st);
 cudaError_t launch_init_spins(const int32_t *perm, const float *mag, float *sx, float *sy, float *sz,
                               int N, int R, int kind, uint64_t seed, cudaStream_t st);
 
