@@ -76,7 +76,8 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
 
     const int temp = a.temp_of[r];
     const float beta = a.beta[temp];
-    double accE = 0.0, accX = 0.0, accY = 0.0, accZ = 0.0;  // since the last measurement
+    // sums of the per-sweep FP32 sums since the last measurement, as float pairs
+    F2 accE{0.f, 0.f}, accX{0.f, 0.f}, accY{0.f, 0.f}, accZ{0.f, 0.f};
     unsigned long long nrej = 0;
     const float pm_scale = (float)((double)(a.nf - 1) / (a.m_max - a.m_min));
     // replica totals, held by thread 0 of rank 0
@@ -206,55 +207,74 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                 }
                 cluster.sync();
             }
-            accE += (double)fE; accX += (double)fX; accY += (double)fY; accZ += (double)fZ;
+            accE = f2_add(accE, fE); accX = f2_add(accX, fX); accY = f2_add(accY, fY); accZ = f2_add(accZ, fZ);
         }
         if (!a.measure) continue;
         // ---- measurement: cluster-wide sums of dE and dM (and, with the
         // optional measurements, of s.a and c s over the slab) ---------------
         {
-            double v[8] = {accE, accX, accY, accZ, 0.0, 0.0, 0.0, 0.0};
-            accE = accX = accY = accZ = 0.0;
+            // float pairs within the CTA for dE and dM (FP64 is a slow pipe
+            // on this GPU), plain FP32 for the order-parameter sums, FP64
+            // across CTAs and into the running totals
+            F2 p4[4] = {accE, accX, accY, accZ};
+            accE = accX = accY = accZ = F2{0.f, 0.f};
+            float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (a.obs) {
-                // FP32 per thread (a few sites each), FP64 from here on
                 float op = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
                 for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
                     int k, rem;
                     fdivmod(l, a.fd_pc, k, rem);
                     obs_add(sx[l], sy[l], sz[l], __ldg(a.obs_atom + (k >> 3)), op, qx, qy, qz);
                 }
-                v[4] = (double)op; v[5] = (double)qx; v[6] = (double)qy; v[7] = (double)qz;
+                v[4] = op; v[5] = qx; v[6] = qy; v[7] = qz;
             }
 #pragma unroll
-            for (int c = 0; c < 8; ++c)
-                for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+            for (int c = 0; c < 4; ++c)
+                for (int o = 16; o > 0; o >>= 1) p4[c] = f2_add(p4[c], f2_shfl_down(p4[c], o));
+            if (a.obs) {
+#pragma unroll
+                for (int c = 4; c < 8; ++c)
+                    for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+            }
             const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            // [warp][12] floats in the first 96 doubles: 4 pairs, 4 floats
+            float *redf = reinterpret_cast<float *>(red);
             if (lane == 0) {
 #pragma unroll
-                for (int c = 0; c < 8; ++c) red[8 * warp + c] = v[c];
+                for (int c = 0; c < 4; ++c) { redf[12 * warp + 2 * c] = p4[c].hi; redf[12 * warp + 2 * c + 1] = p4[c].lo; }
+#pragma unroll
+                for (int c = 4; c < 8; ++c) redf[12 * warp + 4 + c] = v[c];
             }
             __syncthreads();
-            if (threadIdx.x == 0) {
-                double t8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            if (warp == 0) {
+                const int nw = (int)(blockDim.x >> 5);
 #pragma unroll
-                    for (int c = 0; c < 8; ++c) t8[c] += red[8 * w + c];
+                for (int c = 0; c < 4; ++c) {
+                    F2 x = lane < nw ? F2{redf[12 * lane + 2 * c], redf[12 * lane + 2 * c + 1]} : F2{0.f, 0.f};
+                    for (int o = 16; o > 0; o >>= 1) x = f2_add(x, f2_shfl_down(x, o));
+                    if (lane == 0) red[128 + c] = f2_to_double(x);   // this CTA's totals
                 }
 #pragma unroll
-                for (int c = 0; c < 8; ++c) red[128 + c] = t8[c];  // this CTA's total
+                for (int c = 4; c < 8; ++c) {
+                    float x = lane < nw ? redf[12 * lane + 4 + c] : 0.f;
+                    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+                    if (lane == 0) red[128 + c] = (double)x;
+                }
             }
             // P(M) [P(OP), P(SM)] of this CTA's cells
             if (a.na > 1 || a.obs) {
-                const int ncells_local = Hx * Hy * Hzl * 8;  // cells of the slab
+                // cells in the local layout's order: the cell of parity class
+                // p (0..7) and half-coordinates rem holds, for every atom, the
+                // site (at * 8 + p) * per_class + rem, i.e. at * cstride + cl
+                const int ncells_local = per_class * 8;         // cells of the slab
+                const int cstride = per_class * 8;
                 const int cl_end = (ncells_local + 31) & ~31;   // whole warps take part in the vote
                 for (int cl = threadIdx.x; cl < cl_end; cl += blockDim.x) {
                     int bin = -1, bin_op = -1, bin_sm = -1;
                     if (cl < ncells_local) {
-                        const int x = cl % a.Lx, y = (cl / a.Lx) % a.Ly, zl = cl / (a.Lx * a.Ly);
-                        const int z = z0 + zl;
                         float mx = 0.f, my = 0.f, mz = 0.f, op = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
                         for (int at = 0; at < a.na; ++at) {
-                            const int k = (at << 3) | ((x & 1) << 2) | ((y & 1) << 1) | (z & 1);
-                            const int l = k * per_class + (((zl >> 1) * Hy + (y >> 1)) * Hx + (x >> 1));
+                            const int l = at * cstride + cl;
                             const float ox = sx[l], oy = sy[l], oz = sz[l];
                             mx += ox; my += oy; mz += oz;
                             if (a.obs) obs_add(ox, oy, oz, __ldg(a.obs_atom + at), op, qx, qy, qz);
@@ -350,7 +370,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
 
     // ---- end of launch: totals, rejected counts, histogram, spins ----------
     {
-        double v[4] = {accE, accX, accY, accZ};
+        double v[4] = {f2_to_double(accE), f2_to_double(accX), f2_to_double(accY), f2_to_double(accZ)};
         unsigned long long nr = nrej;
         for (int c = 0; c < 4; ++c)
             for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);

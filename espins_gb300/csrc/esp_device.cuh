@@ -84,6 +84,32 @@ __device__ __forceinline__ void trial_spin(int mode, float tilt, float mag, floa
 // clamped to nf; FP32 (an edge flip needs m within ~1e-7 of a bin edge).
 // scale = (nf - 1) / (m_max - m_min).  Returns the 1-based bin.  m is |sum s|
 // for P(M) and P(SM), the signed sum of s.a for P(OP).
+// Unevaluated sums hi + lo of two floats (Knuth's two-sum, Dekker's
+// normalisation): sums of FP32 terms kept to about 2^-46 relative without the
+// FP64 pipe.
+struct F2 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ F2 f2_add(F2 x, F2 y)
+{
+    const float s = __fadd_rn(x.hi, y.hi);
+    const float bb = __fsub_rn(s, x.hi);
+    float e = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, bb)), __fsub_rn(y.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(x.lo, y.lo));
+    const float h = __fadd_rn(s, e);
+    return F2{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ F2 f2_add(F2 x, float y) { return f2_add(x, F2{y, 0.f}); }
+
+__device__ __forceinline__ F2 f2_shfl_down(F2 x, int o)
+{
+    return F2{__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o)};
+}
+
+__device__ __forceinline__ double f2_to_double(F2 x) { return (double)x.hi + (double)x.lo; }
+
 // Adds one spin's s.a to op and c s to (qx, qy, qz), w = (a, c), with
 // explicitly rounded fused multiply-adds: every kernel that measures the order
 // parameter or the staggered magnetisation gets the same bits for a cell.
