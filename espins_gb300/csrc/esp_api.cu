@@ -416,6 +416,7 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     a.fd_pc = make_fastdiv((uint32_t)((h->L[0] / 2) * (h->L[1] / 2) * (h->pz / 2)));
     a.fd_hx = make_fastdiv((uint32_t)(h->L[0] / 2));
     a.fd_hy = make_fastdiv((uint32_t)(h->L[1] / 2));
+    a.rn_inv = 1.0 / (double)h->N;
     a.key0 = (uint32_t)o->seed; a.key1 = (uint32_t)(o->seed >> 32);
     a.mode = o->mcarlo_mode ? 1 : 0; a.tilt = (float)o->tilt_angles_max;
     a.obs = measure ? h->obs : 0;

@@ -50,7 +50,15 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
     unsigned int *hist = reinterpret_cast<unsigned int *>(smem) + a.stencil_words;
     const int nhist = a.obs ? 3 : 1;
     double *red = reinterpret_cast<double *>(hist + ((nhist * a.nf + 3) & ~3));
-    float *sx = reinterpret_cast<float *>(red + 136);
+    // the slot's accumulators, kept by rank 0 for the launch (the slot of a
+    // replica does not change inside a launch): data, obs data, binning
+    // levels, binning sums and variances of E/N, |m| and of |OP|, |SM|
+    double *acc = red + 136;
+    double *c_data = acc, *c_odata = acc + 6;
+    int *c_lev = reinterpret_cast<int *>(acc + 12);
+    double *c_ls = acc + 12 + kClusterMaxLev / 2, *c_bn = c_ls + 2 * kClusterMaxLev;
+    double *c_ols = c_bn + 2 * kClusterMaxLev, *c_obn = c_ols + 2 * kClusterMaxLev;
+    float *sx = reinterpret_cast<float *>(acc + kClusterAccDoubles);
     float *sy = sx + n_local;
     float *sz = sy + n_local;
 
@@ -72,9 +80,24 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
         const size_t g = (size_t)__ldg(a.inv + orig) * a.R + r;
         sx[l] = a.sx[g]; sy[l] = a.sy[g]; sz[l] = a.sz[g];
     }
+    const int temp = a.temp_of[r];
+    const bool cache = a.measure && a.nlev <= kClusterMaxLev;
+    if (rank == 0 && cache) {
+        const int nl2 = 2 * a.nlev;
+        for (int i = threadIdx.x; i < 6; i += blockDim.x) {
+            c_data[i] = a.data[6 * temp + i];
+            c_odata[i] = a.obs ? a.obs_data[6 * temp + i] : 0.0;
+        }
+        for (int i = threadIdx.x; i < a.nlev; i += blockDim.x) c_lev[i] = a.levels[i];
+        for (int i = threadIdx.x; i < nl2; i += blockDim.x) {
+            c_ls[i] = a.lsum[(size_t)temp * nl2 + i];
+            c_bn[i] = a.binning[(size_t)temp * nl2 + i];
+            c_ols[i] = a.obs ? a.obs_lsum[(size_t)temp * nl2 + i] : 0.0;
+            c_obn[i] = a.obs ? a.obs_bin[(size_t)temp * nl2 + i] : 0.0;
+        }
+    }
     cluster.sync();
 
-    const int temp = a.temp_of[r];
     const float beta = a.beta[temp];
     // sums of the per-sweep FP32 sums since the last measurement, as float pairs
     F2 accE{0.f, 0.f}, accX{0.f, 0.f}, accY{0.f, 0.f}, accZ{0.f, 0.f};
@@ -310,11 +333,11 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                 m_run[0] += d4[1]; m_run[1] += d4[2]; m_run[2] += d4[3];
                 // accumulators of mcarlo.F90:536-590 for this temperature slot
                 const double e = e_run;
-                const double rn_inv = 1.0 / (double)a.N;
+                const double rn_inv = a.rn_inv;
                 const double mx = m_run[0] * rn_inv, my = m_run[1] * rn_inv, mz = m_run[2] * rn_inv;
                 const double m2 = mx * mx + my * my + mz * mz;
                 const double ee = e * e, am = sqrt(m2);
-                double *d = a.data + 6 * temp;
+                double *d = cache ? c_data : a.data + 6 * temp;
                 d[0] += e; d[1] += ee; d[2] += ee * ee;
                 d[3] += am; d[4] += m2; d[5] += m2 * m2;
                 const long long step = meas_base + m + 1;
@@ -325,32 +348,34 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                 // orderparam_get / staggered_get (mcarlo.F90:553-568)
                 double aop = 0.0, asm_ = 0.0;
                 if (a.obs) {
-                    double *od = a.obs_data + 6 * temp;
+                    double *od = cache ? c_odata : a.obs_data + 6 * temp;
                     if (a.obs & 1) {
-                        const double op = d4[4] / (double)a.N;
+                        const double op = d4[4] * rn_inv;
                         const double o2 = op * op;
                         aop = sqrt(o2);
                         od[0] += aop; od[1] += o2; od[2] += o2 * o2;
                     }
                     if (a.obs & 2) {
-                        const double qx = d4[5] / (double)a.N, qy = d4[6] / (double)a.N, qz = d4[7] / (double)a.N;
+                        const double qx = d4[5] * rn_inv, qy = d4[6] * rn_inv, qz = d4[7] * rn_inv;
                         const double q2 = qx * qx + qy * qy + qz * qz;
                         asm_ = sqrt(q2);
                         od[3] += asm_; od[4] += q2; od[5] += q2 * q2;
                     }
                 }
                 for (int lv = 0; lv < a.nlev; ++lv) {
-                    double *ls = a.lsum + ((size_t)temp * a.nlev + lv) * 2;
-                    double *bn = a.binning + ((size_t)temp * a.nlev + lv) * 2;
-                    double *ols = a.obs ? a.obs_lsum + ((size_t)temp * a.nlev + lv) * 2 : nullptr;
-                    double *obn = a.obs ? a.obs_bin + ((size_t)temp * a.nlev + lv) * 2 : nullptr;
+                    const size_t g2 = ((size_t)temp * a.nlev + lv) * 2;
+                    double *ls = cache ? c_ls + 2 * lv : a.lsum + g2;
+                    double *bn = cache ? c_bn + 2 * lv : a.binning + g2;
+                    double *ols = !a.obs ? nullptr : (cache ? c_ols + 2 * lv : a.obs_lsum + g2);
+                    double *obn = !a.obs ? nullptr : (cache ? c_obn + 2 * lv : a.obs_bin + g2);
                     ls[0] += e * rn_inv;
                     ls[1] += am;
                     if (ols) { ols[0] += aop; ols[1] += asm_; }
-                    const long long blk = 1LL << a.levels[lv];
+                    const int lev = cache ? c_lev[lv] : a.levels[lv];
+                    const long long blk = 1LL << lev;
                     if ((step & (blk - 1)) == 0) {
                         // 1/2^n is exact, so the product equals the division
-                        const double inv_div = 1.0 / (a.pt_quirk ? (double)(1LL << (lv + 1)) : (double)blk);
+                        const double inv_div = ldexp(1.0, -(a.pt_quirk ? lv + 1 : lev));
                         for (int c = 0; c < 2; ++c) {
                             const double v2 = ls[c] * inv_div;
                             bn[c] += v2 * v2;
@@ -412,6 +437,18 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
             a.m_run[3 * r + 2] = m_run[2] + d4[3];
             a.rej[2 * temp + a.phase] += tn;
         }
+        if (rank == 0 && cache) {
+            const int nl2 = 2 * a.nlev;
+            for (int i = threadIdx.x; i < 6; i += blockDim.x) {
+                a.data[6 * temp + i] = c_data[i];
+                if (a.obs) a.obs_data[6 * temp + i] = c_odata[i];
+            }
+            for (int i = threadIdx.x; i < nl2; i += blockDim.x) {
+                a.lsum[(size_t)temp * nl2 + i] = c_ls[i];
+                a.binning[(size_t)temp * nl2 + i] = c_bn[i];
+                if (a.obs) { a.obs_lsum[(size_t)temp * nl2 + i] = c_ols[i]; a.obs_bin[(size_t)temp * nl2 + i] = c_obn[i]; }
+            }
+        }
     }
     for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
         int k, rem, q1, hx, hy, hzl;
@@ -431,7 +468,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
 size_t cluster_smem_bytes(int n_local, int nf, int nhist, size_t stencil_bytes)
 {
     return ((stencil_bytes + 15) & ~(size_t)15) + (size_t)((nhist * nf + 3) & ~3) * sizeof(unsigned int) +
-           (size_t)136 * sizeof(double) + (size_t)3 * n_local * sizeof(float);
+           (size_t)(136 + kClusterAccDoubles) * sizeof(double) + (size_t)3 * n_local * sizeof(float);
 }
 
 namespace {

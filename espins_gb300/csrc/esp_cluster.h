@@ -68,6 +68,7 @@ struct ClusterArgs {
     const unsigned long long *ctr;
     // divisions by per-class sites and half-cell extents
     FastDiv fd_pc, fd_hx, fd_hy;
+    double rn_inv;                  // 1 / N
     uint32_t key0, key1;
     int mode;
     float tilt;
@@ -81,6 +82,11 @@ struct ClusterArgs {
 };
 
 // nhist: P(M) histogram only (1) or P(M), P(OP), P(SM) (3)
+// binning levels whose sums a cluster keeps in shared memory during a launch
+// (more levels are updated in global memory)
+constexpr int kClusterMaxLev = 32;
+// doubles of that cache: data and obs data (12), levels (16), four [level][2] arrays
+constexpr int kClusterAccDoubles = 12 + kClusterMaxLev / 2 + 8 * kClusterMaxLev;
 size_t cluster_smem_bytes(int n_local, int nf, int nhist, size_t stencil_bytes);
 // nt: threads per CTA, 256 or 512
 cudaError_t cluster_configure(size_t smem, int csize, int nt);
