@@ -263,8 +263,10 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
     extern __shared__ __align__(16) unsigned char smem[];
     ClusterStencil *st = reinterpret_cast<ClusterStencil *>(smem);
     ClusterNbr *nbt = reinterpret_cast<ClusterNbr *>(st + 1);          // [na][maxst]
-    int *toff = reinterpret_cast<int *>(nbt + na * maxst);              // [na][maxst], padded to 4
-    int *inv_s = toff + ((na * maxst + 3) & ~3);                        // [2][nbs], padded to 4
+    // slot offsets of the entries, times G, for each value of (box site & 7):
+    // box_slot(b + o) - box_slot(b) depends on o and b & 7 only
+    int *tq = reinterpret_cast<int *>(nbt + na * maxst);                // [na][maxst][8]
+    int *inv_s = tq + 8 * na * maxst;                                   // [2][nbs], padded to 4
     float *buf = reinterpret_cast<float *>(inv_s + 2 * ((nbs + 3) & ~3));  // [2][3][nbs8*G]
     double *red = reinterpret_cast<double *>(buf + (size_t)6 * nbs8 * G);  // [NT/32][G][4]
     unsigned long long *red_n = reinterpret_cast<unsigned long long *>(red + (NT / 32) * G * 4);
@@ -279,7 +281,11 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
             const int at = i / maxst;
             nbt[i] = a.cpl[i];
             const int4 d = a.offs[i];
-            toff[i] = ((d.z * B + d.y) * B + d.x) * na + d.w - at;
+            const int o = ((d.z * B + d.y) * B + d.x) * na + d.w - at;
+            for (int m = 0; m < 8; ++m) {
+                const int b = (1 << 20) + m;   // any box site with b & 7 == m
+                tq[8 * i + m] = (box_slot(b + o) - box_slot(b)) * G;
+            }
         }
         if (threadIdx.x < kMaxClusterAtoms) {
             s_nbd8[threadIdx.x] = a.nbd8[threadIdx.x];
@@ -388,14 +394,14 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
                 float gx = 0.f, gy = 0.f, gz = 0.f;
                 float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
                 const ClusterNbr *nb = nbt + at * maxst;
-                const int *to = toff + at * maxst;
+                const int *to = tq + 8 * at * maxst + (bsite & 7);
                 const int nbd8 = s_nbd8[at], nall8 = s_nall8[at];
                 int e0 = 0;
                 for (; e0 < nbd8; e0 += 8) {
                     float tx_[8], ty_[8], tz_[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        const int q = box_slot(bsite + to[e0 + j]) * G + g;
+                        const int q = l + to[8 * (e0 + j)];
                         tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
                     }
 #pragma unroll
@@ -422,7 +428,7 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
                     float tx_[8], ty_[8], tz_[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        const int q = box_slot(bsite + to[e0 + j]) * G + g;
+                        const int q = l + to[8 * (e0 + j)];
                         tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
                     }
 #pragma unroll
@@ -568,7 +574,7 @@ size_t tile_p_smem_bytes(int T, int G, int na, int maxst)
 {
     const size_t B = (size_t)T + 2, nbs = B * B * B * na, nbs8 = (nbs + 7) & ~(size_t)7;
     return sizeof(ClusterStencil) + (size_t)na * maxst * sizeof(ClusterNbr) +
-           (size_t)((na * maxst + 3) & ~3) * sizeof(int) + 2 * ((nbs + 3) & ~(size_t)3) * sizeof(int) +
+           (size_t)8 * na * maxst * sizeof(int) + 2 * ((nbs + 3) & ~(size_t)3) * sizeof(int) +
            (size_t)6 * nbs8 * G * sizeof(float) + (size_t)(kTilePThreads / 32) * G * (4 * sizeof(double) + 8);
 }
 
