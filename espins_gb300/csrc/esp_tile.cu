@@ -23,6 +23,118 @@ namespace {
 
 constexpr int kTileThreads = 256;
 
+// One stencil entry's share of the local field g and of the quadratic form Q
+// (delta_energy_get, get_quant.F90:294-297 exchange, :316-325 biquadratic,
+// :327-333 DM) in one fixed sequence of IEEE operations, shared by the
+// one-replica kernel (float) and the two-replica kernel (float2 lanes through
+// fma.rn.f32x2), so the two give identical bits:
+//   g   <- fma(-J, t, g)
+//   Q_ab <- fma(B t_a, t_b, Q_ab)
+//   g_x <- fma(t_z, -D_y, fma(t_y, D_z, g_x)), and cyclically for y, z
+struct FieldQ {
+    float gx, gy, gz, qxx, qyy, qzz, qxy, qxz, qyz;
+};
+struct FieldQ2 {
+    float2 gx, gy, gz, qxx, qyy, qzz, qxy, qxz, qyz;
+};
+
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c)
+{
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+        "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b)
+{
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+
+__device__ __forceinline__ void entry_exchange(FieldQ &f, float nJ, float tx, float ty, float tz)
+{
+    f.gx = fmaf(nJ, tx, f.gx); f.gy = fmaf(nJ, ty, f.gy); f.gz = fmaf(nJ, tz, f.gz);
+}
+__device__ __forceinline__ void entry_bq(FieldQ &f, float Bv, float tx, float ty, float tz)
+{
+    const float bx = __fmul_rn(Bv, tx), by = __fmul_rn(Bv, ty), bz = __fmul_rn(Bv, tz);
+    f.qxx = fmaf(bx, tx, f.qxx); f.qyy = fmaf(by, ty, f.qyy); f.qzz = fmaf(bz, tz, f.qzz);
+    f.qxy = fmaf(bx, ty, f.qxy); f.qxz = fmaf(bx, tz, f.qxz); f.qyz = fmaf(by, tz, f.qyz);
+}
+__device__ __forceinline__ void entry_dm(FieldQ &f, float dx, float dy, float dz, float tx, float ty, float tz)
+{
+    f.gx = fmaf(tz, -dy, fmaf(ty, dz, f.gx));
+    f.gy = fmaf(tx, -dz, fmaf(tz, dx, f.gy));
+    f.gz = fmaf(ty, -dx, fmaf(tx, dy, f.gz));
+}
+__device__ __forceinline__ void entry_exchange(FieldQ2 &f, float2 nJ, float2 tx, float2 ty, float2 tz)
+{
+    f.gx = ffma2(nJ, tx, f.gx); f.gy = ffma2(nJ, ty, f.gy); f.gz = ffma2(nJ, tz, f.gz);
+}
+__device__ __forceinline__ void entry_bq(FieldQ2 &f, float2 Bv, float2 tx, float2 ty, float2 tz)
+{
+    const float2 bx = fmul2(Bv, tx), by = fmul2(Bv, ty), bz = fmul2(Bv, tz);
+    f.qxx = ffma2(bx, tx, f.qxx); f.qyy = ffma2(by, ty, f.qyy); f.qzz = ffma2(bz, tz, f.qzz);
+    f.qxy = ffma2(bx, ty, f.qxy); f.qxz = ffma2(bx, tz, f.qxz); f.qyz = ffma2(by, tz, f.qyz);
+}
+// nd = (-D_x, -D_y, -D_z) duplicated in both lanes
+__device__ __forceinline__ void entry_dm(FieldQ2 &f, float2 dx, float2 dy, float2 dz, float2 ndx, float2 ndy,
+                                         float2 ndz, float2 tx, float2 ty, float2 tz)
+{
+    f.gx = ffma2(tz, ndy, ffma2(ty, dz, f.gx));
+    f.gy = ffma2(tx, ndz, ffma2(tz, dx, f.gy));
+    f.gz = ffma2(ty, ndx, ffma2(tx, dy, f.gz));
+}
+__device__ __forceinline__ FieldQ lane_of(const FieldQ2 &f, int k)
+{
+    FieldQ o;
+    o.gx = k ? f.gx.y : f.gx.x; o.gy = k ? f.gy.y : f.gy.x; o.gz = k ? f.gz.y : f.gz.x;
+    o.qxx = k ? f.qxx.y : f.qxx.x; o.qyy = k ? f.qyy.y : f.qyy.x; o.qzz = k ? f.qzz.y : f.qzz.x;
+    o.qxy = k ? f.qxy.y : f.qxy.x; o.qxz = k ? f.qxz.y : f.qxz.x; o.qyz = k ? f.qyz.y : f.qyz.x;
+    return o;
+}
+
+// The Metropolis trial of one site of replica r (metropolis, get_quant.F90:52-182)
+// given its exchange/biquadratic/DM field: adds the single-ion and field
+// terms, draws the trial spin, and returns whether it is accepted, with the new
+// spin n and the energy change de.
+__device__ __forceinline__ bool tile_trial(const TileArgs &a, const ClusterStencil *st, FieldQ f, int at,
+                                           uint32_t orig, uint32_t r, uint32_t sw_lo, uint32_t sw_hi, float beta,
+                                           float ox, float oy, float oz, float &nx, float &ny, float &nz, float &de)
+{
+    if (a.has_si) {
+        const float4 s = st->si[at];
+        const float dx = __fmul_rn(s.w, s.x), dy = __fmul_rn(s.w, s.y), dz = __fmul_rn(s.w, s.z);
+        f.qxx = fmaf(dx, s.x, f.qxx); f.qyy = fmaf(dy, s.y, f.qyy); f.qzz = fmaf(dz, s.z, f.qzz);
+        f.qxy = fmaf(dx, s.y, f.qxy); f.qxz = fmaf(dx, s.z, f.qxz); f.qyz = fmaf(dy, s.z, f.qyz);
+    }
+    if (a.has_f) {
+        const float4 fl = st->fld[at];
+        f.gx = __fadd_rn(f.gx, fl.x); f.gy = __fadd_rn(f.gy, fl.y); f.gz = __fadd_rn(f.gz, fl.z);
+    }
+    const Philox4 xr = philox4x32_10(orig, r, sw_lo, sw_hi, a.key0, a.key1);
+    trial_spin(a.mode, a.tilt, st->mag[at], ox, oy, oz, xr.x, xr.y, nx, ny, nz);
+    const float dx = __fsub_rn(nx, ox), dy = __fsub_rn(ny, oy), dz = __fsub_rn(nz, oz);
+    de = fmaf(f.gz, dz, fmaf(f.gy, dy, __fmul_rn(f.gx, dx)));
+    if (a.has_b || a.has_si) {
+        const float px = __fadd_rn(nx, ox), py = __fadd_rn(ny, oy), pz = __fadd_rn(nz, oz);
+        const float ax = fmaf(f.qxz, pz, fmaf(f.qxy, py, __fmul_rn(f.qxx, px)));
+        const float ay = fmaf(f.qyz, pz, fmaf(f.qyy, py, __fmul_rn(f.qxy, px)));
+        const float az = fmaf(f.qzz, pz, fmaf(f.qyz, py, __fmul_rn(f.qxz, px)));
+        de = fmaf(dz, az, fmaf(dy, ay, fmaf(dx, ax, de)));
+    }
+    if (de > 0.0f) return expf(-beta * de) >= u24f(xr.z);
+    return true;
+}
+
 __global__ void __launch_bounds__(kTileThreads, 2) k_sweep_tile(const TileArgs a)
 {
     const int T = a.T, B = a.T + 2, G = a.G, na = a.na;
@@ -106,8 +218,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_sweep_tile(const TileArgs a
             const int bsite = (((lz + 1) * B + (ly + 1)) * B + (lx + 1)) * na + at;
             const int l = bsite * G + g;
             const float ox = sx[l], oy = sy[l], oz = sz[l];
-            float gx = 0.f, gy = 0.f, gz = 0.f;
-            float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
+            FieldQ f{};
             const ClusterNbr *nb = nbt + at * maxst;
             const int *to = toff + at * maxst;
             const int nbd8 = s_nbd8[at], nall8 = s_nall8[at];
@@ -122,20 +233,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_sweep_tile(const TileArgs a
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const ClusterNbr &se = nb[e0 + j];
-                    const float J = se.J;
-                    gx = fmaf(-J, tx_[j], gx); gy = fmaf(-J, ty_[j], gy); gz = fmaf(-J, tz_[j], gz);
-                    if (a.has_b) {
-                        const float Bv = se.B;
-                        const float bx = Bv * tx_[j], by = Bv * ty_[j], bz = Bv * tz_[j];
-                        qxx = fmaf(bx, tx_[j], qxx); qyy = fmaf(by, ty_[j], qyy); qzz = fmaf(bz, tz_[j], qzz);
-                        qxy = fmaf(bx, ty_[j], qxy); qxz = fmaf(bx, tz_[j], qxz); qyz = fmaf(by, tz_[j], qyz);
-                    }
-                    if (a.has_d) {
-                        const float dx = se.Dx, dy = se.Dy, dz = se.Dz;
-                        gx += ty_[j] * dz - tz_[j] * dy;
-                        gy += tz_[j] * dx - tx_[j] * dz;
-                        gz += tx_[j] * dy - ty_[j] * dx;
-                    }
+                    entry_exchange(f, -se.J, tx_[j], ty_[j], tz_[j]);
+                    if (a.has_b) entry_bq(f, se.B, tx_[j], ty_[j], tz_[j]);
+                    if (a.has_d) entry_dm(f, se.Dx, se.Dy, se.Dz, tx_[j], ty_[j], tz_[j]);
                 }
             }
             for (; e0 < nall8; e0 += 8) {   // exchange only
@@ -146,39 +246,14 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_sweep_tile(const TileArgs a
                     tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
                 }
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const float J = nb[e0 + j].J;
-                    gx = fmaf(-J, tx_[j], gx); gy = fmaf(-J, ty_[j], gy); gz = fmaf(-J, tz_[j], gz);
-                }
-            }
-            if (a.has_si) {
-                const float4 s = st->si[at];
-                const float dx = s.w * s.x, dy = s.w * s.y, dz = s.w * s.z;
-                qxx = fmaf(dx, s.x, qxx); qyy = fmaf(dy, s.y, qyy); qzz = fmaf(dz, s.z, qzz);
-                qxy = fmaf(dx, s.y, qxy); qxz = fmaf(dx, s.z, qxz); qyz = fmaf(dy, s.z, qyz);
-            }
-            if (a.has_f) {
-                const float4 f = st->fld[at];
-                gx += f.x; gy += f.y; gz += f.z;
+                for (int j = 0; j < 8; ++j) entry_exchange(f, -nb[e0 + j].J, tx_[j], ty_[j], tz_[j]);
             }
             const int orig = (((z0 + lz) * a.Ly + (y0 + ly)) * a.Lx + (x0 + lx)) * na + at;
-            const Philox4 xr = philox4x32_10((uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
-            float nx, ny, nz;
-            trial_spin(a.mode, a.tilt, st->mag[at], ox, oy, oz, xr.x, xr.y, nx, ny, nz);
-            const float dx = nx - ox, dy = ny - oy, dz = nz - oz;
-            float de = gx * dx + gy * dy + gz * dz;
-            if (a.has_b || a.has_si) {
-                const float px2 = nx + ox, py2 = ny + oy, pz2 = nz + oz;
-                de += dx * (qxx * px2 + qxy * py2 + qxz * pz2)
-                    + dy * (qxy * px2 + qyy * py2 + qyz * pz2)
-                    + dz * (qxz * px2 + qyz * py2 + qzz * pz2);
-            }
-            bool acc = true;
-            if (de > 0.0f) acc = expf(-beta * de) >= u24f(xr.z);
-            if (acc) {
+            float nx, ny, nz, de;
+            if (tile_trial(a, st, f, at, (uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, beta, ox, oy, oz, nx, ny, nz, de)) {
                 sx[l] = nx; sy[l] = ny; sz[l] = nz;
                 accE += de;
-                accX += dx; accY += dy; accZ += dz;
+                accX += __fsub_rn(nx, ox); accY += __fsub_rn(ny, oy); accZ += __fsub_rn(nz, oz);
             } else {
                 ++nrej;
             }
@@ -221,12 +296,15 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_sweep_tile(const TileArgs a
 }
 
 // ---------------------------------------------------------------------------
-// Pipelined variant: persistent CTAs of 512 threads, one per SM, loop over the
+// Pipelined variant: persistent CTAs of 256 threads, one per SM, loop over the
 // (tile, replica group) items of the launch's tile parity.  While item k is
 // updated in one shared-memory buffer, the box of item k+1 arrives in the
 // other by cp.async (16-byte chunks: the G replicas of a site are contiguous)
 // and the site-index lookups of item k+2 are in flight in registers.  Tile
-// edge T and group size G are compile-time constants.
+// edge T and group size G are compile-time constants.  A thread updates two
+// replicas of a site: each neighbour costs one slot lookup and three 8-byte
+// shared-memory loads (x, y, z of both replicas sit in one slot), and the
+// field sums run as fma.rn.f32x2 on the pair.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src)
 {
@@ -243,14 +321,22 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // in 4 distinct 8-bank groups.
 __device__ __forceinline__ int box_slot(int b) { return (b & ~7) | ((b >> 1) & 3) | ((b & 1) << 2); }
 
-constexpr int kTilePThreads = 512;
-constexpr int kInvPerThread = 8;   // box sites per thread for the index prefetch (<= 4096 box sites)
+constexpr int kTilePThreads = 256;
+constexpr int kInvPerThread = 16;   // box sites per thread for the index prefetch (<= 4096 box sites)
+
+// Couplings of one stencil entry with every value in both lanes of a float2,
+// for the two-replica arithmetic: -J, B, D and -D.
+struct PairNbr {
+    float2 nJ, B, Dx, Dy, Dz, nDx, nDy, nDz;
+};
 
 template <int T, int G>
 __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArgs a)
 {
-    constexpr int NT = kTilePThreads, B = T + 2, H = T / 2, PC = H * H * H, CH = G / 4;
-    static_assert(G % 4 == 0 && NT % G == 0 && (T & 1) == 0, "tile shape");
+    // SL floats per box slot: x of the G replicas, then y, then z; a thread
+    // updates replicas (2 gp, 2 gp + 1) of a site
+    constexpr int NT = kTilePThreads, B = T + 2, H = T / 2, PC = H * H * H, CH = G / 4, GP = G / 2, SL = 3 * G;
+    static_assert(G % 4 == 0 && 32 % GP == 0 && (T & 1) == 0, "tile shape");
     const int na = a.na, maxst = a.maxst;
     const int ngroups = a.R / G;
     const int hx_t = a.ntx >> 1, hy_t = a.nty >> 1, hz_t = a.ntz >> 1;
@@ -262,13 +348,13 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
 
     extern __shared__ __align__(16) unsigned char smem[];
     ClusterStencil *st = reinterpret_cast<ClusterStencil *>(smem);
-    ClusterNbr *nbt = reinterpret_cast<ClusterNbr *>(st + 1);          // [na][maxst]
-    // slot offsets of the entries, times G, for each value of (box site & 7):
+    PairNbr *pnb = reinterpret_cast<PairNbr *>(st + 1);                // [na][maxst]
+    // slot offsets (in floats) of the entries for each value of (box site & 7):
     // box_slot(b + o) - box_slot(b) depends on o and b & 7 only
-    int *tq = reinterpret_cast<int *>(nbt + na * maxst);                // [na][maxst][8]
+    int *tq = reinterpret_cast<int *>(pnb + na * maxst);                // [na][maxst][8]
     int *inv_s = tq + 8 * na * maxst;                                   // [2][nbs], padded to 4
-    float *buf = reinterpret_cast<float *>(inv_s + 2 * ((nbs + 3) & ~3));  // [2][3][nbs8*G]
-    double *red = reinterpret_cast<double *>(buf + (size_t)6 * nbs8 * G);  // [NT/32][G][4]
+    float *buf = reinterpret_cast<float *>(inv_s + 2 * ((nbs + 3) & ~3));  // [2][nbs8][3][G]
+    double *red = reinterpret_cast<double *>(buf + (size_t)2 * nbs8 * SL);  // [NT/32][G][4]
     unsigned long long *red_n = reinterpret_cast<unsigned long long *>(red + (NT / 32) * G * 4);
 
     __shared__ int s_nbd8[kMaxClusterAtoms], s_nall8[kMaxClusterAtoms];
@@ -276,15 +362,19 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
         const int *src = reinterpret_cast<const int *>(a.stencil);
         int *dst = reinterpret_cast<int *>(st);
         for (int i = threadIdx.x; i < (int)(sizeof(ClusterStencil) / 4); i += NT) dst[i] = src[i];
-        // couplings, and box-site offsets of the entries
         for (int i = threadIdx.x; i < na * maxst; i += NT) {
             const int at = i / maxst;
-            nbt[i] = a.cpl[i];
+            const ClusterNbr c = a.cpl[i];
+            PairNbr p;
+            p.nJ = make_float2(-c.J, -c.J); p.B = make_float2(c.B, c.B);
+            p.Dx = make_float2(c.Dx, c.Dx); p.Dy = make_float2(c.Dy, c.Dy); p.Dz = make_float2(c.Dz, c.Dz);
+            p.nDx = make_float2(-c.Dx, -c.Dx); p.nDy = make_float2(-c.Dy, -c.Dy); p.nDz = make_float2(-c.Dz, -c.Dz);
+            pnb[i] = p;
             const int4 d = a.offs[i];
             const int o = ((d.z * B + d.y) * B + d.x) * na + d.w - at;
             for (int m = 0; m < 8; ++m) {
                 const int b = (1 << 20) + m;   // any box site with b & 7 == m
-                tq[8 * i + m] = (box_slot(b + o) - box_slot(b)) * G;
+                tq[8 * i + m] = (box_slot(b + o) - box_slot(b)) * SL;
             }
         }
         if (threadIdx.x < kMaxClusterAtoms) {
@@ -330,18 +420,19 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
             if (i < nbs) inv_s[stage * ((nbs + 3) & ~3) + i] = regs[j];
         }
     };
-    // the box of item w into buffer `stage`, as 16-byte asynchronous copies
+    // the box of item w into buffer `stage`, as 16-byte asynchronous copies:
+    // chunk k of a box site is component k / CH, replicas 4 (k % CH) ..
     auto issue_box = [&](int w, int stage) {
         int x0, y0, z0, r0, tile;
         item_tile(w, x0, y0, z0, r0, tile);
         const int *inv = inv_s + stage * ((nbs + 3) & ~3);
-        float *dst = buf + (size_t)stage * 3 * nbs8 * G;
+        float *dst = buf + (size_t)stage * nbs8 * SL;
         for (int i = threadIdx.x; i < nbs * 3 * CH; i += NT) {
-            const int c = i % CH, rest = i / CH;
-            const int cp = rest % 3, bs = rest / 3;
+            const int k = i % (3 * CH), bs = i / (3 * CH);
+            const int cp = k / CH, c = k % CH;
             const float *base = cp == 0 ? a.sx : (cp == 1 ? a.sy : a.sz);
             const float *src = base + (size_t)inv[bs] * a.R + r0 + 4 * c;
-            cp_async16(dst + (size_t)cp * nbs8 * G + box_slot(bs) * G + 4 * c, src);
+            cp_async16(dst + box_slot(bs) * SL + 4 * k, src);
         }
         cp_async_commit();
     };
@@ -358,10 +449,10 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
         load_inv(w1, regs);
         store_inv(1, regs);
     }
-    const int g = threadIdx.x % G;
+    const int gp = threadIdx.x % GP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = 0; w < W; ++k, w += gridDim.x) {
-        const int cur = k & 1, nxt = cur ^ 1;
+    for (int kk = 0; w < W; ++kk, w += gridDim.x) {
+        const int cur = kk & 1, nxt = cur ^ 1;
         const int wn = w + gridDim.x, wnn = wn + gridDim.x;
         __syncthreads();   // inv_s[nxt] written, buffer nxt free
         if (wn < W) issue_box(wn, nxt);
@@ -371,102 +462,74 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
 
         int x0, y0, z0, r0, tile;
         item_tile(w, x0, y0, z0, r0, tile);
-        float *sx = buf + (size_t)cur * 3 * nbs8 * G;
-        float *sy = sx + (size_t)nbs8 * G;
-        float *sz = sy + (size_t)nbs8 * G;
-        const int r = r0 + g;
-        const float beta = a.beta[a.temp_of[r]];
-        float accE = 0.f, accX = 0.f, accY = 0.f, accZ = 0.f;
-        unsigned int nrej = 0;
+        float *sb = buf + (size_t)cur * nbs8 * SL;
+        const int r = r0 + 2 * gp;
+        const float beta0 = a.beta[a.temp_of[r]], beta1 = a.beta[a.temp_of[r + 1]];
+        float accE[2] = {0.f, 0.f}, accX[2] = {0.f, 0.f}, accY[2] = {0.f, 0.f}, accZ[2] = {0.f, 0.f};
+        unsigned int nrej[2] = {0u, 0u};
         for (int c = 0; c < st->ncolour; ++c) {
             const int c0 = st->colour_start[c];
-            const int items = (st->colour_start[c + 1] - c0) * PC * G;
+            const int items = (st->colour_start[c + 1] - c0) * PC * GP;
             for (int it = threadIdx.x; it < items; it += NT) {
-                const int si = it / G;
+                const int si = it / GP;
                 const int kcl = st->class_order[c0 + si / PC];
                 const int rem = si % PC;
                 const int hx = rem % H, hy = (rem / H) % H, hz = rem / (H * H);
                 const int at = kcl >> 3;
                 const int lx = 2 * hx + ((kcl >> 2) & 1), ly = 2 * hy + ((kcl >> 1) & 1), lz = 2 * hz + (kcl & 1);
                 const int bsite = (((lz + 1) * B + (ly + 1)) * B + (lx + 1)) * na + at;
-                const int l = box_slot(bsite) * G + g;
-                const float ox = sx[l], oy = sy[l], oz = sz[l];
-                float gx = 0.f, gy = 0.f, gz = 0.f;
-                float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
-                const ClusterNbr *nb = nbt + at * maxst;
+                float *own = sb + box_slot(bsite) * SL + 2 * gp;
+                const float2 ox = *reinterpret_cast<const float2 *>(own);
+                const float2 oy = *reinterpret_cast<const float2 *>(own + G);
+                const float2 oz = *reinterpret_cast<const float2 *>(own + 2 * G);
+                FieldQ2 f;
+                f.gx = f.gy = f.gz = f.qxx = f.qyy = f.qzz = f.qxy = f.qxz = f.qyz = make_float2(0.f, 0.f);
+                const PairNbr *nb = pnb + at * maxst;
                 const int *to = tq + 8 * at * maxst + (bsite & 7);
                 const int nbd8 = s_nbd8[at], nall8 = s_nall8[at];
                 int e0 = 0;
                 for (; e0 < nbd8; e0 += 8) {
-                    float tx_[8], ty_[8], tz_[8];
+                    float2 tx_[8], ty_[8], tz_[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        const int q = l + to[8 * (e0 + j)];
-                        tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
+                        const float *q = own + to[8 * (e0 + j)];
+                        tx_[j] = *reinterpret_cast<const float2 *>(q);
+                        ty_[j] = *reinterpret_cast<const float2 *>(q + G);
+                        tz_[j] = *reinterpret_cast<const float2 *>(q + 2 * G);
                     }
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        // couplings as two 16-byte loads: (J, B, Dx, Dy), (Dz, ...)
-                        const float4 c0 = *reinterpret_cast<const float4 *>(nb + e0 + j);
-                        const float J = c0.x;
-                        gx = fmaf(-J, tx_[j], gx); gy = fmaf(-J, ty_[j], gy); gz = fmaf(-J, tz_[j], gz);
-                        if (a.has_b) {
-                            const float Bv = c0.y;
-                            const float bx = Bv * tx_[j], by = Bv * ty_[j], bz = Bv * tz_[j];
-                            qxx = fmaf(bx, tx_[j], qxx); qyy = fmaf(by, ty_[j], qyy); qzz = fmaf(bz, tz_[j], qzz);
-                            qxy = fmaf(bx, ty_[j], qxy); qxz = fmaf(bx, tz_[j], qxz); qyz = fmaf(by, tz_[j], qyz);
-                        }
-                        if (a.has_d) {
-                            const float dx = c0.z, dy = c0.w, dz = nb[e0 + j].Dz;
-                            gx += ty_[j] * dz - tz_[j] * dy;
-                            gy += tz_[j] * dx - tx_[j] * dz;
-                            gz += tx_[j] * dy - ty_[j] * dx;
-                        }
+                        const PairNbr &p = nb[e0 + j];
+                        entry_exchange(f, p.nJ, tx_[j], ty_[j], tz_[j]);
+                        if (a.has_b) entry_bq(f, p.B, tx_[j], ty_[j], tz_[j]);
+                        if (a.has_d) entry_dm(f, p.Dx, p.Dy, p.Dz, p.nDx, p.nDy, p.nDz, tx_[j], ty_[j], tz_[j]);
                     }
                 }
                 for (; e0 < nall8; e0 += 8) {   // exchange only
-                    float tx_[8], ty_[8], tz_[8];
+                    float2 tx_[8], ty_[8], tz_[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        const int q = l + to[8 * (e0 + j)];
-                        tx_[j] = sx[q]; ty_[j] = sy[q]; tz_[j] = sz[q];
+                        const float *q = own + to[8 * (e0 + j)];
+                        tx_[j] = *reinterpret_cast<const float2 *>(q);
+                        ty_[j] = *reinterpret_cast<const float2 *>(q + G);
+                        tz_[j] = *reinterpret_cast<const float2 *>(q + 2 * G);
                     }
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        const float J = nb[e0 + j].J;
-                        gx = fmaf(-J, tx_[j], gx); gy = fmaf(-J, ty_[j], gy); gz = fmaf(-J, tz_[j], gz);
-                    }
-                }
-                if (a.has_si) {
-                    const float4 s = st->si[at];
-                    const float dx = s.w * s.x, dy = s.w * s.y, dz = s.w * s.z;
-                    qxx = fmaf(dx, s.x, qxx); qyy = fmaf(dy, s.y, qyy); qzz = fmaf(dz, s.z, qzz);
-                    qxy = fmaf(dx, s.y, qxy); qxz = fmaf(dx, s.z, qxz); qyz = fmaf(dy, s.z, qyz);
-                }
-                if (a.has_f) {
-                    const float4 f = st->fld[at];
-                    gx += f.x; gy += f.y; gz += f.z;
+                    for (int j = 0; j < 8; ++j) entry_exchange(f, nb[e0 + j].nJ, tx_[j], ty_[j], tz_[j]);
                 }
                 const int orig = (((z0 + lz) * a.Ly + (y0 + ly)) * a.Lx + (x0 + lx)) * na + at;
-                const Philox4 xr = philox4x32_10((uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
-                float nx, ny, nz;
-                trial_spin(a.mode, a.tilt, st->mag[at], ox, oy, oz, xr.x, xr.y, nx, ny, nz);
-                const float dx = nx - ox, dy = ny - oy, dz = nz - oz;
-                float de = gx * dx + gy * dy + gz * dz;
-                if (a.has_b || a.has_si) {
-                    const float px2 = nx + ox, py2 = ny + oy, pz2 = nz + oz;
-                    de += dx * (qxx * px2 + qxy * py2 + qxz * pz2)
-                        + dy * (qxy * px2 + qyy * py2 + qyz * pz2)
-                        + dz * (qxz * px2 + qyz * py2 + qzz * pz2);
-                }
-                bool acc = true;
-                if (de > 0.0f) acc = expf(-beta * de) >= u24f(xr.z);
-                if (acc) {
-                    sx[l] = nx; sy[l] = ny; sz[l] = nz;
-                    accE += de;
-                    accX += dx; accY += dy; accZ += dz;
-                } else {
-                    ++nrej;
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const float sx0 = k ? ox.y : ox.x, sy0 = k ? oy.y : oy.x, sz0 = k ? oz.y : oz.x;
+                    float nx, ny, nz, de;
+                    if (tile_trial(a, st, lane_of(f, k), at, (uint32_t)orig, (uint32_t)(r + k), sw_lo, sw_hi,
+                                   k ? beta1 : beta0, sx0, sy0, sz0, nx, ny, nz, de)) {
+                        own[k] = nx; own[G + k] = ny; own[2 * G + k] = nz;
+                        accE[k] += de;
+                        accX[k] += __fsub_rn(nx, sx0); accY[k] += __fsub_rn(ny, sy0); accZ[k] += __fsub_rn(nz, sz0);
+                    } else {
+                        ++nrej[k];
+                    }
                 }
             }
             __syncthreads();
@@ -475,25 +538,37 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
         {
             const int *inv = inv_s + cur * ((nbs + 3) & ~3);
             for (int i = threadIdx.x; i < T * T * T * na * 3 * CH; i += NT) {
-                const int c = i % CH, rest = i / CH;
-                const int cp = rest % 3, ts = rest / 3;
+                const int k = i % (3 * CH), ts = i / (3 * CH);
+                const int cp = k / CH, c = k % CH;
                 const int at = na == 1 ? 0 : ts % na, cell = na == 1 ? ts : ts / na;
                 const int lx = cell % T, ly = (cell / T) % T, lz = cell / (T * T);
                 const int bsite = (((lz + 1) * B + (ly + 1)) * B + (lx + 1)) * na + at;
-                const float4 v = *reinterpret_cast<const float4 *>(sx + (size_t)cp * nbs8 * G + box_slot(bsite) * G + 4 * c);
+                const float4 v = *reinterpret_cast<const float4 *>(sb + box_slot(bsite) * SL + 4 * k);
                 float *base = cp == 0 ? a.sx : (cp == 1 ? a.sy : a.sz);
                 *reinterpret_cast<float4 *>(base + (size_t)inv[bsite] * a.R + r0 + 4 * c) = v;
             }
         }
-        double v[4] = {(double)accE, (double)accX, (double)accY, (double)accZ};
-        unsigned long long nr = nrej;
-        for (int o = G; o < 32; o <<= 1) {
-            for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
-            nr += __shfl_xor_sync(0xffffffffu, nr, o);
+        // lanes with the same gp hold the same two replicas
+        double v[2][4];
+        unsigned long long nr[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            v[k][0] = accE[k]; v[k][1] = accX[k]; v[k][2] = accY[k]; v[k][3] = accZ[k];
+            nr[k] = nrej[k];
         }
-        if (lane < G) {
-            for (int q = 0; q < 4; ++q) red[(warp * G + lane) * 4 + q] = v[q];
-            red_n[warp * G + lane] = nr;
+        for (int o = GP; o < 32; o <<= 1) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                for (int q = 0; q < 4; ++q) v[k][q] += __shfl_xor_sync(0xffffffffu, v[k][q], o);
+                nr[k] += __shfl_xor_sync(0xffffffffu, nr[k], o);
+            }
+        }
+        if (lane < GP) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                for (int q = 0; q < 4; ++q) red[(warp * G + 2 * lane + k) * 4 + q] = v[k][q];
+                red_n[warp * G + 2 * lane + k] = nr[k];
+            }
         }
         __syncthreads();   // sums in place; nobody reads inv_s[cur] any more
         if ((int)threadIdx.x < G) {
@@ -573,7 +648,7 @@ cudaError_t launch_tile(const TileArgs &a, size_t smem, cudaStream_t st)
 size_t tile_p_smem_bytes(int T, int G, int na, int maxst)
 {
     const size_t B = (size_t)T + 2, nbs = B * B * B * na, nbs8 = (nbs + 7) & ~(size_t)7;
-    return sizeof(ClusterStencil) + (size_t)na * maxst * sizeof(ClusterNbr) +
+    return sizeof(ClusterStencil) + (size_t)na * maxst * sizeof(PairNbr) +
            (size_t)8 * na * maxst * sizeof(int) + 2 * ((nbs + 3) & ~(size_t)3) * sizeof(int) +
            (size_t)6 * nbs8 * G * sizeof(float) + (size_t)(kTilePThreads / 32) * G * (4 * sizeof(double) + 8);
 }
