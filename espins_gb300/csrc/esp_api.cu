@@ -827,7 +827,9 @@ int cluster_geometry(esp_handle *h, int cs, int nt)
     CK(cluster_configure(smem, cs, nt));
     const int Lx = h->L[0], Ly = h->L[1], Lz = h->L[2], Hx = Lx / 2, Hy = Ly / 2, Hzl = pz / 2;
     const int per_class = Hx * Hy * Hzl;
-    // (owner rank << 24) | local index of stencil entry e of local site l on rank q
+    // stencil entry e of local site l on rank q: its local index, with
+    // 0x80000000 | (owner rank << 24) when the owner is another rank; stored
+    // as [q][e / 4][l][e % 4] so a thread reads four entries in one 16-byte load
     std::vector<uint32_t> tab((size_t)cs * maxst * n_local);
     for (int q = 0; q < cs; ++q)
         for (int l = 0; l < n_local; ++l) {
@@ -837,7 +839,7 @@ int cluster_geometry(esp_handle *h, int cs, int nt)
             const int x = 2 * hx + px, y = 2 * hy + py, z = q * pz + 2 * hzl + pzb;
             const auto &lst = h->prep.stencil[at];
             for (int e = 0; e < maxst; ++e) {
-                uint32_t v = ((uint32_t)q << 24) | (uint32_t)l;  // padding: the site itself
+                uint32_t v = (uint32_t)l;  // padding: the site itself
                 if (e < (int)lst.size()) {
                     const StencilEntry &se = lst[e];
                     const int xn = ((x + se.dx) % Lx + Lx) % Lx, yn = ((y + se.dy) % Ly + Ly) % Ly;
@@ -845,9 +847,9 @@ int cluster_geometry(esp_handle *h, int cs, int nt)
                     const int kn = (se.b << 3) | ((xn & 1) << 2) | ((yn & 1) << 1) | (zn & 1);
                     const int rn = zn / pz;
                     const int ln = kn * per_class + ((((zn - rn * pz) >> 1) * Hy + (yn >> 1)) * Hx + (xn >> 1));
-                    v = ((uint32_t)rn << 24) | (uint32_t)ln;
+                    v = rn == q ? (uint32_t)ln : (0x80000000u | ((uint32_t)rn << 24) | (uint32_t)ln);
                 }
-                tab[((size_t)q * maxst + e) * n_local + l] = v;
+                tab[(((size_t)q * (maxst / 4) + e / 4) * n_local + l) * 4 + e % 4] = v;
             }
         }
     CK(cudaStreamSynchronize(h->st));

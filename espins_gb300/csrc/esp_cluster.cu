@@ -58,9 +58,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
     int *c_lev = reinterpret_cast<int *>(acc + 12);
     double *c_ls = acc + 12 + kClusterMaxLev / 2, *c_bn = c_ls + 2 * kClusterMaxLev;
     double *c_ols = c_bn + 2 * kClusterMaxLev, *c_obn = c_ols + 2 * kClusterMaxLev;
-    float *sx = reinterpret_cast<float *>(acc + kClusterAccDoubles);
-    float *sy = sx + n_local;
-    float *sz = sy + n_local;
+    float *s3 = reinterpret_cast<float *>(acc + kClusterAccDoubles);   // [n_local][x, y, z]
 
     // ---- set-up: stencil and own spins -------------------------------------
     {
@@ -78,7 +76,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
         const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pz;
         const int orig = ((z * a.Ly + y) * a.Lx + x) * a.na + at;
         const size_t g = (size_t)__ldg(a.inv + orig) * a.R + r;
-        sx[l] = a.sx[g]; sy[l] = a.sy[g]; sz[l] = a.sz[g];
+        s3[3 * l] = a.sx[g]; s3[3 * l + 1] = a.sy[g]; s3[3 * l + 2] = a.sz[g];
     }
     const int temp = a.temp_of[r];
     const bool cache = a.measure && a.nlev <= kClusterMaxLev;
@@ -128,40 +126,47 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                     fdivmod(q1, a.fd_hy, hzl, hy);
                     const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pzb = k & 1;
                     const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pzb;
-                    const float ox = sx[l], oy = sy[l], oz = sz[l];
+                    const float ox = s3[3 * l], oy = s3[3 * l + 1], oz = s3[3 * l + 2];
                     float gx = 0.f, gy = 0.f, gz = 0.f;
                     float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
-                    // neighbour k of site l: (owner rank << 24) | local index, from the
-                    // precomputed table shared by every replica's cluster; lists are
-                    // padded to multiples of 8 with zero-coupling self entries
+                    // neighbour e of site l from the precomputed table shared by
+                    // every replica's cluster, four entries per 16-byte word:
+                    // the local index, with bit 31 set and the owner rank in
+                    // bits 24-30 when the neighbour lives in a peer CTA; lists
+                    // are padded to multiples of 8 with zero-coupling self entries
                     const int cnt_k = st->count[k];
                     const ClusterNbr *nb = nbt + k * st->maxst;
-                    const uint32_t *tab = a.nbidx + (size_t)rank * st->maxst * n_local + l;
+                    const uint4 *tab = reinterpret_cast<const uint4 *>(a.nbidx) + (size_t)rank * (st->maxst >> 2) * n_local + l;
                     // a batch of NB neighbours: read from this CTA's shared
                     // memory when every lane of the warp finds all of them
                     // here (warps cover slab planes, so this is the common
                     // case), else through the cluster window
                     auto batch = [&](auto nbc, int e0) {
                         constexpr int NB = decltype(nbc)::value;
-                        uint32_t id[NB];
+                        constexpr int NQ = (NB + 3) / 4;
+                        uint32_t id[4 * NQ];
 #pragma unroll
-                        for (int j = 0; j < NB; ++j) id[j] = __ldg(tab + (size_t)(e0 + j) * n_local);
+                        for (int j = 0; j < NQ; ++j) {
+                            const uint4 w = __ldg(tab + (size_t)((e0 >> 2) + j) * n_local);
+                            id[4 * j] = w.x; id[4 * j + 1] = w.y; id[4 * j + 2] = w.z; id[4 * j + 3] = w.w;
+                        }
                         float tx[NB], ty[NB], tz[NB];
-                        bool loc = true;
+                        uint32_t any_remote = 0u;
 #pragma unroll
-                        for (int j = 0; j < NB; ++j) loc = loc && (int)(id[j] >> 24) == rank;
-                        if (__all_sync(__activemask(), loc)) {
+                        for (int j = 0; j < NB; ++j) any_remote |= id[j];
+                        if (__all_sync(__activemask(), (any_remote >> 31) == 0u)) {
 #pragma unroll
                             for (int j = 0; j < NB; ++j) {
-                                const int ln = (int)(id[j] & 0xffffffu);
-                                tx[j] = sx[ln]; ty[j] = sy[ln]; tz[j] = sz[ln];
+                                const float *p = s3 + 3 * id[j];
+                                tx[j] = p[0]; ty[j] = p[1]; tz[j] = p[2];
                             }
                         } else {
 #pragma unroll
                             for (int j = 0; j < NB; ++j) {
-                                const int rn = (int)(id[j] >> 24), ln = (int)(id[j] & 0xffffffu);
-                                const float *px_ = cluster.map_shared_rank(sx, rn);
-                                tx[j] = px_[ln]; ty[j] = px_[ln + n_local]; tz[j] = px_[ln + 2 * n_local];
+                                const uint32_t v = id[j];
+                                const float *p = (v >> 31) ? cluster.map_shared_rank(s3, (int)((v >> 24) & 0x7fu)) : s3;
+                                p += 3 * (v & 0xffffffu);
+                                tx[j] = p[0]; ty[j] = p[1]; tz[j] = p[2];
                             }
                         }
 #pragma unroll
@@ -221,7 +226,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                     bool acc = true;
                     if (de > 0.0f) acc = expf(-beta * de) >= u24f(xr.z);
                     if (acc) {
-                        sx[l] = nx; sy[l] = ny; sz[l] = nz;
+                        s3[3 * l] = nx; s3[3 * l + 1] = ny; s3[3 * l + 2] = nz;
                         fE += de;
                         fX += dx; fY += dy; fZ += dz;
                     } else {
@@ -247,7 +252,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                 for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
                     int k, rem;
                     fdivmod(l, a.fd_pc, k, rem);
-                    obs_add(sx[l], sy[l], sz[l], __ldg(a.obs_atom + (k >> 3)), op, qx, qy, qz);
+                    obs_add(s3[3 * l], s3[3 * l + 1], s3[3 * l + 2], __ldg(a.obs_atom + (k >> 3)), op, qx, qy, qz);
                 }
                 v[4] = op; v[5] = qx; v[6] = qy; v[7] = qz;
             }
@@ -298,7 +303,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
                         float mx = 0.f, my = 0.f, mz = 0.f, op = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
                         for (int at = 0; at < a.na; ++at) {
                             const int l = at * cstride + cl;
-                            const float ox = sx[l], oy = sy[l], oz = sz[l];
+                            const float ox = s3[3 * l], oy = s3[3 * l + 1], oz = s3[3 * l + 2];
                             mx += ox; my += oy; mz += oz;
                             if (a.obs) obs_add(ox, oy, oz, __ldg(a.obs_atom + at), op, qx, qy, qz);
                         }
@@ -459,7 +464,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
         const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pz;
         const int orig = ((z * a.Ly + y) * a.Lx + x) * a.na + at;
         const size_t g = (size_t)__ldg(a.inv + orig) * a.R + r;
-        a.sx[g] = sx[l]; a.sy[g] = sy[l]; a.sz[g] = sz[l];
+        a.sx[g] = s3[3 * l]; a.sy[g] = s3[3 * l + 1]; a.sz[g] = s3[3 * l + 2];
     }
     // peers may still read this CTA's shared memory until every CTA is done
     cluster.sync();

@@ -39,7 +39,9 @@ inline size_t cluster_stencil_bytes(int nclass, int maxst)
 struct ClusterArgs {
     const ClusterStencil *stencil;  // device copy (header + entries)
     int stencil_words;              // size of that copy in 4-byte words
-    const uint32_t *nbidx;          // [rank][entry][local site]: (owner rank << 24) | local index
+    // [rank][entry / 4][local site][entry % 4]: the neighbour's local index,
+    // | 0x80000000 | (owner rank << 24) when the owner is a peer CTA
+    const uint32_t *nbidx;
     int Lx, Ly, Lz, na, N, R, nclass, pz;  // pz: z planes per CTA (even)
     int has_b, has_d, has_si, has_f;
     // state
