@@ -68,7 +68,7 @@ struct esp_handle {
     // cluster-resident path (translation-invariant lattices)
     int kernel_choice = 0;          // 0 auto, 1 ELL, 2 cluster
     bool cluster_ok = false;
-    int csize = 0, pz = 0, cthreads = 512;
+    int csize = 0, pz = 0, cthreads = 512, csites = 1;
     size_t cluster_smem = 0;
     int cl_maxst = 0;
     size_t cl_sbytes = 0;
@@ -422,7 +422,7 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     a.obs = measure ? h->obs : 0;
     a.obs_atom = h->d_obs_atom; a.obs_data = h->d_obs_data; a.obs_lsum = h->d_obs_lsum; a.obs_bin = h->d_obs_bin;
     a.obs_pm = h->d_obs_pm;
-    CK(launch_cluster(a, h->csize, h->cthreads, h->cluster_smem, h->st));
+    CK(launch_cluster(a, h->csize, h->cthreads, h->csites, h->cluster_smem, h->st));
     h->launches++;
     return ESP_OK;
 }
@@ -678,9 +678,9 @@ int d2h(esp_handle *h, void *dst, const void *src, size_t bytes)
 // Cluster geometries the GPU can run, cheapest first by a model: cs CTAs of
 // nt threads per replica, slabs of an even number of z planes, shared memory
 // within the per-CTA limit; cost = waves of R clusters (occupancy calculator)
-// x sites one SM holds per wave.
+// x CTAs one SM holds per wave x the length of a sweep in colour passes.
 struct ClusterGeom {
-    int cs, nt;
+    int cs, nt, S;
     double cost;
 };
 
@@ -688,18 +688,30 @@ std::vector<ClusterGeom> cluster_candidates(const esp_handle *h)
 {
     std::vector<ClusterGeom> out;
     if (!h->d_stencil_blob) return out;
-    const int nts[2] = {512, 256};
-    for (int nt : nts)
+    std::vector<int> per_colour;   // classes of each colour
+    for (int k = 0; k < (int)h->prep.class_colour.size(); ++k) {
+        const int c = h->prep.class_colour[k];
+        if (c >= (int)per_colour.size()) per_colour.resize(c + 1, 0);
+        ++per_colour[c];
+    }
+    const int geoms[3][2] = {{512, 1}, {512, 2}, {256, 1}};   // threads, sites per thread
+    for (const auto &tg : geoms)
         for (int cs = 1; cs <= 16; ++cs) {
+            const int nt = tg[0], S = tg[1];
             if (h->L[2] % (2 * cs) != 0) continue;
             const size_t smem = cluster_smem_bytes(h->N / cs, h->nf, h->obs ? 3 : 1, h->cl_sbytes);
             if (smem > 226 * 1024) continue;
-            const int active = cluster_max_active(cs, nt, smem, h->R);
+            const int active = cluster_max_active(cs, nt, S, smem, h->R);
             if (active <= 0) continue;
             const double waves = std::ceil((double)h->R / (double)active);
             const double conc = (double)std::min(h->R, active) * cs;
             const double per_sm = std::ceil(conc / (double)std::max(1, h->num_sms));
-            out.push_back({cs, nt, waves * ((double)h->N / cs) * per_sm});
+            // colour passes of a sweep; a pass with two sites per thread
+            // takes ~1.85 times one with one site (measured)
+            const int64_t per_class = (int64_t)(h->L[0] / 2) * (h->L[1] / 2) * (h->L[2] / cs / 2);
+            double passes = 0.0;
+            for (int n : per_colour) passes += (double)ceil_div(n * per_class, (int64_t)S * nt) * (S == 2 ? 1.85 : 1.0);
+            out.push_back({cs, nt, S, waves * per_sm * passes});
         }
     std::stable_sort(out.begin(), out.end(), [](const ClusterGeom &a, const ClusterGeom &b) { return a.cost < b.cost; });
     return out;
@@ -819,12 +831,12 @@ int tile_setup(esp_handle *h)
 
 // Set up the cluster path for cs CTAs of nt threads: slab height, shared
 // memory, the neighbour table of every CTA rank.
-int cluster_geometry(esp_handle *h, int cs, int nt)
+int cluster_geometry(esp_handle *h, int cs, int nt, int S)
 {
     const int maxst = h->cl_maxst;
     const int pz = h->L[2] / cs, n_local = h->N / cs;
     const size_t smem = cluster_smem_bytes(n_local, h->nf, h->obs ? 3 : 1, h->cl_sbytes);
-    CK(cluster_configure(smem, cs, nt));
+    CK(cluster_configure(smem, cs, nt, S));
     const int Lx = h->L[0], Ly = h->L[1], Lz = h->L[2], Hx = Lx / 2, Hy = Ly / 2, Hzl = pz / 2;
     const int per_class = Hx * Hy * Hzl;
     // stencil entry e of local site l on rank q: its local index, with
@@ -859,6 +871,7 @@ int cluster_geometry(esp_handle *h, int cs, int nt)
     if (rc) return rc;
     h->csize = cs;
     h->cthreads = nt;
+    h->csites = S;
     h->pz = pz;
     h->cluster_smem = smem;
     h->cluster_ok = true;
@@ -1122,7 +1135,7 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
     h->ntiles = 0;
     if (h->d_stencil_blob) {
         const std::vector<ClusterGeom> c = cluster_candidates(h);
-        if (!c.empty() && (rc = cluster_geometry(h, c[0].cs, c[0].nt))) return rc;
+        if (!c.empty() && (rc = cluster_geometry(h, c[0].cs, c[0].nt, c[0].S))) return rc;
         if ((rc = tile_setup(h))) return rc;
     }
     h->have_tables = true;
@@ -1435,7 +1448,7 @@ int esp_get_tile_geometry(const esp_handle *h, int32_t *tile, int32_t *replicas,
     return ESP_OK;
 }
 
-int esp_set_cluster_geometry(esp_handle *h, int32_t cluster_size, int32_t threads)
+int esp_set_cluster_geometry(esp_handle *h, int32_t cluster_size, int32_t threads, int32_t sites_per_thread)
 {
     if (!h) return ESP_EINVAL;
     if (!h->have_tables || !h->d_stencil_blob) {
@@ -1443,20 +1456,21 @@ int esp_set_cluster_geometry(esp_handle *h, int32_t cluster_size, int32_t thread
         return ESP_EINVAL;
     }
     for (const ClusterGeom &g : cluster_candidates(h))
-        if (g.cs == cluster_size && g.nt == threads) {
+        if (g.cs == cluster_size && g.nt == threads && g.S == sites_per_thread) {
             int rc = fold(h);
             if (rc) return rc;
-            return cluster_geometry(h, cluster_size, threads);
+            return cluster_geometry(h, cluster_size, threads, sites_per_thread);
         }
     h->err = "cluster geometry not possible for this lattice on this GPU";
     return ESP_EINVAL;
 }
 
-int esp_get_cluster_geometry(const esp_handle *h, int32_t *cluster_size, int32_t *threads)
+int esp_get_cluster_geometry(const esp_handle *h, int32_t *cluster_size, int32_t *threads, int32_t *sites_per_thread)
 {
     if (!h || !cluster_size || !threads) return ESP_EINVAL;
     *cluster_size = h->cluster_ok ? h->csize : 0;
     *threads = h->cluster_ok ? h->cthreads : 0;
+    if (sites_per_thread) *sites_per_thread = h->cluster_ok ? h->csites : 0;
     return ESP_OK;
 }
 
@@ -1749,9 +1763,9 @@ int esp_set_observables(esp_handle *h, int32_t flags, const double *orderparam_a
     if (h->cluster_ok) {
         const std::vector<ClusterGeom> c = cluster_candidates(h);
         bool same = false;
-        for (const ClusterGeom &g : c) same = same || (g.cs == h->csize && g.nt == h->cthreads);
-        if (same) rc = cluster_geometry(h, h->csize, h->cthreads);
-        else if (!c.empty()) rc = cluster_geometry(h, c[0].cs, c[0].nt);
+        for (const ClusterGeom &g : c) same = same || (g.cs == h->csize && g.nt == h->cthreads && g.S == h->csites);
+        if (same) rc = cluster_geometry(h, h->csize, h->cthreads, h->csites);
+        else if (!c.empty()) rc = cluster_geometry(h, c[0].cs, c[0].nt, c[0].S);
         else h->cluster_ok = false;
         if (rc) return rc;
     }
@@ -2674,11 +2688,11 @@ int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out)
     for (size_t i = 0; i < n; ++i) {
         esp_handle *h = b->hs[i];
         if (h->proposal != 0) continue;
-        struct Cand { int kind, cs, nt; };
-        std::vector<Cand> cands{{1, 0, 0}};
+        struct Cand { int kind, cs, nt, S; };
+        std::vector<Cand> cands{{1, 0, 0, 0}};
         if (h->cluster_ok) {
             const std::vector<ClusterGeom> g = cluster_candidates(h);
-            for (size_t k = 0; k < g.size() && k < 3; ++k) cands.push_back({2, g[k].cs, g[k].nt});
+            for (size_t k = 0; k < g.size() && k < 3; ++k) cands.push_back({2, g[k].cs, g[k].nt, g[k].S});
         }
         if (h->tile_ok) {
             // kinds 4 / 5: cs, nt carry the tile edge and the replicas per CTA
@@ -2687,10 +2701,10 @@ int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out)
             for (size_t k = 0; k < g.size() && k < 3; ++k) cands.push_back({g[k].pipe ? 5 : 4, g[k].T, g[k].G});
         }
         double best = 1e300, best_cl = 1e300;
-        Cand pick{1, 0, 0};
+        Cand pick{1, 0, 0, 0};
         for (const Cand &c : cands) {
             int rc = ESP_OK;
-            if (c.kind == 2 && (rc = cluster_geometry(h, c.cs, c.nt))) return batch_fail(b, "cluster geometry", h);
+            if (c.kind == 2 && (rc = cluster_geometry(h, c.cs, c.nt, c.S))) return batch_fail(b, "cluster geometry", h);
             if (c.kind >= 4 && (rc = tile_geometry(h, c.cs, c.nt, c.kind == 5))) return batch_fail(b, "tile geometry", h);
             if ((rc = esp_set_sweep_kernel(h, std::min(c.kind, 4)))) return batch_fail(b, "esp_set_sweep_kernel", h);
             esp_batch one;
@@ -2706,13 +2720,14 @@ int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out)
         }
         if (out && out->cluster_us) out->cluster_us[i] = cands.size() > 1 ? best_cl : -1.0;
         int rc = ESP_OK;
-        if (pick.kind == 2 && (rc = cluster_geometry(h, pick.cs, pick.nt))) return batch_fail(b, "cluster geometry", h);
+        if (pick.kind == 2 && (rc = cluster_geometry(h, pick.cs, pick.nt, pick.S))) return batch_fail(b, "cluster geometry", h);
         if (pick.kind >= 4 && (rc = tile_geometry(h, pick.cs, pick.nt, pick.kind == 5)))
             return batch_fail(b, "tile geometry", h);
         if ((rc = esp_set_sweep_kernel(h, std::min(pick.kind, 4)))) return batch_fail(b, "esp_set_sweep_kernel", h);
         if (out && out->kernel) out->kernel[i] = std::min(pick.kind, 4);
         if (out && out->cluster_size) out->cluster_size[i] = h->cluster_ok ? h->csize : 0;
         if (out && out->cluster_threads) out->cluster_threads[i] = h->cluster_ok ? h->cthreads : 0;
+        if (out && out->cluster_sites) out->cluster_sites[i] = h->cluster_ok ? h->csites : 0;
     }
     // 2. units per graph replay
     const int cands[4] = {1, 2, 4, 8};

@@ -24,11 +24,16 @@ namespace cg = cooperative_groups;
 
 namespace esp {
 
-// NT threads per CTA: 512 (one CTA per SM) or 256 (two per SM), both within
-// 128 registers per thread.
-template <int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArgs a)
+// NT threads per CTA and S sites per thread in a colour pass: 512 x 1 (one
+// CTA per SM), 256 x 1 (two per SM), or 512 x 2, whose threads update two
+// sites of a colour with interleaved instruction streams (fewer, evenly
+// loaded passes when a colour holds between 1 and 2 times 512 sites).  All
+// within 128 registers per thread: a sub-partition of the SM that holds four
+// warps has 16,384 registers for them.
+template <int NT, int S>
+__global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const ClusterArgs a)
 {
+    static_assert(NT % 32 == 0 && NT <= 640, "the reduction scratch holds at most 20 warps");
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     const int csize = (int)cluster.num_blocks();
@@ -108,6 +113,137 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
         m_run[0] = a.m_run[3 * r]; m_run[1] = a.m_run[3 * r + 1]; m_run[2] = a.m_run[3 * r + 2];
     }
 
+    // Metropolis updates of the sites of items its[0..SN) of a colour pass
+    // (class_order from c0): local field from the stencil, trial, test
+    // (metropolis, get_quant.F90:52-182, delta_energy_get :264-337), each
+    // site's arithmetic in the same order as k_sweep_ell
+    auto update = [&](auto snc, const int (&its)[decltype(snc)::value], int c0, uint32_t sw_lo, uint32_t sw_hi,
+                      float &fE, float &fX, float &fY, float &fZ) {
+        constexpr int SN = decltype(snc)::value;
+        int l[SN], at[SN], orig[SN];
+        float ox[SN], oy[SN], oz[SN];
+        float gx[SN], gy[SN], gz[SN], qxx[SN], qyy[SN], qzz[SN], qxy[SN], qxz[SN], qyz[SN];
+        const ClusterNbr *nb[SN];
+        const uint4 *tab[SN];
+        int cnt_k = 0;
+#pragma unroll
+        for (int s = 0; s < SN; ++s) {
+            int ci, rem, q1, hx, hy, hzl;
+            fdivmod(its[s], a.fd_pc, ci, rem);
+            const int k = st->class_order[c0 + ci];
+            l[s] = k * per_class + rem;
+            fdivmod(rem, a.fd_hx, q1, hx);
+            fdivmod(q1, a.fd_hy, hzl, hy);
+            at[s] = k >> 3;
+            const int px = (k >> 2) & 1, py = (k >> 1) & 1, pzb = k & 1;
+            const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pzb;
+            orig[s] = ((z * a.Ly + y) * a.Lx + x) * a.na + at[s];
+            ox[s] = s3[3 * l[s]]; oy[s] = s3[3 * l[s] + 1]; oz[s] = s3[3 * l[s] + 2];
+            gx[s] = gy[s] = gz[s] = 0.f;
+            qxx[s] = qyy[s] = qzz[s] = qxy[s] = qxz[s] = qyz[s] = 0.f;
+            // neighbour e of site l from the precomputed table shared by every
+            // replica's cluster, four entries per 16-byte word: the local
+            // index, with bit 31 set and the owner rank in bits 24-30 when the
+            // neighbour lives in a peer CTA; lists are padded to multiples of
+            // 8 with zero-coupling self entries
+            cnt_k = st->count[k];   // equal for the SN sites
+            nb[s] = nbt + k * st->maxst;
+            tab[s] = reinterpret_cast<const uint4 *>(a.nbidx) + (size_t)rank * (st->maxst >> 2) * n_local + l[s];
+        }
+        // a batch of NB neighbours of every site: read from this CTA's shared
+        // memory when every lane of the warp finds all of them here (warps
+        // cover slab planes, so this is the common case), else through the
+        // cluster window
+        auto batch = [&](auto nbc, int e0) {
+            constexpr int NB = decltype(nbc)::value;
+            constexpr int NQ = (NB + 3) / 4;
+            uint32_t id[SN][4 * NQ];
+#pragma unroll
+            for (int s = 0; s < SN; ++s)
+#pragma unroll
+                for (int j = 0; j < NQ; ++j) {
+                    const uint4 w = __ldg(tab[s] + (size_t)((e0 >> 2) + j) * n_local);
+                    id[s][4 * j] = w.x; id[s][4 * j + 1] = w.y; id[s][4 * j + 2] = w.z; id[s][4 * j + 3] = w.w;
+                }
+            float tx[SN][NB], ty[SN][NB], tz[SN][NB];
+            uint32_t any_remote = 0u;
+#pragma unroll
+            for (int s = 0; s < SN; ++s)
+#pragma unroll
+                for (int j = 0; j < NB; ++j) any_remote |= id[s][j];
+            if (__all_sync(__activemask(), (any_remote >> 31) == 0u)) {
+#pragma unroll
+                for (int s = 0; s < SN; ++s)
+#pragma unroll
+                    for (int j = 0; j < NB; ++j) {
+                        const float *p = s3 + 3 * id[s][j];
+                        tx[s][j] = p[0]; ty[s][j] = p[1]; tz[s][j] = p[2];
+                    }
+            } else {
+#pragma unroll
+                for (int s = 0; s < SN; ++s)
+#pragma unroll
+                    for (int j = 0; j < NB; ++j) {
+                        const uint32_t v = id[s][j];
+                        const float *p = (v >> 31) ? cluster.map_shared_rank(s3, (int)((v >> 24) & 0x7fu)) : s3;
+                        p += 3 * (v & 0xffffffu);
+                        tx[s][j] = p[0]; ty[s][j] = p[1]; tz[s][j] = p[2];
+                    }
+            }
+#pragma unroll
+            for (int s = 0; s < SN; ++s)
+#pragma unroll
+                for (int j = 0; j < NB; ++j) {
+                    const ClusterNbr &se = nb[s][e0 + j];
+                    const float J = se.J;
+                    gx[s] = fmaf(-J, tx[s][j], gx[s]); gy[s] = fmaf(-J, ty[s][j], gy[s]); gz[s] = fmaf(-J, tz[s][j], gz[s]);
+                    if (a.has_b)
+                        bq_form(se.B, tx[s][j], ty[s][j], tz[s][j], qxx[s], qyy[s], qzz[s], qxy[s], qxz[s], qyz[s]);
+                    if (a.has_d) dm_field(se.Dx, se.Dy, se.Dz, tx[s][j], ty[s][j], tz[s][j], gx[s], gy[s], gz[s]);
+                }
+        };
+        int e0 = 0;
+        for (; e0 + 8 <= cnt_k; e0 += 8) batch(std::integral_constant<int, 8>{}, e0);
+        // the last partial batch at its exact size (no padding work)
+        switch (cnt_k - e0) {
+        case 1: batch(std::integral_constant<int, 1>{}, e0); break;
+        case 2: batch(std::integral_constant<int, 2>{}, e0); break;
+        case 3: batch(std::integral_constant<int, 3>{}, e0); break;
+        case 4: batch(std::integral_constant<int, 4>{}, e0); break;
+        case 5: batch(std::integral_constant<int, 5>{}, e0); break;
+        case 6: batch(std::integral_constant<int, 6>{}, e0); break;
+        case 7: batch(std::integral_constant<int, 7>{}, e0); break;
+        default: break;
+        }
+        float nx[SN], ny[SN], nz[SN], de[SN];
+        bool acc[SN];
+#pragma unroll
+        for (int s = 0; s < SN; ++s) {
+            if (a.has_si) si_form(st->si[at[s]], qxx[s], qyy[s], qzz[s], qxy[s], qxz[s], qyz[s]);
+            if (a.has_f) {
+                const float4 f = st->fld[at[s]];
+                gx[s] = __fadd_rn(gx[s], f.x); gy[s] = __fadd_rn(gy[s], f.y); gz[s] = __fadd_rn(gz[s], f.z);
+            }
+            const Philox4 xr = philox4x32_10((uint32_t)orig[s], (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
+            trial_spin(a.mode, a.tilt, st->mag[at[s]], ox[s], oy[s], oz[s], xr.x, xr.y, nx[s], ny[s], nz[s]);
+            const float d = delta_energy(a.has_b || a.has_si, gx[s], gy[s], gz[s], qxx[s], qyy[s], qzz[s], qxy[s],
+                                         qxz[s], qyz[s], ox[s], oy[s], oz[s], nx[s], ny[s], nz[s]);
+            de[s] = d;
+            acc[s] = true;
+            if (d > 0.0f) acc[s] = expf(-beta * d) >= u24f(xr.z);
+        }
+#pragma unroll
+        for (int s = 0; s < SN; ++s) {
+            if (acc[s]) {
+                s3[3 * l[s]] = nx[s]; s3[3 * l[s] + 1] = ny[s]; s3[3 * l[s] + 2] = nz[s];
+                fE += de[s];
+                fX += nx[s] - ox[s]; fY += ny[s] - oy[s]; fZ += nz[s] - oz[s];
+            } else {
+                ++nrej;
+            }
+        }
+    };
+
     for (int m = 0; m < a.n_meas; ++m) {
         for (int sm = 0; sm < a.steps_measure; ++sm) {
             const unsigned long long sweep = sweep_base + (unsigned long long)m * a.steps_measure + sm;
@@ -117,120 +253,34 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_sweep_cluster(const ClusterArg
             for (int c = 0; c < st->ncolour; ++c) {
                 const int c0 = st->colour_start[c];
                 const int items = (st->colour_start[c + 1] - c0) * per_class;
-                for (int it = threadIdx.x; it < items; it += blockDim.x) {
-                    int ci, rem, q1, hx, hy, hzl;
-                    fdivmod(it, a.fd_pc, ci, rem);
-                    const int k = st->class_order[c0 + ci];
-                    const int l = k * per_class + rem;
-                    fdivmod(rem, a.fd_hx, q1, hx);
-                    fdivmod(q1, a.fd_hy, hzl, hy);
-                    const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pzb = k & 1;
-                    const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pzb;
-                    const float ox = s3[3 * l], oy = s3[3 * l + 1], oz = s3[3 * l + 2];
-                    float gx = 0.f, gy = 0.f, gz = 0.f;
-                    float qxx = 0.f, qyy = 0.f, qzz = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
-                    // neighbour e of site l from the precomputed table shared by
-                    // every replica's cluster, four entries per 16-byte word:
-                    // the local index, with bit 31 set and the owner rank in
-                    // bits 24-30 when the neighbour lives in a peer CTA; lists
-                    // are padded to multiples of 8 with zero-coupling self entries
-                    const int cnt_k = st->count[k];
-                    const ClusterNbr *nb = nbt + k * st->maxst;
-                    const uint4 *tab = reinterpret_cast<const uint4 *>(a.nbidx) + (size_t)rank * (st->maxst >> 2) * n_local + l;
-                    // a batch of NB neighbours: read from this CTA's shared
-                    // memory when every lane of the warp finds all of them
-                    // here (warps cover slab planes, so this is the common
-                    // case), else through the cluster window
-                    auto batch = [&](auto nbc, int e0) {
-                        constexpr int NB = decltype(nbc)::value;
-                        constexpr int NQ = (NB + 3) / 4;
-                        uint32_t id[4 * NQ];
+                // S sites of the colour per thread, updated together (their
+                // instruction streams interleave); a thread whose sites have
+                // different stencil lengths, or that has one site left,
+                // updates them one at a time
+                for (int it0 = threadIdx.x; it0 < items; it0 += S * NT) {
+                    int its[S];
 #pragma unroll
-                        for (int j = 0; j < NQ; ++j) {
-                            const uint4 w = __ldg(tab + (size_t)((e0 >> 2) + j) * n_local);
-                            id[4 * j] = w.x; id[4 * j + 1] = w.y; id[4 * j + 2] = w.z; id[4 * j + 3] = w.w;
+                    for (int s = 0; s < S; ++s) its[s] = it0 + s * NT;
+                    if constexpr (S == 1) {
+                        update(std::integral_constant<int, 1>{}, its, c0, sw_lo, sw_hi, fE, fX, fY, fZ);
+                    } else {
+                        bool together = its[S - 1] < items;
+                        if (together) {
+                            const int cnt0 = st->count[st->class_order[c0 + its[0] / per_class]];
+#pragma unroll
+                            for (int s = 1; s < S; ++s)
+                                together = together && st->count[st->class_order[c0 + its[s] / per_class]] == cnt0;
                         }
-                        float tx[NB], ty[NB], tz[NB];
-                        uint32_t any_remote = 0u;
-#pragma unroll
-                        for (int j = 0; j < NB; ++j) any_remote |= id[j];
-                        if (__all_sync(__activemask(), (any_remote >> 31) == 0u)) {
-#pragma unroll
-                            for (int j = 0; j < NB; ++j) {
-                                const float *p = s3 + 3 * id[j];
-                                tx[j] = p[0]; ty[j] = p[1]; tz[j] = p[2];
-                            }
+                        if (together) {
+                            update(std::integral_constant<int, S>{}, its, c0, sw_lo, sw_hi, fE, fX, fY, fZ);
                         } else {
 #pragma unroll
-                            for (int j = 0; j < NB; ++j) {
-                                const uint32_t v = id[j];
-                                const float *p = (v >> 31) ? cluster.map_shared_rank(s3, (int)((v >> 24) & 0x7fu)) : s3;
-                                p += 3 * (v & 0xffffffu);
-                                tx[j] = p[0]; ty[j] = p[1]; tz[j] = p[2];
-                            }
+                            for (int s = 0; s < S; ++s)
+                                if (its[s] < items) {
+                                    const int one[1] = {its[s]};
+                                    update(std::integral_constant<int, 1>{}, one, c0, sw_lo, sw_hi, fE, fX, fY, fZ);
+                                }
                         }
-#pragma unroll
-                        for (int j = 0; j < NB; ++j) {
-                            const ClusterNbr &se = nb[e0 + j];
-                            const float J = se.J;
-                            gx = fmaf(-J, tx[j], gx); gy = fmaf(-J, ty[j], gy); gz = fmaf(-J, tz[j], gz);
-                            if (a.has_b) {
-                                const float Bv = se.B;
-                                const float bx = Bv * tx[j], by = Bv * ty[j], bz = Bv * tz[j];
-                                qxx = fmaf(bx, tx[j], qxx); qyy = fmaf(by, ty[j], qyy); qzz = fmaf(bz, tz[j], qzz);
-                                qxy = fmaf(bx, ty[j], qxy); qxz = fmaf(bx, tz[j], qxz); qyz = fmaf(by, tz[j], qyz);
-                            }
-                            if (a.has_d) {
-                                const float dx = se.Dx, dy = se.Dy, dz = se.Dz;
-                                gx += ty[j] * dz - tz[j] * dy;
-                                gy += tz[j] * dx - tx[j] * dz;
-                                gz += tx[j] * dy - ty[j] * dx;
-                            }
-                        }
-                    };
-                    int e0 = 0;
-                    for (; e0 + 8 <= cnt_k; e0 += 8) batch(std::integral_constant<int, 8>{}, e0);
-                    // the last partial batch at its exact size (no padding work)
-                    switch (cnt_k - e0) {
-                    case 1: batch(std::integral_constant<int, 1>{}, e0); break;
-                    case 2: batch(std::integral_constant<int, 2>{}, e0); break;
-                    case 3: batch(std::integral_constant<int, 3>{}, e0); break;
-                    case 4: batch(std::integral_constant<int, 4>{}, e0); break;
-                    case 5: batch(std::integral_constant<int, 5>{}, e0); break;
-                    case 6: batch(std::integral_constant<int, 6>{}, e0); break;
-                    case 7: batch(std::integral_constant<int, 7>{}, e0); break;
-                    default: break;
-                    }
-                    if (a.has_si) {
-                        const float4 s = st->si[at];
-                        const float dx = s.w * s.x, dy = s.w * s.y, dz = s.w * s.z;
-                        qxx = fmaf(dx, s.x, qxx); qyy = fmaf(dy, s.y, qyy); qzz = fmaf(dz, s.z, qzz);
-                        qxy = fmaf(dx, s.y, qxy); qxz = fmaf(dx, s.z, qxz); qyz = fmaf(dy, s.z, qyz);
-                    }
-                    if (a.has_f) {
-                        const float4 f = st->fld[at];
-                        gx += f.x; gy += f.y; gz += f.z;
-                    }
-                    const int orig = ((z * a.Ly + y) * a.Lx + x) * a.na + at;
-                    const Philox4 xr = philox4x32_10((uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
-                    float nx, ny, nz;
-                    trial_spin(a.mode, a.tilt, st->mag[at], ox, oy, oz, xr.x, xr.y, nx, ny, nz);
-                    const float dx = nx - ox, dy = ny - oy, dz = nz - oz;
-                    float de = gx * dx + gy * dy + gz * dz;
-                    if (a.has_b || a.has_si) {
-                        const float px2 = nx + ox, py2 = ny + oy, pz2 = nz + oz;
-                        de += dx * (qxx * px2 + qxy * py2 + qxz * pz2)
-                            + dy * (qxy * px2 + qyy * py2 + qyz * pz2)
-                            + dz * (qxz * px2 + qyz * py2 + qzz * pz2);
-                    }
-                    bool acc = true;
-                    if (de > 0.0f) acc = expf(-beta * de) >= u24f(xr.z);
-                    if (acc) {
-                        s3[3 * l] = nx; s3[3 * l + 1] = ny; s3[3 * l + 2] = nz;
-                        fE += de;
-                        fX += dx; fY += dy; fZ += dz;
-                    } else {
-                        ++nrej;
                     }
                 }
                 cluster.sync();
@@ -480,24 +530,29 @@ namespace {
 
 using ClusterKernel = void (*)(ClusterArgs);
 
-ClusterKernel cluster_kernel(int nt) { return nt == 256 ? k_sweep_cluster<256> : k_sweep_cluster<512>; }
+ClusterKernel cluster_kernel(int nt, int S)
+{
+    return nt == 256 ? k_sweep_cluster<256, 1> : (S == 2 ? k_sweep_cluster<512, 2> : k_sweep_cluster<512, 1>);
+}
 
 }  // namespace
 
-cudaError_t cluster_configure(size_t smem, int csize, int nt)
+bool cluster_threads_ok(int nt, int S) { return (nt == 256 && S == 1) || (nt == 512 && (S == 1 || S == 2)); }
+
+cudaError_t cluster_configure(size_t smem, int csize, int nt, int S)
 {
-    if (nt != 256 && nt != 512) return cudaErrorInvalidValue;
-    const ClusterKernel k = cluster_kernel(nt);
+    if (!cluster_threads_ok(nt, S)) return cudaErrorInvalidValue;
+    const ClusterKernel k = cluster_kernel(nt, S);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (csize > 8) e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     return e;
 }
 
-int cluster_max_active(int csize, int nt, size_t smem, int R)
+int cluster_max_active(int csize, int nt, int S, size_t smem, int R)
 {
-    if (nt != 256 && nt != 512) return 0;
-    const ClusterKernel k = cluster_kernel(nt);
+    if (!cluster_threads_ok(nt, S)) return 0;
+    const ClusterKernel k = cluster_kernel(nt, S);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
@@ -525,9 +580,9 @@ int cluster_max_active(int csize, int nt, size_t smem, int R)
     return n;
 }
 
-cudaError_t launch_cluster(const ClusterArgs &a, int csize, int nt, size_t smem, cudaStream_t st)
+cudaError_t launch_cluster(const ClusterArgs &a, int csize, int nt, int S, size_t smem, cudaStream_t st)
 {
-    if (nt != 256 && nt != 512) return cudaErrorInvalidValue;
+    if (!cluster_threads_ok(nt, S)) return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(csize * a.R, 1, 1);
     cfg.blockDim = dim3(nt, 1, 1);
@@ -540,7 +595,7 @@ cudaError_t launch_cluster(const ClusterArgs &a, int csize, int nt, size_t smem,
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, cluster_kernel(nt), a);
+    return cudaLaunchKernelEx(&cfg, cluster_kernel(nt, S), a);
 }
 
 }  // namespace esp

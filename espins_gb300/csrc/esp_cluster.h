@@ -91,9 +91,12 @@ constexpr int kClusterMaxLev = 32;
 constexpr int kClusterAccDoubles = 12 + kClusterMaxLev / 2 + 8 * kClusterMaxLev;
 size_t cluster_smem_bytes(int n_local, int nf, int nhist, size_t stencil_bytes);
 // nt: threads per CTA, 256 or 512
-cudaError_t cluster_configure(size_t smem, int csize, int nt);
+// Thread geometries of the kernel: nt threads per CTA, S sites of a colour
+// pass per thread (updated together): (256, 1), (512, 1), (512, 2).
+bool cluster_threads_ok(int nt, int S);
+cudaError_t cluster_configure(size_t smem, int csize, int nt, int S);
 // Clusters of csize CTAs of nt threads with `smem` bytes each that fit on the GPU at once.
-int cluster_max_active(int csize, int nt, size_t smem, int R);
-cudaError_t launch_cluster(const ClusterArgs &a, int csize, int nt, size_t smem, cudaStream_t st);
+int cluster_max_active(int csize, int nt, int S, size_t smem, int R);
+cudaError_t launch_cluster(const ClusterArgs &a, int csize, int nt, int S, size_t smem, cudaStream_t st);
 
 }  // namespace esp

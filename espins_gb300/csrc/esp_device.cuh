@@ -47,6 +47,11 @@ __host__ __device__ __forceinline__ double u53(uint32_t a, uint32_t b)
     return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
 }
 
+// Every sweep kernel evaluates the trial, the local field and the energy
+// change through the functions below, written without implicit contraction
+// (explicit fmaf / __fmul_rn / __fadd_rn), so all kernels round the same way
+// and follow the same trajectory from the same state.
+
 // Trial spin of metropolis (get_quant.F90:80-162) in FP32.
 //  mode 0 'random': cos(theta) = 2u0-1, phi = 2 pi u1, length |mag|
 //  mode 1 'const' : theta = tilt*acos(2u0-1) about the old direction,
@@ -57,26 +62,74 @@ __device__ __forceinline__ void trial_spin(int mode, float tilt, float mag, floa
     const float u0 = u24f(x0), u1 = u24f(x1);
     float sphi, cphi;
     sincospif(2.0f * u1, &sphi, &cphi);
+    const float c = fmaf(2.0f, u0, -1.0f);   // exact: u0 has 24 bits
     if (mode == 0) {
-        const float c = 2.0f * u0 - 1.0f;
-        const float s = sqrtf(fmaxf(0.0f, 1.0f - c * c));
-        nx = mag * s * cphi;
-        ny = mag * s * sphi;
-        nz = mag * c;
+        const float s = sqrtf(fmaxf(0.0f, fmaf(-c, c, 1.0f)));
+        const float ms = __fmul_rn(mag, s);
+        nx = __fmul_rn(ms, cphi);
+        ny = __fmul_rn(ms, sphi);
+        nz = __fmul_rn(mag, c);
     } else {
-        const float theta = tilt * acosf(2.0f * u0 - 1.0f);
+        const float theta = __fmul_rn(tilt, acosf(c));
         float st, ct;
         sincosf(theta, &st, &ct);
-        const float tx = st * cphi, ty = st * sphi, tz = ct;
-        const float sxy = sqrtf(ox * ox + oy * oy);
+        const float tx = __fmul_rn(st, cphi), ty = __fmul_rn(st, sphi), tz = ct;
+        const float sxy = sqrtf(fmaf(oy, oy, __fmul_rn(ox, ox)));
         float c0 = 1.0f, s0 = 0.0f;
         if (sxy > 1e-8f) { c0 = ox / sxy; s0 = oy / sxy; }
-        const float inv = rsqrtf(ox * ox + oy * oy + oz * oz);
-        const float ax = ox * inv, ay = oy * inv, az = oz * inv;
-        nx = mag * (c0 * az * tx - s0 * ty + ax * tz);
-        ny = mag * (s0 * az * tx + c0 * ty + ay * tz);
-        nz = mag * (-sqrtf(ax * ax + ay * ay) * tx + az * tz);
+        const float inv = rsqrtf(fmaf(oz, oz, fmaf(oy, oy, __fmul_rn(ox, ox))));
+        const float ax = __fmul_rn(ox, inv), ay = __fmul_rn(oy, inv), az = __fmul_rn(oz, inv);
+        nx = __fmul_rn(mag, fmaf(ax, tz, fmaf(-s0, ty, __fmul_rn(__fmul_rn(c0, az), tx))));
+        ny = __fmul_rn(mag, fmaf(ay, tz, fmaf(c0, ty, __fmul_rn(__fmul_rn(s0, az), tx))));
+        nz = __fmul_rn(mag, fmaf(az, tz, __fmul_rn(-sqrtf(fmaf(ay, ay, __fmul_rn(ax, ax))), tx)));
     }
+}
+
+// DM share of one neighbour in the local field, g += s_k x D_ik
+// (delta_energy_get, get_quant.F90:327-333)
+__device__ __forceinline__ void dm_field(float dx, float dy, float dz, float tx, float ty, float tz, float &gx,
+                                         float &gy, float &gz)
+{
+    gx = fmaf(tz, -dy, fmaf(ty, dz, gx));
+    gy = fmaf(tx, -dz, fmaf(tz, dx, gy));
+    gz = fmaf(ty, -dx, fmaf(tx, dy, gz));
+}
+
+// Biquadratic share of one neighbour in the quadratic form Q (get_quant.F90:316-325)
+__device__ __forceinline__ void bq_form(float Bv, float tx, float ty, float tz, float &qxx, float &qyy, float &qzz,
+                                        float &qxy, float &qxz, float &qyz)
+{
+    const float bx = __fmul_rn(Bv, tx), by = __fmul_rn(Bv, ty), bz = __fmul_rn(Bv, tz);
+    qxx = fmaf(bx, tx, qxx); qyy = fmaf(by, ty, qyy); qzz = fmaf(bz, tz, qzz);
+    qxy = fmaf(bx, ty, qxy); qxz = fmaf(bx, tz, qxz); qyz = fmaf(by, tz, qyz);
+}
+
+// Single-ion share of Q: Delta a a^T (get_quant.F90:306-314); s = (a, Delta)
+__device__ __forceinline__ void si_form(float4 s, float &qxx, float &qyy, float &qzz, float &qxy, float &qxz,
+                                        float &qyz)
+{
+    const float dx = __fmul_rn(s.w, s.x), dy = __fmul_rn(s.w, s.y), dz = __fmul_rn(s.w, s.z);
+    qxx = fmaf(dx, s.x, qxx); qyy = fmaf(dy, s.y, qyy); qzz = fmaf(dz, s.z, qzz);
+    qxy = fmaf(dx, s.y, qxy); qxz = fmaf(dx, s.z, qxz); qyz = fmaf(dy, s.z, qyz);
+}
+
+// Energy change of s_old -> s_new with local field g and quadratic form Q:
+// g.d + d^T Q (s_new + s_old), d = s_new - s_old (the local form of
+// delta_energy_get); quad = false skips the Q term
+__device__ __forceinline__ float delta_energy(bool quad, float gx, float gy, float gz, float qxx, float qyy, float qzz,
+                                              float qxy, float qxz, float qyz, float ox, float oy, float oz, float nx,
+                                              float ny, float nz)
+{
+    const float dx = __fsub_rn(nx, ox), dy = __fsub_rn(ny, oy), dz = __fsub_rn(nz, oz);
+    float de = fmaf(gz, dz, fmaf(gy, dy, __fmul_rn(gx, dx)));
+    if (quad) {
+        const float px = __fadd_rn(nx, ox), py = __fadd_rn(ny, oy), pz = __fadd_rn(nz, oz);
+        const float ax = fmaf(qxz, pz, fmaf(qxy, py, __fmul_rn(qxx, px)));
+        const float ay = fmaf(qyz, pz, fmaf(qyy, py, __fmul_rn(qxy, px)));
+        const float az = fmaf(qzz, pz, fmaf(qyz, py, __fmul_rn(qxz, px)));
+        de = fmaf(dz, az, fmaf(dy, ay, fmaf(dx, ax, de)));
+    }
+    return de;
 }
 
 // Bin of a unit cell's value m on the P(M) grid of Pm_get

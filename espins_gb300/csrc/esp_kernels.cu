@@ -154,47 +154,26 @@ __global__ void __launch_bounds__(256) k_sweep_ell(const SweepArgs a)
                     const size_t e = (size_t)(k0 + j) * a.N + p;
                     const float J = __ldg(a.J + e);
                     gx = fmaf(-J, tx[j], gx); gy = fmaf(-J, ty[j], gy); gz = fmaf(-J, tz[j], gz);
-                    if (HB) {
-                        const float Bv = __ldg(a.B + e);
-                        const float bx = Bv * tx[j], by = Bv * ty[j], bz = Bv * tz[j];
-                        qxx = fmaf(bx, tx[j], qxx); qyy = fmaf(by, ty[j], qyy); qzz = fmaf(bz, tz[j], qzz);
-                        qxy = fmaf(bx, ty[j], qxy); qxz = fmaf(bx, tz[j], qxz); qyz = fmaf(by, tz[j], qyz);
-                    }
-                    if (HD) {
-                        const float dx = __ldg(a.Dx + e), dy = __ldg(a.Dy + e), dz = __ldg(a.Dz + e);
-                        // s_k x D_ik (the DM term of delta_energy_get as s_i . (s_k x D))
-                        gx += ty[j] * dz - tz[j] * dy;
-                        gy += tz[j] * dx - tx[j] * dz;
-                        gz += tx[j] * dy - ty[j] * dx;
-                    }
+                    if (HB) bq_form(__ldg(a.B + e), tx[j], ty[j], tz[j], qxx, qyy, qzz, qxy, qxz, qyz);
+                    // s_k x D_ik (the DM term of delta_energy_get as s_i . (s_k x D))
+                    if (HD) dm_field(__ldg(a.Dx + e), __ldg(a.Dy + e), __ldg(a.Dz + e), tx[j], ty[j], tz[j], gx, gy, gz);
                 }
             }
             const int orig = __ldg(a.perm + p);
             if (has_si || has_f) {
                 const int at = orig % a.num_atoms;
-                if (has_si) {
-                    const float4 s = __ldg(a.si + at);
-                    const float dx = s.w * s.x, dy = s.w * s.y, dz = s.w * s.z;
-                    qxx = fmaf(dx, s.x, qxx); qyy = fmaf(dy, s.y, qyy); qzz = fmaf(dz, s.z, qzz);
-                    qxy = fmaf(dx, s.y, qxy); qxz = fmaf(dx, s.z, qxz); qyz = fmaf(dy, s.z, qyz);
-                }
+                if (has_si) si_form(__ldg(a.si + at), qxx, qyy, qzz, qxy, qxz, qyz);
                 if (has_f) {
                     const float4 f = __ldg(a.fld + at);
-                    gx += f.x; gy += f.y; gz += f.z;
+                    gx = __fadd_rn(gx, f.x); gy = __fadd_rn(gy, f.y); gz = __fadd_rn(gz, f.z);
                 }
             }
             const Philox4 x = philox4x32_10((uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
             float nx, ny, nz;
             trial_spin(a.mode, a.tilt, __ldg(a.mag + p), ox, oy, oz, x.x, x.y, nx, ny, nz);
             const float dx = nx - ox, dy = ny - oy, dz = nz - oz;
-            float de = gx * dx + gy * dy + gz * dz;
-            if (HB || has_si) {
-                // s_new^T Q s_new - s_old^T Q s_old = d^T Q (s_new + s_old)
-                const float px = nx + ox, py = ny + oy, pz = nz + oz;
-                de += dx * (qxx * px + qxy * py + qxz * pz)
-                    + dy * (qxy * px + qyy * py + qyz * pz)
-                    + dz * (qxz * px + qyz * py + qzz * pz);
-            }
+            // s_new^T Q s_new - s_old^T Q s_old = d^T Q (s_new + s_old)
+            const float de = delta_energy(HB || has_si, gx, gy, gz, qxx, qyy, qzz, qxy, qxz, qyz, ox, oy, oz, nx, ny, nz);
             bool acc = true;
             if (de > 0.0f) acc = expf(-beta * de) >= u24f(x.z);
             if (acc) {

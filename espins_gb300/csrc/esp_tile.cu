@@ -65,15 +65,11 @@ __device__ __forceinline__ void entry_exchange(FieldQ &f, float nJ, float tx, fl
 }
 __device__ __forceinline__ void entry_bq(FieldQ &f, float Bv, float tx, float ty, float tz)
 {
-    const float bx = __fmul_rn(Bv, tx), by = __fmul_rn(Bv, ty), bz = __fmul_rn(Bv, tz);
-    f.qxx = fmaf(bx, tx, f.qxx); f.qyy = fmaf(by, ty, f.qyy); f.qzz = fmaf(bz, tz, f.qzz);
-    f.qxy = fmaf(bx, ty, f.qxy); f.qxz = fmaf(bx, tz, f.qxz); f.qyz = fmaf(by, tz, f.qyz);
+    bq_form(Bv, tx, ty, tz, f.qxx, f.qyy, f.qzz, f.qxy, f.qxz, f.qyz);
 }
 __device__ __forceinline__ void entry_dm(FieldQ &f, float dx, float dy, float dz, float tx, float ty, float tz)
 {
-    f.gx = fmaf(tz, -dy, fmaf(ty, dz, f.gx));
-    f.gy = fmaf(tx, -dz, fmaf(tz, dx, f.gy));
-    f.gz = fmaf(ty, -dx, fmaf(tx, dy, f.gz));
+    dm_field(dx, dy, dz, tx, ty, tz, f.gx, f.gy, f.gz);
 }
 __device__ __forceinline__ void entry_exchange(FieldQ2 &f, float2 nJ, float2 tx, float2 ty, float2 tz)
 {
@@ -110,27 +106,15 @@ __device__ __forceinline__ bool tile_trial(const TileArgs &a, const ClusterStenc
                                            uint32_t orig, uint32_t r, uint32_t sw_lo, uint32_t sw_hi, float beta,
                                            float ox, float oy, float oz, float &nx, float &ny, float &nz, float &de)
 {
-    if (a.has_si) {
-        const float4 s = st->si[at];
-        const float dx = __fmul_rn(s.w, s.x), dy = __fmul_rn(s.w, s.y), dz = __fmul_rn(s.w, s.z);
-        f.qxx = fmaf(dx, s.x, f.qxx); f.qyy = fmaf(dy, s.y, f.qyy); f.qzz = fmaf(dz, s.z, f.qzz);
-        f.qxy = fmaf(dx, s.y, f.qxy); f.qxz = fmaf(dx, s.z, f.qxz); f.qyz = fmaf(dy, s.z, f.qyz);
-    }
+    if (a.has_si) si_form(st->si[at], f.qxx, f.qyy, f.qzz, f.qxy, f.qxz, f.qyz);
     if (a.has_f) {
         const float4 fl = st->fld[at];
         f.gx = __fadd_rn(f.gx, fl.x); f.gy = __fadd_rn(f.gy, fl.y); f.gz = __fadd_rn(f.gz, fl.z);
     }
     const Philox4 xr = philox4x32_10(orig, r, sw_lo, sw_hi, a.key0, a.key1);
     trial_spin(a.mode, a.tilt, st->mag[at], ox, oy, oz, xr.x, xr.y, nx, ny, nz);
-    const float dx = __fsub_rn(nx, ox), dy = __fsub_rn(ny, oy), dz = __fsub_rn(nz, oz);
-    de = fmaf(f.gz, dz, fmaf(f.gy, dy, __fmul_rn(f.gx, dx)));
-    if (a.has_b || a.has_si) {
-        const float px = __fadd_rn(nx, ox), py = __fadd_rn(ny, oy), pz = __fadd_rn(nz, oz);
-        const float ax = fmaf(f.qxz, pz, fmaf(f.qxy, py, __fmul_rn(f.qxx, px)));
-        const float ay = fmaf(f.qyz, pz, fmaf(f.qyy, py, __fmul_rn(f.qxy, px)));
-        const float az = fmaf(f.qzz, pz, fmaf(f.qyz, py, __fmul_rn(f.qxz, px)));
-        de = fmaf(dz, az, fmaf(dy, ay, fmaf(dx, ax, de)));
-    }
+    de = delta_energy(a.has_b || a.has_si, f.gx, f.gy, f.gz, f.qxx, f.qyy, f.qzz, f.qxy, f.qxz, f.qyz, ox, oy, oz, nx,
+                      ny, nz);
     if (de > 0.0f) return expf(-beta * de) >= u24f(xr.z);
     return true;
 }

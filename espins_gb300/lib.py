@@ -55,7 +55,7 @@ class LpTrainOpts(C.Structure):
 class BatchTuning(C.Structure):
     _fields_ = [("units_per_graph", C.c_int32), ("us_per_unit", C.c_double), ("kernel", C.c_void_p),
                 ("ell_us", C.c_void_p), ("cluster_us", C.c_void_p), ("graph_us", C.c_void_p),
-                ("cluster_size", C.c_void_p), ("cluster_threads", C.c_void_p)]
+                ("cluster_size", C.c_void_p), ("cluster_threads", C.c_void_p), ("cluster_sites", C.c_void_p)]
 
 
 class Dims(C.Structure):
@@ -161,10 +161,10 @@ def load(build_if_missing: bool = True):
     lib.esp_set_proposal.argtypes = [vp, C.c_int32]
     lib.esp_get_proposal.argtypes = [vp, P(C.c_int32)]
     lib.esp_set_pt_groups.argtypes = [vp, C.c_int32]
-    lib.esp_set_cluster_geometry.argtypes = [vp, C.c_int32, C.c_int32]
+    lib.esp_set_cluster_geometry.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
     lib.esp_set_tile_geometry.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
     lib.esp_get_tile_geometry.argtypes = [vp, P(C.c_int32), P(C.c_int32), P(C.c_int32)]
-    lib.esp_get_cluster_geometry.argtypes = [vp, P(C.c_int32), P(C.c_int32)]
+    lib.esp_get_cluster_geometry.argtypes = [vp, P(C.c_int32), P(C.c_int32), P(C.c_int32)]
     lib.esp_batch_create.argtypes = [vp, C.c_int32, vp, P(vp)]
     lib.esp_batch_destroy.argtypes = [vp]
     lib.esp_batch_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
@@ -559,14 +559,15 @@ class Engine:
         self._check(self.lib.esp_lp_forward(self.h, _p(f), f.shape[0], _p(out)))
         return out
 
-    def set_cluster_geometry(self, cluster_size: int, threads: int) -> None:
-        self._check(self.lib.esp_set_cluster_geometry(self.h, int(cluster_size), int(threads)))
+    def set_cluster_geometry(self, cluster_size: int, threads: int, sites_per_thread: int = 1) -> None:
+        self._check(self.lib.esp_set_cluster_geometry(self.h, int(cluster_size), int(threads), int(sites_per_thread)))
 
     def cluster_geometry(self):
-        """(CTAs per replica, threads per CTA) of the cluster path, (0, 0) without one."""
-        a, b = C.c_int32(), C.c_int32()
-        self._check(self.lib.esp_get_cluster_geometry(self.h, C.byref(a), C.byref(b)))
-        return a.value, b.value
+        """(CTAs per replica, threads per CTA, sites per thread) of the cluster
+        path, (0, 0, 0) without one."""
+        a, b, s = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(self.lib.esp_get_cluster_geometry(self.h, C.byref(a), C.byref(b), C.byref(s)))
+        return a.value, b.value, s.value
 
     def set_tile_geometry(self, tile: int, replicas: int, pipelined: bool = False) -> None:
         self._check(self.lib.esp_set_tile_geometry(self.h, int(tile), int(replicas), int(bool(pipelined))))
@@ -657,10 +658,11 @@ class Batch:
         gr = np.zeros(4)
         cs = np.zeros(n, dtype=np.int32)
         nt = np.zeros(n, dtype=np.int32)
-        t = BatchTuning(0, 0.0, _p(kern), _p(ell), _p(clu), _p(gr), _p(cs), _p(nt))
+        sp = np.zeros(n, dtype=np.int32)
+        t = BatchTuning(0, 0.0, _p(kern), _p(ell), _p(clu), _p(gr), _p(cs), _p(nt), _p(sp))
         self._check(self.lib.esp_batch_tune(self.b, int(units), C.byref(t)))
         return {"units_per_graph": t.units_per_graph, "us_per_unit": t.us_per_unit,
                 "kernel": [{1: "ell", 2: "cluster", 4: "tile"}.get(int(k), "ell") for k in kern],
                 "ell_us": ell.tolist(),
                 "cluster_us": clu.tolist(), "graph_us": dict(zip((1, 2, 4, 8), gr.tolist())),
-                "cluster_geometry": [(int(a), int(b)) for a, b in zip(cs, nt)]}
+                "cluster_geometry": [(int(a), int(b), int(c)) for a, b, c in zip(cs, nt, sp)]}

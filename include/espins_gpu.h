@@ -266,10 +266,13 @@ int esp_get_replica_of_slot(esp_handle *h, int32_t *replica_out);
  * uses the same random stream and arithmetic in tile order. */
 int esp_set_sweep_kernel(esp_handle *h, int32_t kind);
 /* Geometry of the cluster-resident sweep: CTAs per replica (slabs of z
- * planes) and threads per CTA (256 or 512); ESP_EINVAL where the lattice or
- * the GPU cannot run it.  Trajectories do not depend on it. */
-int esp_set_cluster_geometry(esp_handle *h, int32_t cluster_size, int32_t threads);
-int esp_get_cluster_geometry(const esp_handle *h, int32_t *cluster_size, int32_t *threads);
+ * planes), threads per CTA and sites of a colour pass each thread updates
+ * together: (256, 1), (512, 1) or (512, 2); ESP_EINVAL where the lattice or
+ * the GPU cannot run it.  Trajectories do not depend on it.  The getter
+ * accepts sites_per_thread == NULL. */
+int esp_set_cluster_geometry(esp_handle *h, int32_t cluster_size, int32_t threads, int32_t sites_per_thread);
+int esp_get_cluster_geometry(const esp_handle *h, int32_t *cluster_size, int32_t *threads,
+                             int32_t *sites_per_thread);
 /* Geometry of the tiled sweep: tile edge in cells (even, 2 * tile dividing
  * every supercell edge), replicas per CTA, and the variant: 0 one CTA per
  * tile, 1 persistent CTAs that copy the next tile asynchronously while
@@ -320,6 +323,7 @@ typedef struct {
                                      cluster / tiled candidates (-1: none possible), or NULL */
     double *graph_us;             /* [4] time per unit with 1, 2, 4, 8 units per graph, or NULL */
     int32_t *cluster_size, *cluster_threads;  /* [n] chosen cluster geometry per handle (0: none), or NULL */
+    int32_t *cluster_sites;       /* [n] sites per thread of the chosen cluster geometry, or NULL */
 } esp_batch_tuning;
 int esp_batch_create(esp_handle *const *handles, int32_t n, void *stream, esp_batch **out);
 int esp_batch_destroy(esp_batch *b);

@@ -105,14 +105,14 @@ def test_trajectory_does_not_depend_on_cluster_geometry(case):
     v = rng.normal(size=(len(inp.tems), h.n, 3))
     s0 = v / np.linalg.norm(v, axis=2, keepdims=True)
     outs = []
-    geoms = [(cs, nt) for cs in (1, 2, 4) for nt in (512, 256)]
-    for cs, nt in geoms:
+    geoms = [(cs, nt, sp) for cs in (1, 2, 4) for nt, sp in ((512, 1), (512, 2), (256, 1))]
+    for cs, nt, sp in geoms:
         with _engine(h, inp.tems, "cluster") as e:
             try:
-                e.set_cluster_geometry(cs, nt)
+                e.set_cluster_geometry(cs, nt, sp)
             except Exception:
                 continue          # not possible for this lattice / GPU
-            assert e.cluster_geometry() == (cs, nt)
+            assert e.cluster_geometry() == (cs, nt, sp)
             e.set_spins(s0)
             e.sweep(20, 11, seed=5)
             outs.append(((cs, nt), e.get_spins(), e.rejected(), e.running_energy()))
