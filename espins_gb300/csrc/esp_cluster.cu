@@ -543,7 +543,7 @@ cudaError_t cluster_configure(size_t smem, int csize, int nt, int S)
 {
     if (!cluster_threads_ok(nt, S)) return cudaErrorInvalidValue;
     const ClusterKernel k = cluster_kernel(nt, S);
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k), smem);
     if (e != cudaSuccess) return e;
     if (csize > 8) e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     return e;
@@ -553,7 +553,7 @@ int cluster_max_active(int csize, int nt, int S, size_t smem, int R)
 {
     if (!cluster_threads_ok(nt, S)) return 0;
     const ClusterKernel k = cluster_kernel(nt, S);
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    if (allow_max_dynamic_smem(reinterpret_cast<const void *>(k), smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }

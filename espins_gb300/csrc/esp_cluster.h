@@ -91,6 +91,24 @@ constexpr int kClusterMaxLev = 32;
 constexpr int kClusterAccDoubles = 12 + kClusterMaxLev / 2 + 8 * kClusterMaxLev;
 size_t cluster_smem_bytes(int n_local, int nf, int nhist, size_t stencil_bytes);
 // nt: threads per CTA, 256 or 512
+// The dynamic shared-memory limit is a property of a kernel function, shared
+// by every handle that launches it: raise it to the most the device allows
+// next to the kernel's static shared memory (it is an upper bound, not an
+// allocation), so that configuring one handle never lowers the limit another
+// handle's launches need.  Fails if `need` exceeds that maximum.
+inline cudaError_t allow_max_dynamic_smem(const void *kernel, size_t need)
+{
+    int dev = 0, v = 0;
+    cudaFuncAttributes fa{};
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    const long long room = (long long)v - (long long)fa.sharedSizeBytes;
+    if (room <= 0 || need > (size_t)room) return cudaErrorInvalidValue;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)room);
+}
+
 // Thread geometries of the kernel: nt threads per CTA, S sites of a colour
 // pass per thread (updated together): (256, 1), (512, 1), (512, 2).
 bool cluster_threads_ok(int nt, int S);

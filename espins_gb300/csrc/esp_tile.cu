@@ -618,7 +618,7 @@ size_t tile_smem_bytes(int T, int G, int na, int maxst)
 
 cudaError_t tile_configure(size_t smem)
 {
-    return cudaFuncSetAttribute(k_sweep_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sweep_tile), smem);
 }
 
 cudaError_t launch_tile(const TileArgs &a, size_t smem, cudaStream_t st)
@@ -648,7 +648,7 @@ namespace {
 template <int T, int G>
 cudaError_t launch_p(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
 {
-    if (configure) return cudaFuncSetAttribute(k_sweep_tile_p<T, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (configure) return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sweep_tile_p<T, G>), smem);
     k_sweep_tile_p<T, G><<<blocks, kTilePThreads, smem, st>>>(a);
     return cudaGetLastError();
 }

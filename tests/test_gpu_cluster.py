@@ -121,3 +121,23 @@ def test_trajectory_does_not_depend_on_cluster_geometry(case):
         assert np.array_equal(s, outs[0][1]), g
         assert np.array_equal(rej, outs[0][2]), g
         assert np.max(np.abs(en - outs[0][3])) <= 1e-6 * h.n * 40.0, g
+
+
+def test_a_smaller_lattice_set_up_later_does_not_break_a_larger_ones_launches():
+    """The dynamic shared-memory limit belongs to the kernel function, not to
+    a handle: configuring the cluster path of a small lattice after a large
+    one (same kernel, less shared memory) must leave the large one's
+    launches valid."""
+    big = sc_mcin(16, [(1e-3, NN)], [3.0, 10.0])
+    small = sc_mcin(8, [(1e-3, NN)], [3.0, 10.0])
+    hb, hs = build_hamiltonian(big), build_hamiltonian(small)
+    with _engine(hb, big.tems, "cluster") as eb:
+        eb.set_cluster_geometry(1, 512, 1)
+        eb.init_spins("ferro")
+        with _engine(hs, small.tems, "cluster") as es:
+            es.set_cluster_geometry(1, 512, 1)
+            es.init_spins("ferro")
+            es.sweep(2, 1, seed=3)
+        eb.sweep(2, 1, seed=3)
+        assert eb.sweep_kernel()[0] == "cluster"
+        assert np.all(np.isfinite(eb.running_energy()))
