@@ -566,8 +566,9 @@ def main():
     out_spins = eng2.get_spins()
     t_e2e = time.perf_counter() - t0
     eng2.close()
-    h2d = 12 * N * R + 8 * R
-    d2h = 12 * N * R + 8 * R * (6 + 3 + 4) + 8 * R * eng.num_freq()
+    # spin_matrix crosses as FP64 (3 x 8 B per spin) both ways
+    h2d = 24 * N * R + 8 * R
+    d2h = 24 * N * R + 8 * R * (6 + 3 + 4) + 8 * R * eng.num_freq()
 
     t_local = ms / 1e3
     if ws > 1:

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/espins_gpu.h"
@@ -878,6 +879,45 @@ int cluster_geometry(esp_handle *h, int cs, int nt, int S)
     return ESP_OK;
 }
 
+// Staging for spin_matrix blocks of whole temperature slots, at most 256 MiB
+// (one slot at least), on the device and in pinned host memory; allocated
+// with the tables so that the spin transfers themselves allocate nothing.
+int ensure_stage(esp_handle *h)
+{
+    if (h->d_stage) return ESP_OK;
+    const size_t per_slot = sizeof(double) * 3 * (size_t)h->N;
+    int slots = (int)std::max<size_t>(1, ((size_t)256 << 20) / per_slot);
+    slots = std::min(slots, h->R);
+    CK(dalloc(&h->d_stage, (size_t)3 * h->N * slots));
+    CK(cudaMallocHost((void **)&h->h_stage, sizeof(double) * 3 * (size_t)h->N * slots));
+    h->stage_slots = slots;
+    return ESP_OK;
+}
+
+// Host copy between the caller's arrays and the pinned staging, split over
+// up to 8 threads for large blocks: one core copies (and faults in fresh
+// pages) far below the memory bandwidth.
+void par_memcpy(void *dst, const void *src, size_t bytes)
+{
+    const size_t chunk = (size_t)4 << 20;
+    const int nth = (int)std::min<size_t>(8, bytes / chunk);
+    if (nth <= 1) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    const size_t per = ((bytes + nth - 1) / nth + 63) & ~(size_t)63;
+    std::vector<std::thread> th;
+    th.reserve(nth - 1);
+    for (int i = 1; i < nth; ++i) {
+        const size_t off = per * i;
+        if (off >= bytes) break;
+        const size_t n = std::min(per, bytes - off);
+        th.emplace_back([=] { std::memcpy(static_cast<char *>(dst) + off, static_cast<const char *>(src) + off, n); });
+    }
+    std::memcpy(dst, src, std::min(per, bytes));
+    for (std::thread &t : th) t.join();
+}
+
 }  // namespace
 
 namespace esp {
@@ -1138,6 +1178,7 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t)
         if (!c.empty() && (rc = cluster_geometry(h, c[0].cs, c[0].nt, c[0].S))) return rc;
         if ((rc = tile_setup(h))) return rc;
     }
+    if ((rc = ensure_stage(h))) return rc;
     h->have_tables = true;
     return ESP_OK;
 }
@@ -1160,32 +1201,22 @@ int esp_set_temperatures(esp_handle *h, const double *tems)
     return identity_labels(h);
 }
 
-// Device staging for spin_matrix blocks of whole temperature slots, at most
-// 256 MiB (one slot at least).
-int ensure_stage(esp_handle *h)
-{
-    if (h->d_stage) return ESP_OK;
-    const size_t per_slot = sizeof(double) * 3 * (size_t)h->N;
-    int slots = (int)std::max<size_t>(1, ((size_t)256 << 20) / per_slot);
-    slots = std::min(slots, h->R);
-    CK(dalloc(&h->d_stage, (size_t)3 * h->N * slots));
-    CK(cudaMallocHost((void **)&h->h_stage, sizeof(double) * 3 * (size_t)h->N * slots));
-    h->stage_slots = slots;
-    return ESP_OK;
-}
-
 int esp_set_spins(esp_handle *h, const double *spins)
 {
     int rc = require(h, true, false);
     if (rc) return rc;
     if (!spins) { h->err = "null spins"; return ESP_EINVAL; }
     if ((rc = ensure_stage(h))) return rc;
-    // blocks of slots: copy the FP64 block, then scatter it into the permuted
-    // FP32 state on the device
+    // blocks of slots: copy the FP64 block through the pinned staging (a
+    // parallel host copy, then one DMA), then scatter it into the permuted
+    // FP32 state on the device.  The driver's pageable path is as fast only
+    // for warm, small arrays and falls to ~1 GB/s where it must fault pages in.
     for (int t0 = 0; t0 < h->R; t0 += h->stage_slots) {
         const int nt = std::min(h->stage_slots, h->R - t0);
-        CK(cudaMemcpyAsync(h->d_stage, spins + (size_t)3 * h->N * t0, sizeof(double) * 3 * (size_t)h->N * nt,
-                           cudaMemcpyHostToDevice, h->st));
+        const size_t bytes = sizeof(double) * 3 * (size_t)h->N * nt;
+        CK(cudaStreamSynchronize(h->st));   // the previous block has left the pinned staging
+        par_memcpy(h->h_stage, spins + (size_t)3 * h->N * t0, bytes);
+        CK(cudaMemcpyAsync(h->d_stage, h->h_stage, bytes, cudaMemcpyHostToDevice, h->st));
         CK(launch_spins_in(h->d_stage, h->d_inv, h->d_repl_at, h->d_sx, h->d_sy, h->d_sz, h->N, h->R, t0, nt, h->st));
         h->launches++;
     }
@@ -1219,7 +1250,7 @@ int esp_get_spins(esp_handle *h, double *spins)
         h->launches++;
         CK(cudaMemcpyAsync(h->h_stage, h->d_stage, bytes, cudaMemcpyDeviceToHost, h->st));
         CK(cudaStreamSynchronize(h->st));
-        std::memcpy(spins + (size_t)3 * h->N * t0, h->h_stage, bytes);
+        par_memcpy(spins + (size_t)3 * h->N * t0, h->h_stage, bytes);
     }
     return ESP_OK;
 }
