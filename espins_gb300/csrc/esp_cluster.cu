@@ -30,6 +30,36 @@ namespace esp {
 // loaded passes when a colour holds between 1 and 2 times 512 sites).  All
 // within 128 registers per thread: a sub-partition of the SM that holds four
 // warps has 16,384 registers for them.
+// Warp-aggregated increments of a shared-memory histogram (1-based bins,
+// bin <= 0 adds nothing; every lane of the warp calls together).  Low
+// temperatures put almost every cell in one bin: while a warp's 32 cells share
+// one bin, and the same bin as its previous call, the count stays in a
+// register (one atomic per run instead of one per call); mixed warps add per
+// lane.
+struct WarpRun {
+    int bin = -1;
+    unsigned cnt = 0u;
+};
+__device__ __forceinline__ void hist_add(unsigned *h, WarpRun &run, int bin)
+{
+    const int b0 = __shfl_sync(0xffffffffu, bin, 0);
+    if (__all_sync(0xffffffffu, bin == b0)) {
+        if (b0 == run.bin) {
+            run.cnt += 32u;
+            return;
+        }
+        if ((threadIdx.x & 31) == 0 && run.bin > 0) atomicAdd(h + (run.bin - 1), run.cnt);
+        run.bin = b0;
+        run.cnt = 32u;
+    } else if (bin > 0) {
+        atomicAdd(h + (bin - 1), 1u);
+    }
+}
+__device__ __forceinline__ void hist_flush(unsigned *h, const WarpRun &run)
+{
+    if ((threadIdx.x & 31) == 0 && run.bin > 0) atomicAdd(h + (run.bin - 1), run.cnt);
+}
+
 template <int NT, int S>
 __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const ClusterArgs a)
 {
@@ -347,6 +377,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
                 const int ncells_local = per_class * 8;         // cells of the slab
                 const int cstride = per_class * 8;
                 const int cl_end = (ncells_local + 31) & ~31;   // whole warps take part in the vote
+                WarpRun run_m, run_op, run_sm;
                 for (int cl = threadIdx.x; cl < cl_end; cl += blockDim.x) {
                     int bin = -1, bin_op = -1, bin_sm = -1;
                     if (cl < ncells_local) {
@@ -361,19 +392,16 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
                         if (a.obs & 1) bin_op = pm_bin_value(op, (float)a.m_min, pm_scale, a.nf);
                         if (a.obs & 2) bin_sm = pm_bin(qx, qy, qz, (float)a.m_min, pm_scale, a.nf);
                     }
-                    // lanes with the same bin add once (low temperatures put
-                    // almost every cell in one bin)
-                    const unsigned int peers = __match_any_sync(0xffffffffu, bin);
-                    if (bin > 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
-                        atomicAdd(hist + (bin - 1), (unsigned)__popc(peers));
+                    hist_add(hist, run_m, bin);
                     if (a.obs) {
-                        const unsigned int po = __match_any_sync(0xffffffffu, bin_op);
-                        if (bin_op > 0 && (int)(threadIdx.x & 31) == __ffs(po) - 1)
-                            atomicAdd(hist + a.nf + (bin_op - 1), (unsigned)__popc(po));
-                        const unsigned int ps = __match_any_sync(0xffffffffu, bin_sm);
-                        if (bin_sm > 0 && (int)(threadIdx.x & 31) == __ffs(ps) - 1)
-                            atomicAdd(hist + 2 * a.nf + (bin_sm - 1), (unsigned)__popc(ps));
+                        hist_add(hist + a.nf, run_op, bin_op);
+                        hist_add(hist + 2 * a.nf, run_sm, bin_sm);
                     }
+                }
+                hist_flush(hist, run_m);
+                if (a.obs) {
+                    hist_flush(hist + a.nf, run_op);
+                    hist_flush(hist + 2 * a.nf, run_sm);
                 }
             }
             cluster.sync();
