@@ -405,47 +405,59 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
                 }
             }
             cluster.sync();
-            if (rank == 0 && threadIdx.x == 0) {
-                double d4[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                for (int q = 0; q < csize; ++q) {
-                    const double *pr = cluster.map_shared_rank(red, q);
-#pragma unroll
-                    for (int c = 0; c < 8; ++c) d4[c] += pr[128 + c];
-                }
-                e_run += d4[0];
-                m_run[0] += d4[1]; m_run[1] += d4[2]; m_run[2] += d4[3];
-                // accumulators of mcarlo.F90:536-590 for this temperature slot
-                const double e = e_run;
+            if (rank == 0 && threadIdx.x < 32) {
+                // lane 0 folds the CTAs' sums into the replica totals and the
+                // accumulators of mcarlo.F90:536-590 for this temperature
+                // slot; the binning levels, independent of one another, go
+                // one per lane
                 const double rn_inv = a.rn_inv;
-                const double mx = m_run[0] * rn_inv, my = m_run[1] * rn_inv, mz = m_run[2] * rn_inv;
-                const double m2 = mx * mx + my * my + mz * mz;
-                const double ee = e * e, am = sqrt(m2);
-                double *d = cache ? c_data : a.data + 6 * temp;
-                d[0] += e; d[1] += ee; d[2] += ee * ee;
-                d[3] += am; d[4] += m2; d[5] += m2 * m2;
                 const long long step = meas_base + m + 1;
-                if (a.series) {
-                    double *o = a.series + (((step - 1) % a.series_cap) * a.R + temp) * 2;
-                    o[0] = e; o[1] = am;
-                }
-                // orderparam_get / staggered_get (mcarlo.F90:553-568)
-                double aop = 0.0, asm_ = 0.0;
-                if (a.obs) {
-                    double *od = cache ? c_odata : a.obs_data + 6 * temp;
-                    if (a.obs & 1) {
-                        const double op = d4[4] * rn_inv;
-                        const double o2 = op * op;
-                        aop = sqrt(o2);
-                        od[0] += aop; od[1] += o2; od[2] += o2 * o2;
+                double e = 0.0, am = 0.0, aop = 0.0, asm_ = 0.0;
+                if (threadIdx.x == 0) {
+                    double d4[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                    for (int q = 0; q < csize; ++q) {
+                        const double *pr = cluster.map_shared_rank(red, q);
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) d4[c] += pr[128 + c];
                     }
-                    if (a.obs & 2) {
-                        const double qx = d4[5] * rn_inv, qy = d4[6] * rn_inv, qz = d4[7] * rn_inv;
-                        const double q2 = qx * qx + qy * qy + qz * qz;
-                        asm_ = sqrt(q2);
-                        od[3] += asm_; od[4] += q2; od[5] += q2 * q2;
+                    e_run += d4[0];
+                    m_run[0] += d4[1]; m_run[1] += d4[2]; m_run[2] += d4[3];
+                    e = e_run;
+                    const double mx = m_run[0] * rn_inv, my = m_run[1] * rn_inv, mz = m_run[2] * rn_inv;
+                    const double m2 = mx * mx + my * my + mz * mz;
+                    const double ee = e * e;
+                    am = sqrt(m2);
+                    double *d = cache ? c_data : a.data + 6 * temp;
+                    d[0] += e; d[1] += ee; d[2] += ee * ee;
+                    d[3] += am; d[4] += m2; d[5] += m2 * m2;
+                    if (a.series) {
+                        double *o = a.series + (((step - 1) % a.series_cap) * a.R + temp) * 2;
+                        o[0] = e; o[1] = am;
+                    }
+                    // orderparam_get / staggered_get (mcarlo.F90:553-568)
+                    if (a.obs) {
+                        double *od = cache ? c_odata : a.obs_data + 6 * temp;
+                        if (a.obs & 1) {
+                            const double op = d4[4] * rn_inv;
+                            const double o2 = op * op;
+                            aop = sqrt(o2);
+                            od[0] += aop; od[1] += o2; od[2] += o2 * o2;
+                        }
+                        if (a.obs & 2) {
+                            const double qx = d4[5] * rn_inv, qy = d4[6] * rn_inv, qz = d4[7] * rn_inv;
+                            const double q2 = qx * qx + qy * qy + qz * qz;
+                            asm_ = sqrt(q2);
+                            od[3] += asm_; od[4] += q2; od[5] += q2 * q2;
+                        }
                     }
                 }
-                for (int lv = 0; lv < a.nlev; ++lv) {
+                if (a.nlev > 0) {
+                    e = __shfl_sync(0xffffffffu, e, 0);
+                    am = __shfl_sync(0xffffffffu, am, 0);
+                    aop = __shfl_sync(0xffffffffu, aop, 0);
+                    asm_ = __shfl_sync(0xffffffffu, asm_, 0);
+                }
+                for (int lv = threadIdx.x; lv < a.nlev; lv += 32) {
                     const size_t g2 = ((size_t)temp * a.nlev + lv) * 2;
                     double *ls = cache ? c_ls + 2 * lv : a.lsum + g2;
                     double *bn = cache ? c_bn + 2 * lv : a.binning + g2;

@@ -134,7 +134,11 @@ int esp_set_stream(esp_handle *h, void *cuda_stream);
 int esp_upload_tables(esp_handle *h, const esp_tables *t);
 /* tems(R) in Kelvin, in the order of the temperature slots. */
 int esp_set_temperatures(esp_handle *h, const double *tems);
-/* spin_matrix(3,N,R) (mcarlo.F90:269-322, pt.F90:442-491). */
+/* spin_matrix(3,N,R) (mcarlo.F90:269-322, pt.F90:442-491).  The copy goes
+ * through a staging area of pinned host and device memory (at most 256 MiB
+ * each, in whole temperature slots) that esp_upload_tables allocates, so
+ * neither this call nor esp_get_spins allocates; the host side of the copy
+ * runs on up to 8 threads. */
 int esp_set_spins(esp_handle *h, const double *spins);
 /* Start configurations of the reference: 0 ferro (0,0,m), 1 rand
  * (theta = pi*u1, phi = 2 pi*u2, the same for every temperature as in
