@@ -115,6 +115,7 @@ struct esp_handle {
     // pinned host copy that esp_get_spins reads back through (a copy straight
     // into the caller's pages would fault them in inside the transfer)
     double *d_stage = nullptr, *h_stage = nullptr;
+    float *d_slab = nullptr;   // spins in the cluster path's slab layout during its launches
     int stage_slots = 0;
     // structure factor (esp_set_structure_factor)
     int sf_nq = 0, sf_every = 1;
@@ -201,7 +202,7 @@ void free_tables(esp_handle *h)
     dfree(h->d_J); dfree(h->d_B); dfree(h->d_Dx); dfree(h->d_Dy); dfree(h->d_Dz); dfree(h->d_mag);
     dfree(h->d_si); dfree(h->d_fld); dfree(h->d_scratch); dfree(h->d_part); dfree(h->d_part_rej);
     dfree(h->d_tc_part); dfree(h->d_tc_part_rej);
-    dfree(h->d_stencil_blob); dfree(h->d_nbidx); dfree(h->d_lp_axis);
+    dfree(h->d_stencil_blob); dfree(h->d_nbidx); dfree(h->d_lp_axis); dfree(h->d_slab);
     dfree(h->d_tile_offs); dfree(h->d_tile_cpl); dfree(h->d_tile_part); dfree(h->d_tile_rej);
     h->cluster_ok = false;
     h->tile_ok = false;
@@ -399,7 +400,7 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     a.Lx = h->L[0]; a.Ly = h->L[1]; a.Lz = h->L[2]; a.na = h->na; a.N = h->N; a.R = h->R;
     a.nclass = 8 * h->na; a.pz = h->pz;
     a.has_b = h->prep.has_b; a.has_d = h->prep.has_d; a.has_si = h->hsi; a.has_f = h->hfld;
-    a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz; a.inv = h->d_inv;
+    a.slab = h->d_slab;
     a.temp_of = h->d_temp_of; a.beta = h->d_beta; a.e_run = h->d_e_run; a.m_run = h->d_m_run; a.rej = h->d_rej;
     a.phase = phase;
     a.measure = measure; a.n_meas = (int)n_meas; a.steps_measure = steps_measure; a.meas_base = meas_base;
@@ -423,8 +424,17 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     a.obs = measure ? h->obs : 0;
     a.obs_atom = h->d_obs_atom; a.obs_data = h->d_obs_data; a.obs_lsum = h->d_obs_lsum; a.obs_bin = h->d_obs_bin;
     a.obs_pm = h->d_obs_pm;
+    // the spin arrays stay the state between launches; the kernel works on
+    // the slab copy, made and returned by two coalesced transposes
+    SlabArgs sa;
+    sa.sx = h->d_sx; sa.sy = h->d_sy; sa.sz = h->d_sz; sa.slab = h->d_slab; sa.inv = h->d_inv;
+    sa.Lx = h->L[0]; sa.Ly = h->L[1]; sa.na = h->na; sa.R = h->R; sa.pz = h->pz; sa.cs = h->csize;
+    sa.n_local = h->N / h->csize;
+    sa.fd_pc = a.fd_pc; sa.fd_hx = a.fd_hx; sa.fd_hy = a.fd_hy;
+    CK(launch_to_slabs(sa, h->st));
     CK(launch_cluster(a, h->csize, h->cthreads, h->csites, h->cluster_smem, h->st));
-    h->launches++;
+    CK(launch_from_slabs(sa, h->st));
+    h->launches += 3;
     return ESP_OK;
 }
 
@@ -870,6 +880,7 @@ int cluster_geometry(esp_handle *h, int cs, int nt, int S)
     CK(dalloc(&h->d_nbidx, tab.size()));
     int rc = h2d(h, h->d_nbidx, tab.data(), sizeof(uint32_t) * tab.size());
     if (rc) return rc;
+    if (!h->d_slab) CK(dalloc(&h->d_slab, (size_t)3 * h->N * h->R));
     h->csize = cs;
     h->cthreads = nt;
     h->csites = S;

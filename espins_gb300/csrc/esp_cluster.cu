@@ -102,17 +102,9 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
         for (int i = threadIdx.x; i < a.stencil_words; i += blockDim.x) dst[i] = src[i];
         for (int i = threadIdx.x; i < nhist * a.nf; i += blockDim.x) hist[i] = 0u;
     }
-    for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
-        int k, rem, q1, hx, hy, hzl;
-        fdivmod(l, a.fd_pc, k, rem);
-        fdivmod(rem, a.fd_hx, q1, hx);
-        fdivmod(q1, a.fd_hy, hzl, hy);
-        const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
-        const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pz;
-        const int orig = ((z * a.Ly + y) * a.Lx + x) * a.na + at;
-        const size_t g = (size_t)__ldg(a.inv + orig) * a.R + r;
-        s3[3 * l] = a.sx[g]; s3[3 * l + 1] = a.sy[g]; s3[3 * l + 2] = a.sz[g];
-    }
+    // this CTA's slab: one contiguous block of 3 n_local floats
+    float *slab = a.slab + ((size_t)r * csize + rank) * 3 * n_local;
+    for (int i = threadIdx.x; i < 3 * n_local; i += blockDim.x) s3[i] = slab[i];
     const int temp = a.temp_of[r];
     const bool cache = a.measure && a.nlev <= kClusterMaxLev;
     if (rank == 0 && cache) {
@@ -545,19 +537,77 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
             }
         }
     }
-    for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
-        int k, rem, q1, hx, hy, hzl;
-        fdivmod(l, a.fd_pc, k, rem);
-        fdivmod(rem, a.fd_hx, q1, hx);
-        fdivmod(q1, a.fd_hy, hzl, hy);
-        const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
-        const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pz;
-        const int orig = ((z * a.Ly + y) * a.Lx + x) * a.na + at;
-        const size_t g = (size_t)__ldg(a.inv + orig) * a.R + r;
-        a.sx[g] = s3[3 * l]; a.sy[g] = s3[3 * l + 1]; a.sz[g] = s3[3 * l + 2];
-    }
+    for (int i = threadIdx.x; i < 3 * n_local; i += blockDim.x) slab[i] = s3[i];
     // peers may still read this CTA's shared memory until every CTA is done
     cluster.sync();
+}
+
+// Position p (spin-array row) of local site l of rank q.
+__device__ __forceinline__ int slab_row(const SlabArgs &a, int q, int l)
+{
+    int k, rem, q1, hx, hy, hzl;
+    fdivmod(l, a.fd_pc, k, rem);
+    fdivmod(rem, a.fd_hx, q1, hx);
+    fdivmod(q1, a.fd_hy, hzl, hy);
+    const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
+    const int x = 2 * hx + px, y = 2 * hy + py, z = q * a.pz + 2 * hzl + pz;
+    return __ldg(a.inv + ((z * a.Ly + y) * a.Lx + x) * a.na + at);
+}
+
+// grid (n_local / 32, cs, R / 32) rounded up, blocks of 32 x 8 threads
+__global__ void __launch_bounds__(256) k_to_slabs(const SlabArgs a)
+{
+    __shared__ float t[3][32][33];   // [component][replica][site]
+    __shared__ int rows[32];
+    const int l0 = blockIdx.x * 32, q = blockIdx.y, r0 = blockIdx.z * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    if (ty == 0) rows[tx] = l0 + tx < a.n_local ? slab_row(a, q, l0 + tx) : 0;
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8)
+        if (l0 + j < a.n_local && r0 + tx < a.R) {
+            const size_t g = (size_t)rows[j] * a.R + r0 + tx;
+            t[0][tx][j] = a.sx[g]; t[1][tx][j] = a.sy[g]; t[2][tx][j] = a.sz[g];
+        }
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8)
+        if (r0 + j < a.R && l0 + tx < a.n_local) {
+            float *o = a.slab + (((size_t)(r0 + j) * a.cs + q) * a.n_local + l0 + tx) * 3;
+            o[0] = t[0][j][tx]; o[1] = t[1][j][tx]; o[2] = t[2][j][tx];
+        }
+}
+
+__global__ void __launch_bounds__(256) k_from_slabs(const SlabArgs a)
+{
+    __shared__ float t[3][32][33];   // [component][replica][site]
+    __shared__ int rows[32];
+    const int l0 = blockIdx.x * 32, q = blockIdx.y, r0 = blockIdx.z * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    if (ty == 0) rows[tx] = l0 + tx < a.n_local ? slab_row(a, q, l0 + tx) : 0;
+    for (int j = ty; j < 32; j += 8)
+        if (r0 + j < a.R && l0 + tx < a.n_local) {
+            const float *i = a.slab + (((size_t)(r0 + j) * a.cs + q) * a.n_local + l0 + tx) * 3;
+            t[0][j][tx] = i[0]; t[1][j][tx] = i[1]; t[2][j][tx] = i[2];
+        }
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8)
+        if (l0 + j < a.n_local && r0 + tx < a.R) {
+            const size_t g = (size_t)rows[j] * a.R + r0 + tx;
+            a.sx[g] = t[0][tx][j]; a.sy[g] = t[1][tx][j]; a.sz[g] = t[2][tx][j];
+        }
+}
+
+cudaError_t launch_to_slabs(const SlabArgs &a, cudaStream_t st)
+{
+    const dim3 grid((a.n_local + 31) / 32, a.cs, (a.R + 31) / 32), block(32, 8);
+    k_to_slabs<<<grid, block, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_from_slabs(const SlabArgs &a, cudaStream_t st)
+{
+    const dim3 grid((a.n_local + 31) / 32, a.cs, (a.R + 31) / 32), block(32, 8);
+    k_from_slabs<<<grid, block, 0, st>>>(a);
+    return cudaGetLastError();
 }
 
 size_t cluster_smem_bytes(int n_local, int nf, int nhist, size_t stencil_bytes)

@@ -44,9 +44,9 @@ struct ClusterArgs {
     const uint32_t *nbidx;
     int Lx, Ly, Lz, na, N, R, nclass, pz;  // pz: z planes per CTA (even)
     int has_b, has_d, has_si, has_f;
-    // state
-    float *sx, *sy, *sz;            // element (p, r) at p*R + r
-    const int32_t *inv;             // reference site -> p
+    // state: the slabs of every replica, [r][rank][local site][x, y, z],
+    // converted from and to the handle's spin arrays around the launch
+    float *slab;
     const int32_t *temp_of;
     const float *beta;
     double *e_run, *m_run;
@@ -82,6 +82,21 @@ struct ClusterArgs {
     double *obs_lsum, *obs_bin;     // [R slots][nlev][2]
     unsigned long long *obs_pm;     // [R slots][2][nf]
 };
+
+// The handle's spin arrays (element (p, r) at p*R + r, p = inv[reference
+// site]) to and from the slab layout of the cluster path, [r][rank][l][3]
+// with l the kernel's local site order (class-major, then half-cell x, y, z
+// within the rank's pz planes): shared-memory transposes of 32 sites x 32
+// replicas, coalesced on both sides.
+struct SlabArgs {
+    float *sx, *sy, *sz;
+    float *slab;
+    const int32_t *inv;
+    int Lx, Ly, na, R, pz, cs, n_local;
+    FastDiv fd_pc, fd_hx, fd_hy;
+};
+cudaError_t launch_to_slabs(const SlabArgs &a, cudaStream_t st);
+cudaError_t launch_from_slabs(const SlabArgs &a, cudaStream_t st);
 
 // nhist: P(M) histogram only (1) or P(M), P(OP), P(SM) (3)
 // binning levels whose sums a cluster keeps in shared memory during a launch
