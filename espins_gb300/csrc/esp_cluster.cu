@@ -8,11 +8,14 @@
 // own.  A launch runs `n_meas` units of `steps_measure` sweeps, each unit
 // followed by the measurement of mcarlo.F90:536-590 / pt.F90:789-849
 // (accumulators, binning, Pm_get histogram), all without touching global
-// memory; spins are read at the start and written back at the end.
+// memory; each CTA reads its slab at the start and writes it back at the end
+// as one contiguous block (k_to_slabs / k_from_slabs convert the spin arrays
+// around the launch).
 //
-// Updates, random numbers and the order of the local-field sums are those of
+// Updates, random numbers and the local-field arithmetic are those of
 // k_sweep_ell (same colouring, same Philox counter (site, replica, sweep), the
-// stencil lists in the merged-list order), so both kernels produce the same
+// stencil lists in the merged-list order, the shared explicitly rounded
+// trial / field / energy functions), so both kernels produce the same
 // trajectory.  Waits are cluster barriers only (hardware, no spinning).
 #include <cooperative_groups.h>
 #include <type_traits>
