@@ -400,7 +400,11 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     a.Lx = h->L[0]; a.Ly = h->L[1]; a.Lz = h->L[2]; a.na = h->na; a.N = h->N; a.R = h->R;
     a.nclass = 8 * h->na; a.pz = h->pz;
     a.has_b = h->prep.has_b; a.has_d = h->prep.has_d; a.has_si = h->hsi; a.has_f = h->hfld;
-    a.slab = h->d_slab;
+    // slabs of at least 4096 sites are staged contiguously (two transposes);
+    // smaller ones are gathered by the kernel itself
+    const bool staged = h->N / h->csize >= 4096;
+    a.slab = staged ? h->d_slab : nullptr;
+    a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz; a.inv = h->d_inv;
     a.temp_of = h->d_temp_of; a.beta = h->d_beta; a.e_run = h->d_e_run; a.m_run = h->d_m_run; a.rej = h->d_rej;
     a.phase = phase;
     a.measure = measure; a.n_meas = (int)n_meas; a.steps_measure = steps_measure; a.meas_base = meas_base;
@@ -431,10 +435,10 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     sa.Lx = h->L[0]; sa.Ly = h->L[1]; sa.na = h->na; sa.R = h->R; sa.pz = h->pz; sa.cs = h->csize;
     sa.n_local = h->N / h->csize;
     sa.fd_pc = a.fd_pc; sa.fd_hx = a.fd_hx; sa.fd_hy = a.fd_hy;
-    CK(launch_to_slabs(sa, h->st));
+    if (staged) CK(launch_to_slabs(sa, h->st));
     CK(launch_cluster(a, h->csize, h->cthreads, h->csites, h->cluster_smem, h->st));
-    CK(launch_from_slabs(sa, h->st));
-    h->launches += 3;
+    if (staged) CK(launch_from_slabs(sa, h->st));
+    h->launches += staged ? 3 : 1;
     return ESP_OK;
 }
 

@@ -105,9 +105,26 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
         for (int i = threadIdx.x; i < a.stencil_words; i += blockDim.x) dst[i] = src[i];
         for (int i = threadIdx.x; i < nhist * a.nf; i += blockDim.x) hist[i] = 0u;
     }
-    // this CTA's slab: one contiguous block of 3 n_local floats
-    float *slab = a.slab + ((size_t)r * csize + rank) * 3 * n_local;
-    for (int i = threadIdx.x; i < 3 * n_local; i += blockDim.x) s3[i] = slab[i];
+    // this CTA's slab: one contiguous block of 3 n_local floats, or gathered
+    // from the spin arrays
+    float *slab = a.slab ? a.slab + ((size_t)r * csize + rank) * 3 * n_local : nullptr;
+    auto slab_global = [&](int l) -> size_t {
+        int k, rem, q1, hx, hy, hzl;
+        fdivmod(l, a.fd_pc, k, rem);
+        fdivmod(rem, a.fd_hx, q1, hx);
+        fdivmod(q1, a.fd_hy, hzl, hy);
+        const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
+        const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pz;
+        return (size_t)__ldg(a.inv + ((z * a.Ly + y) * a.Lx + x) * a.na + at) * a.R + r;
+    };
+    if (slab) {
+        for (int i = threadIdx.x; i < 3 * n_local; i += blockDim.x) s3[i] = slab[i];
+    } else {
+        for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
+            const size_t g = slab_global(l);
+            s3[3 * l] = a.sx[g]; s3[3 * l + 1] = a.sy[g]; s3[3 * l + 2] = a.sz[g];
+        }
+    }
     const int temp = a.temp_of[r];
     const bool cache = a.measure && a.nlev <= kClusterMaxLev;
     if (rank == 0 && cache) {
@@ -540,7 +557,14 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
             }
         }
     }
-    for (int i = threadIdx.x; i < 3 * n_local; i += blockDim.x) slab[i] = s3[i];
+    if (slab) {
+        for (int i = threadIdx.x; i < 3 * n_local; i += blockDim.x) slab[i] = s3[i];
+    } else {
+        for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
+            const size_t g = slab_global(l);
+            a.sx[g] = s3[3 * l]; a.sy[g] = s3[3 * l + 1]; a.sz[g] = s3[3 * l + 2];
+        }
+    }
     // peers may still read this CTA's shared memory until every CTA is done
     cluster.sync();
 }

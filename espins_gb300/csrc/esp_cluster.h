@@ -45,8 +45,12 @@ struct ClusterArgs {
     int Lx, Ly, Lz, na, N, R, nclass, pz;  // pz: z planes per CTA (even)
     int has_b, has_d, has_si, has_f;
     // state: the slabs of every replica, [r][rank][local site][x, y, z],
-    // converted from and to the handle's spin arrays around the launch
+    // converted from and to the handle's spin arrays around the launch; or,
+    // with slab == null (small slabs, where two more launches cost more than
+    // they save), the spin arrays themselves, element (p, r) at p*R + r
     float *slab;
+    float *sx, *sy, *sz;
+    const int32_t *inv;             // reference site -> p
     const int32_t *temp_of;
     const float *beta;
     double *e_run, *m_run;

@@ -23,6 +23,9 @@ def _cases():
         "sc_j1": sc_mcin(8, [(1e-3, NN)], [3.0, 10.0, 30.0]),
         "sc_j123_dm_si": sc_mcin(8, [(1e-3, NN), (3e-4, NNN), (-5e-5, N3)], [5.0, 20.0, 40.0], dm=1e-4, si=-3e-5),
         "sc_j1j2_bq_si": sc_mcin(12, [(1e-3, NN), (-6e-4, NNN)], [2.0, 8.0, 30.0, 12.0], bq=5e-5, si=2e-4),
+        # 4096 sites: one CTA per replica stages its slab through the
+        # contiguous buffer, two or more gather it directly
+        "sc16_j1j2_dm": sc_mcin(16, [(1e-3, NN), (3e-4, NNN)], [3.0, 12.0, 40.0], dm=1e-4),
         "bcc_pt": parse_mcin(lattice_mcin(BCC, 8, [(2e-3, BCC1), (5e-4, NN), (-1e-4, NNN)], tems=[10.0, 20.0, 40.0, 80.0],
                                           single_ion=-5e-5, pt=True, pt_steps_swap=5), "bcc"),
     }
@@ -94,7 +97,7 @@ def test_cluster_kernel_is_chosen_for_invariant_lattices_only():
         assert e.sweep_kernel()[0] == "ell"
 
 
-@pytest.mark.parametrize("case", ["sc_j1j2_bq_si", "bcc_pt"])
+@pytest.mark.parametrize("case", ["sc_j1j2_bq_si", "bcc_pt", "sc16_j1j2_dm"])
 def test_trajectory_does_not_depend_on_cluster_geometry(case):
     """Every (CTAs per replica, threads per CTA) geometry the GPU can run gives
     the same spins and rejected counts (same colour order and random stream);
