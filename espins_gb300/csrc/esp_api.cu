@@ -899,12 +899,24 @@ int cluster_geometry(esp_handle *h, int cs, int nt, int S)
 // with the tables so that the spin transfers themselves allocate nothing.
 int ensure_stage(esp_handle *h)
 {
-    if (h->d_stage) return ESP_OK;
+    if (h->d_stage && h->h_stage && h->stage_slots > 0) return ESP_OK;
+    // set up both halves or neither: a handle left with one of them would
+    // loop forever over zero-slot blocks in esp_set_spins / esp_get_spins
+    dfree(h->d_stage);
+    if (h->h_stage) cudaFreeHost(h->h_stage);
+    h->h_stage = nullptr;
+    h->stage_slots = 0;
     const size_t per_slot = sizeof(double) * 3 * (size_t)h->N;
     int slots = (int)std::max<size_t>(1, ((size_t)256 << 20) / per_slot);
     slots = std::min(slots, h->R);
     CK(dalloc(&h->d_stage, (size_t)3 * h->N * slots));
-    CK(cudaMallocHost((void **)&h->h_stage, sizeof(double) * 3 * (size_t)h->N * slots));
+    cudaError_t e = cudaMallocHost((void **)&h->h_stage, sizeof(double) * 3 * (size_t)h->N * slots);
+    if (e != cudaSuccess) {
+        dfree(h->d_stage);
+        h->h_stage = nullptr;
+        h->err = std::string("cudaMallocHost of the spin staging: ") + cudaGetErrorString(e);
+        return ESP_ENOMEM;
+    }
     h->stage_slots = slots;
     return ESP_OK;
 }

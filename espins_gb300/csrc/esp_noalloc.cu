@@ -54,26 +54,27 @@ __global__ void __launch_bounds__(kThreads) k_energy_noalloc_part(esp_energy_arg
     const double *s = a.spins + (size_t)3 * N * r;
     double e = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-        const float ox = (float)s[3 * i], oy = (float)s[3 * i + 1], oz = (float)s[3 * i + 2];
+        const size_t si = (size_t)3 * i;
+        const float ox = (float)s[si], oy = (float)s[si + 1], oz = (float)s[si + 2];
         float pair = 0.f;
         for (int k = 0; k < a.j_nn[i]; ++k) {
             const size_t el = (size_t)k * N + i;
-            const int j = a.j_nbors[el] - 1;
-            const float d = ox * (float)s[3 * j] + oy * (float)s[3 * j + 1] + oz * (float)s[3 * j + 2];
+            const size_t sj = (size_t)3 * (a.j_nbors[el] - 1);
+            const float d = ox * (float)s[sj] + oy * (float)s[sj + 1] + oz * (float)s[sj + 2];
             pair -= (float)a.j_val[el] * d;
         }
         if (HB)
             for (int k = 0; k < a.b_nn[i]; ++k) {
                 const size_t el = (size_t)k * N + i;
-                const int j = a.b_nbors[el] - 1;
-                const float d = ox * (float)s[3 * j] + oy * (float)s[3 * j + 1] + oz * (float)s[3 * j + 2];
+                const size_t sj = (size_t)3 * (a.b_nbors[el] - 1);
+                const float d = ox * (float)s[sj] + oy * (float)s[sj + 1] + oz * (float)s[sj + 2];
                 pair += (float)a.b_val[el] * d * d;
             }
         if (HD)
             for (int k = 0; k < a.d_nn[i]; ++k) {
                 const size_t el = (size_t)k * N + i;
-                const int j = a.d_nbors[el] - 1;
-                const float tx = (float)s[3 * j], ty = (float)s[3 * j + 1], tz = (float)s[3 * j + 2];
+                const size_t sj = (size_t)3 * (a.d_nbors[el] - 1);
+                const float tx = (float)s[sj], ty = (float)s[sj + 1], tz = (float)s[sj + 2];
                 const float cx = oy * tz - oz * ty, cy = oz * tx - ox * tz, cz = ox * ty - oy * tx;
                 pair += (float)a.d_val[3 * el] * cx + (float)a.d_val[3 * el + 1] * cy + (float)a.d_val[3 * el + 2] * cz;
             }

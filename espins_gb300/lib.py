@@ -1,8 +1,8 @@
 """ctypes binding of libespins_gpu.so (the C ABI in include/espins_gpu.h).
 
 This is the same binding a Python host of the library would write; a Fortran
-host uses the iso_c_binding interface block shown in INTEGRATION.md.  There is
-no CPU fallback: if the library cannot be loaded or no GPU is present, the
+host binds the same entry points with an iso_c_binding interface block.  There
+is no CPU fallback: if the library cannot be loaded or no GPU is present, the
 calls raise.
 """
 from __future__ import annotations

@@ -45,17 +45,14 @@ def fortran_e(x: float, w: int = 15, d: int = 8) -> str:
         body = "0." + "0" * d + "E+00"
         return body.rjust(w)
     sign = "-" if x < 0 else ""
-    a = abs(x)
-    e = math.floor(math.log10(a)) + 1
-    m = a / 10.0 ** e
-    digits = round(m * 10 ** d)
-    if digits >= 10 ** d:  # rounding carried into a new digit
-        digits //= 10
-        e += 1
-    if digits < 10 ** (d - 1):
-        digits *= 10
-        e -= 1
-    s = f"{sign}0.{digits:0{d}d}E{'+' if e >= 0 else '-'}{abs(e):02d}"
+    # the d significant digits of the exact binary value, correctly rounded
+    mant, ex = f"{abs(x):.{d - 1}E}".split("E")
+    digits = mant.replace(".", "")
+    e = int(ex) + 1
+    if abs(e) <= 99:
+        s = f"{sign}0.{digits}E{'+' if e >= 0 else '-'}{abs(e):02d}"
+    else:  # a three-digit exponent takes the place of the letter
+        s = f"{sign}0.{digits}{'+' if e >= 0 else '-'}{abs(e):03d}"
     return s.rjust(w)
 
 
@@ -413,31 +410,56 @@ def write_binerror(path: str, tems, binning: np.ndarray, levels, n: int, pt: boo
                 fh.write(f"  {lvs}        " + "   ".join(fortran_e(v) for v in vals[:ncol]) + "\n")
 
 
+def _steps_line(T: float, tot: int, rej: int, tag: str, pt: bool) -> str:
+    """Format 124 of mcarlo.F90:853 (f10.8, 1x, a) / pt.F90:1126 (f10.8, 4x, a)."""
+    ratio = (tot - rej) / tot if tot else 0.0
+    return (f"   {fortran_f(T, 9, 4)} {tot:14d} {rej:14d}     {tot - rej:14d}       {ratio:10.8f}"
+            + (" " * 4 if pt else " ") + "  <-- " + tag)
+
+
 def mcout_block(tems, res: dict, n: int, pt: bool) -> str:
-    """Accept/reject table and energy triple per temperature (mcarlo.F90:736-753)."""
+    """The .mcout summary of the measurement phase, line for line as the
+    reference prints it.
+
+    mcarlo (mcarlo.F90:736-753): per temperature the WARMUP and MCARLO lines
+    (format 124; ' No Warm-up step is done! ' without warm-up), the energy
+    triple, Delta E and Delta M, a dashed line.  pt_mcarlo (pt.F90:983-1021):
+    the final swap table (format 128; Fortran writes no trailing blanks for a
+    closing 2x) and then per temperature the MCARLO line, the energy triple
+    marked ENERGY3, Delta E, Delta M and the dashed line.  The sections that
+    pt_mcarlo prints during its warm-up (WARMUP1, WARMUP2, the swap log) are
+    not part of this block."""
     out = []
     norm = 1.0 / res["steps_mc_eff"]
+    mark = "  <-- ENERGY3" if pt else "  <-- ENERGY"
+    if pt:
+        out += ["", " *----------------------------------- MONTECARLO ------------------------------------*",
+                " |  Temp_i     Temp_f         Tot-Swaps       Rej-Swaps      Acc-Swaps  Acc/Tot Ratio|",
+                " +-----------------------------------------------------------------------------------+"]
+        for t, T in enumerate(tems):
+            tries, acc = (int(x) for x in res["num_swaps"][t])
+            Tf = tems[int(res["map"][t]) - 1]
+            ratio = acc / tries if tries else 0.0
+            out.append(f"  {fortran_f(T, 9, 4)}  {fortran_f(Tf, 9, 4)} {tries:14d} {tries - acc:14d} "
+                       f"{acc:14d}   {ratio:14.8f}")
+        out += ["", " *----------------------------------- MONTECARLO ------------------------------------*",
+                " |     Temp      Total Steps    Rejected Steps    Accepted Steps   Acc/Tot Ratio     |",
+                " +-----------------------------------------------------------------------------------+"]
     for t, T in enumerate(tems):
-        tot = int(res["steps_tot"][1])
-        rej = int(res["rejected"][t][1])
-        out.append(f"   {fortran_f(T, 9, 4)} {tot:14d} {rej:14d}     {tot - rej:14d}       "
-                   f"{(tot - rej) / tot:10.8f} {' ' * 3 if pt else ''} <-- MCARLO")
+        if not pt:
+            if int(res["steps_tot"][0]) > 0:
+                out.append(_steps_line(T, int(res["steps_tot"][0]), int(res["rejected"][t][0]), "WARMUP", False))
+            else:
+                out.append("  No Warm-up step is done! ")
+        out.append(_steps_line(T, int(res["steps_tot"][1]), int(res["rejected"][t][1]), "MCARLO", pt))
         E = res["energy"][t]
-        out.append(f"     Initial Energy                           = {fortran_e(E[0], 15, 7)}  <-- ENERGY")
-        out.append(f"     Final Energy by adding differences       = {fortran_e(E[1], 15, 7)}  <-- ENERGY")
-        out.append(f"     Final Energy by direct calculations      = {fortran_e(E[2], 15, 7)}  <-- ENERGY")
+        out.append(f"     Initial Energy                           = {fortran_e(E[0], 15, 7)}{mark}")
+        out.append(f"     Final Energy by adding differences       = {fortran_e(E[1], 15, 7)}{mark}")
+        out.append(f"     Final Energy by direct calculations      = {fortran_e(E[2], 15, 7)}{mark}")
         d = res["data"][t]
         dE = math.sqrt(max(d[1] - d[0] ** 2, 0.0) * norm) / n
         dM = math.sqrt(max(d[4] - d[3] ** 2, 0.0) * norm)
         out.append(f"                                 Delta E      = +/- {dE:15.9f}")
         out.append(f"                                 Delta M      = +/- {dM:15.9f}")
         out.append(" " + "-" * 85)
-    if pt:
-        out.append(" |  Temp_i     Temp_f         Tot-Swaps       Rej-Swaps      Acc-Swaps  Acc/Tot Ratio|")
-        for t, T in enumerate(tems):
-            tries, acc = (int(x) for x in res["num_swaps"][t])
-            Tf = tems[int(res["map"][t]) - 1]
-            ratio = acc / tries if tries else 0.0
-            out.append(f"  {fortran_f(T, 9, 4)}  {fortran_f(Tf, 9, 4)} {tries:14d} {tries - acc:14d} "
-                       f"{acc:14d}   {ratio:14.8f}  ")
     return "\n".join(out) + "\n"

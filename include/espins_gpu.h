@@ -6,8 +6,8 @@
  * `call mcarlo_main()` / `call pt_main()`), with all data held in module
  * globals.  A Fortran host keeps param_read and jij_get/bij_get/dij_get,
  * hands the resulting ELL tables to esp_upload_tables, and calls esp_run in
- * place of mcarlo_main/pt_main.  INTEGRATION.md shows the iso_c_binding
- * interface block.
+ * place of mcarlo_main/pt_main, binding these entry points through an
+ * iso_c_binding interface block (bind(C) functions and derived types).
  *
  * Conventions
  *  - Every entry point returns an int status: ESP_OK (0) or an ESP_E* code;

@@ -17,7 +17,14 @@ outputs as text and writes small fixtures next to itself:
 * ``<name>_sconfig.npz``                final spins per temperature
                                         (``_sconfig.dat``, 6 decimals)
 
-Run from the repository root:  python tests/golden/make_golden.py [reference_dir]
+For the byte-compatibility tests of the output writers the fixture also keeps
+verbatim text: every ``_mc.dat`` data line, the ``.mcout`` summary block of
+the first temperatures (with parallel tempering also the final swap table and
+its numbers), the header and first temperature block of ``_sconfig.dat`` and
+the header and kept blocks of ``_pm.dat``.
+
+Run from the repository root, naming the checkout of the reference:
+    python tests/golden/make_golden.py <reference_dir>
 """
 from __future__ import annotations
 
@@ -77,6 +84,22 @@ def parse_pm_dat(text: str, keep):
     return out
 
 
+def pm_dat_lines(text: str, keep):
+    """{T: verbatim lines} of the kept _pm.dat blocks, '#T=' line first."""
+    out, cur = {}, None
+    for ln in text.splitlines():
+        s = ln.strip()
+        if s.startswith("#T="):
+            t = float(s[3:])
+            cur = [ln] if any(abs(t - k) < 1e-4 for k in keep) else None
+            if cur is not None:
+                out["%.4f" % t] = cur
+            continue
+        if cur is not None and s and not s.startswith("#"):
+            cur.append(ln)
+    return out
+
+
 def parse_mcout(text: str) -> dict:
     out = {"seeds": [], "rows": []}
     lines = text.splitlines()
@@ -108,6 +131,53 @@ def parse_mcout(text: str) -> dict:
         if m and cur is not None:
             cur["d" + m.group(1)] = float(m.group(2))
     return out
+
+
+MCOUT_BLOCK_TEMPS = 4
+
+
+def mcout_blocks(text: str, pt: bool):
+    """Verbatim lines of the .mcout summary: per temperature the block from its
+    first '<-- WARMUP' / '<-- MCARLO' line of the measurement summary to the
+    dashed line after 'Delta M' (mcarlo.F90:736-753, pt.F90:1011-1021), for the
+    first MCOUT_BLOCK_TEMPS temperatures; with pt also the final swap table
+    (pt.F90:983-990): its three header lines and rows."""
+    lines = text.splitlines()
+    out = {"blocks": [], "swap_lines": []}
+    if pt:
+        # the last MONTECARLO swap table
+        idx = [i for i, ln in enumerate(lines) if "Temp_i     Temp_f" in ln]
+        if idx:
+            i = idx[-1] - 1
+            j = i + 3
+            while j < len(lines) and lines[j].strip():
+                j += 1
+            out["swap_lines"] = lines[i:j]
+    i = 0
+    while i < len(lines) and len(out["blocks"]) < MCOUT_BLOCK_TEMPS:
+        ln = lines[i]
+        starts = ln.rstrip().endswith("<-- WARMUP") or (ln.rstrip().endswith("<-- MCARLO") and not (
+            i > 0 and lines[i - 1].rstrip().endswith("<-- WARMUP")))
+        # the measurement summary lines of PT are marked ENERGY3
+        if starts and (not pt or (i + 1 < len(lines) and "ENERGY3" in lines[i + 1])):
+            j = i
+            while j < len(lines) and not lines[j].startswith(" ----"):
+                j += 1
+            out["blocks"].append(lines[i:j + 1])
+            i = j + 1
+            continue
+        i += 1
+    return out
+
+
+def parse_swaps(lines):
+    """(T_i, T_f, tries, rejected, accepted, ratio) rows of a swap table."""
+    rows = []
+    for ln in lines:
+        s = ln.split()
+        if len(s) == 6 and not ln.strip().startswith(("|", "*", "+")):
+            rows.append([float(s[0]), float(s[1]), int(s[2]), int(s[3]), int(s[4]), float(s[5])])
+    return rows
 
 
 def parse_mc_dat(text: str):
@@ -143,11 +213,21 @@ def main(ref_root: str) -> None:
             fh.write(mcin)
         gold = {"source": os.path.join(d, seed)}
         with open(os.path.join(base, seed + ".mcout")) as fh:
-            gold.update(parse_mcout(fh.read()))
+            mcout = fh.read()
+        gold.update(parse_mcout(mcout))
+        pt = bool(re.search(r"^\s*pt\s*=\s*\.true\.", mcin, re.I | re.M))
+        blk = mcout_blocks(mcout, pt)
+        gold["mcout_blocks"] = blk["blocks"]
+        if pt:
+            gold["swap_lines"] = blk["swap_lines"]
+            gold["swaps"] = parse_swaps(blk["swap_lines"])
         mcdat = os.path.join(base, seed + "_mc.dat")
         if os.path.exists(mcdat):
             with open(mcdat) as fh:
-                gold["mc_dat"] = parse_mc_dat(fh.read())
+                text = fh.read()
+            gold["mc_dat"] = parse_mc_dat(text)
+            gold["mc_dat_lines"] = [ln for ln in text.splitlines() if ln.strip() and not ln.strip().startswith("#")]
+            gold["mc_dat_head"] = text.splitlines()[1:4]
         for kind in ("op", "staggered"):
             f = os.path.join(base, seed + "_" + kind + ".dat")
             if os.path.exists(f):
@@ -164,11 +244,20 @@ def main(ref_root: str) -> None:
         pmf = os.path.join(base, seed + "_pm.dat")
         if PM_TEMPS.get(name) and os.path.exists(pmf):
             with open(pmf) as fh:
-                gold["pm_dat"] = parse_pm_dat(fh.read(), PM_TEMPS[name])
+                text = fh.read()
+            gold["pm_dat"] = parse_pm_dat(text, PM_TEMPS[name])
+            gold["pm_dat_head"] = text.splitlines()[1:4]
+            gold["pm_dat_lines"] = pm_dat_lines(text, PM_TEMPS[name])
         scf = os.path.join(base, seed + "_sconfig.dat")
         if keep != 0 and os.path.exists(scf):
             with open(scf) as fh:
-                sc, temps, spins = parse_sconfig(fh.read(), keep)
+                text = fh.read()
+            sc, temps, spins = parse_sconfig(text, keep)
+            nw = int(text.splitlines()[2].split()[0])
+            # header after the date line, and the first temperature's block
+            # (small lattices only)
+            if nw <= 256:
+                gold["sconfig_lines"] = text.splitlines()[1:3 + 1 + nw]
             np.savez_compressed(os.path.join(HERE, name + "_sconfig.npz"),
                                 supercell=np.array(sc), temps=temps, spins=spins)
         with open(os.path.join(HERE, name + "_golden.json"), "w") as fh:
@@ -177,4 +266,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference_dir>")
+    main(sys.argv[1])

@@ -7,7 +7,7 @@ The script's input (its shipped E.dat: temperature and energy per site) and
 its converged temperatures (the array Tout, full precision) for two settings
 are written to optimize_t_golden.json next to this file.
 
-Run from the repository root:  python tests/golden/make_optimize_t_golden.py [reference_dir]
+Run from the repository root:  python tests/golden/make_optimize_t_golden.py <reference_dir>
 """
 import json
 import os
@@ -45,4 +45,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_optimize_t_golden.py <reference_dir>")
+    main(sys.argv[1])

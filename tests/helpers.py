@@ -61,6 +61,12 @@ NNN = [(a, b, 0) for a in (1, -1) for b in (1, -1)] + [(a, 0, b) for a in (1, -1
 N3 = [(a, b, c) for a in (1, -1) for b in (1, -1) for c in (1, -1)]
 
 
+# FP32 site arithmetic against the FP64 oracle: errors relative to the
+# coupling-magnitude scales below (energy_scale for totals, site_scale per site)
+ENERGY_RTOL = 2e-6
+FIELD_RTOL = 2e-6
+
+
 def energy_scale(h):
     """Sum of |coupling| magnitudes: the floor for relative energy errors."""
     s = 0.5 * np.abs(h.jij.val).sum()

@@ -13,7 +13,13 @@ The reference has no unit tests; its example runs are the known answers:
 * energy fixtures: the final spins of every temperature and the printed
   "Final Energy by direct calculations" (energy_get, get_quant.F90:186-261);
 * MT19937 (mtprng.f90) against numpy's MT19937 for non-negative seeds, and
-  Philox4x32-10 against the Random123 known-answer vectors.
+  Philox4x32-10 against the Random123 known-answer vectors;
+* byte compatibility of the output writers: the replayed numbers rendered by
+  espins_gb300.writers give the reference's own lines character for
+  character -- the _mc.dat row (format 125, mcarlo.F90:854), the .mcout
+  summary block (mcarlo.F90:736-753), the _sconfig.dat header and spin block
+  (mcarlo.F90:112-114,813-816) and the _pm.dat block (mcarlo.F90:784-811);
+  read_sconfig (get_quant.F90:543-598) reads the reference's file back.
 """
 import json
 import os
@@ -22,6 +28,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from espins_gb300 import writers as W
 from espins_gb300.mcin import K_B, read_mcin
 from espins_gb300.tables import build_hamiltonian, build_shells
 
@@ -109,7 +116,12 @@ def _e8(x):
     return float("%.7E" % x)
 
 
-def _replay(golden_dir, name, rank, check_mcdat=True, check_obs=False, check_spincorr=False):
+def _file_lines(path):
+    with open(path) as fh:
+        return fh.read().splitlines()
+
+
+def _replay(golden_dir, name, rank, check_mcdat=True, check_obs=False, check_spincorr=False, tmp_path=None):
     inp, g = _load(golden_dir, name)
     h = build_hamiltonian(inp)
     H = O.Ham(h)
@@ -145,6 +157,18 @@ def _replay(golden_dir, name, rank, check_mcdat=True, check_obs=False, check_spi
         for a, b in zip(got[1:], ref[1:]):
             # Fortran E15.8 keeps 8 significant digits
             assert float("%.7E" % a) == pytest.approx(b, rel=1e-12, abs=1e-300)
+        # the writers render the same numbers as the reference's lines
+        assert W.mc_dat_row(T, d, N) == g["mc_dat_lines"][t_index]
+        res = {"steps_mc_eff": inp.steps_mc, "steps_tot": r["steps_tot"], "rejected": [r["rejected"]],
+               "energy": [r["energy"]], "data": [d]}
+        assert W.mcout_block([T], res, N, False).splitlines() == g["mcout_blocks"][t_index]
+        if tmp_path is not None and "sconfig_lines" in g and t_index == 0:
+            allspins = np.repeat(s[None], inp.tems_num, axis=0)
+            path = os.path.join(str(tmp_path), "x_sconfig.dat")
+            W.write_sconfig(path, inp.supercell_size, inp.tems, allspins)
+            lines = _file_lines(path)
+            assert lines[0].startswith(" Created on ")
+            assert lines[1:1 + len(g["sconfig_lines"])] == g["sconfig_lines"]
     if check_obs:
         N = h.n
         beta = 1.0 / T
@@ -165,6 +189,14 @@ def _replay(golden_dir, name, rank, check_mcdat=True, check_obs=False, check_spi
         for f in range(pm.size):
             assert _e8(pm[f]) == pytest.approx(rows[f, 1], rel=1e-12, abs=1e-300), f
             assert _e8(pop[f]) == pytest.approx(rows[f, 2], rel=1e-12, abs=1e-300), f
+        if tmp_path is not None:
+            m_max = float(np.abs(inp.mag_cell).sum())
+            path = os.path.join(str(tmp_path), "x_pm.dat")
+            W.write_pm_dat(path, [T], pm[None], -m_max, m_max, pm_op=pop[None], pt=False)
+            lines = _file_lines(path)
+            assert lines[0].startswith(" #written on ")
+            assert lines[1:4] == g["pm_dat_head"]
+            assert lines[4:] == g["pm_dat_lines"]["%.4f" % T]
     if check_spincorr:
         # global_spincorr * normalize / N (mcarlo.F90:717-723), printed f12.9
         normalize = 1.0 / inp.steps_mc
@@ -178,8 +210,8 @@ def _replay(golden_dir, name, rank, check_mcdat=True, check_obs=False, check_spi
     return r
 
 
-def test_seed_exact_replay_ex01_negative_seed(golden_dir):
-    _replay(golden_dir, "ex01_cubic", rank=0)
+def test_seed_exact_replay_ex01_negative_seed(golden_dir, tmp_path):
+    _replay(golden_dir, "ex01_cubic", rank=0, tmp_path=tmp_path)
 
 
 def test_seed_exact_replay_ex01_positive_seed(golden_dir):
@@ -190,5 +222,61 @@ def test_seed_exact_replay_ex05_biquadratic_singleion(golden_dir):
     _replay(golden_dir, "ex05_snwo", rank=0, check_mcdat=True, check_spincorr=True)
 
 
-def test_seed_exact_replay_ex03_biquadratic_dm(golden_dir):
-    _replay(golden_dir, "ex03_fef3", rank=1, check_mcdat=True, check_obs=True)
+def test_seed_exact_replay_ex03_biquadratic_dm(golden_dir, tmp_path):
+    _replay(golden_dir, "ex03_fef3", rank=1, check_mcdat=True, check_obs=True, tmp_path=tmp_path)
+
+
+def test_read_sconfig_reads_the_reference_file(golden_dir, tmp_path):
+    """read_sconfig on the reference's _sconfig.dat text (header and the first
+    temperature block of example01): spins normalised to unit length, and the
+    reference's error checks (mcarlo_read_sconfig, get_quant.F90:543-598)."""
+    _, g = _load(golden_dir, "ex01_cubic")
+    lines = list(g["sconfig_lines"])
+    n = int(lines[1].split()[0])
+    lines[1] = f"{n:6d}{1:6d}"            # the fixture keeps one temperature block
+    path = os.path.join(str(tmp_path), "ref_sconfig.dat")
+    with open(path, "w") as fh:
+        fh.write(" Created on  1Dec2019 at 16:53:37 \n" + "\n".join(lines) + "\n")
+    z = np.load(os.path.join(golden_dir, "ex01_cubic_sconfig.npz"))
+    got = W.read_sconfig(path, n, [25.0])
+    want = z["spins"][0] / np.linalg.norm(z["spins"][0], axis=1, keepdims=True)
+    assert got.shape == (1, n, 3)
+    assert np.allclose(got[0], want, atol=1e-15)
+    with pytest.raises(ValueError, match="Wrong matrix size"):
+        W.read_sconfig(path, n + 1, [25.0])
+    with pytest.raises(ValueError, match="Wrong temperature number"):
+        W.read_sconfig(path, n, [25.0, 30.0])
+    with pytest.raises(ValueError, match="Mismatch in temperatures"):
+        W.read_sconfig(path, n, [25.01])
+    lines[3] = "    0.000000    0.000000    0.000000"
+    with open(path, "w") as fh:
+        fh.write(" Created\n" + "\n".join(lines) + "\n")
+    with pytest.raises(ValueError, match="zero"):
+        W.read_sconfig(path, n, [25.0])
+
+
+def test_pt_mcout_block_layout(golden_dir):
+    """The parallel-tempering summary (pt.F90:983-1021) rendered from
+    example02's printed numbers reproduces its lines: the final swap table
+    (format 128) and, per temperature, the MCARLO line and the energy triple
+    marked ENERGY3.  (Delta E / Delta M need the unprinted accumulators.)"""
+    inp, g = _load(golden_dir, "ex02_cubic_pt", nodes=32)
+    tems = [r["T"] for r in g["rows"]]
+    R = len(tems)
+    sw = g["swaps"]
+    res = {
+        "steps_mc_eff": inp.steps_mc,
+        "steps_tot": [0, g["rows"][0]["mc"][0]],
+        "rejected": [[0, r["mc"][1]] for r in g["rows"]],
+        "energy": [[r["E_init"], r["E_add"], r["E_direct"]] for r in g["rows"]],
+        "data": [[0.0] * 6 for _ in range(R)],
+        "num_swaps": [[row[2], row[4]] for row in sw],
+        "map": [1 + min(range(R), key=lambda k: abs(tems[k] - row[1])) for row in sw],
+    }
+    lines = W.mcout_block(tems, res, 2744, True).splitlines()
+    n_swap = len(g["swap_lines"])
+    assert lines[1:1 + n_swap] == g["swap_lines"]
+    blocks = lines[1 + n_swap + 4:]
+    for t, ref in enumerate(g["mcout_blocks"]):
+        got = blocks[7 * t: 7 * t + 7]
+        assert got[:4] == ref[:4], t

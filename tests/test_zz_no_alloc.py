@@ -4,19 +4,22 @@ It exists for hosts that cannot let a library call cudaMalloc: the caller owns
 every device buffer (here torch allocates them, standing in for such a host)
 and the entry point's partial sums live in a fixed array inside the library.
 Its results must match the regular entry point esp_energy, which allocates its
-scratch per handle, within the energy tolerance of the parity tests
-(2e-6 of the sum of coupling magnitudes), on two calls in a row with
-different inputs.  The file sorts last so that a stop-at-first-failure run
-has run every other test before it.
+scratch per handle, and the FP64 oracle's energy_get of the same (FP32-rounded)
+spins, within the energy tolerance of the parity tests, on two calls in a row
+with different inputs; the second Hamiltonian adds a Zeeman field, so every
+term of energy_get (exchange, biquadratic, DM, single-ion, field) is covered.
+The file sorts last so that a stop-at-first-failure run has run every other
+test before it.
 """
 import ctypes as C
 
 import numpy as np
 import pytest
 
+import oracle as O
 from espins_gb300 import lib as L
 from espins_gb300.tables import build_hamiltonian
-from helpers import NN, NNN, energy_scale, sc_mcin
+from helpers import ENERGY_RTOL, NN, NNN, energy_scale, sc_mcin
 
 pytestmark = pytest.mark.gpu
 
@@ -41,6 +44,8 @@ def _device_args(torch, h, spins):
         a.d_nn, a.d_nbors, a.d_val = d(h.dij.nn, torch.int32), d(h.dij.nb + 1, torch.int32), d(h.dij.val, torch.float64)
     if h.si_axis is not None:
         a.si_axis, a.si_delta = d(h.si_axis, torch.float64), d(h.si_delta, torch.float64)
+    if h.field_axis is not None:
+        a.field_axis, a.field_val = d(h.field_axis, torch.float64), d(h.field_val, torch.float64)
     return a, keep
 
 
@@ -56,15 +61,19 @@ def test_energy_noalloc_matches_esp_energy_twice():
     torch = pytest.importorskip("torch")
     assert torch.cuda.is_available()
     lib = L.load()
-    inp = sc_mcin(6, [(1e-3, NN), (3e-4, NNN)], [5.0, 12.0, 25.0], bq=1e-4, dm=2e-4, si=-3e-5)
-    h = build_hamiltonian(inp)
+    field = "ham_field = .true.\nbegin field_axes_cart\nFe 0.3 -0.2 0.9 2.5\nend field_axes_cart\n"
     rng = np.random.default_rng(11)
-    tol = 2e-6 * energy_scale(h)
     stream = torch.cuda.current_stream()
-    for call, R in enumerate((3, 5)):
+    for call, (R, extra) in enumerate(((3, ""), (5, field))):
+        inp = sc_mcin(6, [(1e-3, NN), (3e-4, NNN)], [5.0, 12.0, 25.0], bq=1e-4, dm=2e-4, si=-3e-5, extra=extra)
+        h = build_hamiltonian(inp)
+        assert (h.field_axis is not None) == bool(extra)
+        tol = ENERGY_RTOL * energy_scale(h)
         v = rng.normal(size=(R, h.n, 3))
         spins = v / np.linalg.norm(v, axis=2, keepdims=True)
         ref = _regular_energy(h, spins, np.linspace(5.0, 25.0, R))
+        H = O.Ham(h)
+        oracle = np.array([H.energy(np.float32(s).astype(np.float64).reshape(-1)) for s in spins])
         args, keep = _device_args(torch, h, spins)
         out = torch.full((R,), float("nan"), dtype=torch.float64, device="cuda")
         rc = lib.esp_energy_noalloc(C.byref(args), C.c_void_p(out.data_ptr()), C.c_void_p(stream.cuda_stream))
@@ -72,6 +81,7 @@ def test_energy_noalloc_matches_esp_energy_twice():
         torch.cuda.synchronize()
         got = out.cpu().numpy()
         assert np.max(np.abs(got - ref)) <= tol, (call, got, ref, tol)
+        assert np.max(np.abs(got - oracle)) <= tol, (call, got, oracle, tol)
 
 
 def test_energy_noalloc_rejects_too_many_replicas():
