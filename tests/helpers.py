@@ -62,9 +62,11 @@ N3 = [(a, b, c) for a in (1, -1) for b in (1, -1) for c in (1, -1)]
 
 
 # FP32 site arithmetic against the FP64 oracle: errors relative to the
-# coupling-magnitude scales below (energy_scale for totals, site_scale per site)
-ENERGY_RTOL = 2e-6
-FIELD_RTOL = 2e-6
+# coupling-magnitude scales below (energy_scale for totals, site_scale per
+# site).  Measured on GB300 over the reference examples and the benchmark
+# Hamiltonians: at most 4.1e-8 for totals and 3.9e-7 for local fields.
+ENERGY_RTOL = 1e-6
+FIELD_RTOL = 1e-6
 
 
 def energy_scale(h):
@@ -89,3 +91,33 @@ def site_scale(h):
     if h.si_delta is not None:
         sc = sc + np.abs(h.si_delta).max()
     return sc
+
+
+def bonferroni_z(K, alpha=0.01):
+    """Two-sided normal bound z with K * P(|Z| > z) = alpha."""
+    import math
+    lo, hi = 0.0, 10.0
+    for _ in range(100):
+        mid = 0.5 * (lo + hi)
+        if K * math.erfc(mid / math.sqrt(2.0)) > alpha:
+            lo = mid
+        else:
+            hi = mid
+    return hi
+
+
+def check_z(z, labels, what):
+    """The 3-sigma criterion of the statistical tests over K = z.size
+    comparisons: every |z| <= 3, except that up to ceil(1 + 0.0027 K) of them
+    (0.27% is the two-sided 3-sigma tail) may lie between 3 and the Bonferroni
+    bound of the family (two-sided 1% over K).  labels(i) names comparison i
+    of the flattened z.  Returns the worst |z|."""
+    import math
+    az = np.abs(np.asarray(z, dtype=float)).reshape(-1)
+    assert np.all(np.isfinite(az)), (what, z)
+    K = az.size
+    over = [(labels(i), float(az[i])) for i in np.nonzero(az > 3.0)[0]]
+    assert len(over) <= math.ceil(1 + 0.0027 * K), (what, over)
+    zK = bonferroni_z(K)
+    assert np.all(az <= zK), (what, zK, over)
+    return float(az.max()) if K else 0.0

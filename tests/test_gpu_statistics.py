@@ -7,15 +7,23 @@ independent chains (COPIES replicas on the GPU, ORACLE_CHAINS typewriter
 chains on the CPU) and requires |<x>_gpu - <x>_oracle| <= 3 sigma for
 x = E/N and |m|, with sigma combined from every chain's binning analysis
 (mcarlo.F90:635-656): the largest of the binning error estimates over block
-sizes 2^5..2^9.  Seeds are fixed, so the outcome is deterministic.
+sizes 2^5..2^9.  The derived columns of _mc.dat -- C, chi and the Binder
+cumulants U_E, U_M (mcarlo.F90:725-731) -- are compared the same way, with
+the GPU chains' jackknife errors (40 blocks of each chain's measurement
+series) and, for the oracle's chains, whose series are not kept, the GPU
+chains' error per chain (same chain length and move set) scaled to the
+number of oracle chains.  Over all temperatures and observables of a test the
+3-sigma criterion of helpers.check_z applies.  Seeds are fixed, so the
+outcome is deterministic.
 """
 import numpy as np
 import pytest
 
 import oracle as O
+from espins_gb300 import analysis as A
 from espins_gb300.lib import Engine
 from espins_gb300.tables import build_hamiltonian
-from helpers import NN, NNN, energy_scale, sc_mcin
+from helpers import NN, NNN, check_z, energy_scale, sc_mcin
 
 pytestmark = pytest.mark.gpu
 
@@ -36,8 +44,39 @@ def _gpu_run(h, tems, pt, warm, mc, pss=10, mode=0, tilt=0.125, seed=12345):
         e.upload(h)
         e.set_temperatures(tems)
         e.init_spins("ferro")
-        return e.run(warm, mc, 1, pt=pt, pt_steps_swap=pss, mode=mode, tilt=tilt, seed=seed,
-                     binning_level=LEVELS)
+        e.set_series(mc)
+        res = e.run(warm, mc, 1, pt=pt, pt_steps_swap=pss, mode=mode, tilt=tilt, seed=seed,
+                    binning_level=LEVELS)
+        res["series"] = e.series()
+    assert res["series"].shape[0] == mc
+    return res
+
+
+DERIVED = ("C", "chi", "U_E", "U_M")
+
+
+def _derived(T, n, gpu_series, or_data):
+    """C, chi, U_E, U_M: (mean over GPU chains, its sigma) and (mean over the
+    oracle's chains, its estimated sigma).  gpu_series: list of (E, |m|)
+    series per GPU chain; or_data: list of normalised accumulators (6,)."""
+    gv, gs = [], []
+    for ser in gpu_series:
+        v, s = A.jackknife_observables(ser[:, 0], ser[:, 1], T, n, 40)
+        gv.append(v[2:]); gs.append(s[2:])
+    gv, gs = np.array(gv), np.array(gs)
+    ov = np.array([A.observables_of(T, d, n)[2:] for d in or_data])
+    per_chain = np.sqrt((gs ** 2).mean(axis=0))
+    return gv.mean(axis=0), np.sqrt((gs ** 2).sum(axis=0)) / len(gv), ov.mean(axis=0), per_chain / np.sqrt(len(ov))
+
+
+def _check_derived(h, tems, gpu_series, or_data, what):
+    """gpu_series[t]: per-chain (E, |m|) series; or_data[t]: per-chain accumulators."""
+    z = np.zeros((len(tems), len(DERIVED)))
+    for t, T in enumerate(tems):
+        g, sg, o, so = _derived(T, h.n, gpu_series[t], or_data[t])
+        z[t] = (g - o) / np.sqrt(sg ** 2 + so ** 2)
+    worst = check_z(z, lambda i: (float(tems[i // len(DERIVED)]), DERIVED[i % len(DERIVED)]), what)
+    print(f"\n{what}: worst |z| of C, chi, U_E, U_M = {worst:.2f}")
 
 
 def _mean_sigma(datas, bins, n):
@@ -64,7 +103,9 @@ def _gpu_copies(h, tems, warm, mc, **kw):
     d = res["data"].reshape(len(tems), COPIES, 6)
     b = res["binning"].reshape(len(tems), COPIES, len(LEVELS), 2)
     e = res["energy"]
-    return [list(x) for x in d], [list(x) for x in b], e
+    ser = res["series"].reshape(mc, len(tems), COPIES, 2)
+    series = [[ser[:, t, c, :] for c in range(COPIES)] for t in range(len(tems))]
+    return [list(x) for x in d], [list(x) for x in b], e, series
 
 
 def _oracle_chains(h, tems, warm, mc, seed0, **kw):
@@ -88,9 +129,10 @@ def test_plain_metropolis_matches_reference_algorithm(mode):
     h = build_hamiltonian(inp)
     tems = inp.tems
     warm, mc = 2000, 40000
-    gd, gb, e = _gpu_copies(h, tems, warm, mc, mode=mode, tilt=0.3)
+    gd, gb, e, gs = _gpu_copies(h, tems, warm, mc, mode=mode, tilt=0.3)
     od, ob = _oracle_chains(h, tems, warm, mc, 1000, mode=mode, tilt=0.3)
     _check(h, tems, gd, gb, od, ob, f"plain mode={mode}")
+    _check_derived(h, tems, gs, od, f"plain mode={mode}")
     # the energy bookkeeping of the run: final by differences == direct, up to
     # the FP32 rounding of ~1e7 accumulated energy differences
     assert np.max(np.abs(e[:, 1] - e[:, 2])) <= 1e-5 * energy_scale(h)
@@ -101,9 +143,10 @@ def test_plain_metropolis_biquadratic_dm_singleion():
     h = build_hamiltonian(inp)
     tems = inp.tems
     warm, mc = 2000, 30000
-    gd, gb, _ = _gpu_copies(h, tems, warm, mc)
+    gd, gb, _, gs = _gpu_copies(h, tems, warm, mc)
     od, ob = _oracle_chains(h, tems, warm, mc, 77)
     _check(h, tems, gd, gb, od, ob, "J+B+D+SI")
+    _check_derived(h, tems, gs, od, "J+B+D+SI")
 
 
 def test_parallel_tempering_matches_reference_algorithm():
@@ -121,6 +164,7 @@ def test_parallel_tempering_matches_reference_algorithm():
     gb = res["binning"] * h.n
     ob = r["binning"] * h.n
     _check(h, tems, [[d] for d in res["data"]], [[b] for b in gb], [[d] for d in or_data], [[b] for b in ob], "pt")
+    _check_derived(h, tems, [[res["series"][:, t, :]] for t in range(len(tems))], [[d] for d in or_data], "pt")
     # swap acceptance per temperature: binomial tolerance
     ga = res["num_swaps"][:, 1] / np.maximum(res["num_swaps"][:, 0], 1)
     oa = r["num_swaps"][:, 1] / np.maximum(r["num_swaps"][:, 0], 1)
