@@ -1,32 +1,40 @@
 #!/usr/bin/env python
 """Throughput benchmark of the GB300 Monte Carlo path.
 
-Workload (default ``bcc24_pt``): parallel tempering on a bcc lattice of 24^3
-conventional cells (27,648 spins), J1=+2.0, J2=+0.5, J3=-0.1 meV, easy-axis
-single-ion 0.05 meV along z, 48 replicas geometrically spaced 10-80 K, a
-replica exchange every 10 sweeps, FP32 spins and fields with FP64 energy
-totals and swap exponent, uniform random start on S^2 from seed 2.  Inputs are
-synthetic (the reference ships no benchmark data).
+Workload (default ``batch512_pt``, the largest configuration that fits one
+GPU): 512 independent simple-cubic lattices with L drawn uniformly from
+{8, 12, ..., 48} (seed 3; 17.6 M sites), J1 = +1.0 meV, nearest-neighbour
+biquadratic 0.1 meV and DM 0.2 meV along the unit bond vector, 16 parallel-
+tempering replicas per lattice log-spaced 2-25 K (3.4 GB of FP32 spins),
+every lattice advanced in replayed CUDA graphs with the sweep kernel chosen
+per size by the library's autotuner.  Inputs are synthetic (the reference
+ships no benchmark data): uniform random spins on S^2.
 
-A step is one swap interval of the measurement phase for all replicas:
-10 sweeps (every colour class), 10 measurements (energy/magnetisation
-accumulators, binning, P(M) histogram) and one exchange (esp_advance(1)).
-Metric: site updates/s = steps * 10 * N * R / time.
+A step is one swap interval of the measurement phase for all replicas of all
+lattices: 10 sweeps (every colour class), 10 measurements (energy and
+magnetisation accumulators, binning, P(M)) and one exchange within each
+lattice.  Metric: site updates/s = steps * 10 * sum(N * R) / time.
 
 * ``value``: device time of the timed steps, CUDA events on the library's
-  stream, L2 flushed (256 MB write) before every timed step, outside the events.
-* ``e2e``: the same metric through the C ABI with host buffers: set spins from
-  host memory, run the steps, collect results and read the spins back, wall
-  clock, copies included.
-* ``roofline``: the sweep kernel, 24 B of compulsory spin traffic per site
-  update (read + write of one FP32 3-vector), against the measured HBM copy
-  bandwidth.
+  stream (the state is larger than L2; the single-lattice workloads flush L2
+  with a 256 MB write before every timed step, outside the events).
+* ``e2e``: the same metric through the C ABI with host buffers, as one job:
+  every lattice's spin_matrix set from host memory, esp_begin, the steps,
+  esp_collect and esp_get_spins of every lattice, wall clock.
+* ``roofline``: the dominant sweep kernel (the largest lattice size), 24 B of
+  compulsory spin traffic per site update (read + write of one FP32
+  3-vector), against the measured HBM copy bandwidth; ``traffic`` from the
+  ncu capture summarised in profiles/dram_traffic.json.
 * ``cpu_baseline``: the FP64 oracle (a restatement of the reference's Fortran:
   typewriter sweeps, MT19937) on the host cores, one thread per block of
   temperatures as the reference's MPI ranks, on a bounded sample.
+* ``secondary``: the HBM-resident single-lattice workload sc128_pt (SC 128^3
+  x 64 replicas), device-timed, from a separate process.
 
-``--impl reference`` times that CPU implementation alone (the reference itself
-is Fortran + MPI and cannot be built in this image).
+``--impl reference`` times that CPU implementation alone on the same
+workload (the reference itself is Fortran + MPI and cannot be built in this
+image).  Other workloads: ``--workload bcc24_pt | sc16_plain |
+sc48_frustrated_pt | sc128_pt``.
 
 ``--proposal compare`` (with ``--workload sc48_frustrated_pt``) measures the
 learned proposal instead: it collects 10^7 (environment, spin) pairs from the
@@ -54,14 +62,18 @@ sys.path.insert(0, ROOT)
 def _args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", default="bcc24_pt")
+    p.add_argument("--workload", default="batch512_pt")
+    p.add_argument("--secondary", dest="secondary", action="store_true", default=True,
+                   help="with batch512_pt: also a short device-timed run of sc128_pt (separate process)")
+    p.add_argument("--no-secondary", dest="secondary", action="store_false")
     p.add_argument("--L", type=int, default=None)
     p.add_argument("--replicas", type=int, default=None)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--proposal", choices=["plain", "learned", "compare"], default="plain")
     p.add_argument("--lp-engine", choices=["mma", "tcgen05"], default="tcgen05")
@@ -151,71 +163,137 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(inp, ham, seconds: float, threads: int, seed: int, max_intervals=None):
-    """The oracle's PT main phase on host threads, bounded to about `seconds`."""
+def _oracle_lib():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import ctypes as C
 
     import oracle as O
     lib = O.lib()
     lib.or_pt_bench.argtypes = [C.POINTER(O.OrHam), C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int64,
-                                C.c_int64, C.c_int64, C.c_int, C.c_double, C.c_int32]
+                                C.c_int64, C.c_int64, C.c_int, C.c_double, C.c_int32, C.POINTER(C.c_double)]
     lib.or_pt_bench.restype = C.c_int64
-    H = O.Ham(ham)
-    R = inp.tems_num
-    tems = np.ascontiguousarray(inp.tems, dtype=np.float64)
-    spins = np.ascontiguousarray(_uniform_spins(R, ham.n, ham.mag, seed).reshape(-1))
-    pss = inp.pt_steps_swap if inp.pt else 1
-    mode = 1 if inp.mcarlo_mode.startswith("const") else 0
+    return O, lib
 
-    def run(k):
-        t0 = time.perf_counter()
-        n = lib.or_pt_bench(H.ref, threads, R, tems.ctypes.data, spins.ctypes.data, k, pss,
-                            inp.steps_measure, mode, inp.tilt_angles_max, seed)
-        return n, time.perf_counter() - t0
 
-    n1, t1 = run(1)
+class PortRun:
+    """The oracle's PT main phase (the reference's algorithm: typewriter
+    sweeps, MT19937, measurements after every steps_measure sweeps, pt_swap)
+    on one lattice's replicas, block-split over host threads as the reference
+    splits temperatures over MPI ranks.  Each call of run(k) times k swap
+    intervals inside the C code, from the barrier after the threads' set-up to
+    the last interval, so neither the initial energies nor the thread
+    start-up are timed; the spins carry over between calls."""
+
+    def __init__(self, inp, ham, threads, seed, tems=None):
+        import ctypes as C
+        O, self.lib = _oracle_lib()
+        self.C = C
+        self.H = O.Ham(ham)
+        self.tems = np.ascontiguousarray(inp.tems if tems is None else tems, dtype=np.float64)
+        self.R = self.tems.size
+        self.spins = np.ascontiguousarray(_uniform_spins(self.R, ham.n, ham.mag, seed).reshape(-1))
+        self.pss = inp.pt_steps_swap if inp.pt else 1
+        self.measure = inp.steps_measure
+        self.mode = 1 if inp.mcarlo_mode.startswith("const") else 0
+        self.tilt = inp.tilt_angles_max
+        self.threads = max(1, min(threads, self.R))
+        self.seed = seed
+
+    def run(self, k):
+        secs = self.C.c_double(0.0)
+        n = self.lib.or_pt_bench(self.H.ref, self.threads, self.R, self.tems.ctypes.data, self.spins.ctypes.data,
+                                 int(k), self.pss, self.measure, self.mode, self.tilt, self.seed, self.C.byref(secs))
+        return int(n), float(secs.value)
+
+
+def cpu_baseline(inp, ham, seconds: float, threads: int, seed: int):
+    """The oracle port on host threads for about `seconds` of sweeps."""
+    pr = PortRun(inp, ham, threads, seed)
+    n1, t1 = pr.run(1)
     k = max(1, int(seconds / max(t1, 1e-6)))
-    if max_intervals:
-        k = min(k, max_intervals)
-    n, t = run(k)
+    n, t = pr.run(k)
     return n / t, {"swap_intervals": k, "updates": int(n), "seconds": t,
-                   "sweeps_per_interval": pss * inp.steps_measure}
+                   "sweeps_per_interval": pr.pss * pr.measure, "threads": pr.threads}
+
+
+def batch_port_rate(sizes, threads, seed, intervals, warm_intervals=1):
+    """The oracle port on the 512-lattice workload: one lattice of every size
+    (its 16 temperatures on min(16, threads) threads) runs `intervals` swap
+    intervals after `warm_intervals` untimed ones; the whole batch's time is
+    the per-size time weighted by the number of lattices of that size.
+    Returns (site updates/s, seconds per interval of the whole batch, detail)."""
+    from espins_gb300.tables import build_hamiltonian
+    from espins_gb300.workloads import batch_lattice_mcin
+    tot_upd, tot_sec, detail = 0.0, 0.0, {}
+    for L, count in sizes.items():
+        inp = batch_lattice_mcin(L)
+        ham = build_hamiltonian(inp, check=False)
+        pr = PortRun(inp, ham, threads, seed + L)
+        if warm_intervals:
+            pr.run(warm_intervals)
+        n, t = pr.run(intervals)
+        tot_upd += count * n
+        tot_sec += count * t
+        detail[str(L)] = {"updates": n, "seconds": t, "threads": pr.threads}
+    return tot_upd / tot_sec, tot_sec / intervals, detail
 
 
 def reference_arm(a, ws, rank):
-    """--impl reference: the CPU implementation of the path on all host threads."""
-    from espins_gb300.tables import build_hamiltonian
-    from espins_gb300.workloads import workload
+    """--impl reference: the CPU implementation of the path (the FP64 oracle
+    port of the reference's Fortran, which cannot be built here) on all host
+    threads, on the same workload, config and metric as our arm.  Warm-up
+    intervals run first, untimed; the timed region is one call over all K
+    intervals, timed inside the C code (sweeps, measurements and swaps only).
+    The 512-lattice workload runs one lattice of every size and weights the
+    sizes by their counts."""
     if rank != 0:
         return
-    inp = workload(a.workload, L=a.L, replicas=a.replicas)
-    ham = build_hamiltonian(inp, check=False)
     threads = os.cpu_count() or 1
-    R = inp.tems_num
-    spins_per_step = (inp.pt_steps_swap if inp.pt else 1) * inp.steps_measure * ham.n * R
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    # each step: one swap interval of every temperature; bounded sample per step
-    rates = []
-    for _ in range(a.warmup):
-        cpu_baseline(inp, ham, 0.0, threads, a.seed, max_intervals=1)
-    t_tot, u_tot = 0.0, 0
-    for _ in range(a.steps):
-        r, info = cpu_baseline(inp, ham, 0.0, threads, a.seed, max_intervals=1)
-        t_tot += info["seconds"]; u_tot += info["updates"]
-    value = u_tot / t_tot
+    if a.workload == "batch512_pt":
+        from espins_gb300.workloads import batch_lattice_sizes
+        sizes = batch_lattice_sizes(512, 3)
+        value, sec_per_step, detail = batch_port_rate(sizes, threads, a.seed, a.steps, a.warmup)
+        config = _batch_config(sizes)
+        sample = (f"one lattice of each of the {len(sizes)} sizes (16 temperatures on 16 threads) for "
+                  f"{a.warmup} untimed + {a.steps} timed swap intervals of 10 sweeps; the batch's time is the "
+                  "per-size time weighted by the lattice counts; FP64 C restatement of the Fortran "
+                  "(typewriter order, MT19937)")
+        t_tot = sec_per_step * a.steps
+        threads_used = min(threads, 16)
+    else:
+        from espins_gb300.tables import build_hamiltonian
+        from espins_gb300.workloads import workload
+        inp = workload(a.workload, L=a.L, replicas=a.replicas)
+        ham = build_hamiltonian(inp, check=False)
+        pr = PortRun(inp, ham, threads, a.seed)
+        if a.warmup:
+            pr.run(a.warmup)
+        n, t_tot = pr.run(a.steps)
+        value = n / t_tot
+        config = _config(inp, ham, a.workload) | {"proposal": a.proposal}
+        sample = (f"{a.warmup} untimed + {a.steps} timed swap intervals of all {pr.R} temperatures "
+                  "in one call; FP64 C restatement of the Fortran (typewriter order, MT19937), temperatures "
+                  "block-split over threads")
+        threads_used = pr.threads
     line = {
         "impl": "reference", "metric": "site updates/s", "value": value, "unit": "site updates/s",
         "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * t_tot / a.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": _config(inp, ham, a.workload),
-        "cpu_baseline": {"value": value, "unit": "site updates/s", "cores": threads, "kind": "port",
-                         "sample": f"{a.steps} steps of one swap interval ({spins_per_step} site updates) each; "
-                                   "FP64 C restatement of the Fortran (typewriter order, MT19937), "
-                                   "temperatures block-split over threads"},
+        "data": "synthetic", "config": config,
+        "cpu_baseline": {"value": value, "unit": "site updates/s", "cores": threads_used, "kind": "port",
+                         "sample": sample},
         "e2e": {"value": value, "unit": "site updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def _batch_config(sizes):
+    nsites = sum(L ** 3 * c for L, c in sizes.items())
+    return {"workload": "batch512_pt", "lattices": 512, "sizes": {str(k): v for k, v in sizes.items()},
+            "sites": nsites, "replicas_per_lattice": 16, "temperatures_K": [2.0, 25.0],
+            "pt_steps_swap": 10, "sweeps_per_step": 10,
+            "l2": f"state {12 * nsites * 16 / 1e9:.2f} GB of spins, larger than L2 (no flush needed)",
+            "parallelism": "all lattices in one device; independent jobs per GPU when n_gpus > 1"}
 
 
 def _config(inp, ham, name):
@@ -330,6 +408,41 @@ def learned_compare(a, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def _traffic(key, units_per_launch):
+    """DRAM bytes per launch of the dominant kernel from the ncu capture
+    summarised in profiles/dram_traffic.json (bytes per site update of that
+    kernel on a captured case, scaled by the site updates of one launch here;
+    the traffic grows in proportion to the updates), or None."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if not os.path.exists(path):
+        return None, None
+    with open(path) as fh:
+        d = json.load(fh)
+    e = d.get(key)
+    if not e:
+        return None, None
+    return float(e["dram_bytes_per_update"]) * units_per_launch, e.get("capture")
+
+
+def secondary_sc128(a, local):
+    """The HBM-resident single-lattice workload (SC 128^3 x 64 replicas) as a
+    second figure: a separate process of this script, device-timed steps only."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--workload", "sc128_pt", "--steps", "5", "--warmup", "3",
+           "--no-cpu-baseline", "--no-secondary", "--no-e2e"]
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES=os.environ.get("CUDA_VISIBLE_DEVICES", str(local)))
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, env=env)
+    except subprocess.TimeoutExpired:
+        return {"workload": "sc128_pt", "error": "timed out"}
+    for ln in r.stdout.splitlines()[::-1]:
+        if ln.startswith("{"):
+            d = json.loads(ln)
+            return {"workload": "sc128_pt", "value": d["value"], "unit": d["unit"], "ms_per_step": d["ms_per_step"],
+                    "steps": d["steps"], "roofline": d["roofline"], "clocks": d.get("clocks"),
+                    "config": d["config"]}
+    return {"workload": "sc128_pt", "error": (r.stderr or r.stdout)[-400:]}
+
+
 def batch_bench(a, ws, rank, local):
     """512 independent SC lattices (L in {8..48}, seed 3) x 16 PT replicas in
     one batch: one handle per lattice size, lattices of a size as replica
@@ -344,8 +457,9 @@ def batch_bench(a, ws, rank, local):
     dev = torch.device("cuda", local)
     sizes = batch_lattice_sizes(512, 3)
     stream = torch.cuda.Stream(dev)
-    engines, upd_per_unit, nsites = [], 0, 0
+    engines, upd_per_unit, nsites, starts_h = [], 0, 0, []
     total_units = a.warmup + a.steps + 64
+    scheds = []
     for L, count in sizes.items():
         inp = batch_lattice_mcin(L)
         ham = build_hamiltonian(inp, check=False)
@@ -354,9 +468,16 @@ def batch_bench(a, ws, rank, local):
         e.upload(ham)
         e.set_temperatures(np.tile(inp.tems, count))
         e.set_pt_groups(16)
-        e.init_spins("rand", seed=a.seed + L)     # one random configuration per lattice size (pt.F90:448-459)
-        e.begin(e.schedule(0, total_units * 10, 1, pt=True, pt_steps_swap=10, seed=3000 + L + 1000 * rank,
-                           binning_level=[1, 2, 3, 4, 5]))
+        e.set_stream(stream.cuda_stream)
+        # one random configuration per lattice (pt.F90:448-459 starts every
+        # replica of a lattice from the same one)
+        s0 = _uniform_spins(count, ham.n, ham.mag, a.seed + 7 * L)
+        starts_h.append(np.repeat(s0, 16, axis=0))
+        e.set_spins(starts_h[-1])
+        sched = e.schedule(0, total_units * 10, 1, pt=True, pt_steps_swap=10, seed=3000 + L + 1000 * rank,
+                           binning_level=[1, 2, 3, 4, 5])
+        scheds.append(sched)
+        e.begin(sched)
         engines.append(e)
         upd_per_unit += 10 * ham.n * R
         nsites += ham.n * count
@@ -366,11 +487,13 @@ def batch_bench(a, ws, rank, local):
     torch.cuda.synchronize(dev)
     sampler = ClockSampler(local)
     sampler.start()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
     l0 = sum(e.launch_count() for e in engines)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
     torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
     for k in range(a.steps):
         starts[k].record(stream)
         b.advance(1)
@@ -379,38 +502,94 @@ def batch_bench(a, ws, rank, local):
     launches = sum(e.launch_count() for e in engines) - l0
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     clocks = sampler.stop()
-    # end to end: the same units through the C ABI plus the results of every
-    # lattice (accumulators, P(M), binning, swaps) read back to the host
-    t1 = time.perf_counter()
-    b.advance(a.steps)
-    res = [e.collect() for e in engines]
-    t_e2e = time.perf_counter() - t1
-    d2h = sum(r["data"].nbytes + r["pm"].nbytes + r["binning"].nbytes + r["num_swaps"].nbytes + r["rejected"].nbytes
-              + r["energy"].nbytes + r["map"].nbytes for r in res)
     b.close()
+    if ws > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+
+    # the dominant kernel: the sweeps of the largest lattice size, timed live
+    # on the same stream (whole sweeps of every replica, one launch of the
+    # sweep kernel per call plus the slab transposes around it)
+    big = int(np.argmax([e.n * e.R for e in engines]))
+    eb = engines[big]
+    kernel, _ = eb.sweep_kernel()
+    nsw = 10
+    eb.sweep(nsw, 10 ** 9, a.seed)
+    torch.cuda.synchronize(dev)
+    k0 = eb.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    ev0.record(stream)
+    for r in range(reps):
+        eb.sweep(nsw, 10 ** 9 + (r + 1) * nsw, a.seed)
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    sweep_launches = eb.launch_count() - k0
+    kern_launches = reps if kernel == "cluster" else sweep_launches
+    per_launch_s = ev0.elapsed_time(ev1) * 1e-3 / kern_launches
+    upd_per_launch = nsw * reps * eb.n * eb.R / kern_launches
+    peak, peak_kind = _peaks()
+    achieved = 24.0 * upd_per_launch / per_launch_s / 1e9
+    traffic, capture = _traffic(f"batch512_pt:L{list(sizes)[big]}", upd_per_launch)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "traffic_capture": capture,
+                "kernel": {"cluster": "k_sweep_cluster", "tile": "k_sweep_tile"}.get(kernel, "k_sweep_ell"),
+                "lattice": f"L={list(sizes)[big]} x {eb.R} replicas",
+                "site_updates_per_launch": upd_per_launch, "launch_us": per_launch_s * 1e6,
+                "timing": "CUDA events around whole-sweep calls (each: the sweep kernel plus its two slab "
+                          "transposes) on the launching stream",
+                "peak_source": peak_kind, "step_rate_frac": 24.0 * (a.steps * upd_per_unit / (ms * 1e-3)) / 1e9 / peak}
+
+    # end to end through the C ABI, one job: every lattice's spin_matrix from
+    # host memory (FP64), esp_begin, the steps through a new batch, the
+    # results of every lattice and its final spins back to host memory
+    torch.cuda.synchronize(dev)
+    t1 = time.perf_counter()
+    for e, s0, sched in zip(engines, starts_h, scheds):
+        e.set_spins(s0)
+        e.begin(sched)
+    b2 = Batch(engines, stream.cuda_stream)
+    b2.set_units_per_graph(tuning["units_per_graph"])
+    b2.advance(a.steps)
+    res = [e.collect() for e in engines]
+    outs = [e.get_spins() for e in engines]
+    t_e2e = time.perf_counter() - t1
+    b2.close()
+    if ws > 1:
+        import torch.distributed as dist
+        te = torch.tensor([t_e2e], dtype=torch.float64)
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        t_e2e = float(te.item())
+    h2d = sum(x.nbytes for x in starts_h)
+    d2h = sum(o.nbytes for o in outs) + sum(
+        r["data"].nbytes + r["pm"].nbytes + r["binning"].nbytes + r["num_swaps"].nbytes + r["rejected"].nbytes
+        + r["energy"].nbytes + r["map"].nbytes for r in res)
     for e in engines:
         e.close()
     value = a.steps * upd_per_unit / (ms * 1e-3)
-    peak, peak_kind = _peaks()
-    achieved = 24.0 * value / 1e9
     if rank == 0:
         line = {
             "metric": "site updates/s", "value": ws * value, "unit": "site updates/s", "n_gpus": ws,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batch512_pt", "lattices": 512, "sizes": {str(k): v for k, v in sizes.items()},
-                       "sites": nsites, "replicas_per_lattice": 16, "temperatures_K": [2.0, 25.0],
-                       "pt_steps_swap": 10, "sweeps_per_step": 10,
-                       "l2": f"state {12 * nsites * 16 / 1e9:.2f} GB of spins, larger than L2 (no flush needed)",
-                       "parallelism": "all lattices in one device; independent jobs per GPU when n_gpus > 1"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": "batch (per-size kernel choice)",
-                         "peak_source": peak_kind},
+            "config": _batch_config(sizes),
+            "roofline": roofline,
             "e2e": {"value": ws * a.steps * upd_per_unit / t_e2e, "unit": "site updates/s",
-                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h / a.steps,
-                    "path": "esp_batch_advance + esp_collect of every handle"},
+                    "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps, "steps": a.steps,
+                    "path": "per lattice size: esp_set_spins + esp_begin; esp_batch_advance; per lattice size: "
+                            "esp_collect + esp_get_spins (one job: the spins cross once each way, FP64)"},
             "gpu_launches": int(launches), "clocks": clocks, "tuning": tuning,
         }
+        if not a.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            v, sec, detail = batch_port_rate(sizes, threads, a.seed, 2, 1)
+            line["cpu_baseline"] = {"value": v, "unit": "site updates/s", "cores": min(threads, 16), "kind": "port",
+                                    "sample": "one lattice of each size (16 temperatures on 16 threads), 1 untimed + "
+                                              "2 timed swap intervals of 10 sweeps, weighted by the lattice counts"}
+        if a.secondary:
+            line["secondary"] = secondary_sc128(a, local)
         print(json.dumps(line), flush=True)
 
 
@@ -420,12 +599,15 @@ def main():
     if a.proposal == "compare":
         learned_compare(a, rank, local)
         return
-    if a.workload == "batch512_pt" and a.impl == "ours":
-        batch_bench(a, ws, rank, local)
-        return
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
+    if a.workload == "batch512_pt" and a.impl == "ours":
+        batch_bench(a, ws, rank, local)
+        if ws > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
     if a.impl == "reference":
         reference_arm(a, ws, rank)
         if ws > 1:
@@ -528,8 +710,9 @@ def main():
     else:
         peak, peak_kind = _peaks()
         achieved = bytes_per_launch / per_launch_s / 1e9
+        traffic, capture = _traffic(a.workload, bytes_per_launch / 24.0)
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "traffic": None,
+                    "frac": achieved / peak, "traffic": traffic, "traffic_capture": capture,
                     "kernel": {"cluster": "k_sweep_cluster", "tile": "k_sweep_tile"}.get(kernel, "k_sweep_ell"),
                     "cluster_geometry": list(eng.cluster_geometry()) if kernel == "cluster" else None,
                     "tile_geometry": list(eng.tile_geometry()) if kernel == "tile" else None,
@@ -540,32 +723,34 @@ def main():
 
     # end to end through the C ABI with host buffers
     e2e_steps = max(1, min(a.steps, 50))
-    eng2 = Engine(N, ham.num_atoms, ham.supercell, R, inp.boundary_open)
-    eng2.upload(ham)
-    eng2.set_temperatures(inp.tems)
-    if a.proposal == "learned":
-        eng2.lp_init(seed=seed)
-        eng2.lp_set_engine(a.lp_engine)
-        eng2.set_proposal("learned")
-    elif kernel == "cluster":
-        eng2.set_cluster_geometry(*eng.cluster_geometry())
-        eng2.set_sweep_kernel("cluster")
-    elif kernel == "tile":
-        eng2.set_tile_geometry(*eng.tile_geometry())
-        eng2.set_sweep_kernel("tile")
-    elif kernel == "ell":
-        eng2.set_sweep_kernel("ell")
-    sched2 = eng2.schedule(0, e2e_steps * pss, inp.steps_measure, pt=inp.pt, pt_steps_swap=pss, mode=mode,
-                           tilt=inp.tilt_angles_max, seed=seed)
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    eng2.set_spins(spins0)
-    eng2.begin(sched2)
-    eng2.advance(e2e_steps)
-    r2 = eng2.collect()
-    out_spins = eng2.get_spins()
-    t_e2e = time.perf_counter() - t0
-    eng2.close()
+    t_e2e = None
+    if not a.no_e2e:
+        eng2 = Engine(N, ham.num_atoms, ham.supercell, R, inp.boundary_open)
+        eng2.upload(ham)
+        eng2.set_temperatures(inp.tems)
+        if a.proposal == "learned":
+            eng2.lp_init(seed=seed)
+            eng2.lp_set_engine(a.lp_engine)
+            eng2.set_proposal("learned")
+        elif kernel == "cluster":
+            eng2.set_cluster_geometry(*eng.cluster_geometry())
+            eng2.set_sweep_kernel("cluster")
+        elif kernel == "tile":
+            eng2.set_tile_geometry(*eng.tile_geometry())
+            eng2.set_sweep_kernel("tile")
+        elif kernel == "ell":
+            eng2.set_sweep_kernel("ell")
+        sched2 = eng2.schedule(0, e2e_steps * pss, inp.steps_measure, pt=inp.pt, pt_steps_swap=pss, mode=mode,
+                               tilt=inp.tilt_angles_max, seed=seed)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        eng2.set_spins(spins0)
+        eng2.begin(sched2)
+        eng2.advance(e2e_steps)
+        r2 = eng2.collect()
+        out_spins = eng2.get_spins()
+        t_e2e = time.perf_counter() - t0
+        eng2.close()
     # spin_matrix crosses as FP64 (3 x 8 B per spin) both ways
     h2d = 24 * N * R + 8 * R
     d2h = 24 * N * R + 8 * R * (6 + 3 + 4) + 8 * R * eng.num_freq()
@@ -576,13 +761,14 @@ def main():
         tt = torch.tensor([t_local], dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_max = float(tt.item())
-        te = torch.tensor([t_e2e], dtype=torch.float64)
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        t_e2e = float(te.item())
+        if t_e2e is not None:
+            te = torch.tensor([t_e2e], dtype=torch.float64)
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+            t_e2e = float(te.item())
     else:
         t_max = t_local
     value = ws * a.steps * updates_per_step / t_max
-    e2e_value = ws * e2e_steps * updates_per_step / t_e2e
+    e2e_value = ws * e2e_steps * updates_per_step / t_e2e if t_e2e else None
     if rank == 0:
         line = {
             "metric": "site updates/s", "value": value, "unit": "site updates/s", "n_gpus": ws,
@@ -591,9 +777,11 @@ def main():
             "dtype": "bf16+f32" if a.proposal == "learned" else "f32",
             "data": "synthetic", "config": _config(inp, ham, a.workload) | {"proposal": a.proposal},
             "roofline": roofline,
-            "e2e": {"value": e2e_value, "unit": "site updates/s", "h2d_bytes_per_step": h2d / e2e_steps,
-                    "d2h_bytes_per_step": d2h / e2e_steps, "steps": e2e_steps,
-                    "path": "esp_set_spins + esp_begin + esp_advance + esp_collect + esp_get_spins"},
+            "e2e": None if e2e_value is None else {
+                "value": e2e_value, "unit": "site updates/s", "h2d_bytes_per_step": h2d / e2e_steps,
+                "d2h_bytes_per_step": d2h / e2e_steps, "steps": e2e_steps,
+                "path": "esp_set_spins + esp_begin + esp_advance + esp_collect + esp_get_spins (one job: the "
+                        "spins cross once each way, FP64)"},
             "gpu_launches": int(launches), "colours": ncol,
             "autotuner": {"kernel": tuning["kernel"][0], "cluster_geometry": tuning["cluster_geometry"][0],
                           "ell_us_per_unit": tuning["ell_us"][0], "cluster_us_per_unit": tuning["cluster_us"][0]},

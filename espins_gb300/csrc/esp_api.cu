@@ -134,6 +134,7 @@ struct esp_handle {
     int proposal = 0;               // 0 plain Metropolis, 1 learned
     int lp_engine = 0;              // network on 0: mma.sync (warp tiles), 1: tcgen05 (128-row tiles)
     int *d_tc_err = nullptr;        // set by a tensor-core completion wait that gave up
+    int tc_force_timeout = 0;       // test hook: tcgen05 waits report a give-up (esp_lp_force_tc_timeout)
     // partial sums of the tcgen05 learned sweep (128-thread blocks)
     int tc_grid = 0, tc_slots = 0;
     double *d_tc_part = nullptr;
@@ -471,6 +472,7 @@ int do_sweep_colour(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o
         la.w.w1 = h->d_lp_w1; la.w.w2 = h->d_lp_w2; la.w.w3 = h->d_lp_w3;
         la.w.b1 = h->d_lp_p + kPadB1; la.w.b2 = h->d_lp_p + kPadB2; la.w.b3 = h->d_lp_p + kPadB3;
         la.axis = h->hsi ? h->d_lp_axis : nullptr;
+        la.tc_force_timeout = h->tc_force_timeout;
         if (h->lp_engine == 1) {
             // d_tc_err exists: esp_lp_set_engine allocates it (no allocation here,
             // this may run inside a graph capture)
@@ -1587,6 +1589,9 @@ int esp_begin(esp_handle *h, const esp_schedule *s)
     }
     CK(cudaMemsetAsync(h->d_rej, 0, sizeof(unsigned long long) * 2 * R, h->st));
     CK(cudaMemsetAsync(h->d_swaps, 0, sizeof(long long) * 2 * R, h->st));
+    // a tensor-core wait that gave up is reported by the esp_collect of the
+    // run it happened in; a new run starts clean
+    if (h->d_tc_err) CK(cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->st));
     esp_sweep_opts o;
     o.mcarlo_mode = s->mcarlo_mode; o.tilt_angles_max = s->tilt_angles_max; o.seed = s->seed; o.phase = 0;
     u.e_init.assign(R, 0.0);
@@ -2432,7 +2437,8 @@ int esp_lp_forward(esp_handle *h, const float *features, int64_t n, float *out)
     w.b1 = h->d_lp_p + kPadB1; w.b2 = h->d_lp_p + kPadB2; w.b3 = h->d_lp_p + kPadB3;
     if (h->lp_engine == 1) {
         if (e == cudaSuccess) e = cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->st);
-        if (e == cudaSuccess) e = launch_lp_forward_tc(w, dx, (int)n, dout, h->d_tc_err, h->num_sms, h->st);
+        if (e == cudaSuccess)
+            e = launch_lp_forward_tc(w, dx, (int)n, dout, h->d_tc_err, h->num_sms, h->st, h->tc_force_timeout);
     } else if (e == cudaSuccess) {
         e = launch_lp_forward(w, dx, (int)n, dout, h->st);
     }
@@ -2460,6 +2466,15 @@ int esp_lp_set_engine(esp_handle *h, int32_t engine)
         CK(cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->st));
     }
     h->lp_engine = engine;
+    return ESP_OK;
+}
+
+int esp_lp_force_tc_timeout(esp_handle *h, int32_t on)
+{
+    if (!h) return ESP_EINVAL;
+    int rc = fold(h);
+    if (rc) return rc;
+    h->tc_force_timeout = on ? 1 : 0;
     return ESP_OK;
 }
 

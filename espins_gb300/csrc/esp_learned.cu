@@ -274,6 +274,7 @@ __global__ void __launch_bounds__(kTcRows * NG, 1) k_sweep_lp_tc(const LpSweepAr
     uint32_t sw_lo, sw_hi;
     sweep_index(a, sw_lo, sw_hi);
     uint32_t phase = 0;
+    bool pending = false;
     int pi = tid < S ? (int)(tid / R) : a.n_c;
     while (group_any<NG>(g, pi < a.n_c)) {
         const bool act = pi < a.n_c;
@@ -294,12 +295,14 @@ __global__ void __launch_bounds__(kTcRows * NG, 1) k_sweep_lp_tc(const LpSweepAr
         }
         tc_store_x_row(s.t[g], lane, f);
         float o[kMlpOut];
-        tc_forward(s, g, phase, o);
+        // a completion wait that gave up stops the group (the same for all its
+        // threads): none of its remaining trials is made, no spin written
+        if (!tc_forward(s, g, phase, o, la.tc_force_timeout, pending)) break;
         if (act && mag > 0.f)
             lp_trial(a, fr, o, p, r, orig, mag, beta, gx, gy, gz, q, sw_lo, sw_hi, accE, accX, accY, accZ, nrej);
         pi += pstep;
     }
-    tc_teardown(s);
+    tc_teardown(s, g, pending, phase);
     if (threadIdx.x == 0 && s.error) atomicExch(err, 1);
     // the group's activation tile becomes its reduction scratch
     __syncthreads();

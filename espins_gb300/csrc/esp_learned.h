@@ -25,6 +25,9 @@ struct LpSweepArgs {
     SweepArgs s;
     LpWeights w;
     const float4 *axis;   // [num_atoms] or null
+    // test hook of the tcgen05 engine: every group reports a completion wait
+    // that gave up after its first layer's MMAs completed (0: off)
+    int tc_force_timeout;
 };
 
 struct LpCollectArgs {

@@ -14,13 +14,14 @@ namespace esp {
 namespace {
 
 __global__ void __launch_bounds__(kTcRows) k_lp_forward_tc(const LpWeights w, const __nv_bfloat16 *x, int n,
-                                                            float *out, int *err)
+                                                            float *out, int *err, int force_timeout)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     TcSmem &s = *reinterpret_cast<TcSmem *>(smem);
     tc_stage_weights(w, s);
     tc_setup(s);
     uint32_t phase = 0;
+    bool pending = false;
     const int t = threadIdx.x;
     for (int base = blockIdx.x * kTcRows; base < n; base += gridDim.x * kTcRows) {
         const int i = base + t;
@@ -33,11 +34,11 @@ __global__ void __launch_bounds__(kTcRows) k_lp_forward_tc(const LpWeights w, co
         *reinterpret_cast<uint4 *>(xb + kmajor_offset(t, 0, kMlpInPad)) = v0;
         *reinterpret_cast<uint4 *>(xb + kmajor_offset(t, 8, kMlpInPad)) = v1;
         float o[kMlpOut];
-        tc_forward(s, 0, phase, o);
+        if (!tc_forward(s, 0, phase, o, force_timeout, pending)) break;   // the CTA's one group: uniform
         if (i < n)
             for (int k = 0; k < kMlpOut; ++k) out[(size_t)i * kMlpOut + k] = o[k];
     }
-    tc_teardown(s);
+    tc_teardown(s, 0, pending, phase);
     if (t == 0 && s.error) atomicExch(err, 1);
 }
 
@@ -51,12 +52,12 @@ cudaError_t lp_tc_configure()
 }
 
 cudaError_t launch_lp_forward_tc(const LpWeights &w, const __nv_bfloat16 *x, int n, float *out, int *err,
-                                 int num_sms, cudaStream_t st)
+                                 int num_sms, cudaStream_t st, int force_timeout)
 {
     if (n <= 0) return cudaSuccess;
     int blocks = (n + kTcRows - 1) / kTcRows;
     if (blocks > 2 * num_sms) blocks = 2 * num_sms;
-    k_lp_forward_tc<<<blocks, kTcRows, sizeof(TcSmem), st>>>(w, x, n, out, err);
+    k_lp_forward_tc<<<blocks, kTcRows, sizeof(TcSmem), st>>>(w, x, n, out, err, force_timeout);
     return cudaGetLastError();
 }
 

@@ -99,9 +99,15 @@ __device__ __forceinline__ void tc_setup(TcSmemG<NG> &s)
     tc_fence_after();
 }
 
+// Tear-down by the whole CTA.  A group whose completion wait gave up with its
+// MMAs possibly still in flight (pending) first waits for them once more,
+// bounded, so the tensor memory is not freed under a running MMA; if that
+// wait gives up too, the memory is freed regardless (the launch has already
+// reported the error).
 template <int NG>
-__device__ __forceinline__ void tc_teardown(TcSmemG<NG> &s)
+__device__ __forceinline__ void tc_teardown(TcSmemG<NG> &s, int g = 0, bool pending = false, uint32_t phase = 0)
 {
+    if (pending && (threadIdx.x & (kTcRows - 1)) == 0) mbar_wait(smem_u32(&s.t[g].bar), phase, kTcWaitLimit);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -120,10 +126,17 @@ __device__ __forceinline__ void tc_store_x_row(TcTile &s, int t, const float *f)
 }
 
 // Issue (the group's thread 0) the MMAs of one layer of group g, commit, and
-// wait (every thread of the group).  Returns false when the wait gave up.
+// wait (every thread of the group).  Returns true, the same for every thread
+// of the group, when the layer's results are in tensor memory.  When a wait
+// gives up (or `force` asks the test hook to report a give-up after the MMAs
+// completed) it returns false and sets s.error; `pending` then tells whether
+// the MMAs may still be running (no thread of the group saw them complete),
+// and `phase` is the phase still to wait for.  After a false return the
+// group must issue no more MMAs and read neither tensor memory nor touch the
+// operands the MMAs read.
 template <int NG>
 __device__ __forceinline__ bool tc_layer(TcSmemG<NG> &s, int g, const __nv_bfloat16 *a, int K,
-                                         const __nv_bfloat16 *b, int N, uint32_t &phase)
+                                         const __nv_bfloat16 *b, int N, uint32_t &phase, int force, bool &pending)
 {
     fence_async_smem();     // this thread's operand writes -> tensor cores
     tc_fence_before();
@@ -138,11 +151,19 @@ __device__ __forceinline__ bool tc_layer(TcSmemG<NG> &s, int g, const __nv_bfloa
             tc_mma(d, smem_desc(a0 + 256u * kk, 128u, sbo), smem_desc(b0 + 256u * kk, 128u, sbo), idesc, kk > 0);
         tc_commit(smem_u32(&s.t[g].bar));
     }
-    const bool ok = mbar_wait(smem_u32(&s.t[g].bar), phase, kTcWaitLimit);
-    phase ^= 1u;
-    tc_fence_after();
-    if (!ok) s.error = 1;
-    return ok;
+    const bool seen = mbar_wait(smem_u32(&s.t[g].bar), phase, kTcWaitLimit);
+    const bool fail = group_any<NG>(g, !seen || force != 0);
+    if (!fail) {
+        phase ^= 1u;
+        tc_fence_after();
+        return true;
+    }
+    // give-up: the layer's MMAs are complete if any thread of the group saw it
+    const bool done = group_any<NG>(g, seen);
+    if (done) phase ^= 1u;
+    pending = !done;
+    if ((threadIdx.x & (kTcRows - 1)) == 0) s.error = 1;
+    return false;
 }
 
 // This thread's tensor-memory lane in group g's columns.
@@ -178,17 +199,20 @@ __device__ __forceinline__ void tc_hidden_epilogue(TcSmemG<NG> &s, int g, const 
 }
 
 // The whole network for the 128 rows of group g's X; thread t of the group
-// gets row t's 20 outputs.  Returns false if a wait gave up (s.error is then
-// set).
+// gets row t's 20 outputs.  Returns false (for the whole group) if a wait
+// gave up: s.error is then set, `pending` says whether MMAs may still run, and
+// neither o nor the group's operands or tensor memory have been touched
+// after the failed layer.
 template <int NG>
-__device__ __forceinline__ bool tc_forward(TcSmemG<NG> &s, int g, uint32_t &phase, float *o)
+__device__ __forceinline__ bool tc_forward(TcSmemG<NG> &s, int g, uint32_t &phase, float *o, int force,
+                                           bool &pending)
 {
     TcTile &tl = s.t[g];
-    bool ok = tc_layer(s, g, tl.x, kMlpInPad, s.w1, kMlpHid, phase);
+    if (!tc_layer(s, g, tl.x, kMlpInPad, s.w1, kMlpHid, phase, force, pending)) return false;
     tc_hidden_epilogue(s, g, s.b1);
-    ok = tc_layer(s, g, tl.h, kMlpHid, s.w2, kMlpHid, phase) && ok;
+    if (!tc_layer(s, g, tl.h, kMlpHid, s.w2, kMlpHid, phase, 0, pending)) return false;
     tc_hidden_epilogue(s, g, s.b2);
-    ok = tc_layer(s, g, tl.h, kMlpHid, s.w3, kMlpOutPad, phase) && ok;
+    if (!tc_layer(s, g, tl.h, kMlpHid, s.w3, kMlpOutPad, phase, 0, pending)) return false;
     const uint32_t lane_base = tc_lane_base(s, g);
     float v[16];
     tmem_ld16(lane_base, v);
@@ -199,7 +223,7 @@ __device__ __forceinline__ bool tc_forward(TcSmemG<NG> &s, int g, uint32_t &phas
     for (int i = 0; i < kMlpOut - 16; ++i) o[16 + i] = v[i] + s.b3[16 + i];
     // the next layer 1 overwrites the accumulators: every load done first
     tc_fence_before();
-    return ok;
+    return true;
 }
 
 }  // namespace esp

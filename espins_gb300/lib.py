@@ -27,6 +27,7 @@ EXPORTED = [
     "esp_energy_noalloc", "esp_set_sweep_kernel", "esp_get_sweep_kernel", "esp_set_series", "esp_get_series",
     "esp_lp_num_params", "esp_lp_init_weights", "esp_lp_set_weights", "esp_lp_get_weights", "esp_lp_reserve",
     "esp_lp_collect", "esp_lp_get_data", "esp_lp_train", "esp_lp_loss_grad", "esp_lp_forward", "esp_lp_set_engine",
+    "esp_lp_force_tc_timeout",
     "esp_set_proposal", "esp_get_proposal",
     "esp_set_pt_groups", "esp_set_cluster_geometry", "esp_get_cluster_geometry",
     "esp_set_tile_geometry", "esp_get_tile_geometry", "esp_batch_create", "esp_batch_destroy", "esp_batch_last_error",
@@ -158,6 +159,7 @@ def load(build_if_missing: bool = True):
     lib.esp_lp_loss_grad.argtypes = [vp, vp, vp, C.c_int64, P(C.c_double), vp]
     lib.esp_lp_forward.argtypes = [vp, vp, C.c_int64, vp]
     lib.esp_lp_set_engine.argtypes = [vp, C.c_int32]
+    lib.esp_lp_force_tc_timeout.argtypes = [vp, C.c_int32]
     lib.esp_set_proposal.argtypes = [vp, C.c_int32]
     lib.esp_get_proposal.argtypes = [vp, P(C.c_int32)]
     lib.esp_set_pt_groups.argtypes = [vp, C.c_int32]
@@ -586,6 +588,10 @@ class Engine:
     def lp_set_engine(self, engine: str) -> None:
         """'mma' (warp-level mma.sync) or 'tcgen05' (tensor-memory MMAs on 128-trial tiles)."""
         self._check(self.lib.esp_lp_set_engine(self.h, {"mma": 0, "tcgen05": 1}[engine]))
+
+    def lp_force_tc_timeout(self, on: bool) -> None:
+        """Test hook: tcgen05 completion waits report a give-up (see the header)."""
+        self._check(self.lib.esp_lp_force_tc_timeout(self.h, int(bool(on))))
 
     def set_proposal(self, kind: str) -> None:
         """'plain' (the reference's trial moves) or 'learned'."""

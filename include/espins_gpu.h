@@ -387,6 +387,13 @@ int esp_lp_forward(esp_handle *h, const float *features, int64_t n, float *out);
  * 128-trial tiles with tensor-memory accumulators.  ESP_ETIMEOUT if a
  * completion wait gave up. */
 int esp_lp_set_engine(esp_handle *h, int32_t engine);
+/* Test hook, no counterpart in the reference: with on != 0 every tcgen05
+ * completion wait of the learned sweep and of esp_lp_forward reports that it
+ * gave up, right after its first layer's MMAs have completed, so a host can
+ * check the give-up path without a real hang: the sweep then makes no trial
+ * and writes no spin, and esp_collect / esp_lp_forward return ESP_ETIMEOUT.
+ * esp_begin clears the recorded give-up. */
+int esp_lp_force_tc_timeout(esp_handle *h, int32_t on);
 /* 0: the reference's trial moves (default); 1: the learned proposal (needs
  * weights).  Applies to esp_sweep, esp_sweep_colour, esp_run and esp_advance. */
 int esp_set_proposal(esp_handle *h, int32_t kind);

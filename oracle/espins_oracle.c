@@ -1040,9 +1040,13 @@ int or_build_ell(int num_atoms, const double *atoms_frac, const double *mag_cell
 /* runs pt_steps_swap typewriter sweeps of its temperatures with its own    */
 /* MT19937 stream, measuring after every steps_measure sweeps               */
 /* (pt.F90:773-864: E accumulators, magnetization_get, Pm_get), then thread */
-/* 0 performs pt_swap.  Returns the number of site updates done.            */
+/* 0 performs pt_swap.  Returns the number of site updates done; with       */
+/* seconds != NULL also the wall time of the swap intervals alone (from the */
+/* barrier all threads reach after their set-up to the last one), without   */
+/* the initial energies and the thread start-up.                            */
 /* ------------------------------------------------------------------------ */
 #include <pthread.h>
+#include <time.h>
 
 typedef struct {
     const or_ham *h;
@@ -1058,7 +1062,15 @@ typedef struct {
     double *tmp;
     or_mt root_mt;
     int64_t updates;
+    double t_start, t_end;
 } or_bench_ctx;
+
+static double or_now(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
 
 static void *or_bench_worker(void *arg)
 {
@@ -1072,6 +1084,8 @@ static void *or_bench_worker(void *arg)
     or_mt mt;
     or_mt_init(&mt, c->seed + c->tid);
     c->updates = 0;
+    pthread_barrier_wait(c->bar);
+    if (c->tid == 0) c->t_start = or_now();
     for (int64_t lsw = 1; lsw <= c->n_swap_intervals; ++lsw) {
         for (int t = t0; t < t1; ++t) {
             double beta = 1.0 / c->tems[t];
@@ -1094,12 +1108,13 @@ static void *or_bench_worker(void *arg)
                        &c->root_mt, c->tmp);
         pthread_barrier_wait(c->bar);
     }
+    if (c->tid == 0) c->t_end = or_now();
     return NULL;
 }
 
 int64_t or_pt_bench(const or_ham *h, int nthreads, int R, const double *tems, double *spins,
                     int64_t n_swap_intervals, int64_t pss, int64_t steps_measure, int mode,
-                    double tilt, int32_t seed)
+                    double tilt, int32_t seed, double *seconds)
 {
     if (nthreads > R) nthreads = R;
     if (nthreads < 1) nthreads = 1;
@@ -1129,6 +1144,7 @@ int64_t or_pt_bench(const or_ham *h, int nthreads, int R, const double *tems, do
     }
     int64_t total = 0;
     for (int k = 0; k < nthreads; ++k) { pthread_join(th[k], NULL); total += ctx[k].updates; }
+    if (seconds) *seconds = ctx[0].t_end - ctx[0].t_start;
     pthread_barrier_destroy(&bar);
     free(ctx); free(th); free(e2); free(data); free(pm); free(rej); free(sw); free(map); free(tmp);
     return total;

@@ -11,14 +11,18 @@
   network against the reference algorithm's chains within 3 sigma, so the
   proposal-density correction is exact;
 * what training gains: lower loss, higher acceptance and a shorter
-  integrated autocorrelation time of E than the plain sampler.
+  integrated autocorrelation time of E than the plain sampler;
+* the give-up path of the tcgen05 engine's bounded completion waits, made to
+  run by the test hook esp_lp_force_tc_timeout (no real hang): esp_collect
+  and esp_lp_forward return ESP_ETIMEOUT, the sweep makes no trial and
+  writes no spin, and the handle works again after the hook is switched off.
 """
 import numpy as np
 import pytest
 
 import oracle as O
 from espins_gb300 import analysis
-from espins_gb300.lib import LP_NUM_PARAMS, Engine
+from espins_gb300.lib import ESP_ETIMEOUT, LP_NUM_PARAMS, Engine, EspError
 from espins_gb300.tables import build_hamiltonian
 from helpers import NN, NNN, energy_scale, sc_mcin
 from test_gpu_statistics import LEVELS, _check, _mean_sigma, _oracle_chains
@@ -93,6 +97,36 @@ def test_tcgen05_forward_matches_fp64_network_and_mma_path():
     # both engines round the hidden activations to bf16 the same way; only the
     # FP32 accumulation order differs
     assert np.max(np.abs(got - ref)) <= 5e-3 * scale, np.max(np.abs(got - ref)) / scale
+
+
+def test_tcgen05_give_up_path_reports_timeout_and_writes_nothing():
+    p = _weights(21)
+    with _small_engine(R=4) as e:
+        e.lp_set_weights(p)
+        e.lp_set_engine("tcgen05")
+        e.set_proposal("learned")
+        e.init_spins("rand", seed=5)
+        before, e_before = e.get_spins(), e.running_energy()
+        e.lp_force_tc_timeout(True)
+        e.begin(e.schedule(0, 2, 1, seed=9))
+        e.advance(2)
+        with pytest.raises(EspError) as ei:
+            e.collect()
+        assert ei.value.code == ESP_ETIMEOUT
+        assert np.array_equal(e.get_spins(), before)
+        assert np.array_equal(e.running_energy(), e_before)
+        assert np.all(e.rejected()[:, 1] == 0)      # no trial was made, so none was rejected
+        x = np.random.default_rng(3).normal(size=(200, 12)).astype(np.float32)
+        with pytest.raises(EspError) as ei:
+            e.lp_forward(x)
+        assert ei.value.code == ESP_ETIMEOUT
+        # hook off: a new run sweeps and collects normally
+        e.lp_force_tc_timeout(False)
+        e.begin(e.schedule(0, 2, 1, seed=9))
+        e.advance(2)
+        res = e.collect()
+        assert not np.array_equal(e.get_spins(), before)
+        assert res["rejected"][:, 1].sum() < 2 * 4 * e.n
 
 
 def test_training_loss_and_gradient_match_fp64_network():
