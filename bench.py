@@ -74,12 +74,22 @@ def _args():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--geometry", default=None,
+                   help="batch512_pt: cluster geometry CTAs,threads,sites for every size instead of the "
+                        "autotuner (profiling)")
+    p.add_argument("--only-L", type=int, default=None,
+                   help="batch512_pt: run only the lattices of this size (profiling of a small case)")
+    p.add_argument("--max-lattices", type=int, default=None,
+                   help="batch512_pt: at most this many lattices per size (profiling of a small case)")
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--proposal", choices=["plain", "learned", "compare"], default="plain")
     p.add_argument("--lp-engine", choices=["mma", "tcgen05"], default="tcgen05")
     p.add_argument("--train-pairs", type=int, default=10_000_000)
     p.add_argument("--train-steps", type=int, default=3000)
     p.add_argument("--measure-sweeps", type=int, default=20000)
+    p.add_argument("--plain-sweeps", type=int, default=200000,
+                   help="--proposal compare: sweeps of the plain sampler's measurement window (its low-temperature "
+                        "autocorrelation times reach ~2000 sweeps, so its window is longer than the learned one's)")
     return p.parse_args()
 
 
@@ -289,7 +299,7 @@ def reference_arm(a, ws, rank):
 
 def _batch_config(sizes):
     nsites = sum(L ** 3 * c for L, c in sizes.items())
-    return {"workload": "batch512_pt", "lattices": 512, "sizes": {str(k): v for k, v in sizes.items()},
+    return {"workload": "batch512_pt", "lattices": sum(sizes.values()), "sizes": {str(k): v for k, v in sizes.items()},
             "sites": nsites, "replicas_per_lattice": 16, "temperatures_K": [2.0, 25.0],
             "pt_steps_swap": 10, "sweeps_per_step": 10,
             "l2": f"state {12 * nsites * 16 / 1e9:.2f} GB of spins, larger than L2 (no flush needed)",
@@ -352,14 +362,16 @@ def learned_compare(a, rank, local):
     torch.cuda.synchronize(dev)
     t_train = ev0.elapsed_time(ev1) * 1e-3
     out = {}
+    from espins_gb300 import analysis as A
     for kind in ("plain", "learned"):
+        sweeps = a.plain_sweeps if kind == "plain" else a.measure_sweeps
         eng.set_proposal(kind)
         eng.set_spins(start)
-        eng.set_series(a.measure_sweeps)
-        sched = eng.schedule(0, a.measure_sweeps, 1, pt=inp.pt, pt_steps_swap=pss, seed=seed + 17)
+        eng.set_series(sweeps)
+        sched = eng.schedule(0, sweeps, 1, pt=inp.pt, pt_steps_swap=pss, seed=seed + 17)
         eng.begin(sched)
         eng.advance(max(1, 500 // pss))          # settle after the switch (not in the series window)
-        units = -(-a.measure_sweeps // pss) - max(1, 500 // pss)
+        units = -(-sweeps // pss) - max(1, 500 // pss)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(dev)
         e0.record(stream)
@@ -374,19 +386,42 @@ def learned_compare(a, rank, local):
         tau = np.maximum(tau_e, tau_m)
         sweeps_per_s = units * pss / secs
         ups = sweeps_per_s * N * R
-        trials = -(-a.measure_sweeps // pss) * pss * N     # per temperature slot, whole run
+        trials = -(-sweeps // pss) * pss * N     # per temperature slot, whole run
         acc = 1.0 - res["rejected"][:, 1] / trials
+        # the _mc.dat observables of the measurement window with jackknife errors
+        obs = np.zeros((R, 6)); err = np.zeros((R, 6))
+        for t in range(R):
+            obs[t], err[t] = A.jackknife_observables(ser[:, t, 0], ser[:, t, 1], float(inp.tems[t]), N, 40)
         out[kind] = {
+            "sweeps": int(units * pss), "seconds": secs,
             "site_updates_per_s": ups,
             "independent_samples_per_s": float(np.sum(sweeps_per_s / (2.0 * tau))),
             "per_slot_samples_per_s": (sweeps_per_s / (2.0 * tau)).tolist(),
             "tau_int_E": tau_e.tolist(), "tau_int_absM": tau_m.tolist(),
             "tau_int_binning_E": [analysis.binning_tau(ser[:, t, 0]) for t in range(R)],
             "acceptance": acc.tolist(), "kernel": eng.sweep_kernel()[0],
-            "mean_E_per_site": (res["data"][:, 0] / N).tolist(), "mean_absM": res["data"][:, 3].tolist(),
+            "observables": obs.tolist(), "sigma": err.tolist(),
         }
     eng.close()
     gains = np.asarray(out["learned"]["per_slot_samples_per_s"]) / np.asarray(out["plain"]["per_slot_samples_per_s"])
+    # every observable of every slot, learned against plain at 3 sigma (the
+    # criterion over K comparisons: |z| <= 3 except ceil(1 + 0.0027 K) of them,
+    # none beyond the Bonferroni bound of two-sided 1%)
+    zl = (np.asarray(out["learned"]["observables"]) - np.asarray(out["plain"]["observables"])) / np.sqrt(
+        np.asarray(out["learned"]["sigma"]) ** 2 + np.asarray(out["plain"]["sigma"]) ** 2)
+    K = zl.size
+    az = np.abs(zl)
+    over = int((az > 3.0).sum())
+    allowed = int(np.ceil(1 + 0.0027 * K))
+    import math
+    lo, hi = 0.0, 10.0
+    for _ in range(100):
+        mid = 0.5 * (lo + hi)
+        if K * math.erfc(mid / math.sqrt(2.0)) > 0.01:
+            lo = mid
+        else:
+            hi = mid
+    passed = bool(over <= allowed and np.all(az <= hi))
     if rank == 0:
         line = {
             "metric": "independent samples/s", "value": out["learned"]["independent_samples_per_s"],
@@ -401,6 +436,9 @@ def learned_compare(a, rank, local):
             "gain_geomean": float(np.exp(np.mean(np.log(gains)))),
             "gain_min": float(gains.min()), "gain_max": float(gains.max()),
             "slots_with_gain_ge_2": int((gains >= 2.0).sum()),
+            "observables_3sigma": {"names": list(A.OBSERVABLES), "z": zl.tolist(), "comparisons": K,
+                                   "over_3sigma": over, "allowed_over_3sigma": allowed, "bonferroni_z": hi,
+                                   "worst_abs_z": float(az.max()), "pass": passed},
             "training": {"pairs": int(rows), "collect_s": t_collect, "steps": a.train_steps, "batch": 4096,
                          "seconds": t_train, "loss_first": float(np.mean(loss[:20])),
                          "loss_last": float(np.mean(loss[-50:]))},
@@ -412,7 +450,7 @@ def _traffic(key, units_per_launch):
     """DRAM bytes per launch of the dominant kernel from the ncu capture
     summarised in profiles/dram_traffic.json (bytes per site update of that
     kernel on a captured case, scaled by the site updates of one launch here;
-    the traffic grows in proportion to the updates), or None."""
+    the traffic grows in proportion to the updates), or (None, None)."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if not os.path.exists(path):
         return None, None
@@ -456,6 +494,11 @@ def batch_bench(a, ws, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     sizes = batch_lattice_sizes(512, 3)
+    if a.only_L is not None:
+        sizes = {L: c for L, c in sizes.items() if L == a.only_L}
+    if a.max_lattices is not None:
+        sizes = {L: min(c, a.max_lattices) for L, c in sizes.items()}
+    reduced = a.only_L is not None or a.max_lattices is not None
     stream = torch.cuda.Stream(dev)
     engines, upd_per_unit, nsites, starts_h = [], 0, 0, []
     total_units = a.warmup + a.steps + 64
@@ -482,7 +525,15 @@ def batch_bench(a, ws, rank, local):
         upd_per_unit += 10 * ham.n * R
         nsites += ham.n * count
     b = Batch(engines, stream.cuda_stream)
-    tuning = b.tune(units=2)
+    if a.geometry:
+        cs, nt, sp = (int(x) for x in a.geometry.split(","))
+        for e in engines:
+            e.set_cluster_geometry(cs, nt, sp)
+            e.set_sweep_kernel("cluster")
+        b.set_units_per_graph(1)
+        tuning = {"units_per_graph": 1, "fixed_geometry": [cs, nt, sp]}
+    else:
+        tuning = b.tune(units=2)
     b.advance(a.warmup)
     torch.cuda.synchronize(dev)
     sampler = ClockSampler(local)
@@ -494,11 +545,13 @@ def batch_bench(a, ws, rank, local):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
     torch.cuda.synchronize(dev)
+    torch.cuda.nvtx.range_push("timed")     # lets a profiler take the timed launches only
     for k in range(a.steps):
         starts[k].record(stream)
         b.advance(1)
         ends[k].record(stream)
     torch.cuda.synchronize(dev)
+    torch.cuda.nvtx.range_pop()
     launches = sum(e.launch_count() for e in engines) - l0
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     clocks = sampler.stop()
@@ -574,7 +627,8 @@ def batch_bench(a, ws, rank, local):
             "metric": "site updates/s", "value": ws * value, "unit": "site updates/s", "n_gpus": ws,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": _batch_config(sizes),
+            "config": _batch_config(sizes) | ({"reduced": "a subset of the 512 lattices (profiling case)"}
+                                              if reduced else {}),
             "roofline": roofline,
             "e2e": {"value": ws * a.steps * upd_per_unit / t_e2e, "unit": "site updates/s",
                     "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps, "steps": a.steps,
@@ -582,13 +636,13 @@ def batch_bench(a, ws, rank, local):
                             "esp_collect + esp_get_spins (one job: the spins cross once each way, FP64)"},
             "gpu_launches": int(launches), "clocks": clocks, "tuning": tuning,
         }
-        if not a.no_cpu_baseline:
+        if not a.no_cpu_baseline and not reduced:
             threads = os.cpu_count() or 1
             v, sec, detail = batch_port_rate(sizes, threads, a.seed, 2, 1)
             line["cpu_baseline"] = {"value": v, "unit": "site updates/s", "cores": min(threads, 16), "kind": "port",
                                     "sample": "one lattice of each size (16 temperatures on 16 threads), 1 untimed + "
                                               "2 timed swap intervals of 10 sweeps, weighted by the lattice counts"}
-        if a.secondary:
+        if a.secondary and not reduced:
             line["secondary"] = secondary_sc128(a, local)
         print(json.dumps(line), flush=True)
 

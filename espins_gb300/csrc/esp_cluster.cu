@@ -63,7 +63,9 @@ __device__ __forceinline__ void hist_flush(unsigned *h, const WarpRun &run)
     if ((threadIdx.x & 31) == 0 && run.bin > 0) atomicAdd(h + (run.bin - 1), run.cnt);
 }
 
-template <int NT, int S>
+// HB, HD: the lattice has biquadratic / DM couplings (a.has_b, a.has_d), as
+// compile-time flags so the neighbour loop carries no tests for absent terms.
+template <int NT, int S, bool HB, bool HD>
 __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const ClusterArgs a)
 {
     static_assert(NT % 32 == 0 && NT <= 640, "the reduction scratch holds at most 20 warps");
@@ -87,11 +89,14 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
     const ClusterNbr *nbt = reinterpret_cast<const ClusterNbr *>(st + 1);
     unsigned int *hist = reinterpret_cast<unsigned int *>(smem) + a.stencil_words;
     const int nhist = a.obs ? 3 : 1;
+    // reduction scratch: [0, 112) warp partials; [128, 144) a CTA's totals of
+    // a measurement, two buffers by the measurement's parity; [144, 149) the
+    // CTA's end-of-launch totals
     double *red = reinterpret_cast<double *>(hist + ((nhist * a.nf + 3) & ~3));
     // the slot's accumulators, kept by rank 0 for the launch (the slot of a
     // replica does not change inside a launch): data, obs data, binning
     // levels, binning sums and variances of E/N, |m| and of |OP|, |SM|
-    double *acc = red + 136;
+    double *acc = red + kClusterRedDoubles;
     double *c_data = acc, *c_odata = acc + 6;
     int *c_lev = reinterpret_cast<int *>(acc + 12);
     double *c_ls = acc + 12 + kClusterMaxLev / 2, *c_bn = c_ls + 2 * kClusterMaxLev;
@@ -239,9 +244,9 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
                     const ClusterNbr &se = nb[s][e0 + j];
                     const float J = se.J;
                     gx[s] = fmaf(-J, tx[s][j], gx[s]); gy[s] = fmaf(-J, ty[s][j], gy[s]); gz[s] = fmaf(-J, tz[s][j], gz[s]);
-                    if (a.has_b)
+                    if (HB)
                         bq_form(se.B, tx[s][j], ty[s][j], tz[s][j], qxx[s], qyy[s], qzz[s], qxy[s], qxz[s], qyz[s]);
-                    if (a.has_d) dm_field(se.Dx, se.Dy, se.Dz, tx[s][j], ty[s][j], tz[s][j], gx[s], gy[s], gz[s]);
+                    if (HD) dm_field(se.Dx, se.Dy, se.Dz, tx[s][j], ty[s][j], tz[s][j], gx[s], gy[s], gz[s]);
                 }
         };
         int e0 = 0;
@@ -268,7 +273,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
             }
             const Philox4 xr = philox4x32_10((uint32_t)orig[s], (uint32_t)r, sw_lo, sw_hi, a.key0, a.key1);
             trial_spin(a.mode, a.tilt, st->mag[at[s]], ox[s], oy[s], oz[s], xr.x, xr.y, nx[s], ny[s], nz[s]);
-            const float d = delta_energy(a.has_b || a.has_si, gx[s], gy[s], gz[s], qxx[s], qyy[s], qzz[s], qxy[s],
+            const float d = delta_energy(HB || a.has_si, gx[s], gy[s], gz[s], qxx[s], qyy[s], qzz[s], qxy[s],
                                          qxz[s], qyz[s], ox[s], oy[s], oz[s], nx[s], ny[s], nz[s]);
             de[s] = d;
             acc[s] = true;
@@ -285,6 +290,90 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
             }
         }
     };
+
+    // Rank 0's warp 0 folds measurement m (the CTAs' totals in buffer m & 1)
+    // into the replica totals and the accumulators of mcarlo.F90:536-590 for
+    // this temperature slot: lane 0 the sums, one binning level per lane.
+    auto fold_measurement = [&](const int m) {
+        // lane 0 folds the CTAs' sums into the replica totals and the
+        // accumulators of mcarlo.F90:536-590 for this temperature
+        // slot; the binning levels, independent of one another, go
+        // one per lane
+        const double rn_inv = a.rn_inv;
+        const long long step = meas_base + m + 1;
+        double e = 0.0, am = 0.0, aop = 0.0, asm_ = 0.0;
+        if (threadIdx.x == 0) {
+            double d4[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int q = 0; q < csize; ++q) {
+                const double *pr = cluster.map_shared_rank(red, q);
+#pragma unroll
+                for (int c = 0; c < 8; ++c) d4[c] += pr[128 + 8 * (m & 1) + c];
+            }
+            e_run += d4[0];
+            m_run[0] += d4[1]; m_run[1] += d4[2]; m_run[2] += d4[3];
+            e = e_run;
+            const double mx = m_run[0] * rn_inv, my = m_run[1] * rn_inv, mz = m_run[2] * rn_inv;
+            const double m2 = mx * mx + my * my + mz * mz;
+            const double ee = e * e;
+            am = sqrt(m2);
+            double *d = cache ? c_data : a.data + 6 * temp;
+            d[0] += e; d[1] += ee; d[2] += ee * ee;
+            d[3] += am; d[4] += m2; d[5] += m2 * m2;
+            if (a.series) {
+                double *o = a.series + (((step - 1) % a.series_cap) * a.R + temp) * 2;
+                o[0] = e; o[1] = am;
+            }
+            // orderparam_get / staggered_get (mcarlo.F90:553-568)
+            if (a.obs) {
+                double *od = cache ? c_odata : a.obs_data + 6 * temp;
+                if (a.obs & 1) {
+                    const double op = d4[4] * rn_inv;
+                    const double o2 = op * op;
+                    aop = sqrt(o2);
+                    od[0] += aop; od[1] += o2; od[2] += o2 * o2;
+                }
+                if (a.obs & 2) {
+                    const double qx = d4[5] * rn_inv, qy = d4[6] * rn_inv, qz = d4[7] * rn_inv;
+                    const double q2 = qx * qx + qy * qy + qz * qz;
+                    asm_ = sqrt(q2);
+                    od[3] += asm_; od[4] += q2; od[5] += q2 * q2;
+                }
+            }
+        }
+        if (a.nlev > 0) {
+            e = __shfl_sync(0xffffffffu, e, 0);
+            am = __shfl_sync(0xffffffffu, am, 0);
+            aop = __shfl_sync(0xffffffffu, aop, 0);
+            asm_ = __shfl_sync(0xffffffffu, asm_, 0);
+        }
+        for (int lv = threadIdx.x; lv < a.nlev; lv += 32) {
+            const size_t g2 = ((size_t)temp * a.nlev + lv) * 2;
+            double *ls = cache ? c_ls + 2 * lv : a.lsum + g2;
+            double *bn = cache ? c_bn + 2 * lv : a.binning + g2;
+            double *ols = !a.obs ? nullptr : (cache ? c_ols + 2 * lv : a.obs_lsum + g2);
+            double *obn = !a.obs ? nullptr : (cache ? c_obn + 2 * lv : a.obs_bin + g2);
+            ls[0] += e * rn_inv;
+            ls[1] += am;
+            if (ols) { ols[0] += aop; ols[1] += asm_; }
+            const int lev = cache ? c_lev[lv] : a.levels[lv];
+            const long long blk = 1LL << lev;
+            if ((step & (blk - 1)) == 0) {
+                // 1/2^n is exact, so the product equals the division
+                const double inv_div = ldexp(1.0, -(a.pt_quirk ? lv + 1 : lev));
+                for (int c = 0; c < 2; ++c) {
+                    const double v2 = ls[c] * inv_div;
+                    bn[c] += v2 * v2;
+                    ls[c] = 0.0;
+                    if (ols) {
+                        const double w2 = ols[c] * inv_div;
+                        obn[c] += w2 * w2;
+                        ols[c] = 0.0;
+                    }
+                }
+            }
+        }
+    };
+    int pending = -1;   // measurement whose totals wait for rank 0's fold
 
     for (int m = 0; m < a.n_meas; ++m) {
         for (int sm = 0; sm < a.steps_measure; ++sm) {
@@ -326,6 +415,10 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
                     }
                 }
                 cluster.sync();
+                if (pending >= 0) {
+                    if (rank == 0 && threadIdx.x < 32) fold_measurement(pending);
+                    pending = -1;
+                }
             }
             accE = f2_add(accE, fE); accX = f2_add(accX, fX); accY = f2_add(accY, fY); accZ = f2_add(accZ, fZ);
         }
@@ -372,13 +465,13 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
                 for (int c = 0; c < 4; ++c) {
                     F2 x = lane < nw ? F2{redf[12 * lane + 2 * c], redf[12 * lane + 2 * c + 1]} : F2{0.f, 0.f};
                     for (int o = 16; o > 0; o >>= 1) x = f2_add(x, f2_shfl_down(x, o));
-                    if (lane == 0) red[128 + c] = f2_to_double(x);   // this CTA's totals
+                    if (lane == 0) red[128 + 8 * (m & 1) + c] = f2_to_double(x);   // this CTA's totals
                 }
 #pragma unroll
                 for (int c = 4; c < 8; ++c) {
                     float x = lane < nw ? redf[12 * lane + 4 + c] : 0.f;
                     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-                    if (lane == 0) red[128 + c] = (double)x;
+                    if (lane == 0) red[128 + 8 * (m & 1) + c] = (double)x;
                 }
             }
             // P(M) [P(OP), P(SM)] of this CTA's cells
@@ -416,92 +509,19 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
                     hist_flush(hist + 2 * a.nf, run_sm);
                 }
             }
-            cluster.sync();
-            if (rank == 0 && threadIdx.x < 32) {
-                // lane 0 folds the CTAs' sums into the replica totals and the
-                // accumulators of mcarlo.F90:536-590 for this temperature
-                // slot; the binning levels, independent of one another, go
-                // one per lane
-                const double rn_inv = a.rn_inv;
-                const long long step = meas_base + m + 1;
-                double e = 0.0, am = 0.0, aop = 0.0, asm_ = 0.0;
-                if (threadIdx.x == 0) {
-                    double d4[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                    for (int q = 0; q < csize; ++q) {
-                        const double *pr = cluster.map_shared_rank(red, q);
-#pragma unroll
-                        for (int c = 0; c < 8; ++c) d4[c] += pr[128 + c];
-                    }
-                    e_run += d4[0];
-                    m_run[0] += d4[1]; m_run[1] += d4[2]; m_run[2] += d4[3];
-                    e = e_run;
-                    const double mx = m_run[0] * rn_inv, my = m_run[1] * rn_inv, mz = m_run[2] * rn_inv;
-                    const double m2 = mx * mx + my * my + mz * mz;
-                    const double ee = e * e;
-                    am = sqrt(m2);
-                    double *d = cache ? c_data : a.data + 6 * temp;
-                    d[0] += e; d[1] += ee; d[2] += ee * ee;
-                    d[3] += am; d[4] += m2; d[5] += m2 * m2;
-                    if (a.series) {
-                        double *o = a.series + (((step - 1) % a.series_cap) * a.R + temp) * 2;
-                        o[0] = e; o[1] = am;
-                    }
-                    // orderparam_get / staggered_get (mcarlo.F90:553-568)
-                    if (a.obs) {
-                        double *od = cache ? c_odata : a.obs_data + 6 * temp;
-                        if (a.obs & 1) {
-                            const double op = d4[4] * rn_inv;
-                            const double o2 = op * op;
-                            aop = sqrt(o2);
-                            od[0] += aop; od[1] += o2; od[2] += o2 * o2;
-                        }
-                        if (a.obs & 2) {
-                            const double qx = d4[5] * rn_inv, qy = d4[6] * rn_inv, qz = d4[7] * rn_inv;
-                            const double q2 = qx * qx + qy * qy + qz * qz;
-                            asm_ = sqrt(q2);
-                            od[3] += asm_; od[4] += q2; od[5] += q2 * q2;
-                        }
-                    }
-                }
-                if (a.nlev > 0) {
-                    e = __shfl_sync(0xffffffffu, e, 0);
-                    am = __shfl_sync(0xffffffffu, am, 0);
-                    aop = __shfl_sync(0xffffffffu, aop, 0);
-                    asm_ = __shfl_sync(0xffffffffu, asm_, 0);
-                }
-                for (int lv = threadIdx.x; lv < a.nlev; lv += 32) {
-                    const size_t g2 = ((size_t)temp * a.nlev + lv) * 2;
-                    double *ls = cache ? c_ls + 2 * lv : a.lsum + g2;
-                    double *bn = cache ? c_bn + 2 * lv : a.binning + g2;
-                    double *ols = !a.obs ? nullptr : (cache ? c_ols + 2 * lv : a.obs_lsum + g2);
-                    double *obn = !a.obs ? nullptr : (cache ? c_obn + 2 * lv : a.obs_bin + g2);
-                    ls[0] += e * rn_inv;
-                    ls[1] += am;
-                    if (ols) { ols[0] += aop; ols[1] += asm_; }
-                    const int lev = cache ? c_lev[lv] : a.levels[lv];
-                    const long long blk = 1LL << lev;
-                    if ((step & (blk - 1)) == 0) {
-                        // 1/2^n is exact, so the product equals the division
-                        const double inv_div = ldexp(1.0, -(a.pt_quirk ? lv + 1 : lev));
-                        for (int c = 0; c < 2; ++c) {
-                            const double v2 = ls[c] * inv_div;
-                            bn[c] += v2 * v2;
-                            ls[c] = 0.0;
-                            if (ols) {
-                                const double w2 = ols[c] * inv_div;
-                                obn[c] += w2 * w2;
-                                ols[c] = 0.0;
-                            }
-                        }
-                    }
-                }
-            }
-            cluster.sync();
+            // the totals of this measurement wait in buffer (m & 1) of every
+            // CTA; rank 0 folds them after the next cluster barrier (the next
+            // colour pass, or the end of the launch), so a measurement adds no
+            // cluster barrier of its own
+            pending = m;
         }
     }
 
     // ---- end of launch: totals, rejected counts, histogram, spins ----------
     {
+        // warp 0 may still read the last measurement's warp partials, which
+        // the warp partials below overwrite
+        __syncthreads();
         double v[4] = {f2_to_double(accE), f2_to_double(accX), f2_to_double(accY), f2_to_double(accZ)};
         unsigned long long nr = nrej;
         for (int c = 0; c < 4; ++c)
@@ -520,8 +540,8 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
                 for (int c = 0; c < 4; ++c) t4[c] += red[4 * w + c];
                 tn += reinterpret_cast<unsigned long long *>(red + 96)[w];
             }
-            for (int c = 0; c < 4; ++c) red[128 + c] = t4[c];
-            reinterpret_cast<unsigned long long *>(red)[132] = tn;
+            for (int c = 0; c < 4; ++c) red[144 + c] = t4[c];
+            reinterpret_cast<unsigned long long *>(red)[148] = tn;
         }
         if (a.na > 1)
             for (int i = threadIdx.x; i < a.nf; i += blockDim.x)
@@ -530,13 +550,16 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
             for (int i = threadIdx.x; i < 2 * a.nf; i += blockDim.x)
                 if (hist[a.nf + i]) atomicAdd(a.obs_pm + (size_t)temp * 2 * a.nf + i, (unsigned long long)hist[a.nf + i]);
         cluster.sync();
+        // the launch's last measurement, then the sums since it
+        if (pending >= 0 && rank == 0 && threadIdx.x < 32) fold_measurement(pending);
+        if (rank == 0) __syncthreads();   // the fold's accumulator writes before the write-back below
         if (rank == 0 && threadIdx.x == 0) {
             double d4[4] = {0, 0, 0, 0};
             unsigned long long tn = 0;
             for (int q = 0; q < csize; ++q) {
                 const double *pr = cluster.map_shared_rank(red, q);
-                for (int c = 0; c < 4; ++c) d4[c] += pr[128 + c];
-                tn += reinterpret_cast<const unsigned long long *>(pr)[132];
+                for (int c = 0; c < 4; ++c) d4[c] += pr[144 + c];
+                tn += reinterpret_cast<const unsigned long long *>(pr)[148];
             }
             a.e_run[r] = e_run + d4[0];
             a.m_run[3 * r] = m_run[0] + d4[1];
@@ -640,16 +663,24 @@ cudaError_t launch_from_slabs(const SlabArgs &a, cudaStream_t st)
 size_t cluster_smem_bytes(int n_local, int nf, int nhist, size_t stencil_bytes)
 {
     return ((stencil_bytes + 15) & ~(size_t)15) + (size_t)((nhist * nf + 3) & ~3) * sizeof(unsigned int) +
-           (size_t)(136 + kClusterAccDoubles) * sizeof(double) + (size_t)3 * n_local * sizeof(float);
+           (size_t)(kClusterRedDoubles + kClusterAccDoubles) * sizeof(double) + (size_t)3 * n_local * sizeof(float);
 }
 
 namespace {
 
 using ClusterKernel = void (*)(ClusterArgs);
 
-ClusterKernel cluster_kernel(int nt, int S)
+template <bool HB, bool HD>
+ClusterKernel cluster_kernel_t(int nt, int S)
 {
-    return nt == 256 ? k_sweep_cluster<256, 1> : (S == 2 ? k_sweep_cluster<512, 2> : k_sweep_cluster<512, 1>);
+    return nt == 256 ? k_sweep_cluster<256, 1, HB, HD>
+                     : (S == 2 ? k_sweep_cluster<512, 2, HB, HD> : k_sweep_cluster<512, 1, HB, HD>);
+}
+
+ClusterKernel cluster_kernel(int nt, int S, bool hb, bool hd)
+{
+    return hb ? (hd ? cluster_kernel_t<true, true>(nt, S) : cluster_kernel_t<true, false>(nt, S))
+              : (hd ? cluster_kernel_t<false, true>(nt, S) : cluster_kernel_t<false, false>(nt, S));
 }
 
 }  // namespace
@@ -659,17 +690,20 @@ bool cluster_threads_ok(int nt, int S) { return (nt == 256 && S == 1) || (nt == 
 cudaError_t cluster_configure(size_t smem, int csize, int nt, int S)
 {
     if (!cluster_threads_ok(nt, S)) return cudaErrorInvalidValue;
-    const ClusterKernel k = cluster_kernel(nt, S);
-    cudaError_t e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k), smem);
-    if (e != cudaSuccess) return e;
-    if (csize > 8) e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaError_t e = cudaSuccess;
+    for (int v = 0; v < 4 && e == cudaSuccess; ++v) {
+        const ClusterKernel k = cluster_kernel(nt, S, v & 1, v & 2);
+        e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k), smem);
+        if (e == cudaSuccess && csize > 8) e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    }
     return e;
 }
 
 int cluster_max_active(int csize, int nt, int S, size_t smem, int R)
 {
     if (!cluster_threads_ok(nt, S)) return 0;
-    const ClusterKernel k = cluster_kernel(nt, S);
+    // the variant with every term uses the most registers
+    const ClusterKernel k = cluster_kernel(nt, S, true, true);
     if (allow_max_dynamic_smem(reinterpret_cast<const void *>(k), smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
@@ -712,7 +746,7 @@ cudaError_t launch_cluster(const ClusterArgs &a, int csize, int nt, int S, size_
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, cluster_kernel(nt, S), a);
+    return cudaLaunchKernelEx(&cfg, cluster_kernel(nt, S, a.has_b != 0, a.has_d != 0), a);
 }
 
 }  // namespace esp

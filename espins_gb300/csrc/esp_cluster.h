@@ -108,6 +108,8 @@ cudaError_t launch_from_slabs(const SlabArgs &a, cudaStream_t st);
 constexpr int kClusterMaxLev = 32;
 // doubles of that cache: data and obs data (12), levels (16), four [level][2] arrays
 constexpr int kClusterAccDoubles = 12 + kClusterMaxLev / 2 + 8 * kClusterMaxLev;
+// doubles of the reduction scratch before that cache
+constexpr int kClusterRedDoubles = 152;
 size_t cluster_smem_bytes(int n_local, int nf, int nhist, size_t stencil_bytes);
 // nt: threads per CTA, 256 or 512
 // The dynamic shared-memory limit is a property of a kernel function, shared
