@@ -87,7 +87,10 @@ def _args():
     p.add_argument("--train-pairs", type=int, default=10_000_000)
     p.add_argument("--train-steps", type=int, default=3000)
     p.add_argument("--measure-sweeps", type=int, default=20000)
-    p.add_argument("--plain-sweeps", type=int, default=200000,
+    p.add_argument("--chains", type=int, default=4,
+                   help="--proposal compare: independent PT chains (replica groups) per sampler; the spread of "
+                        "their averages is part of each observable's error")
+    p.add_argument("--plain-sweeps", type=int, default=100000,
                    help="--proposal compare: sweeps of the plain sampler's measurement window (its low-temperature "
                         "autocorrelation times reach ~2000 sweeps, so its window is longer than the learned one's)")
     return p.parse_args()
@@ -328,16 +331,21 @@ def learned_compare(a, rank, local):
     dev = torch.device("cuda", local)
     inp = workload(a.workload, L=a.L, replicas=a.replicas)
     ham = build_hamiltonian(inp, check=False)
-    R, N = inp.tems_num, ham.n
+    nT, N = inp.tems_num, ham.n
+    C = max(1, a.chains)
+    R = nT * C                      # chain c holds slots [c nT, (c+1) nT)
     pss = inp.pt_steps_swap if inp.pt else 1
     seed = 4 + 1000 * rank
     stream = torch.cuda.current_stream(dev)
     eng = Engine(N, ham.num_atoms, ham.supercell, R, inp.boundary_open)
     eng.upload(ham)
-    eng.set_temperatures(inp.tems)
+    eng.set_temperatures(np.tile(inp.tems, C))
+    if C > 1:
+        eng.set_pt_groups(nT)       # each chain exchanges only within itself
     eng.set_stream(stream.cuda_stream)
     _, ncol = eng.colouring()
-    # plain PT warm-up, then one colour class of every replica per swap interval
+    # plain PT warm-up from independent random configurations, then one
+    # colour class of every replica per swap interval
     eng.set_spins(_uniform_spins(R, N, ham.mag, seed))
     warm = 2000
     n_coll = -(-a.train_pairs // (N * R // ncol))
@@ -381,26 +389,38 @@ def learned_compare(a, rank, local):
         secs = e0.elapsed_time(e1) * 1e-3
         res = eng.collect()
         ser = eng.series()[-units * pss:]
-        tau_e = np.array([analysis.tau_int(ser[:, t, 0]) for t in range(R)])
-        tau_m = np.array([analysis.tau_int(ser[:, t, 1]) for t in range(R)])
-        tau = np.maximum(tau_e, tau_m)
+        tau_e = np.array([[analysis.tau_int(ser[:, c * nT + t, 0]) for t in range(nT)] for c in range(C)])
+        tau_m = np.array([[analysis.tau_int(ser[:, c * nT + t, 1]) for t in range(nT)] for c in range(C)])
+        tau = np.maximum(tau_e, tau_m).mean(axis=0)       # per slot, over the chains
         sweeps_per_s = units * pss / secs
         ups = sweeps_per_s * N * R
         trials = -(-sweeps // pss) * pss * N     # per temperature slot, whole run
-        acc = 1.0 - res["rejected"][:, 1] / trials
-        # the _mc.dat observables of the measurement window with jackknife errors
-        obs = np.zeros((R, 6)); err = np.zeros((R, 6))
-        for t in range(R):
-            obs[t], err[t] = A.jackknife_observables(ser[:, t, 0], ser[:, t, 1], float(inp.tems[t]), N, 40)
+        acc = (1.0 - res["rejected"][:, 1] / trials).reshape(C, nT).mean(axis=0)
+        # the _mc.dat observables of the measurement window per chain
+        # (jackknife errors), averaged over the chains; the error of the
+        # average is the larger of the combined jackknife error and the
+        # chains' spread, which also holds modes slower than the window
+        obs = np.zeros((C, nT, 6)); err = np.zeros((C, nT, 6))
+        for c in range(C):
+            for t in range(nT):
+                k = c * nT + t
+                obs[c, t], err[c, t] = A.jackknife_observables(ser[:, k, 0], ser[:, k, 1], float(inp.tems[t]), N, 40)
+        mean = obs.mean(axis=0)
+        sig = np.sqrt((err ** 2).sum(axis=0)) / C
+        if C > 1:
+            sig = np.maximum(sig, obs.std(axis=0, ddof=1) / np.sqrt(C))
         out[kind] = {
-            "sweeps": int(units * pss), "seconds": secs,
+            "sweeps": int(units * pss), "seconds": secs, "chains": C,
             "site_updates_per_s": ups,
-            "independent_samples_per_s": float(np.sum(sweeps_per_s / (2.0 * tau))),
-            "per_slot_samples_per_s": (sweeps_per_s / (2.0 * tau)).tolist(),
-            "tau_int_E": tau_e.tolist(), "tau_int_absM": tau_m.tolist(),
-            "tau_int_binning_E": [analysis.binning_tau(ser[:, t, 0]) for t in range(R)],
+            # every chain yields an independent sample per 2 tau sweeps
+            "independent_samples_per_s": float(np.sum(C * sweeps_per_s / (2.0 * tau))),
+            "per_slot_samples_per_s": (C * sweeps_per_s / (2.0 * tau)).tolist(),
+            "tau_int_E": tau_e.mean(axis=0).tolist(), "tau_int_absM": tau_m.mean(axis=0).tolist(),
+            "tau_int_binning_E": [analysis.binning_tau(ser[:, t, 0]) for t in range(nT)],
             "acceptance": acc.tolist(), "kernel": eng.sweep_kernel()[0],
-            "observables": obs.tolist(), "sigma": err.tolist(),
+            "observables": mean.tolist(), "sigma": sig.tolist(),
+            "chain_spread_over_jackknife": (obs.std(axis=0, ddof=1) / np.maximum(err.mean(axis=0), 1e-300)).max(
+                axis=1).tolist() if C > 1 else None,
         }
     eng.close()
     gains = np.asarray(out["learned"]["per_slot_samples_per_s"]) / np.asarray(out["plain"]["per_slot_samples_per_s"])
@@ -427,7 +447,10 @@ def learned_compare(a, rank, local):
             "metric": "independent samples/s", "value": out["learned"]["independent_samples_per_s"],
             "unit": "samples/s", "n_gpus": 1, "steps": a.measure_sweeps, "warmup": 500,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32",
-            "data": "synthetic", "config": _config(inp, ham, a.workload) | {"proposal": "learned vs plain"},
+            "data": "synthetic",
+            "config": _config(inp, ham, a.workload) | {"proposal": "learned vs plain", "independent_chains": C,
+                                                       "plain_sweeps": a.plain_sweeps,
+                                                       "learned_sweeps": a.measure_sweeps},
             "plain": out["plain"], "learned": out["learned"],
             "ratio_independent_samples": out["learned"]["independent_samples_per_s"]
             / out["plain"]["independent_samples_per_s"],

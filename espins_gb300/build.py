@@ -21,7 +21,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17"]
 
 CU_SOURCES = ["esp_kernels.cu", "esp_api.cu", "esp_noalloc.cu", "esp_cluster.cu", "esp_learned.cu", "esp_tile.cu",
-              "esp_lp_tc.cu"]
+              "esp_lp_tc.cu", "esp_gemm_tc.cu"]
 CXX_SOURCES = ["esp_tables.cpp"]
 HEADERS = ["esp_device.cuh", "esp_kernels.h", "esp_tables.h", "esp_errors.h", "esp_cluster.h", "esp_learned.h",
            "esp_mlp.cuh", "esp_vmf.cuh", "esp_tile.h", "esp_tc.cuh", "esp_lp_tc.cuh", "esp_lp_tc.h"]

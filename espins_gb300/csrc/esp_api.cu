@@ -135,6 +135,7 @@ struct esp_handle {
     int lp_engine = 0;              // network on 0: mma.sync (warp tiles), 1: tcgen05 (128-row tiles)
     int *d_tc_err = nullptr;        // set by a tensor-core completion wait that gave up
     int tc_force_timeout = 0;       // test hook: tcgen05 waits report a give-up (esp_lp_force_tc_timeout)
+    float *d_lp_gwork = nullptr;    // partial tiles of the tcgen05 training GEMMs split along K
     // partial sums of the tcgen05 learned sweep (128-thread blocks)
     int tc_grid = 0, tc_slots = 0;
     double *d_tc_part = nullptr;
@@ -258,6 +259,7 @@ void free_all(esp_handle *h)
     dfree(h->d_lp_x); dfree(h->d_lp_t); dfree(h->d_lp_loss);
     dfree(h->d_ctr);
     dfree(h->d_tc_err);
+    dfree(h->d_lp_gwork);
 }
 
 SweepArgs sweep_args(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o)
@@ -985,6 +987,7 @@ int esp_create(const esp_dims *dims, esp_handle **out)
     if (e == cudaSuccess) e = lp_configure(h->device);
     if (e == cudaSuccess) e = lp_tc_configure();
     if (e == cudaSuccess) e = lp_tc_sweep_configure();
+    if (e == cudaSuccess) e = gemm_tc_configure();
     if (e != cudaSuccess) {
         set_global_error("CUDA unavailable: %s", cudaGetErrorString(e));
         delete h;
@@ -2201,6 +2204,18 @@ int lp_ensure_loss(esp_handle *h, long long n)
     return ESP_OK;
 }
 
+// ESP_ETIMEOUT when a tensor-core completion wait of the tcgen05 engine gave up
+// since the flag was last cleared.
+int lp_tc_status(esp_handle *h, const char *what)
+{
+    if (h->lp_engine != 1 || !h->d_tc_err) return ESP_OK;
+    int flag = 0;
+    int rc = d2h(h, &flag, h->d_tc_err, sizeof(int));
+    if (rc) return rc;
+    if (flag) { h->err = std::string(what) + ": a tensor-core completion wait gave up"; return ESP_ETIMEOUT; }
+    return ESP_OK;
+}
+
 // Forward and backward pass over the B rows in the batch buffers, the first
 // n_real of which are samples: loss (mean -log q over those) into *d_loss,
 // gradients into d_lp_g (padded layout).
@@ -2211,42 +2226,48 @@ int lp_pass(esp_handle *h, int B, int n_real, double *d_loss)
     float *G = h->d_lp_g;
     GemmArgs g;
     auto reset = [&]() { std::memset(&g, 0, sizeof(g)); };
+    // the network's engine also runs the training GEMMs: warp-level mma.sync
+    // tiles, or tcgen05 with tensor-memory accumulators
+    auto gemm = [&](bool ta, bool tb) -> cudaError_t {
+        if (h->lp_engine == 1) return launch_gemm_tc(g, ta, tb, h->num_sms, h->d_lp_gwork, h->d_tc_err, st);
+        return launch_gemm(g, ta, tb, st);
+    };
     // H1 = relu(X W1^T + b1)
     reset(); g.A = h->d_lp_xb; g.lda = kMlpInPad; g.B = h->d_lp_w1; g.ldb = kMlpInPad;
     g.M = B; g.N = kMlpHid; g.K = kMlpInPad; g.Cb = h->d_lp_h1; g.ldcb = kMlpHid; g.bias = P + kPadB1; g.relu = 1;
-    CK(launch_gemm(g, false, false, st));
+    CK(gemm(false, false));
     // H2 = relu(H1 W2^T + b2)
     reset(); g.A = h->d_lp_h1; g.lda = kMlpHid; g.B = h->d_lp_w2; g.ldb = kMlpHid;
     g.M = B; g.N = kMlpHid; g.K = kMlpHid; g.Cb = h->d_lp_h2; g.ldcb = kMlpHid; g.bias = P + kPadB2; g.relu = 1;
-    CK(launch_gemm(g, false, false, st));
+    CK(gemm(false, false));
     // O = H2 W3^T + b3
     reset(); g.A = h->d_lp_h2; g.lda = kMlpHid; g.B = h->d_lp_w3; g.ldb = kMlpHid;
     g.M = B; g.N = kMlpOutPad; g.K = kMlpHid; g.C = h->d_lp_o; g.ldc = kMlpOutPad; g.bias = P + kPadB3;
-    CK(launch_gemm(g, false, false, st));
+    CK(gemm(false, false));
     // dO
     CK(launch_lp_head(h->d_lp_o, h->d_lp_tb, n_real, B, 1.f / (float)n_real, h->d_lp_do, d_loss, st));
     // dW3 = dO^T H2, db3
     reset(); g.A = h->d_lp_do; g.lda = kMlpOutPad; g.B = h->d_lp_h2; g.ldb = kMlpHid;
     g.M = kMlpOutPad; g.N = kMlpHid; g.K = B; g.C = G + kPadW3; g.ldc = kMlpHid;
-    CK(launch_gemm(g, true, true, st));
+    CK(gemm(true, true));
     CK(launch_colsum(h->d_lp_do, B, kMlpOutPad, kMlpOutPad, G + kPadB3, st));
     // dZ2 = (dO W3) . [H2 > 0]
     reset(); g.A = h->d_lp_do; g.lda = kMlpOutPad; g.B = h->d_lp_w3; g.ldb = kMlpHid;
     g.M = B; g.N = kMlpHid; g.K = kMlpOutPad; g.Cb = h->d_lp_dz2; g.ldcb = kMlpHid; g.mask = h->d_lp_h2; g.ldm = kMlpHid;
-    CK(launch_gemm(g, false, true, st));
+    CK(gemm(false, true));
     // dW2 = dZ2^T H1, db2
     reset(); g.A = h->d_lp_dz2; g.lda = kMlpHid; g.B = h->d_lp_h1; g.ldb = kMlpHid;
     g.M = kMlpHid; g.N = kMlpHid; g.K = B; g.C = G + kPadW2; g.ldc = kMlpHid;
-    CK(launch_gemm(g, true, true, st));
+    CK(gemm(true, true));
     CK(launch_colsum(h->d_lp_dz2, B, kMlpHid, kMlpHid, G + kPadB2, st));
     // dZ1 = (dZ2 W2) . [H1 > 0]
     reset(); g.A = h->d_lp_dz2; g.lda = kMlpHid; g.B = h->d_lp_w2; g.ldb = kMlpHid;
     g.M = B; g.N = kMlpHid; g.K = kMlpHid; g.Cb = h->d_lp_dz1; g.ldcb = kMlpHid; g.mask = h->d_lp_h1; g.ldm = kMlpHid;
-    CK(launch_gemm(g, false, true, st));
+    CK(gemm(false, true));
     // dW1 = dZ1^T X, db1
     reset(); g.A = h->d_lp_dz1; g.lda = kMlpHid; g.B = h->d_lp_xb; g.ldb = kMlpInPad;
     g.M = kMlpHid; g.N = kMlpInPad; g.K = B; g.C = G + kPadW1; g.ldc = kMlpInPad;
-    CK(launch_gemm(g, true, true, st));
+    CK(gemm(true, true));
     CK(launch_colsum(h->d_lp_dz1, B, kMlpHid, kMlpHid, G + kPadB1, st));
     h->launches += 13;
     return ESP_OK;
@@ -2378,6 +2399,7 @@ int esp_lp_train(esp_handle *h, const esp_lp_train_opts *o, double *loss)
     int rc = lp_ensure_batch(h, B);
     if (rc) return rc;
     if ((rc = lp_ensure_loss(h, std::max(1, o->steps)))) return rc;
+    if (h->lp_engine == 1) CK(cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->st));
     for (int s = 0; s < o->steps; ++s) {
         CK(launch_lp_gather(h->d_lp_x, h->d_lp_t, h->lp_n, B, o->seed, (uint64_t)(h->lp_adam_t), h->d_lp_xb,
                             h->d_lp_tb, h->st));
@@ -2393,7 +2415,7 @@ int esp_lp_train(esp_handle *h, const esp_lp_train_opts *o, double *loss)
     } else {
         CK(cudaStreamSynchronize(h->st));
     }
-    return ESP_OK;
+    return lp_tc_status(h, "esp_lp_train");
 }
 
 int esp_lp_loss_grad(esp_handle *h, const float *features, const float *targets, int64_t n, double *loss,
@@ -2405,6 +2427,7 @@ int esp_lp_loss_grad(esp_handle *h, const float *features, const float *targets,
     int rc = lp_ensure_batch(h, B);
     if (rc) return rc;
     if ((rc = lp_ensure_loss(h, 1))) return rc;
+    if (h->lp_engine == 1) CK(cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->st));
     std::vector<__nv_bfloat16> x;
     bf16_rows(features, n, x);
     x.resize((size_t)B * kMlpInPad, __float2bfloat16_rn(0.f));   // zero rows up to the multiple of 8
@@ -2417,7 +2440,7 @@ int esp_lp_loss_grad(esp_handle *h, const float *features, const float *targets,
     if ((rc = d2h(h, g.data(), h->d_lp_g, sizeof(float) * kPadParams))) return rc;
     if (grad) lp_padded_to_logical(g, grad);
     if (loss && (rc = d2h(h, loss, h->d_lp_loss, sizeof(double)))) return rc;
-    return ESP_OK;
+    return lp_tc_status(h, "esp_lp_loss_grad");
 }
 
 int esp_lp_forward(esp_handle *h, const float *features, int64_t n, float *out)
@@ -2465,6 +2488,7 @@ int esp_lp_set_engine(esp_handle *h, int32_t engine)
         CK(dalloc(&h->d_tc_err, 1));
         CK(cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->st));
     }
+    if (engine == 1 && !h->d_lp_gwork) CK(dalloc(&h->d_lp_gwork, kGemmTcWorkFloats));
     h->lp_engine = engine;
     return ESP_OK;
 }

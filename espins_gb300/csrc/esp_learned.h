@@ -65,6 +65,17 @@ cudaError_t launch_sweep_lp_tc(const LpSweepArgs &a, bool hb, bool hd, int block
 cudaError_t launch_lp_collect(const LpCollectArgs &a, bool hb, bool hd, int max_blocks, cudaStream_t st);
 // C = op(A) op(B): ta -> A stored [K][M] (else [M][K]); tb -> B stored [K][N] (else [N][K])
 cudaError_t launch_gemm(const GemmArgs &g, bool ta, bool tb, cudaStream_t st);
+// The same GEMM on the tcgen05 tensor cores (esp_gemm_tc.cu): 128-row tiles
+// with tensor-memory accumulators; M, K multiples of 8, N of 16.  Pure FP32
+// outputs (no bias, ReLU, mask, BF16 copy or accumulation) with M*N at most
+// kGemmTcSplitMN are split along K into `work` (kGemmTcMaxSplit * M * N
+// floats) and summed in a fixed order.  err is set when a completion wait
+// gave up.
+constexpr int kGemmTcMaxSplit = 64;
+constexpr int kGemmTcSplitMN = 128 * 128;
+constexpr size_t kGemmTcWorkFloats = (size_t)kGemmTcMaxSplit * kGemmTcSplitMN;
+cudaError_t gemm_tc_configure();
+cudaError_t launch_gemm_tc(const GemmArgs &g, bool ta, bool tb, int num_sms, float *work, int *err, cudaStream_t st);
 cudaError_t launch_lp_gather(const __nv_bfloat16 *x_all, const float *t_all, long long n_all, int batch,
                              uint64_t seed, uint64_t step, __nv_bfloat16 *xb, float *tb, cudaStream_t st);
 // rows >= n_real of the n_rows in the batch get zero gradients and no loss

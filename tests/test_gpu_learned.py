@@ -129,17 +129,25 @@ def test_tcgen05_give_up_path_reports_timeout_and_writes_nothing():
         assert res["rejected"][:, 1].sum() < 2 * 4 * e.n
 
 
-def test_training_loss_and_gradient_match_fp64_network():
+@pytest.mark.parametrize("engine", ["mma", "tcgen05"])
+@pytest.mark.parametrize("n", [1000, 4096])
+def test_training_loss_and_gradient_match_fp64_network(engine, n):
+    """Forward, loss head and backward GEMMs of a training step (mma.sync
+    tiles, or tcgen05 with tensor-memory accumulators and the weight
+    gradients split along the batch) against the FP64 network."""
     p = _weights(3)
     rng = np.random.default_rng(4)
-    n = 1000
     x = rng.normal(size=(n, 12)).astype(np.float32)
     s = rng.normal(size=(n, 3))
     s /= np.linalg.norm(s, axis=1, keepdims=True)
     t = np.column_stack([s, np.abs(rng.normal(size=n)) * 5]).astype(np.float32)
     with _small_engine() as e:
         e.lp_set_weights(p)
+        e.lp_set_engine(engine)
         loss, g = e.lp_loss_grad(x, t)
+        # deterministic: the same gradient again
+        loss2, g2 = e.lp_loss_grad(x, t)
+        assert loss2 == loss and np.array_equal(g2, g)
     lo, go = O.lp_loss_grad(_rounded(p), bf16(x), t.astype(np.float64))
     assert abs(loss - lo) <= 1e-2 * abs(lo), (loss, lo)
     assert np.linalg.norm(g - go) <= 5e-2 * np.linalg.norm(go)
