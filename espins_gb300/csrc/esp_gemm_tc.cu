@@ -37,6 +37,11 @@ struct alignas(128) GemmTcSmem {
     uint32_t tmem;
 };
 
+// Dynamic shared memory per CTA: more than the operands need, so that at most
+// three CTAs share an SM and their tensor-memory allocations (up to 128
+// columns each) fit the SM's 512 columns without waiting.
+constexpr size_t kGemmTcSmemBytes = 72 * 1024;
+
 // Tensor-memory columns to allocate for n accumulator columns (a power of
 // two, at least 32).
 __host__ __device__ constexpr uint32_t tmem_cols_for(int n) { return n <= 32 ? 32u : (n <= 64 ? 64u : 128u); }
@@ -194,7 +199,8 @@ int split_count(const GemmArgs &g, int num_sms, int &k_per)
 
 cudaError_t gemm_tc_configure()
 {
-    const int bytes = (int)sizeof(GemmTcSmem);
+    static_assert(sizeof(GemmTcSmem) <= kGemmTcSmemBytes, "operand tiles exceed the shared-memory request");
+    const int bytes = (int)kGemmTcSmemBytes;
     cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -218,7 +224,7 @@ cudaError_t launch_gemm_tc(const GemmArgs &g, bool ta, bool tb, int num_sms, flo
     if (splits > 1 && !work) return cudaErrorInvalidValue;
     float *part = splits > 1 ? work : nullptr;
     const dim3 grid(mt, nt, splits);
-    const size_t sm = sizeof(GemmTcSmem);
+    const size_t sm = kGemmTcSmemBytes;
     if (!ta && !tb) k_gemm_tc<false, false><<<grid, kGtThreads, sm, st>>>(g, BN, k_per, part, err);
     else if (ta && tb) k_gemm_tc<true, true><<<grid, kGtThreads, sm, st>>>(g, BN, k_per, part, err);
     else if (!ta) k_gemm_tc<false, true><<<grid, kGtThreads, sm, st>>>(g, BN, k_per, part, err);
