@@ -90,6 +90,9 @@ def _args():
     p.add_argument("--chains", type=int, default=4,
                    help="--proposal compare: independent PT chains (replica groups) per sampler; the spread of "
                         "their averages is part of each observable's error")
+    p.add_argument("--equil-sweeps", type=int, default=5000,
+                   help="--proposal compare: learned-sampler sweeps after training that equilibrate the common start "
+                        "of both measurement windows")
     p.add_argument("--plain-sweeps", type=int, default=100000,
                    help="--proposal compare: sweeps of the plain sampler's measurement window (its low-temperature "
                         "autocorrelation times reach ~2000 sweeps, so its window is longer than the learned one's)")
@@ -369,6 +372,15 @@ def learned_compare(a, rank, local):
     ev1.record(stream)
     torch.cuda.synchronize(dev)
     t_train = ev0.elapsed_time(ev1) * 1e-3
+    # a common, equilibrated start for both windows: the plain chains' slow
+    # relaxation at low temperature (tau of thousands of sweeps) would
+    # otherwise bias the plain window; a biased learned sampler would show as
+    # a drift of the plain window away from this start (its two halves differ)
+    eng.set_proposal("learned")
+    eng.set_spins(start)
+    eng.begin(eng.schedule(0, a.equil_sweeps + pss, 1, pt=inp.pt, pt_steps_swap=pss, seed=seed + 31))
+    eng.advance(max(1, a.equil_sweeps // pss))
+    start = eng.get_spins()
     out = {}
     from espins_gb300 import analysis as A
     for kind in ("plain", "learned"):
@@ -406,6 +418,9 @@ def learned_compare(a, rank, local):
                 k = c * nT + t
                 obs[c, t], err[c, t] = A.jackknife_observables(ser[:, k, 0], ser[:, k, 1], float(inp.tems[t]), N, 40)
         mean = obs.mean(axis=0)
+        half = ser.shape[0] // 2
+        e_halves = np.array([[ser[:half, c * nT + t, 0].mean() / N, ser[half:, c * nT + t, 0].mean() / N]
+                             for t in range(nT) for c in range(C)]).reshape(nT, C, 2).mean(axis=1)
         sig = np.sqrt((err ** 2).sum(axis=0)) / C
         if C > 1:
             sig = np.maximum(sig, obs.std(axis=0, ddof=1) / np.sqrt(C))
@@ -419,6 +434,7 @@ def learned_compare(a, rank, local):
             "tau_int_binning_E": [analysis.binning_tau(ser[:, t, 0]) for t in range(nT)],
             "acceptance": acc.tolist(), "kernel": eng.sweep_kernel()[0],
             "observables": mean.tolist(), "sigma": sig.tolist(),
+            "E_per_site_first_second_half": e_halves.tolist(),
             "chain_spread_over_jackknife": (obs.std(axis=0, ddof=1) / np.maximum(err.mean(axis=0), 1e-300)).max(
                 axis=1).tolist() if C > 1 else None,
         }
@@ -450,6 +466,7 @@ def learned_compare(a, rank, local):
             "data": "synthetic",
             "config": _config(inp, ham, a.workload) | {"proposal": "learned vs plain", "independent_chains": C,
                                                        "plain_sweeps": a.plain_sweeps,
+                                                       "equilibration_sweeps": a.equil_sweeps,
                                                        "learned_sweeps": a.measure_sweeps},
             "plain": out["plain"], "learned": out["learned"],
             "ratio_independent_samples": out["learned"]["independent_samples_per_s"]

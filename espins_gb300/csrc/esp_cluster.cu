@@ -276,8 +276,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
             const float d = delta_energy(HB || a.has_si, gx[s], gy[s], gz[s], qxx[s], qyy[s], qzz[s], qxy[s],
                                          qxz[s], qyz[s], ox[s], oy[s], oz[s], nx[s], ny[s], nz[s]);
             de[s] = d;
-            acc[s] = true;
-            if (d > 0.0f) acc[s] = expf(-beta * d) >= u24f(xr.z);
+            acc[s] = metropolis_accept(beta, d, xr.z);
         }
 #pragma unroll
         for (int s = 0; s < SN; ++s) {

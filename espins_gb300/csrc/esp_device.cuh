@@ -60,8 +60,15 @@ __device__ __forceinline__ void trial_spin(int mode, float tilt, float mag, floa
                                            uint32_t x0, uint32_t x1, float &nx, float &ny, float &nz)
 {
     const float u0 = u24f(x0), u1 = u24f(x1);
+    // phi = 2 pi u1 = psi + pi with psi = 2 pi (u1 - 1/2) in [-pi, pi), where
+    // the hardware sine and cosine are accurate to ~4e-7 (u1 - 1/2 is exact)
     float sphi, cphi;
-    sincospif(2.0f * u1, &sphi, &cphi);
+    {
+        float sp, cp;
+        __sincosf(__fmul_rn(6.28318530717958648f, u1 - 0.5f), &sp, &cp);
+        sphi = -sp;
+        cphi = -cp;
+    }
     const float c = fmaf(2.0f, u0, -1.0f);   // exact: u0 has 24 bits
     if (mode == 0) {
         const float s = sqrtf(fmaxf(0.0f, fmaf(-c, c, 1.0f)));
@@ -72,7 +79,7 @@ __device__ __forceinline__ void trial_spin(int mode, float tilt, float mag, floa
     } else {
         const float theta = __fmul_rn(tilt, acosf(c));
         float st, ct;
-        sincosf(theta, &st, &ct);
+        __sincosf(theta, &st, &ct);   // theta in [0, pi]
         const float tx = __fmul_rn(st, cphi), ty = __fmul_rn(st, sphi), tz = ct;
         const float sxy = sqrtf(fmaf(oy, oy, __fmul_rn(ox, ox)));
         float c0 = 1.0f, s0 = 0.0f;
@@ -83,6 +90,15 @@ __device__ __forceinline__ void trial_spin(int mode, float tilt, float mag, floa
         ny = __fmul_rn(mag, fmaf(ay, tz, fmaf(c0, ty, __fmul_rn(__fmul_rn(s0, az), tx))));
         nz = __fmul_rn(mag, fmaf(az, tz, __fmul_rn(-sqrtf(fmaf(ay, ay, __fmul_rn(ax, ax))), tx)));
     }
+}
+
+// The Boltzmann test of metropolis (get_quant.F90:166-178): accept a move
+// with energy change de when de <= 0, else when exp(-beta de) >= u (the
+// third uniform).  The hardware exponential is within a few parts in 1e6 of
+// exp, which moves only decisions where exp(-beta de) lies that close to u.
+__device__ __forceinline__ bool metropolis_accept(float beta, float de, uint32_t u_bits)
+{
+    return !(de > 0.0f) || __expf(-beta * de) >= u24f(u_bits);
 }
 
 // DM share of one neighbour in the local field, g += s_k x D_ik

@@ -174,8 +174,7 @@ __global__ void __launch_bounds__(256) k_sweep_ell(const SweepArgs a)
             const float dx = nx - ox, dy = ny - oy, dz = nz - oz;
             // s_new^T Q s_new - s_old^T Q s_old = d^T Q (s_new + s_old)
             const float de = delta_energy(HB || has_si, gx, gy, gz, qxx, qyy, qzz, qxy, qxz, qyz, ox, oy, oz, nx, ny, nz);
-            bool acc = true;
-            if (de > 0.0f) acc = expf(-beta * de) >= u24f(x.z);
+            const bool acc = metropolis_accept(beta, de, x.z);
             if (acc) {
                 a.sx[idx] = nx; a.sy[idx] = ny; a.sz[idx] = nz;
                 accE += de;

@@ -115,8 +115,7 @@ __device__ __forceinline__ bool tile_trial(const TileArgs &a, const ClusterStenc
     trial_spin(a.mode, a.tilt, st->mag[at], ox, oy, oz, xr.x, xr.y, nx, ny, nz);
     de = delta_energy(a.has_b || a.has_si, f.gx, f.gy, f.gz, f.qxx, f.qyy, f.qzz, f.qxy, f.qxz, f.qyz, ox, oy, oz, nx,
                       ny, nz);
-    if (de > 0.0f) return expf(-beta * de) >= u24f(xr.z);
-    return true;
+    return metropolis_accept(beta, de, xr.z);
 }
 
 __global__ void __launch_bounds__(kTileThreads, 2) k_sweep_tile(const TileArgs a)

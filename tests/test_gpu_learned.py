@@ -24,7 +24,7 @@ import oracle as O
 from espins_gb300 import analysis
 from espins_gb300.lib import ESP_ETIMEOUT, LP_NUM_PARAMS, Engine, EspError
 from espins_gb300.tables import build_hamiltonian
-from helpers import NN, NNN, energy_scale, sc_mcin
+from helpers import NN, NNN, energy_scale, exact_energy_axial, sc_mcin
 from test_gpu_statistics import LEVELS, _check, _mean_sigma, _oracle_chains
 
 pytestmark = pytest.mark.gpu
@@ -250,6 +250,53 @@ def test_learned_sampler_is_exact_on_independent_sites(out_scale, engine):
         g, sg = _mean_sigma(gd[t], gb[t], h.n)
         want = _exact_energy_per_site(h, T)
         assert abs(g[0] - want) <= 3 * sg[0] + 1e-5 * abs(want), (T, g[0], want, sg[0])
+
+
+def _offset_network(seed):
+    """Weights whose outputs are a fixed offset from zero (W3 = 0, b3 set):
+    each component's direction tilted by a few hundredths of a radian, its
+    kappa changed by tens of per cent, unequal weights -- a proposal that
+    differs from the target everywhere but still covers its peak."""
+    p = _weights(seed, out_scale=0.0)
+    b3 = np.zeros(20)
+    for k in range(4):
+        b3[5 * k] = 0.03 * (k - 1.5)
+        b3[5 * k + 1] = 0.02 * (1.5 - k)
+        b3[5 * k + 3] = 0.25 * (k - 1.5)
+        b3[5 * k + 4] = 0.4 * k
+    p[18176:20736] = 0.0
+    p[20736:] = b3
+    return p.astype(np.float32)
+
+
+@pytest.mark.parametrize("engine", ["mma", "tcgen05"])
+@pytest.mark.parametrize("net", ["zero", "offset"])
+def test_learned_sampler_is_exact_at_large_kappa(net, engine):
+    """The same exactness at the concentrations of a cold ordered lattice:
+    independent sites in a 100 T field along z (67 K) with an easy-plane term
+    along x, at 0.5-2 K, so the proposals' kappa is 30-130 -- where the
+    sampler's inverse CDF and the log-densities of the Hastings ratio lose
+    the most precision.  Two networks: the zero one (the Heisenberg
+    conditional, which misses the anisotropy) and one with a fixed offset on
+    every output.  (A random network's outputs point anywhere; at these
+    concentrations a proposal that misses the target's peak by more than its
+    width is almost never accepted, so such a chain stays near its start in
+    any affordable run, which would say nothing about exactness.)"""
+    tems = [0.5, 1.0, 2.0]
+    extra = ("ham_field = .true.\nbegin field_axes_cart\nFe 0 0 1 100.0\nend field_axes_cart\n"
+             "ham_singleion = .true.\nbegin singleion_axes_cart\nFe 1 0 0 2e-4\nend singleion_axes_cart\n")
+    inp = sc_mcin(6, [(1e-12, NN)], tems, extra=extra)
+    h = build_hamiltonian(inp)
+    F = float(h.field_val[0] * h.field_axis[0][2])
+    D = float(h.si_delta[0])
+    warm, mc = 500, 20000
+    w = _weights(9, out_scale=0.0) if net == "zero" else _offset_network(9)
+    gd, gb, res = _learned_copies(h, tems, warm, mc, w, engine=engine)
+    for t, T in enumerate(tems):
+        g, sg = _mean_sigma(gd[t], gb[t], h.n)
+        want = exact_energy_axial(F, D, T)
+        print(f"\nT={T}: E/N {g[0]:.6f} +- {sg[0]:.6f}, exact {want:.6f}")
+        assert abs(g[0] - want) <= 3 * sg[0] + 1e-6 * abs(want), (T, g[0], want, sg[0])
 
 
 @pytest.mark.parametrize("engine", ["mma", "tcgen05"])

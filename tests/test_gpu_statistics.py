@@ -23,13 +23,14 @@ import oracle as O
 from espins_gb300 import analysis as A
 from espins_gb300.lib import Engine
 from espins_gb300.tables import build_hamiltonian
-from helpers import NN, NNN, check_z, energy_scale, sc_mcin
+from helpers import NN, NNN, check_z, energy_scale, exact_energy_axial, sc_mcin
 
 pytestmark = pytest.mark.gpu
 
 LEVELS = [1, 2, 3, 4, 5, 6, 7, 8, 9]
 COPIES = 4
 ORACLE_CHAINS = 2
+PT_CHAINS = 4
 
 
 def _sigma(binning):
@@ -38,11 +39,13 @@ def _sigma(binning):
     return np.sqrt(np.max(np.maximum(b, 0.0), axis=0))
 
 
-def _gpu_run(h, tems, pt, warm, mc, pss=10, mode=0, tilt=0.125, seed=12345):
+def _gpu_run(h, tems, pt, warm, mc, pss=10, mode=0, tilt=0.125, seed=12345, pt_group=None):
     R = len(tems)
     with Engine(h.n, h.num_atoms, h.supercell, R) as e:
         e.upload(h)
         e.set_temperatures(tems)
+        if pt_group:
+            e.set_pt_groups(pt_group)
         e.init_spins("ferro")
         e.set_series(mc)
         res = e.run(warm, mc, 1, pt=pt, pt_steps_swap=pss, mode=mode, tilt=tilt, seed=seed,
@@ -138,6 +141,30 @@ def test_plain_metropolis_matches_reference_algorithm(mode):
     assert np.max(np.abs(e[:, 1] - e[:, 2])) <= 1e-5 * energy_scale(h)
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+def test_plain_sampler_is_exact_on_independent_sites(mode):
+    """The plain Metropolis move (uniform or cone trial spin, Boltzmann test:
+    metropolis, get_quant.F90:52-182) on sites without couplings in a 100 T
+    field along z (67 K) with an easy-plane term along x, at 0.5-8 K:
+    <E>/N of COPIES replicas per temperature against a fine quadrature of
+    the exact single-site distribution.  An answer with no run in between,
+    sharp enough (sigma ~1e-3 K) to see a bias of the trial direction or of
+    the acceptance test."""
+    tems = [0.5, 2.0, 8.0]
+    extra = ("ham_field = .true.\nbegin field_axes_cart\nFe 0 0 1 100.0\nend field_axes_cart\n"
+             "ham_singleion = .true.\nbegin singleion_axes_cart\nFe 1 0 0 2e-4\nend singleion_axes_cart\n")
+    inp = sc_mcin(6, [(1e-12, NN)], tems, extra=extra)
+    h = build_hamiltonian(inp)
+    F = float(h.field_val[0] * h.field_axis[0][2])
+    D = float(h.si_delta[0])
+    gd, gb, _, _ = _gpu_copies(h, tems, 2000, 20000, mode=mode, tilt=0.3)
+    for t, T in enumerate(tems):
+        g, sg = _mean_sigma(gd[t], gb[t], h.n)
+        want = exact_energy_axial(F, D, T)
+        print(f"\nmode {mode} T={T}: E/N {g[0]:.6f} +- {sg[0]:.6f}, exact {want:.6f}")
+        assert abs(g[0] - want) <= 3 * sg[0] + 1e-6 * abs(want), (mode, T, g[0], want, sg[0])
+
+
 def test_plain_metropolis_biquadratic_dm_singleion():
     inp = sc_mcin(6, [(1e-3, NN), (3e-4, NNN)], [5.0, 12.0, 25.0], bq=1e-4, dm=2e-4, si=-3e-5)
     h = build_hamiltonian(inp)
@@ -150,28 +177,49 @@ def test_plain_metropolis_biquadratic_dm_singleion():
 
 
 def test_parallel_tempering_matches_reference_algorithm():
+    """PT_CHAINS independent parallel-tempering chains on the GPU (replica
+    groups of one handle) against the oracle's chain.  The error of the GPU's
+    mean is the larger of the chains' combined binning error and their
+    spread; the oracle's chain, as long as each GPU chain and of the same
+    algorithm, is given at least a GPU chain's error (the spread times
+    sqrt(PT_CHAINS)), since its binning blocks (at most 2^9 measurements) can
+    be shorter than the exchange's slowest mode at the lowest temperature."""
     inp = sc_mcin(6, [(1e-3, NN)], list(np.geomspace(8.0, 30.0, 8)))
     h = build_hamiltonian(inp)
-    tems = inp.tems
+    tems = np.asarray(inp.tems)
+    nT = len(tems)
     warm, mc, pss = 4000, 40000, 10
-    res = _gpu_run(h, tems, True, warm, mc, pss=pss)
+    res = _gpu_run(h, np.tile(tems, PT_CHAINS), True, warm, mc, pss=pss, pt_group=nT)
     H = O.Ham(h)
-    s = np.zeros((len(tems), h.n, 3)); s[:, :, 2] = 1.0
+    s = np.zeros((nT, h.n, 3)); s[:, :, 2] = 1.0
     r = H.pt(O.MT(4242), tems, s.reshape(-1), warm, mc, 1, pss, binning_level=LEVELS, want_pm=False)
     steps = r["steps_mc_eff"]
     or_data = r["data"] / steps
     # PT binning variances carry an extra 1/N (pt.F90:935); undo it for sigma
-    gb = res["binning"] * h.n
+    gb = (res["binning"] * h.n).reshape(PT_CHAINS, nT, len(LEVELS), 2)
     ob = r["binning"] * h.n
-    _check(h, tems, [[d] for d in res["data"]], [[b] for b in gb], [[d] for d in or_data], [[b] for b in ob], "pt")
-    _check_derived(h, tems, [[res["series"][:, t, :]] for t in range(len(tems))], [[d] for d in or_data], "pt")
-    # swap acceptance per temperature: binomial tolerance
-    ga = res["num_swaps"][:, 1] / np.maximum(res["num_swaps"][:, 0], 1)
+    gd = res["data"].reshape(PT_CHAINS, nT, 6)
+    for t, T in enumerate(tems):
+        x = np.array([[gd[c, t, 0] / h.n, gd[c, t, 3]] for c in range(PT_CHAINS)])
+        sb = np.array([_sigma(gb[c, t]) for c in range(PT_CHAINS)])
+        spread = x.std(axis=0, ddof=1)
+        sg = np.maximum(np.sqrt((sb ** 2).sum(axis=0)) / PT_CHAINS, spread / np.sqrt(PT_CHAINS))
+        o = np.array([or_data[t, 0] / h.n, or_data[t, 3]])
+        so = np.maximum(_sigma(ob[t]), np.maximum(np.sqrt((sb ** 2).mean(axis=0)), spread))
+        z = (x.mean(axis=0) - o) / np.sqrt(sg ** 2 + so ** 2)
+        assert np.all(np.abs(z) <= 3.0), ("pt", T, x.mean(axis=0), o, sg, so)
+    ser = res["series"].reshape(-1, PT_CHAINS, nT, 2)
+    _check_derived(h, tems, [[ser[:, c, t, :] for c in range(PT_CHAINS)] for t in range(nT)],
+                   [[d] for d in or_data], "pt")
+    # swap acceptance per temperature (first chain): binomial tolerance
+    ns = res["num_swaps"][:nT]
+    ga = ns[:, 1] / np.maximum(ns[:, 0], 1)
     oa = r["num_swaps"][:, 1] / np.maximum(r["num_swaps"][:, 0], 1)
-    ntries = np.maximum(res["num_swaps"][:, 0], 1)
+    ntries = np.maximum(ns[:, 0], 1)
     sig = np.sqrt(np.maximum(oa * (1 - oa), 1e-4) / ntries) * 2.0
     assert np.all(np.abs(ga - oa) <= 4 * sig + 0.02), (ga, oa)
-    # map is a permutation, tries are counted as the reference counts them
-    assert sorted(res["map"].tolist()) == list(range(1, len(tems) + 1))
+    # map is a permutation within each chain, tries are counted as the reference counts them
+    for c in range(PT_CHAINS):
+        assert sorted(res["map"][c * nT:(c + 1) * nT].tolist()) == list(range(c * nT + 1, (c + 1) * nT + 1))
     nsw = steps // pss
-    assert res["num_swaps"][0, 0] == (nsw + 1) // 2
+    assert ns[0, 0] == (nsw + 1) // 2
