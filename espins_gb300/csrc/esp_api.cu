@@ -70,6 +70,13 @@ struct esp_handle {
     int kernel_choice = 0;          // 0 auto, 1 ELL, 2 cluster
     bool cluster_ok = false;
     int csize = 0, pz = 0, cthreads = 512, csites = 1;
+    // Which copy of the spins is current: the spin arrays (element (p, r) at
+    // p*R + r) and/or the cluster path's slab copy.  The cluster kernel leaves
+    // the state in the slabs; the arrays are brought up to date (one
+    // transpose) only when something else reads them, and the slabs only when
+    // the cluster kernel runs after something wrote the arrays.  At least one
+    // of the two always holds the state.
+    bool arrays_ok = true, slab_ok = false;
     size_t cluster_smem = 0;
     int cl_maxst = 0;
     size_t cl_sbytes = 0;
@@ -348,8 +355,14 @@ bool use_tile(const esp_handle *h)
 }
 
 // n sweeps of eight tile-parity launches each
+int arrays_current(esp_handle *h);
+void arrays_written(esp_handle *h);
+
 int tile_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o)
 {
+    int rc0 = arrays_current(h);
+    if (rc0) return rc0;
+    arrays_written(h);
     const int phase = o->phase ? 1 : 0;
     if (phase != h->pending_phase) {
         int rc = fold(h);
@@ -391,6 +404,52 @@ int tile_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o
 // One launch of the cluster-resident kernel: n_meas units of steps_measure
 // sweeps starting at global sweep `first`, each unit followed by a
 // measurement when `measure` is set.
+SlabArgs slab_args(const esp_handle *h)
+{
+    SlabArgs sa;
+    sa.sx = h->d_sx; sa.sy = h->d_sy; sa.sz = h->d_sz; sa.slab = h->d_slab; sa.inv = h->d_inv;
+    sa.Lx = h->L[0]; sa.Ly = h->L[1]; sa.na = h->na; sa.R = h->R; sa.pz = h->pz; sa.cs = h->csize;
+    sa.n_local = h->N / h->csize;
+    sa.fd_pc = make_fastdiv((uint32_t)((h->L[0] / 2) * (h->L[1] / 2) * (h->pz / 2)));
+    sa.fd_hx = make_fastdiv((uint32_t)(h->L[0] / 2));
+    sa.fd_hy = make_fastdiv((uint32_t)(h->L[1] / 2));
+    return sa;
+}
+
+// Slabs of at least 4096 sites are staged contiguously (two transposes);
+// smaller ones are gathered and scattered by the cluster kernel itself.
+bool cluster_staged(const esp_handle *h)
+{
+    return h->cluster_ok && h->csize > 0 && h->N / h->csize >= 4096;
+}
+
+// Bring the spin arrays up to date before a kernel reads them.
+int arrays_current(esp_handle *h)
+{
+    if (h->arrays_ok) return ESP_OK;
+    CK(launch_from_slabs(slab_args(h), h->st));
+    h->launches++;
+    h->arrays_ok = true;
+    return ESP_OK;
+}
+
+// A kernel wrote the spin arrays: the slab copy is stale.
+void arrays_written(esp_handle *h)
+{
+    h->arrays_ok = true;
+    h->slab_ok = false;
+}
+
+// Bring the slab copy up to date before the cluster kernel works on it.
+int slab_current(esp_handle *h)
+{
+    if (h->slab_ok) return ESP_OK;
+    CK(launch_to_slabs(slab_args(h), h->st));
+    h->launches++;
+    h->slab_ok = true;
+    return ESP_OK;
+}
+
 int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first, int measure, long long meas_base,
                 const esp_sweep_opts *o, int phase, int nlev, bool pt_quirk)
 {
@@ -403,9 +462,7 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     a.Lx = h->L[0]; a.Ly = h->L[1]; a.Lz = h->L[2]; a.na = h->na; a.N = h->N; a.R = h->R;
     a.nclass = 8 * h->na; a.pz = h->pz;
     a.has_b = h->prep.has_b; a.has_d = h->prep.has_d; a.has_si = h->hsi; a.has_f = h->hfld;
-    // slabs of at least 4096 sites are staged contiguously (two transposes);
-    // smaller ones are gathered by the kernel itself
-    const bool staged = h->N / h->csize >= 4096;
+    const bool staged = cluster_staged(h);
     a.slab = staged ? h->d_slab : nullptr;
     a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz; a.inv = h->d_inv;
     a.temp_of = h->d_temp_of; a.beta = h->d_beta; a.e_run = h->d_e_run; a.m_run = h->d_m_run; a.rej = h->d_rej;
@@ -431,17 +488,18 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     a.obs = measure ? h->obs : 0;
     a.obs_atom = h->d_obs_atom; a.obs_data = h->d_obs_data; a.obs_lsum = h->d_obs_lsum; a.obs_bin = h->d_obs_bin;
     a.obs_pm = h->d_obs_pm;
-    // the spin arrays stay the state between launches; the kernel works on
-    // the slab copy, made and returned by two coalesced transposes
-    SlabArgs sa;
-    sa.sx = h->d_sx; sa.sy = h->d_sy; sa.sz = h->d_sz; sa.slab = h->d_slab; sa.inv = h->d_inv;
-    sa.Lx = h->L[0]; sa.Ly = h->L[1]; sa.na = h->na; sa.R = h->R; sa.pz = h->pz; sa.cs = h->csize;
-    sa.n_local = h->N / h->csize;
-    sa.fd_pc = a.fd_pc; sa.fd_hx = a.fd_hx; sa.fd_hy = a.fd_hy;
-    if (staged) CK(launch_to_slabs(sa, h->st));
+    // a staged slab stays the state after the launch (the arrays are brought
+    // back by a transpose when something reads them); an unstaged launch
+    // reads and writes the arrays themselves
+    if (staged) {
+        if ((rc = slab_current(h))) return rc;
+    } else if ((rc = arrays_current(h))) {
+        return rc;
+    }
     CK(launch_cluster(a, h->csize, h->cthreads, h->csites, h->cluster_smem, h->st));
-    if (staged) CK(launch_from_slabs(sa, h->st));
-    h->launches += staged ? 3 : 1;
+    h->launches++;
+    if (staged) h->arrays_ok = false;
+    else arrays_written(h);
     return ESP_OK;
 }
 
@@ -460,6 +518,9 @@ int cluster_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts
 
 int do_sweep_colour(esp_handle *h, int c, int64_t sweep, const esp_sweep_opts *o)
 {
+    int rc0 = arrays_current(h);
+    if (rc0) return rc0;
+    arrays_written(h);
     const int phase = o->phase ? 1 : 0;
     if (phase != h->pending_phase) {
         int rc = fold(h);
@@ -514,6 +575,8 @@ int do_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o)
 // energy by replica into d_tmp_e / d_tmp_m
 int do_energy(esp_handle *h)
 {
+    int rc = arrays_current(h);
+    if (rc) return rc;
     CK(launch_energy(energy_args(h), h->d_tmp_e, h->d_tmp_m, h->e_blocks, h->st));
     h->launches += 2;
     return ESP_OK;
@@ -565,6 +628,8 @@ int by_slot(esp_handle *h, const double *d_by_rep, int width, double *out)
 // One spincorr_get measurement of every replica, accumulated per slot.
 int spincorr_measure(esp_handle *h)
 {
+    int rc0 = arrays_current(h);
+    if (rc0) return rc0;
     ScArgs a;
     a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz;
     a.off = h->d_sc_off; a.nb = h->d_sc_nb; a.w = h->d_sc_w;
@@ -580,6 +645,8 @@ int spincorr_measure(esp_handle *h)
 // the step against the device measurement counter instead.
 int sfactor_measure(esp_handle *h, long long step)
 {
+    int rc0 = arrays_current(h);
+    if (rc0) return rc0;
     SfArgs a;
     a.sx = h->d_sx; a.sy = h->d_sy; a.sz = h->d_sz; a.inv = h->d_inv;
     a.site_n = h->d_sf_n; a.site_f = h->d_sf_f; a.q_fix = h->d_sf_qfix; a.q_frac = h->d_sf_qf; a.q_cart = h->d_sf_qc;
@@ -610,6 +677,8 @@ int extra_measure(esp_handle *h, long long step)
 
 int measure(esp_handle *h, long long step, int nlev, bool pt_quirk, long long &const_hits)
 {
+    int rc0 = arrays_current(h);
+    if (rc0) return rc0;
     int rc = fold(h);
     if (rc) return rc;
     MeasureArgs m;
@@ -852,6 +921,11 @@ int tile_setup(esp_handle *h)
 // memory, the neighbour table of every CTA rank.
 int cluster_geometry(esp_handle *h, int cs, int nt, int S)
 {
+    // a slab copy of the old geometry goes back to the arrays first
+    if (h->cluster_ok) {
+        int rc0 = arrays_current(h);
+        if (rc0) return rc0;
+    }
     const int maxst = h->cl_maxst;
     const int pz = h->L[2] / cs, n_local = h->N / cs;
     const size_t smem = cluster_smem_bytes(n_local, h->nf, h->obs ? 3 : 1, h->cl_sbytes);
@@ -895,6 +969,7 @@ int cluster_geometry(esp_handle *h, int cs, int nt, int S)
     h->pz = pz;
     h->cluster_smem = smem;
     h->cluster_ok = true;
+    h->slab_ok = false;   // slabs of this geometry are made from the arrays when needed
     return ESP_OK;
 }
 
@@ -1053,6 +1128,11 @@ int esp_set_stream(esp_handle *h, void *stream)
 int esp_upload_tables(esp_handle *h, const esp_tables *t)
 {
     if (!h || !t) return ESP_EINVAL;
+    if (h->cluster_ok) {   // the state back in the arrays before the tables change
+        int rc0 = arrays_current(h);
+        if (rc0) return rc0;
+    }
+    h->slab_ok = false;
     PrepInput in;
     in.N = h->N; in.num_atoms = h->na; in.L[0] = h->L[0]; in.L[1] = h->L[1]; in.L[2] = h->L[2];
     in.open_boundary = h->open;
@@ -1239,6 +1319,7 @@ int esp_set_spins(esp_handle *h, const double *spins)
     if (rc) return rc;
     if (!spins) { h->err = "null spins"; return ESP_EINVAL; }
     if ((rc = ensure_stage(h))) return rc;
+    arrays_written(h);   // every slot is overwritten below
     // blocks of slots: copy the FP64 block through the pinned staging (a
     // parallel host copy, then one DMA), then scatter it into the permuted
     // FP32 state on the device.  The driver's pageable path is as fast only
@@ -1262,6 +1343,7 @@ int esp_init_spins(esp_handle *h, int32_t kind, uint64_t seed)
     int rc = require(h, true, false);
     if (rc) return rc;
     if (kind != 0 && kind != 1) { h->err = "kind must be 0 (ferro) or 1 (rand)"; return ESP_EINVAL; }
+    arrays_written(h);
     CK(launch_init_spins(h->d_perm, h->d_mag, h->d_sx, h->d_sy, h->d_sz, h->N, h->R, kind, seed, h->st));
     h->launches++;
     if ((rc = reset_running(h))) return rc;
@@ -1275,6 +1357,7 @@ int esp_get_spins(esp_handle *h, double *spins)
     if (rc) return rc;
     if (!spins) { h->err = "null spins"; return ESP_EINVAL; }
     if ((rc = ensure_stage(h))) return rc;
+    if ((rc = arrays_current(h))) return rc;
     for (int t0 = 0; t0 < h->R; t0 += h->stage_slots) {
         const int nt = std::min(h->stage_slots, h->R - t0);
         const size_t bytes = sizeof(double) * 3 * (size_t)h->N * nt;
@@ -1387,6 +1470,7 @@ int esp_local_terms(esp_handle *h, double *g_out, double *q_out)
 {
     int rc = require(h, true, false);
     if (rc) return rc;
+    if ((rc = arrays_current(h))) return rc;
     const size_t NR = (size_t)h->N * h->R;
     float *dg = nullptr, *dq = nullptr;
     CK(dalloc(&dg, NR * 3));
@@ -2354,6 +2438,7 @@ int esp_lp_collect(esp_handle *h, int32_t colour, int64_t *rows)
     if (rc) return rc;
     if (colour < 0 || colour >= h->prep.num_colours) { h->err = "bad colour"; return ESP_EINVAL; }
     if (h->lp_cap == 0) { h->err = "no training-set storage (esp_lp_reserve)"; return ESP_ESTATE; }
+    if ((rc = arrays_current(h))) return rc;
     esp_sweep_opts o{};
     LpCollectArgs c;
     c.s = sweep_args(h, colour, 0, &o);
@@ -2541,6 +2626,9 @@ struct esp_batch {
     struct Delta {
         int64_t c[4];
         long long const_hits, launches;
+        // which spin copies are current before a replay (the graph relies on
+        // them) and after it
+        bool arrays_before, slab_before, arrays_after, slab_after;
     };
     std::vector<Delta> deltas;
 };
@@ -2587,10 +2675,24 @@ int batch_capture(esp_batch *b, int K)
             if (dalloc(&h->d_ctr, 4) != cudaSuccess) { b->err = "device allocation failed"; return ESP_ENOMEM; }
             h->ctr_valid = false;
         }
+        // the graph is recorded from a fixed state of the spin copies, made
+        // here outside the graph and restored before every replay: a handle
+        // on the staged cluster path starts from its slab (the recorded
+        // launches work on it), any other handle from its arrays
+        if (use_cluster(h) && cluster_staged(h)) {
+            rc = slab_current(h);
+            h->arrays_ok = false;   // not relied upon by the graph
+        } else {
+            rc = arrays_current(h);
+            h->slab_ok = false;
+        }
+        if (rc) return batch_fail(b, "spin copies", h);
         mirrors(h, base[i].data());
         hits0[i] = h->run.const_hits;
         launches0[i] = h->launches;
     }
+    std::vector<std::array<bool, 2>> copies0(n);
+    for (size_t i = 0; i < n; ++i) copies0[i] = {b->hs[i]->arrays_ok, b->hs[i]->slab_ok};
     cudaError_t e = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) { b->err = std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e); return ESP_ECUDA; }
     for (size_t i = 0; i < n; ++i) {
@@ -2615,6 +2717,9 @@ int batch_capture(esp_batch *b, int K)
         if (rc == ESP_OK && launch_bump(h->d_ctr, d, b->st) != cudaSuccess) { rc = ESP_ECUDA; bad = h; }
         b->deltas[i].const_hits = h->run.const_hits - hits0[i];
         b->deltas[i].launches = h->launches - launches0[i] + 1;
+        b->deltas[i].arrays_before = copies0[i][0]; b->deltas[i].slab_before = copies0[i][1];
+        b->deltas[i].arrays_after = h->arrays_ok; b->deltas[i].slab_after = h->slab_ok;
+        h->arrays_ok = copies0[i][0]; h->slab_ok = copies0[i][1];
         set_mirrors(h, base[i].data());
         h->run.const_hits = hits0[i];
         h->launches = launches0[i];
@@ -2637,6 +2742,16 @@ int batch_capture(esp_batch *b, int K)
 
 int batch_replay(esp_batch *b)
 {
+    // the copies of the spins the graph was recorded with (a host call
+    // between replays may have brought the arrays back or written them)
+    for (size_t i = 0; i < b->hs.size(); ++i) {
+        esp_handle *h = b->hs[i];
+        const esp_batch::Delta &d = b->deltas[i];
+        int rc = ESP_OK;
+        if (d.slab_before && !h->slab_ok) rc = slab_current(h);
+        if (rc == ESP_OK && d.arrays_before && !h->arrays_ok) rc = arrays_current(h);
+        if (rc) return batch_fail(b, "spin copies", h);
+    }
     for (esp_handle *h : b->hs) {
         int64_t now[4];
         mirrors(h, now);
@@ -2662,6 +2777,8 @@ int batch_replay(esp_batch *b)
         set_mirrors(h, now);
         h->run.const_hits += b->deltas[i].const_hits;
         h->launches += b->deltas[i].launches;
+        h->arrays_ok = b->deltas[i].arrays_after;
+        h->slab_ok = b->deltas[i].slab_after;
     }
     return ESP_OK;
 }

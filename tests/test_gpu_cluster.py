@@ -148,3 +148,39 @@ def test_a_smaller_lattice_set_up_later_does_not_break_a_larger_ones_launches():
         eb.sweep(2, 1, seed=3)
         assert eb.sweep_kernel()[0] == "cluster"
         assert np.all(np.isfinite(eb.running_energy()))
+
+
+def test_spin_copies_stay_consistent_across_kernels_and_reads():
+    """The cluster path leaves the state in its slab copy and brings the spin
+    arrays back only when something reads them; the arrays' writers make the
+    slab stale.  Reading the spins in the middle of a run changes nothing
+    (same final spins and counters as a run without the read), and switching
+    between the cluster, ELL and cluster kernels again keeps the running
+    energy equal to the direct one."""
+    inp = _cases()["sc16_j1j2_dm"]   # 4096 sites: one CTA per replica, staged slab
+    h = build_hamiltonian(inp)
+    rng = np.random.default_rng(8)
+    v = rng.normal(size=(len(inp.tems), h.n, 3))
+    s0 = v / np.linalg.norm(v, axis=2, keepdims=True)
+    out = []
+    for read in (False, True):
+        with _engine(h, inp.tems, "cluster") as e:
+            e.set_cluster_geometry(1, 512, 1)
+            e.set_spins(s0)
+            e.sweep(6, 0, seed=3)
+            if read:
+                mid = e.get_spins()
+                assert np.all(np.isfinite(mid)) and not np.array_equal(mid, s0)
+            e.sweep(6, 6, seed=3)
+            out.append((e.get_spins(), e.rejected(), e.running_energy()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    with _engine(h, inp.tems, "cluster") as e:
+        e.set_cluster_geometry(1, 512, 1)
+        e.set_spins(s0)
+        tol = 1e-5 * energy_scale(h)
+        for k, kind in enumerate(("cluster", "ell", "cluster", "ell")):
+            e.set_sweep_kernel(kind)
+            e.sweep(4, 4 * k, seed=9)
+            run, direct = e.running_energy(), e.energy()
+            assert np.max(np.abs(run - direct)) <= tol, (kind, run - direct)
