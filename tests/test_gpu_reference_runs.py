@@ -29,11 +29,15 @@ start far more slowly than that schedule: after its 10^5 plain warm-up sweeps
 copies still sit in different metastable states (U_M of single copies
 0.37-0.42 at 4 K, their mean 0.389 against the reference's 0.373), while a
 plain warm-up of 2e6 sweeps (the reference ran 5e6) gives 0.3730 +- 0.0019
-and the reference's |m|, chi and E/N too.  So this example warms up by
-parallel tempering, each copy a ladder of the 64 temperatures exchanging
-every 10 measurements (an equilibrium sampler of the same ensemble: replicas
-relaxed at higher temperatures exchange down), and then runs the
-reference's plain Metropolis measurement phase at fixed temperatures.  Per temperature the test compares
+and the reference's |m|, chi and E/N too (a parallel-tempering warm-up of
+the short schedule does not: the slow relaxation is at the lowest
+temperature itself).  So this example warms up with heat-bath moves -- the
+library's learned proposal with a zero network, which for a pure exchange
+Hamiltonian is the exact conditional vMF(-g/|g|, beta |g|) of every site,
+accepted every time -- and then runs the reference's plain Metropolis
+measurement phase from that state.  Any exact sampler of the ensemble may
+warm up; the heat bath relaxes the low temperatures where a Metropolis
+trial is accepted a few per cent of the time.  Per temperature the test compares
 <|m|>, <E>/N, C, chi, U_E and U_M (mcarlo.F90:725-733, pt.F90:995-1024)
 with the reference's row:
 
@@ -77,15 +81,15 @@ import numpy as np
 import pytest
 
 from espins_gb300 import analysis as A
-from espins_gb300.lib import Engine
+from espins_gb300.lib import LP_NUM_PARAMS, Engine
 from espins_gb300.tables import build_hamiltonian
 from helpers import check_z, example
 
 pytestmark = pytest.mark.gpu
 
 SCALE = {"ex01_cubic": 1.0, "ex02_cubic_pt": 1.0, "ex04_bmno_mc": 0.02}
-# examples whose warm-up is parallel tempering (exchange every 10 measurements)
-PT_WARMUP = {"ex04_bmno_mc"}
+# examples whose warm-up is heat bath (the learned proposal with a zero network)
+HEATBATH_WARMUP = {"ex04_bmno_mc"}
 
 
 def copies(name, T):
@@ -126,14 +130,13 @@ def _run(name):
         e.set_temperatures(np.tile(T0, C0))
         e.init_spins("ferro")
         e.set_series(mc)
-        if name in PT_WARMUP:
-            # warm-up: every measurement of it with exchanges inside each
-            # copy's ladder; then a new esp_begin keeps the spins and starts
-            # the plain measurement phase
-            e.set_pt_groups(nT)
-            e.begin(e.schedule(0, warm, inp.steps_measure, pt=True, pt_steps_swap=10, mode=mode,
-                               tilt=inp.tilt_angles_max, seed=SEED + 1))
-            e.advance(warm // 10)
+        if name in HEATBATH_WARMUP:
+            # warm-up with heat-bath moves, then a new esp_begin keeps the
+            # spins and starts the plain measurement phase
+            e.lp_set_weights(np.zeros(LP_NUM_PARAMS, dtype=np.float32))
+            e.set_proposal("learned")
+            e.begin(e.schedule(warm, 1, inp.steps_measure, mode=mode, tilt=inp.tilt_angles_max, seed=SEED + 1))
+            e.set_proposal("plain")
             e.begin(e.schedule(0, mc, inp.steps_measure, pt=False, mode=mode, tilt=inp.tilt_angles_max, seed=SEED))
         else:
             e.begin(e.schedule(warm, mc, inp.steps_measure, pt=inp.pt, pt_steps_swap=inp.pt_steps_swap, mode=mode,
