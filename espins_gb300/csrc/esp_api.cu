@@ -83,11 +83,12 @@ struct esp_handle {
     // tiled path (translation-invariant lattices with nearest-cell stencils)
     bool tile_ok = false;
     int tile_T = 0, tile_G = 0, tile_nt[3] = {0, 0, 0}, ntiles = 0;
-    bool tile_pipe = false;         // persistent cp.async-pipelined variant
+    int tile_variant = 0;           // 0 one CTA per tile; pipelined persistent: 1 one CTA per SM, 2 two
     size_t tile_smem = 0;
     int4 *d_tile_offs = nullptr;
     ClusterNbr *d_tile_cpl = nullptr;
     int tile_maxst = 0, tile_nbd8[kMaxClusterAtoms] = {}, tile_nall8[kMaxClusterAtoms] = {};
+    int tile_nbd2[kMaxClusterAtoms] = {}, tile_nall4[kMaxClusterAtoms] = {};
     double *d_tile_part = nullptr;
     unsigned long long *d_tile_rej = nullptr;
     long long tile_pending = 0;
@@ -328,7 +329,7 @@ int fold(esp_handle *h)
         t.part = h->d_tile_part; t.part_rej = h->d_tile_rej; t.e_run = h->d_e_run; t.m_run = h->d_m_run;
         t.rej = h->d_rej; t.temp_of = h->d_temp_of; t.R = h->R; t.ntiles = h->ntiles; t.phase = h->pending_phase;
         CK(launch_tile_fold(t, h->st));
-        h->launches++;
+        h->launches += 2;
         h->tile_pending = 0;
     }
     if (h->pending_sweeps == 0) return ESP_OK;
@@ -377,6 +378,8 @@ int tile_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o
     for (int at = 0; at < kMaxClusterAtoms; ++at) {
         a.nbd8[at] = h->tile_nbd8[at];
         a.nall8[at] = h->tile_nall8[at];
+        a.nbd2[at] = h->tile_nbd2[at];
+        a.nall4[at] = h->tile_nall4[at];
     }
     a.Lx = h->L[0]; a.Ly = h->L[1]; a.Lz = h->L[2]; a.na = h->na; a.N = h->N; a.R = h->R;
     a.T = h->tile_T; a.G = h->tile_G;
@@ -392,7 +395,7 @@ int tile_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o
         a.sweep = (unsigned long long)(first + w - (h->capturing ? h->cap_base[0] : 0));
         for (int ph = 0; ph < 8; ++ph) {
             a.phase = ph;
-            if (h->tile_pipe) CK(launch_tile_p(a, h->tile_smem, h->num_sms, h->st));
+            if (h->tile_variant) CK(launch_tile_p(a, h->tile_smem, h->num_sms, 3 - h->tile_variant, h->st));
             else CK(launch_tile(a, h->tile_smem, h->st));
             h->launches++;
         }
@@ -811,7 +814,7 @@ std::vector<ClusterGeom> cluster_candidates(const esp_handle *h)
 // has fewer than two CTAs per SM.  Shared memory stays within two CTAs per SM.
 struct TileGeom {
     int T, G;
-    bool pipe;
+    int variant;   // 0 one CTA per tile; pipelined persistent CTAs: 1 one per SM, 2 two per SM
     double cost;
 };
 
@@ -828,16 +831,24 @@ std::vector<TileGeom> tile_candidates(const esp_handle *h)
             const double b = (double)(T + 2) / T;
             const double bytes = 12.0 * (b * b * b + 1.0) / std::min(1.0, G / 8.0);
             const double items = (double)(ntiles / 8) * (h->R / G);
-            // pipelined persistent variant: the copies overlap the updates
-            if (tile_p_supported(T, G, h->na) && tile_p_smem_bytes(T, G, h->na, h->tile_maxst) <= 226 * 1024) {
-                double cost = 0.5 * bytes;
-                if (items < 4.0 * h->num_sms) cost *= 4.0 * h->num_sms / items;
-                out.push_back({T, G, true, cost});
+            // pipelined persistent variants: the copies overlap the updates,
+            // within a CTA (one per SM) or across the two CTAs of an SM
+            if (tile_p_supported(T, G, h->na)) {
+                if (tile_p_smem_bytes(T, G, h->na, h->tile_maxst, 1) <= 110 * 1024) {
+                    double cost = 0.45 * bytes;
+                    if (items < 8.0 * h->num_sms) cost *= 8.0 * h->num_sms / items;
+                    out.push_back({T, G, 2, cost});
+                }
+                if (tile_p_smem_bytes(T, G, h->na, h->tile_maxst, 2) <= 226 * 1024) {
+                    double cost = 0.5 * bytes;
+                    if (items < 4.0 * h->num_sms) cost *= 4.0 * h->num_sms / items;
+                    out.push_back({T, G, 1, cost});
+                }
             }
             if (tile_smem_bytes(T, G, h->na, h->tile_maxst) <= 113 * 1024) {
                 double cost = bytes;
                 if (items < 2.0 * h->num_sms) cost *= 2.0 * h->num_sms / items;
-                out.push_back({T, G, false, cost});
+                out.push_back({T, G, 0, cost});
             }
         }
     }
@@ -845,10 +856,11 @@ std::vector<TileGeom> tile_candidates(const esp_handle *h)
     return out;
 }
 
-int tile_geometry(esp_handle *h, int T, int G, bool pipe)
+int tile_geometry(esp_handle *h, int T, int G, int variant)
 {
-    const size_t smem = pipe ? tile_p_smem_bytes(T, G, h->na, h->tile_maxst) : tile_smem_bytes(T, G, h->na, h->tile_maxst);
-    if (pipe) CK(tile_p_configure(T, G, smem));
+    const size_t smem = variant ? tile_p_smem_bytes(T, G, h->na, h->tile_maxst, 3 - variant)
+                                : tile_smem_bytes(T, G, h->na, h->tile_maxst);
+    if (variant) CK(tile_p_configure(T, G, 3 - variant, smem));
     else CK(tile_configure(smem));
     CK(cudaStreamSynchronize(h->st));
     int rc = fold(h);
@@ -856,13 +868,15 @@ int tile_geometry(esp_handle *h, int T, int G, bool pipe)
     const int nt[3] = {h->L[0] / T, h->L[1] / T, h->L[2] / T};
     const int ntiles = nt[0] * nt[1] * nt[2];
     if (ntiles != h->ntiles) {
+        // the tiles' slots, then the fold's chunk slots
+        const size_t slots = (size_t)(ntiles + tile_fold_chunks(ntiles)) * h->R;
         dfree(h->d_tile_part); dfree(h->d_tile_rej);
-        CK(dalloc(&h->d_tile_part, (size_t)ntiles * h->R * 4));
-        CK(dalloc(&h->d_tile_rej, (size_t)ntiles * h->R));
-        CK(cudaMemsetAsync(h->d_tile_part, 0, sizeof(double) * 4 * (size_t)ntiles * h->R, h->st));
-        CK(cudaMemsetAsync(h->d_tile_rej, 0, sizeof(unsigned long long) * (size_t)ntiles * h->R, h->st));
+        CK(dalloc(&h->d_tile_part, slots * 4));
+        CK(dalloc(&h->d_tile_rej, slots));
+        CK(cudaMemsetAsync(h->d_tile_part, 0, sizeof(double) * 4 * slots, h->st));
+        CK(cudaMemsetAsync(h->d_tile_rej, 0, sizeof(unsigned long long) * slots, h->st));
     }
-    h->tile_T = T; h->tile_G = G; h->tile_pipe = pipe;
+    h->tile_T = T; h->tile_G = G; h->tile_variant = variant;
     for (int d = 0; d < 3; ++d) h->tile_nt[d] = nt[d];
     h->ntiles = ntiles;
     h->tile_smem = smem;
@@ -887,9 +901,12 @@ int tile_setup(esp_handle *h)
         }
         h->tile_nbd8[at] = ((int)bd[at].size() + 7) & ~7;
         h->tile_nall8[at] = h->tile_nbd8[at] + (((int)jo[at].size() + 7) & ~7);
+        h->tile_nbd2[at] = ((int)bd[at].size() + 1) & ~1;
+        h->tile_nall4[at] = h->tile_nbd8[at] + (((int)jo[at].size() + 3) & ~3);
         maxst = std::max(maxst, h->tile_nall8[at]);
     }
-    for (int at = h->na; at < kMaxClusterAtoms; ++at) h->tile_nbd8[at] = h->tile_nall8[at] = 0;
+    for (int at = h->na; at < kMaxClusterAtoms; ++at)
+        h->tile_nbd8[at] = h->tile_nall8[at] = h->tile_nbd2[at] = h->tile_nall4[at] = 0;
     std::vector<int4> offs((size_t)h->na * maxst);
     std::vector<ClusterNbr> cpl((size_t)h->na * maxst);
     for (int at = 0; at < h->na; ++at) {
@@ -914,7 +931,7 @@ int tile_setup(esp_handle *h)
     if ((rc = h2d(h, h->d_tile_cpl, cpl.data(), sizeof(ClusterNbr) * cpl.size()))) return rc;
     const std::vector<TileGeom> c = tile_candidates(h);
     if (c.empty()) return ESP_OK;
-    return tile_geometry(h, c[0].T, c[0].G, c[0].pipe);
+    return tile_geometry(h, c[0].T, c[0].G, c[0].variant);
 }
 
 // Set up the cluster path for cs CTAs of nt threads: slab height, shared
@@ -1580,8 +1597,8 @@ int esp_set_tile_geometry(esp_handle *h, int32_t tile, int32_t replicas, int32_t
 {
     if (!h) return ESP_EINVAL;
     for (const TileGeom &g : tile_candidates(h))
-        if (g.T == tile && g.G == replicas && g.pipe == (pipelined != 0))
-            return tile_geometry(h, tile, replicas, g.pipe);
+        if (g.T == tile && g.G == replicas && g.variant == pipelined)
+            return tile_geometry(h, tile, replicas, g.variant);
     h->err = "tile geometry not possible for this lattice";
     return ESP_EINVAL;
 }
@@ -1591,7 +1608,7 @@ int esp_get_tile_geometry(const esp_handle *h, int32_t *tile, int32_t *replicas,
     if (!h || !tile || !replicas) return ESP_EINVAL;
     *tile = h->tile_ok ? h->tile_T : 0;
     *replicas = h->tile_ok ? h->tile_G : 0;
-    if (pipelined) *pipelined = h->tile_ok && h->tile_pipe ? 1 : 0;
+    if (pipelined) *pipelined = h->tile_ok ? h->tile_variant : 0;
     return ESP_OK;
 }
 
@@ -2909,17 +2926,17 @@ int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out)
             for (size_t k = 0; k < g.size() && k < 3; ++k) cands.push_back({2, g[k].cs, g[k].nt, g[k].S});
         }
         if (h->tile_ok) {
-            // kinds 4 / 5: cs, nt carry the tile edge and the replicas per CTA
-            // (5: the pipelined variant)
+            // kinds 4 + variant: cs, nt carry the tile edge and the replicas per
+            // CTA (5, 6: the pipelined variants)
             const std::vector<TileGeom> g = tile_candidates(h);
-            for (size_t k = 0; k < g.size() && k < 3; ++k) cands.push_back({g[k].pipe ? 5 : 4, g[k].T, g[k].G});
+            for (size_t k = 0; k < g.size() && k < 3; ++k) cands.push_back({4 + g[k].variant, g[k].T, g[k].G});
         }
         double best = 1e300, best_cl = 1e300;
         Cand pick{1, 0, 0, 0};
         for (const Cand &c : cands) {
             int rc = ESP_OK;
             if (c.kind == 2 && (rc = cluster_geometry(h, c.cs, c.nt, c.S))) return batch_fail(b, "cluster geometry", h);
-            if (c.kind >= 4 && (rc = tile_geometry(h, c.cs, c.nt, c.kind == 5))) return batch_fail(b, "tile geometry", h);
+            if (c.kind >= 4 && (rc = tile_geometry(h, c.cs, c.nt, c.kind - 4))) return batch_fail(b, "tile geometry", h);
             if ((rc = esp_set_sweep_kernel(h, std::min(c.kind, 4)))) return batch_fail(b, "esp_set_sweep_kernel", h);
             esp_batch one;
             one.hs.assign(1, h);
@@ -2935,7 +2952,7 @@ int esp_batch_tune(esp_batch *b, int32_t units, esp_batch_tuning *out)
         if (out && out->cluster_us) out->cluster_us[i] = cands.size() > 1 ? best_cl : -1.0;
         int rc = ESP_OK;
         if (pick.kind == 2 && (rc = cluster_geometry(h, pick.cs, pick.nt, pick.S))) return batch_fail(b, "cluster geometry", h);
-        if (pick.kind >= 4 && (rc = tile_geometry(h, pick.cs, pick.nt, pick.kind == 5)))
+        if (pick.kind >= 4 && (rc = tile_geometry(h, pick.cs, pick.nt, pick.kind - 4)))
             return batch_fail(b, "tile geometry", h);
         if ((rc = esp_set_sweep_kernel(h, std::min(pick.kind, 4)))) return batch_fail(b, "esp_set_sweep_kernel", h);
         if (out && out->kernel) out->kernel[i] = std::min(pick.kind, 4);

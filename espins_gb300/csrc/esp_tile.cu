@@ -313,12 +313,21 @@ struct PairNbr {
     float2 nJ, B, Dx, Dy, Dz, nDx, nDy, nDz;
 };
 
-template <int T, int G>
-__global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArgs a)
+// NB box buffers per CTA.  NB = 2: one CTA per SM, the next item's box copied
+// while this one's sites are updated.  NB = 1: two CTAs per SM at <= 128
+// registers a thread, twice the warps; each CTA copies its box, then updates,
+// and the other CTA's updates cover the copy.  EG stencil entries per group
+// of neighbour loads in flight.
+template <int T, int G, int NB>
+__global__ void __launch_bounds__(kTilePThreads, NB == 1 ? 2 : 1) k_sweep_tile_p(const TileArgs a)
 {
     // SL floats per box slot: x of the G replicas, then y, then z; a thread
     // updates replicas (2 gp, 2 gp + 1) of a site
     constexpr int NT = kTilePThreads, B = T + 2, H = T / 2, PC = H * H * H, CH = G / 4, GP = G / 2, SL = 3 * G;
+    // entries per group of neighbour loads in flight: B/DM entries (EB), then
+    // exchange-only ones (EG); the bounds skip the table's padding beyond them
+    constexpr int EB = NB == 2 ? 8 : 2, EG = NB == 2 ? 8 : 4;
+    static_assert(NB == 1 || NB == 2, "box buffers");
     static_assert(G % 4 == 0 && 32 % GP == 0 && (T & 1) == 0, "tile shape");
     const int na = a.na, maxst = a.maxst;
     const int ngroups = a.R / G;
@@ -335,12 +344,13 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
     // slot offsets (in floats) of the entries for each value of (box site & 7):
     // box_slot(b + o) - box_slot(b) depends on o and b & 7 only
     int *tq = reinterpret_cast<int *>(pnb + na * maxst);                // [na][maxst][8]
-    int *inv_s = tq + 8 * na * maxst;                                   // [2][nbs], padded to 4
-    float *buf = reinterpret_cast<float *>(inv_s + 2 * ((nbs + 3) & ~3));  // [2][nbs8][3][G]
-    double *red = reinterpret_cast<double *>(buf + (size_t)2 * nbs8 * SL);  // [NT/32][G][4]
+    int *inv_s = tq + 8 * na * maxst;                                   // [NB][nbs], padded to 4
+    float *buf = reinterpret_cast<float *>(inv_s + NB * ((nbs + 3) & ~3));  // [NB][nbs8][3][G]
+    double *red = reinterpret_cast<double *>(buf + (size_t)NB * nbs8 * SL);  // [NT/32][G][4]
     unsigned long long *red_n = reinterpret_cast<unsigned long long *>(red + (NT / 32) * G * 4);
 
     __shared__ int s_nbd8[kMaxClusterAtoms], s_nall8[kMaxClusterAtoms];
+    __shared__ int s_nbd2[kMaxClusterAtoms], s_nall4[kMaxClusterAtoms];
     {
         const int *src = reinterpret_cast<const int *>(a.stencil);
         int *dst = reinterpret_cast<int *>(st);
@@ -363,6 +373,8 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
         if (threadIdx.x < kMaxClusterAtoms) {
             s_nbd8[threadIdx.x] = a.nbd8[threadIdx.x];
             s_nall8[threadIdx.x] = a.nall8[threadIdx.x];
+            s_nbd2[threadIdx.x] = a.nbd2[threadIdx.x];
+            s_nall4[threadIdx.x] = a.nall4[threadIdx.x];
         }
     }
 
@@ -423,24 +435,36 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
     int w = blockIdx.x;
     if (w >= W) return;
     int regs[kInvPerThread];
-    load_inv(w, regs);
-    store_inv(0, regs);
-    __syncthreads();
-    issue_box(w, 0);
-    const int w1 = w + gridDim.x;
-    if (w1 < W) {
-        load_inv(w1, regs);
-        store_inv(1, regs);
+    if constexpr (NB == 2) {
+        load_inv(w, regs);
+        store_inv(0, regs);
+        __syncthreads();
+        issue_box(w, 0);
+        const int w1 = w + gridDim.x;
+        if (w1 < W) {
+            load_inv(w1, regs);
+            store_inv(1, regs);
+        }
     }
     const int gp = threadIdx.x % GP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int kk = 0; w < W; ++kk, w += gridDim.x) {
-        const int cur = kk & 1, nxt = cur ^ 1;
+        const int cur = NB == 2 ? (kk & 1) : 0;
         const int wn = w + gridDim.x, wnn = wn + gridDim.x;
-        __syncthreads();   // inv_s[nxt] written, buffer nxt free
-        if (wn < W) issue_box(wn, nxt);
-        if (wnn < W) load_inv(wnn, regs);   // in flight during the update
-        if (wn < W) cp_async_wait<1>(); else cp_async_wait<0>();
+        if constexpr (NB == 2) {
+            __syncthreads();   // inv_s[nxt] written, buffer nxt free
+            if (wn < W) issue_box(wn, cur ^ 1);
+            if (wnn < W) load_inv(wnn, regs);   // in flight during the update
+            if (wn < W) cp_async_wait<1>(); else cp_async_wait<0>();
+        } else {
+            // the previous item's write-back and sums are done (barrier at
+            // the end of the loop body): its index table and box are free
+            load_inv(w, regs);
+            store_inv(0, regs);
+            __syncthreads();
+            issue_box(w, 0);
+            cp_async_wait<0>();
+        }
         __syncthreads();   // box of item w visible to every thread
 
         int x0, y0, z0, r0, tile;
@@ -469,36 +493,37 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
                 f.gx = f.gy = f.gz = f.qxx = f.qyy = f.qzz = f.qxy = f.qxz = f.qyz = make_float2(0.f, 0.f);
                 const PairNbr *nb = pnb + at * maxst;
                 const int *to = tq + 8 * at * maxst + (bsite & 7);
-                const int nbd8 = s_nbd8[at], nall8 = s_nall8[at];
+                const int nbd = NB == 2 ? s_nbd8[at] : s_nbd2[at];
+                const int nall = NB == 2 ? s_nall8[at] : s_nall4[at];
                 int e0 = 0;
-                for (; e0 < nbd8; e0 += 8) {
-                    float2 tx_[8], ty_[8], tz_[8];
+                for (; e0 < nbd; e0 += EB) {
+                    float2 tx_[EB], ty_[EB], tz_[EB];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
+                    for (int j = 0; j < EB; ++j) {
                         const float *q = own + to[8 * (e0 + j)];
                         tx_[j] = *reinterpret_cast<const float2 *>(q);
                         ty_[j] = *reinterpret_cast<const float2 *>(q + G);
                         tz_[j] = *reinterpret_cast<const float2 *>(q + 2 * G);
                     }
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
+                    for (int j = 0; j < EB; ++j) {
                         const PairNbr &p = nb[e0 + j];
                         entry_exchange(f, p.nJ, tx_[j], ty_[j], tz_[j]);
                         if (a.has_b) entry_bq(f, p.B, tx_[j], ty_[j], tz_[j]);
                         if (a.has_d) entry_dm(f, p.Dx, p.Dy, p.Dz, p.nDx, p.nDy, p.nDz, tx_[j], ty_[j], tz_[j]);
                     }
                 }
-                for (; e0 < nall8; e0 += 8) {   // exchange only
-                    float2 tx_[8], ty_[8], tz_[8];
+                for (e0 = s_nbd8[at]; e0 < nall; e0 += EG) {   // exchange only
+                    float2 tx_[EG], ty_[EG], tz_[EG];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
+                    for (int j = 0; j < EG; ++j) {
                         const float *q = own + to[8 * (e0 + j)];
                         tx_[j] = *reinterpret_cast<const float2 *>(q);
                         ty_[j] = *reinterpret_cast<const float2 *>(q + G);
                         tz_[j] = *reinterpret_cast<const float2 *>(q + 2 * G);
                     }
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) entry_exchange(f, nb[e0 + j].nJ, tx_[j], ty_[j], tz_[j]);
+                    for (int j = 0; j < EG; ++j) entry_exchange(f, nb[e0 + j].nJ, tx_[j], ty_[j], tz_[j]);
                 }
                 const int orig = (((z0 + lz) * a.Ly + (y0 + ly)) * a.Lx + (x0 + lx)) * na + at;
 #pragma unroll
@@ -567,40 +592,63 @@ __global__ void __launch_bounds__(kTilePThreads, 1) k_sweep_tile_p(const TileArg
             o[0] += s0; o[1] += s1; o[2] += s2; o[3] += s3;
             a.part_rej[slot] += sn;
         }
-        if (wnn < W) store_inv(cur, regs);
+        if constexpr (NB == 2) {
+            if (wnn < W) store_inv(cur, regs);
+        }
     }
 }
 
-// e_run / m_run / rejected of every replica from the tiles' slots, in tile
-// order, and the slots cleared.  One block per replica.
-__global__ void __launch_bounds__(256) k_tile_fold(TileFoldArgs a)
+// e_run / m_run / rejected of every replica from the tiles' slots, and the
+// slots cleared, in two passes with a fixed summation order (deterministic
+// for any grid).  Pass 1: block b sums tiles [32 b, 32 b + 32) of every slot
+// word, thread q of the words (4 R doubles, then R counts) walking the tiles
+// in order, so a warp reads 32 consecutive words of a tile.
+__global__ void __launch_bounds__(256) k_tile_fold_chunks(TileFoldArgs a)
 {
-    __shared__ double s_v[4][256];
-    __shared__ unsigned long long s_n[256];
-    const int r = blockIdx.x, t = threadIdx.x;
-    double v0 = 0, v1 = 0, v2 = 0, v3 = 0;
-    unsigned long long n = 0;
-    for (int tile = t; tile < a.ntiles; tile += blockDim.x) {
-        const size_t slot = (size_t)tile * a.R + r;
-        double *o = a.part + 4 * slot;
-        v0 += o[0]; v1 += o[1]; v2 += o[2]; v3 += o[3];
-        o[0] = 0.0; o[1] = 0.0; o[2] = 0.0; o[3] = 0.0;
-        n += a.part_rej[slot];
-        a.part_rej[slot] = 0ull;
-    }
-    s_v[0][t] = v0; s_v[1][t] = v1; s_v[2][t] = v2; s_v[3][t] = v3; s_n[t] = n;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (t < w) {
-            for (int c = 0; c < 4; ++c) s_v[c][t] += s_v[c][t + w];
-            s_n[t] += s_n[t + w];
+    const int t0 = blockIdx.x * kTileFoldChunk;
+    const int t1 = min(a.ntiles, t0 + kTileFoldChunk);
+    const int W = 4 * a.R;
+    double *chunk = a.part + (size_t)a.ntiles * W;
+    unsigned long long *chunk_rej = a.part_rej + (size_t)a.ntiles * a.R;
+    for (int q = threadIdx.x; q < W + a.R; q += blockDim.x) {
+        // loads first, then the clearing stores, so the loads of a thread
+        // are all in flight together
+        if (q < W) {
+            double *o = a.part + (size_t)t0 * W + q;
+            double s = 0.0;
+#pragma unroll 8
+            for (int k = 0; k < t1 - t0; ++k) s += o[(size_t)k * W];
+            for (int k = 0; k < t1 - t0; ++k) o[(size_t)k * W] = 0.0;
+            chunk[(size_t)blockIdx.x * W + q] = s;
+        } else {
+            unsigned long long *o = a.part_rej + (size_t)t0 * a.R + (q - W);
+            unsigned long long n = 0;
+#pragma unroll 8
+            for (int k = 0; k < t1 - t0; ++k) n += o[(size_t)k * a.R];
+            for (int k = 0; k < t1 - t0; ++k) o[(size_t)k * a.R] = 0ull;
+            chunk_rej[(size_t)blockIdx.x * a.R + (q - W)] = n;
         }
-        __syncthreads();
     }
-    if (t == 0) {
-        a.e_run[r] += s_v[0][0];
-        a.m_run[3 * r] += s_v[1][0]; a.m_run[3 * r + 1] += s_v[2][0]; a.m_run[3 * r + 2] += s_v[3][0];
-        a.rej[2 * a.temp_of[r] + a.phase] += s_n[0];
+}
+
+// Pass 2: thread q sums slot word q over the chunks in order.
+__global__ void __launch_bounds__(256) k_tile_fold_total(TileFoldArgs a)
+{
+    const int W = 4 * a.R, nch = tile_fold_chunks(a.ntiles);
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const double *chunk = a.part + (size_t)a.ntiles * W;
+    const unsigned long long *chunk_rej = a.part_rej + (size_t)a.ntiles * a.R;
+    if (q < W) {
+        double s = 0.0;
+        for (int b = 0; b < nch; ++b) s += chunk[(size_t)b * W + q];
+        const int r = q >> 2, c = q & 3;
+        if (c == 0) a.e_run[r] += s;
+        else a.m_run[3 * r + c - 1] += s;
+    } else if (q < W + a.R) {
+        const int r = q - W;
+        unsigned long long n = 0;
+        for (int b = 0; b < nch; ++b) n += chunk_rej[(size_t)b * a.R + r];
+        a.rej[2 * a.temp_of[r] + a.phase] += n;
     }
 }
 
@@ -628,12 +676,12 @@ cudaError_t launch_tile(const TileArgs &a, size_t smem, cudaStream_t st)
     return cudaGetLastError();
 }
 
-size_t tile_p_smem_bytes(int T, int G, int na, int maxst)
+size_t tile_p_smem_bytes(int T, int G, int na, int maxst, int nb)
 {
     const size_t B = (size_t)T + 2, nbs = B * B * B * na, nbs8 = (nbs + 7) & ~(size_t)7;
     return sizeof(ClusterStencil) + (size_t)na * maxst * sizeof(PairNbr) +
-           (size_t)8 * na * maxst * sizeof(int) + 2 * ((nbs + 3) & ~(size_t)3) * sizeof(int) +
-           (size_t)6 * nbs8 * G * sizeof(float) + (size_t)(kTilePThreads / 32) * G * (4 * sizeof(double) + 8);
+           (size_t)8 * na * maxst * sizeof(int) + nb * ((nbs + 3) & ~(size_t)3) * sizeof(int) +
+           (size_t)3 * nb * nbs8 * G * sizeof(float) + (size_t)(kTilePThreads / 32) * G * (4 * sizeof(double) + 8);
 }
 
 bool tile_p_supported(int T, int G, int na)
@@ -644,50 +692,57 @@ bool tile_p_supported(int T, int G, int na)
 }
 
 namespace {
-template <int T, int G>
+template <int T, int G, int NB>
 cudaError_t launch_p(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
 {
-    if (configure) return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sweep_tile_p<T, G>), smem);
-    k_sweep_tile_p<T, G><<<blocks, kTilePThreads, smem, st>>>(a);
+    if (configure) return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sweep_tile_p<T, G, NB>), smem);
+    k_sweep_tile_p<T, G, NB><<<blocks, kTilePThreads, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-template <int T>
+template <int T, int NB>
 cudaError_t launch_pg(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
 {
-    if (a.G == 4) return launch_p<T, 4>(a, smem, blocks, st, configure);
-    if (a.G == 8) return launch_p<T, 8>(a, smem, blocks, st, configure);
-    if (a.G == 16) return launch_p<T, 16>(a, smem, blocks, st, configure);
+    if (a.G == 4) return launch_p<T, 4, NB>(a, smem, blocks, st, configure);
+    if (a.G == 8) return launch_p<T, 8, NB>(a, smem, blocks, st, configure);
+    if (a.G == 16) return launch_p<T, 16, NB>(a, smem, blocks, st, configure);
     return cudaErrorInvalidValue;
 }
 
+template <int NB>
 cudaError_t launch_pt(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
 {
-    if (a.T == 4) return launch_pg<4>(a, smem, blocks, st, configure);
-    if (a.T == 6) return launch_pg<6>(a, smem, blocks, st, configure);
-    if (a.T == 8) return launch_pg<8>(a, smem, blocks, st, configure);
+    if (a.T == 4) return launch_pg<4, NB>(a, smem, blocks, st, configure);
+    if (a.T == 6) return launch_pg<6, NB>(a, smem, blocks, st, configure);
+    if (a.T == 8) return launch_pg<8, NB>(a, smem, blocks, st, configure);
     return cudaErrorInvalidValue;
 }
 }  // namespace
 
-cudaError_t tile_p_configure(int T, int G, size_t smem)
+cudaError_t tile_p_configure(int T, int G, int nb, size_t smem)
 {
     TileArgs a{};
     a.T = T; a.G = G;
-    return launch_pt(a, smem, 0, nullptr, true);
+    if (nb == 1) return launch_pt<1>(a, smem, 0, nullptr, true);
+    if (nb == 2) return launch_pt<2>(a, smem, 0, nullptr, true);
+    return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_tile_p(const TileArgs &a, size_t smem, int num_sms, cudaStream_t st)
+cudaError_t launch_tile_p(const TileArgs &a, size_t smem, int num_sms, int nb, cudaStream_t st)
 {
-    if (!tile_p_supported(a.T, a.G, a.na) || a.R % a.G != 0) return cudaErrorInvalidValue;
+    if (!tile_p_supported(a.T, a.G, a.na) || a.R % a.G != 0 || (nb != 1 && nb != 2)) return cudaErrorInvalidValue;
     const int items = (a.ntx / 2) * (a.nty / 2) * (a.ntz / 2) * (a.R / a.G);
-    const int blocks = items < num_sms ? items : num_sms;
-    return launch_pt(a, smem, blocks, st, false);
+    const int slots = nb == 1 ? 2 * num_sms : num_sms;   // persistent CTAs: one per SM, or two
+    const int blocks = items < slots ? items : slots;
+    return nb == 1 ? launch_pt<1>(a, smem, blocks, st, false) : launch_pt<2>(a, smem, blocks, st, false);
 }
 
 cudaError_t launch_tile_fold(const TileFoldArgs &a, cudaStream_t st)
 {
-    k_tile_fold<<<a.R, 256, 0, st>>>(a);
+    k_tile_fold_chunks<<<tile_fold_chunks(a.ntiles), 256, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_tile_fold_total<<<(5 * a.R + 255) / 256, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

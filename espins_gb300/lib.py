@@ -571,14 +571,16 @@ class Engine:
         self._check(self.lib.esp_get_cluster_geometry(self.h, C.byref(a), C.byref(b), C.byref(s)))
         return a.value, b.value, s.value
 
-    def set_tile_geometry(self, tile: int, replicas: int, pipelined: bool = False) -> None:
-        self._check(self.lib.esp_set_tile_geometry(self.h, int(tile), int(replicas), int(bool(pipelined))))
+    def set_tile_geometry(self, tile: int, replicas: int, variant: int = 0) -> None:
+        """variant 0: one CTA per tile; persistent pipelined CTAs, 1: one per
+        SM, 2: two per SM."""
+        self._check(self.lib.esp_set_tile_geometry(self.h, int(tile), int(replicas), int(variant)))
 
     def tile_geometry(self):
-        """(tile edge in cells, replicas per CTA, pipelined) of the tiled path, (0, 0, False) without one."""
+        """(tile edge in cells, replicas per CTA, variant) of the tiled path, (0, 0, 0) without one."""
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
         self._check(self.lib.esp_get_tile_geometry(self.h, C.byref(a), C.byref(b), C.byref(c)))
-        return a.value, b.value, bool(c.value)
+        return a.value, b.value, c.value
 
     def set_pt_groups(self, group_size: int) -> None:
         """Replica exchange only inside consecutive groups of `group_size`

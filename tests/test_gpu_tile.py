@@ -70,7 +70,7 @@ def test_tiled_trajectory_does_not_depend_on_replica_grouping():
             e.set_temperatures(inp.tems)
             e.set_sweep_kernel("tile")
             e.set_tile_geometry(T, G)
-            assert e.tile_geometry() == (T, G, False)
+            assert e.tile_geometry() == (T, G, 0)
             e.set_spins(s0)
             e.sweep(30, 5, seed=9)
             outs.append(((T, G), e.get_spins(), e.rejected(), e.running_energy(), e.energy()))
@@ -85,8 +85,9 @@ def test_tiled_trajectory_does_not_depend_on_replica_grouping():
 
 @pytest.mark.parametrize("case", ["sc", "bcc"])
 def test_pipelined_tiles_follow_the_one_tile_per_cta_kernel(case):
-    """The persistent cp.async-pipelined variant updates the same tiles in the
-    same order within each tile: identical trajectories."""
+    """The persistent cp.async-pipelined variants (one CTA per SM with two box
+    buffers, two CTAs per SM with one each) update the same tiles in the same
+    order within each tile: identical trajectories."""
     tems = [3.0, 6.0, 12.0, 20.0, 30.0, 45.0, 60.0, 80.0]
     if case == "sc":
         inp = sc_mcin(16, [(1e-3, NN), (3e-4, NNN), (-5e-5, N3)], tems, dm=1e-4, si=-3e-5)
@@ -98,17 +99,18 @@ def test_pipelined_tiles_follow_the_one_tile_per_cta_kernel(case):
     v = rng.normal(size=(len(tems), h.n, 3))
     s0 = v / np.linalg.norm(v, axis=2, keepdims=True)
     outs = []
-    for pipelined in (False, True):
+    for variant in (0, 1, 2):
         with Engine(h.n, h.num_atoms, h.supercell, len(tems)) as e:
             e.upload(h)
             e.set_temperatures(tems)
             e.set_sweep_kernel("tile")
-            e.set_tile_geometry(4, 4, pipelined)
-            assert e.tile_geometry() == (4, 4, pipelined)
+            e.set_tile_geometry(4, 4, variant)
+            assert e.tile_geometry() == (4, 4, variant)
             e.set_spins(s0)
             e.sweep(12, 3, seed=21)
             outs.append((e.get_spins(), e.rejected(), e.running_energy(), e.energy()))
-    assert np.array_equal(outs[0][0], outs[1][0])
-    assert np.array_equal(outs[0][1], outs[1][1])
+    for k in (1, 2):
+        assert np.array_equal(outs[0][0], outs[k][0])
+        assert np.array_equal(outs[0][1], outs[k][1])
     for s, rej, run, direct in outs:
         assert np.max(np.abs(run - direct)) <= 1e-5 * energy_scale(h)
