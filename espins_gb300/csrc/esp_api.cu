@@ -125,6 +125,13 @@ struct esp_handle {
     double *d_stage = nullptr, *h_stage = nullptr;
     float *d_slab = nullptr;   // spins in the cluster path's slab layout during its launches
     int stage_slots = 0;
+    // the device reads / writes pageable host memory through the host's page
+    // tables (a coherent CPU-GPU link): the spin transfers can skip the
+    // staging.  host_transfer: bit 0 esp_set_spins reads the caller's array,
+    // bit 1 esp_get_spins writes it, -1 the default
+    bool host_direct_ok = false;
+    int host_transfer = -1;
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};   // a staging half's copy has finished
     // structure factor (esp_set_structure_factor)
     int sf_nq = 0, sf_every = 1;
     double sf_p[3] = {1.0, 0.0, 0.0}, sf_pnorm = 1.0;
@@ -260,6 +267,10 @@ void free_all(esp_handle *h)
     if (h->h_stage) cudaFreeHost(h->h_stage);
     h->h_stage = nullptr;
     h->stage_slots = 0;
+    for (cudaEvent_t &ev : h->stage_ev) {
+        if (ev) cudaEventDestroy(ev);
+        ev = nullptr;
+    }
     dfree(h->d_series);
     free_lp_batch(h);
     dfree(h->d_lp_p); dfree(h->d_lp_g); dfree(h->d_lp_m); dfree(h->d_lp_v);
@@ -990,12 +1001,24 @@ int cluster_geometry(esp_handle *h, int cs, int nt, int S)
     return ESP_OK;
 }
 
+// Which spin transfers read / write the caller's array directly (bit 0 / 1)
+// where the device can.  None by default: measured on a GB300 with a
+// coherent CPU link, the device read the caller's array at ~45 GB/s against
+// ~38 GB/s staged, and wrote freshly allocated (not yet touched) pages at
+// 2.7 GB/s, faulting each in, against ~26 GB/s staged.
+constexpr int kHostTransferDefault = 0;
+int host_transfer_mode(const esp_handle *h)
+{
+    if (!h->host_direct_ok) return 0;
+    return h->host_transfer >= 0 ? h->host_transfer : kHostTransferDefault;
+}
+
 // Staging for spin_matrix blocks of whole temperature slots, at most 256 MiB
 // (one slot at least), on the device and in pinned host memory; allocated
 // with the tables so that the spin transfers themselves allocate nothing.
 int ensure_stage(esp_handle *h)
 {
-    if (h->d_stage && h->h_stage && h->stage_slots > 0) return ESP_OK;
+    if (h->d_stage && h->h_stage && h->stage_slots > 0 && h->stage_ev[0] && h->stage_ev[1]) return ESP_OK;
     // set up both halves or neither: a handle left with one of them would
     // loop forever over zero-slot blocks in esp_set_spins / esp_get_spins
     dfree(h->d_stage);
@@ -1013,17 +1036,32 @@ int ensure_stage(esp_handle *h)
         h->err = std::string("cudaMallocHost of the spin staging: ") + cudaGetErrorString(e);
         return ESP_ENOMEM;
     }
+    for (cudaEvent_t &ev : h->stage_ev) {
+        if (!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
+            dfree(h->d_stage);
+            cudaFreeHost(h->h_stage);
+            h->h_stage = nullptr;
+            h->err = std::string("cudaEventCreate: ") + cudaGetErrorString(e);
+            return ESP_ECUDA;
+        }
+    }
     h->stage_slots = slots;
     return ESP_OK;
 }
 
+// The staging as two halves of `half` slots each (one half, the whole
+// staging, when it holds a single slot): the host copy of one block runs while
+// the other half's block crosses the link and is converted on the device.
+int stage_half(const esp_handle *h) { return h->stage_slots >= 2 ? h->stage_slots / 2 : h->stage_slots; }
+
 // Host copy between the caller's arrays and the pinned staging, split over
-// up to 8 threads for large blocks: one core copies (and faults in fresh
-// pages) far below the memory bandwidth.
+// up to 16 threads (the host's cores) for large blocks: one core copies (and
+// faults in fresh pages) far below the memory bandwidth.
 void par_memcpy(void *dst, const void *src, size_t bytes)
 {
     const size_t chunk = (size_t)4 << 20;
-    const int nth = (int)std::min<size_t>(8, bytes / chunk);
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nth = (int)std::min<size_t>(std::min(16u, hw), bytes / chunk);
     if (nth <= 1) {
         std::memcpy(dst, src, bytes);
         return;
@@ -1075,6 +1113,14 @@ int esp_create(const esp_dims *dims, esp_handle **out)
     h->open = dims->open_boundary != 0;
     cudaError_t e = cudaGetDevice(&h->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+    if (e == cudaSuccess) {
+        int pageable = 0, host_tables = 0;
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, h->device) != cudaSuccess) pageable = 0;
+        if (cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, h->device) !=
+            cudaSuccess)
+            host_tables = 0;
+        h->host_direct_ok = pageable == 1 && host_tables == 1;
+    }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = lp_configure(h->device);
     if (e == cudaSuccess) e = lp_tc_configure();
@@ -1337,17 +1383,34 @@ int esp_set_spins(esp_handle *h, const double *spins)
     if (!spins) { h->err = "null spins"; return ESP_EINVAL; }
     if ((rc = ensure_stage(h))) return rc;
     arrays_written(h);   // every slot is overwritten below
+    if (host_transfer_mode(h) & 1) {
+        // one kernel reads the caller's FP64 array over the CPU-GPU link
+        CK(launch_spins_in(spins, h->d_inv, h->d_repl_at, h->d_sx, h->d_sy, h->d_sz, h->N, h->R, 0, h->R, h->st));
+        h->launches++;
+        if ((rc = reset_running(h))) return rc;
+        CK(cudaStreamSynchronize(h->st));
+        return ESP_OK;
+    }
     // blocks of slots: copy the FP64 block through the pinned staging (a
     // parallel host copy, then one DMA), then scatter it into the permuted
-    // FP32 state on the device.  The driver's pageable path is as fast only
-    // for warm, small arrays and falls to ~1 GB/s where it must fault pages in.
-    for (int t0 = 0; t0 < h->R; t0 += h->stage_slots) {
-        const int nt = std::min(h->stage_slots, h->R - t0);
+    // FP32 state on the device; the blocks alternate between the staging's
+    // halves, so the host copy of one overlaps the DMA and conversion of the
+    // previous.  The driver's pageable path is as fast only for warm, small
+    // arrays and falls to ~1 GB/s where it must fault pages in.
+    const int half = stage_half(h);
+    const size_t half_el = (size_t)3 * h->N * half;
+    CK(cudaStreamSynchronize(h->st));   // the halves' events belong to this call from here on
+    for (int t0 = 0, k = 0; t0 < h->R; t0 += half, ++k) {
+        const int nt = std::min(half, h->R - t0), b = h->stage_slots >= 2 ? (k & 1) : 0;
         const size_t bytes = sizeof(double) * 3 * (size_t)h->N * nt;
-        CK(cudaStreamSynchronize(h->st));   // the previous block has left the pinned staging
-        par_memcpy(h->h_stage, spins + (size_t)3 * h->N * t0, bytes);
-        CK(cudaMemcpyAsync(h->d_stage, h->h_stage, bytes, cudaMemcpyHostToDevice, h->st));
-        CK(launch_spins_in(h->d_stage, h->d_inv, h->d_repl_at, h->d_sx, h->d_sy, h->d_sz, h->N, h->R, t0, nt, h->st));
+        if (k >= (h->stage_slots >= 2 ? 2 : 1))
+            CK(cudaEventSynchronize(h->stage_ev[b]));   // this half's previous block has left the pinned memory
+        par_memcpy(h->h_stage + b * half_el, spins + (size_t)3 * h->N * t0, bytes);
+        CK(cudaMemcpyAsync(h->d_stage + b * half_el, h->h_stage + b * half_el, bytes, cudaMemcpyHostToDevice,
+                           h->st));
+        CK(cudaEventRecord(h->stage_ev[b], h->st));
+        CK(launch_spins_in(h->d_stage + b * half_el, h->d_inv, h->d_repl_at, h->d_sx, h->d_sy, h->d_sz, h->N, h->R,
+                           t0, nt, h->st));
         h->launches++;
     }
     if ((rc = reset_running(h))) return rc;
@@ -1375,15 +1438,38 @@ int esp_get_spins(esp_handle *h, double *spins)
     if (!spins) { h->err = "null spins"; return ESP_EINVAL; }
     if ((rc = ensure_stage(h))) return rc;
     if ((rc = arrays_current(h))) return rc;
-    for (int t0 = 0; t0 < h->R; t0 += h->stage_slots) {
-        const int nt = std::min(h->stage_slots, h->R - t0);
-        const size_t bytes = sizeof(double) * 3 * (size_t)h->N * nt;
-        CK(launch_spins_out(h->d_stage, h->d_inv, h->d_repl_at, h->d_sx, h->d_sy, h->d_sz, h->N, h->R, t0, nt, h->st));
+    if (host_transfer_mode(h) & 2) {
+        // one kernel writes the caller's FP64 array over the CPU-GPU link
+        CK(launch_spins_out(spins, h->d_inv, h->d_repl_at, h->d_sx, h->d_sy, h->d_sz, h->N, h->R, 0, h->R, h->st));
         h->launches++;
-        CK(cudaMemcpyAsync(h->h_stage, h->d_stage, bytes, cudaMemcpyDeviceToHost, h->st));
         CK(cudaStreamSynchronize(h->st));
-        par_memcpy(spins + (size_t)3 * h->N * t0, h->h_stage, bytes);
+        return ESP_OK;
     }
+    // blocks alternate between the staging's halves: block k is gathered and
+    // crosses the link while the host copies block k - 1 out of the other half
+    const int half = stage_half(h);
+    const size_t half_el = (size_t)3 * h->N * half;
+    int prev_t0 = -1, prev_b = 0;
+    size_t prev_bytes = 0;
+    auto drain = [&]() -> int {
+        CK(cudaEventSynchronize(h->stage_ev[prev_b]));
+        par_memcpy(spins + (size_t)3 * h->N * prev_t0, h->h_stage + prev_b * half_el, prev_bytes);
+        prev_t0 = -1;
+        return ESP_OK;
+    };
+    for (int t0 = 0, k = 0; t0 < h->R; t0 += half, ++k) {
+        const int nt = std::min(half, h->R - t0), b = h->stage_slots >= 2 ? (k & 1) : 0;
+        const size_t bytes = sizeof(double) * 3 * (size_t)h->N * nt;
+        if (prev_t0 >= 0 && b == prev_b && (rc = drain())) return rc;   // one half only: empty it first
+        CK(launch_spins_out(h->d_stage + b * half_el, h->d_inv, h->d_repl_at, h->d_sx, h->d_sy, h->d_sz, h->N, h->R,
+                            t0, nt, h->st));
+        h->launches++;
+        CK(cudaMemcpyAsync(h->h_stage + b * half_el, h->d_stage + b * half_el, bytes, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaEventRecord(h->stage_ev[b], h->st));
+        if (prev_t0 >= 0 && (rc = drain())) return rc;
+        prev_t0 = t0; prev_b = b; prev_bytes = bytes;
+    }
+    if (prev_t0 >= 0 && (rc = drain())) return rc;
     return ESP_OK;
 }
 
@@ -1601,6 +1687,25 @@ int esp_set_tile_geometry(esp_handle *h, int32_t tile, int32_t replicas, int32_t
             return tile_geometry(h, tile, replicas, g.variant);
     h->err = "tile geometry not possible for this lattice";
     return ESP_EINVAL;
+}
+
+int esp_set_host_transfer(esp_handle *h, int32_t mode)
+{
+    if (!h || mode < -1 || mode > 3) return ESP_EINVAL;
+    if (mode > 0 && !h->host_direct_ok) {
+        h->err = "the device does not access pageable host memory through the host's page tables";
+        return ESP_EINVAL;
+    }
+    h->host_transfer = mode;
+    return ESP_OK;
+}
+
+int esp_get_host_transfer(const esp_handle *h, int32_t *mode, int32_t *direct_supported)
+{
+    if (!h || !mode) return ESP_EINVAL;
+    *mode = host_transfer_mode(h);
+    if (direct_supported) *direct_supported = h->host_direct_ok ? 1 : 0;
+    return ESP_OK;
 }
 
 int esp_get_tile_geometry(const esp_handle *h, int32_t *tile, int32_t *replicas, int32_t *pipelined)

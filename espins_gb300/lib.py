@@ -33,7 +33,7 @@ EXPORTED = [
     "esp_set_tile_geometry", "esp_get_tile_geometry", "esp_batch_create", "esp_batch_destroy", "esp_batch_last_error",
     "esp_batch_set_units_per_graph", "esp_batch_advance", "esp_batch_tune",
     "esp_set_observables", "esp_collect_observables", "esp_set_spin_correlation", "esp_collect_spin_correlation",
-    "esp_set_structure_factor", "esp_collect_structure_factor",
+    "esp_set_structure_factor", "esp_collect_structure_factor", "esp_set_host_transfer", "esp_get_host_transfer",
 ]
 
 OBS_ORDER_PARAMETER, OBS_STAGGERED = 1, 2
@@ -166,6 +166,8 @@ def load(build_if_missing: bool = True):
     lib.esp_set_cluster_geometry.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
     lib.esp_set_tile_geometry.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
     lib.esp_get_tile_geometry.argtypes = [vp, P(C.c_int32), P(C.c_int32), P(C.c_int32)]
+    lib.esp_set_host_transfer.argtypes = [vp, C.c_int32]
+    lib.esp_get_host_transfer.argtypes = [vp, P(C.c_int32), P(C.c_int32)]
     lib.esp_get_cluster_geometry.argtypes = [vp, P(C.c_int32), P(C.c_int32), P(C.c_int32)]
     lib.esp_batch_create.argtypes = [vp, C.c_int32, vp, P(vp)]
     lib.esp_batch_destroy.argtypes = [vp]
@@ -575,6 +577,18 @@ class Engine:
         """variant 0: one CTA per tile; persistent pipelined CTAs, 1: one per
         SM, 2: two per SM."""
         self._check(self.lib.esp_set_tile_geometry(self.h, int(tile), int(replicas), int(variant)))
+
+    def set_host_transfer(self, mode: int) -> None:
+        """Spin transfers: bit 0 esp_set_spins, bit 1 esp_get_spins read /
+        write the caller's array from the device directly (a set bit) or go
+        through the pinned staging; -1 the default."""
+        self._check(self.lib.esp_set_host_transfer(self.h, int(mode)))
+
+    def host_transfer(self):
+        """(mode in effect, whether the device reads and writes pageable host memory)."""
+        m, d = C.c_int32(), C.c_int32()
+        self._check(self.lib.esp_get_host_transfer(self.h, C.byref(m), C.byref(d)))
+        return m.value, bool(d.value)
 
     def tile_geometry(self):
         """(tile edge in cells, replicas per CTA, variant) of the tiled path, (0, 0, 0) without one."""

@@ -136,10 +136,22 @@ int esp_upload_tables(esp_handle *h, const esp_tables *t);
 int esp_set_temperatures(esp_handle *h, const double *tems);
 /* spin_matrix(3,N,R) (mcarlo.F90:269-322, pt.F90:442-491).  The copy goes
  * through a staging area of pinned host and device memory (at most 256 MiB
- * each, in whole temperature slots) that esp_upload_tables allocates, so
- * neither this call nor esp_get_spins allocates; the host side of the copy
- * runs on up to 8 threads. */
+ * each, two halves of whole temperature slots) that esp_upload_tables
+ * allocates: the host copy of one block (on up to 16 threads) overlaps the
+ * DMA and device-side conversion of the previous one.  Neither this call nor
+ * esp_get_spins allocates. */
 int esp_set_spins(esp_handle *h, const double *spins);
+/* How esp_set_spins (bit 0) and esp_get_spins (bit 1) move the spins: a set
+ * bit has one kernel read / write the caller's array directly, where the
+ * device accesses pageable host memory through the host's page tables (a
+ * coherent CPU-GPU link), a clear bit goes through the pinned staging; -1
+ * restores the default (staged: on a GB300 the direct reads were barely
+ * faster and direct writes into not yet touched pages fault each page in).
+ * ESP_EINVAL for a direct mode on a device without that access.  No
+ * counterpart in the reference. */
+int esp_set_host_transfer(esp_handle *h, int32_t mode);
+/* The mode in effect, and whether the device supports direct access. */
+int esp_get_host_transfer(const esp_handle *h, int32_t *mode, int32_t *direct_supported);
 /* Start configurations of the reference: 0 ferro (0,0,m), 1 rand
  * (theta = pi*u1, phi = 2 pi*u2, the same for every temperature as in
  * pt.F90:448-459), drawn from the Philox stream keyed by seed. */

@@ -9,6 +9,8 @@ Tolerances (FP32 site fields, FP64 totals), the 1e-6 relative bar:
   where |exp(-beta dE) - u| < 1e-4 (FP32 rounding of dE can flip those), and
   the new spins within 2e-6 of the oracle's FP64 trial spins.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -187,3 +189,39 @@ def test_pt_swap_kernel_takes_the_host_protocol_decisions():
             for s in want:
                 expect[s], expect[s + 1] = before[s + 1], before[s]
             assert np.array_equal(after, expect), (step, want)
+
+
+@pytest.mark.parametrize("L,R", [(8, 6), (64, 80)])
+def test_spin_transfers_agree_across_host_paths(L, R):
+    """esp_set_spins / esp_get_spins through the pinned staging (in 256 MiB
+    blocks of slots: the 64^3 x 80 case takes two) and, where the device
+    reads and writes pageable host memory, directly: every mode leaves the
+    same FP32 state (the FP64 input rounded) and returns it unchanged."""
+    h = build_hamiltonian(sc_mcin(L, [(1e-3, NN)], list(np.linspace(5.0, 50.0, R))), check=False)
+    rng = np.random.default_rng(L)
+    v = rng.normal(size=(R, h.n, 3))
+    s0 = v / np.linalg.norm(v, axis=2, keepdims=True)
+    want = s0.astype(np.float32).astype(np.float64)
+    with _engine(h, R) as e:
+        _, direct = e.host_transfer()
+        modes = [0, 1, 2, 3] if direct else [0]
+        if not direct:
+            with pytest.raises(RuntimeError):
+                e.set_host_transfer(3)
+        energies = []
+        for m in modes:
+            e.set_host_transfer(m)
+            assert e.host_transfer() == (m, direct)
+            e.set_spins(s0)
+            energies.append(e.energy())
+            out = e.get_spins()
+            assert np.array_equal(out, want), m
+            # into an array whose pages are already resident
+            reused = np.full_like(out, 7.0)
+            assert e.lib.esp_get_spins(e.h, reused.ctypes.data_as(ctypes.c_void_p)) == 0
+            assert np.array_equal(reused, want), m
+        for en in energies[1:]:
+            assert np.array_equal(en, energies[0])
+        e.set_host_transfer(-1)
+        print(f"\nL={L} R={R}: direct host access {'supported' if direct else 'not supported'}, "
+              f"default mode {e.host_transfer()[0]}")
