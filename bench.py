@@ -78,7 +78,7 @@ def _args():
                    help="batch512_pt: cluster geometry CTAs,threads,sites for every size instead of the "
                         "autotuner (profiling)")
     p.add_argument("--tile", default=None,
-                   help="single-lattice workloads: tiled sweep with geometry edge,replicas,variant instead of "
+                   help="tiled sweep with geometry edge,replicas,variant (every size of batch512_pt) instead of "
                         "the autotuner's choice (profiling)")
     p.add_argument("--only-L", type=int, default=None,
                    help="batch512_pt: run only the lattices of this size (profiling of a small case)")
@@ -568,13 +568,17 @@ def batch_bench(a, ws, rank, local):
         upd_per_unit += 10 * ham.n * R
         nsites += ham.n * count
     b = Batch(engines, stream.cuda_stream)
-    if a.geometry:
-        cs, nt, sp = (int(x) for x in a.geometry.split(","))
+    if a.geometry or a.tile:
+        fixed = [int(x) for x in (a.geometry or a.tile).split(",")]
         for e in engines:
-            e.set_cluster_geometry(cs, nt, sp)
-            e.set_sweep_kernel("cluster")
+            if a.geometry:
+                e.set_cluster_geometry(*fixed)
+                e.set_sweep_kernel("cluster")
+            else:
+                e.set_tile_geometry(*fixed)
+                e.set_sweep_kernel("tile")
         b.set_units_per_graph(1)
-        tuning = {"units_per_graph": 1, "fixed_geometry": [cs, nt, sp]}
+        tuning = {"units_per_graph": 1, "kernel": "cluster" if a.geometry else "tile", "fixed_geometry": fixed}
     else:
         tuning = b.tune(units=2)
     b.advance(a.warmup)
@@ -628,7 +632,9 @@ def batch_bench(a, ws, rank, local):
     upd_per_launch = nsw * reps * eb.n * eb.R / kern_launches
     peak, peak_kind = _peaks()
     achieved = 24.0 * upd_per_launch / per_launch_s / 1e9
-    traffic, capture = _traffic(f"batch512_pt:L{list(sizes)[big]}", upd_per_launch)
+    # the capture of the kernel the autotuner chose for that size
+    traffic, capture = _traffic(f"batch512_pt:L{list(sizes)[big]}" + ("" if kernel == "cluster" else f":{kernel}"),
+                                upd_per_launch)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "traffic_capture": capture,
                 "kernel": {"cluster": "k_sweep_cluster", "tile": "k_sweep_tile"}.get(kernel, "k_sweep_ell"),

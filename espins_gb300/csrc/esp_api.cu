@@ -70,6 +70,7 @@ struct esp_handle {
     int kernel_choice = 0;          // 0 auto, 1 ELL, 2 cluster
     bool cluster_ok = false;
     int csize = 0, pz = 0, cthreads = 512, csites = 1;
+    int cl_nA = 0;                  // ranks with pz planes; the others hold pz - 2
     // Which copy of the spins is current: the spin arrays (element (p, r) at
     // p*R + r) and/or the cluster path's slab copy.  The cluster kernel leaves
     // the state in the slabs; the arrays are brought up to date (one
@@ -422,9 +423,11 @@ SlabArgs slab_args(const esp_handle *h)
 {
     SlabArgs sa;
     sa.sx = h->d_sx; sa.sy = h->d_sy; sa.sz = h->d_sz; sa.slab = h->d_slab; sa.inv = h->d_inv;
-    sa.Lx = h->L[0]; sa.Ly = h->L[1]; sa.na = h->na; sa.R = h->R; sa.pz = h->pz; sa.cs = h->csize;
-    sa.n_local = h->N / h->csize;
+    sa.Lx = h->L[0]; sa.Ly = h->L[1]; sa.na = h->na; sa.R = h->R; sa.pz = h->pz; sa.nA = h->cl_nA;
+    sa.cs = h->csize; sa.N = h->N;
+    sa.n_local = (h->L[0] / 2) * (h->L[1] / 2) * (h->pz / 2) * 8 * h->na;
     sa.fd_pc = make_fastdiv((uint32_t)((h->L[0] / 2) * (h->L[1] / 2) * (h->pz / 2)));
+    sa.fd_pc2 = make_fastdiv((uint32_t)std::max(1, (h->L[0] / 2) * (h->L[1] / 2) * (h->pz / 2 - 1)));
     sa.fd_hx = make_fastdiv((uint32_t)(h->L[0] / 2));
     sa.fd_hy = make_fastdiv((uint32_t)(h->L[1] / 2));
     return sa;
@@ -474,7 +477,7 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     a.stencil_words = h->stencil_words;
     a.nbidx = h->d_nbidx;
     a.Lx = h->L[0]; a.Ly = h->L[1]; a.Lz = h->L[2]; a.na = h->na; a.N = h->N; a.R = h->R;
-    a.nclass = 8 * h->na; a.pz = h->pz;
+    a.nclass = 8 * h->na; a.pz = h->pz; a.nA = h->cl_nA;
     a.has_b = h->prep.has_b; a.has_d = h->prep.has_d; a.has_si = h->hsi; a.has_f = h->hfld;
     const bool staged = cluster_staged(h);
     a.slab = staged ? h->d_slab : nullptr;
@@ -494,6 +497,7 @@ int cluster_run(esp_handle *h, int64_t n_meas, int steps_measure, int64_t first,
     }
     a.sweep_base = (unsigned long long)first;
     a.fd_pc = make_fastdiv((uint32_t)((h->L[0] / 2) * (h->L[1] / 2) * (h->pz / 2)));
+    a.fd_pc2 = make_fastdiv((uint32_t)std::max(1, (h->L[0] / 2) * (h->L[1] / 2) * (h->pz / 2 - 1)));
     a.fd_hx = make_fastdiv((uint32_t)(h->L[0] / 2));
     a.fd_hy = make_fastdiv((uint32_t)(h->L[1] / 2));
     a.rn_inv = 1.0 / (double)h->N;
@@ -777,10 +781,23 @@ int d2h(esp_handle *h, void *dst, const void *src, size_t bytes)
     return ESP_OK;
 }
 
+// Split of Lz planes into cs slabs of an even number of planes, as equal as
+// possible: nA slabs of pz planes, cs - nA of pz - 2 (nA == cs: all equal).
+bool slab_split(int Lz, int cs, int &pz, int &nA)
+{
+    if (Lz % 2 != 0 || cs < 1) return false;
+    const int pairs = Lz / 2, q = pairs / cs, rem = pairs % cs;
+    if (q < 1) return false;
+    pz = 2 * (rem ? q + 1 : q);
+    nA = rem ? rem : cs;
+    return true;
+}
+
 // Cluster geometries the GPU can run, cheapest first by a model: cs CTAs of
-// nt threads per replica, slabs of an even number of z planes, shared memory
-// within the per-CTA limit; cost = waves of R clusters (occupancy calculator)
-// x CTAs one SM holds per wave x the length of a sweep in colour passes.
+// nt threads per replica, slabs of an even number of z planes (as equal as
+// possible), shared memory within the per-CTA limit; cost = waves of R
+// clusters (occupancy calculator) x CTAs one SM holds per wave x the length of
+// a sweep in colour passes of the largest slab.
 struct ClusterGeom {
     int cs, nt, S;
     double cost;
@@ -800,8 +817,11 @@ std::vector<ClusterGeom> cluster_candidates(const esp_handle *h)
     for (const auto &tg : geoms)
         for (int cs = 1; cs <= 16; ++cs) {
             const int nt = tg[0], S = tg[1];
-            if (h->L[2] % (2 * cs) != 0) continue;
-            const size_t smem = cluster_smem_bytes(h->N / cs, h->nf, h->obs ? 3 : 1, h->cl_sbytes);
+            int pz = 0, nA = 0;
+            if (!slab_split(h->L[2], cs, pz, nA)) continue;
+            // the largest slab sets the shared memory and the pace
+            const int n_big = (h->L[0] / 2) * (h->L[1] / 2) * (pz / 2) * 8 * h->na;
+            const size_t smem = cluster_smem_bytes(n_big, h->nf, h->obs ? 3 : 1, h->cl_sbytes);
             if (smem > 226 * 1024) continue;
             const int active = cluster_max_active(cs, nt, S, smem, h->R);
             if (active <= 0) continue;
@@ -810,7 +830,7 @@ std::vector<ClusterGeom> cluster_candidates(const esp_handle *h)
             const double per_sm = std::ceil(conc / (double)std::max(1, h->num_sms));
             // colour passes of a sweep; a pass with two sites per thread
             // takes ~1.85 times one with one site (measured)
-            const int64_t per_class = (int64_t)(h->L[0] / 2) * (h->L[1] / 2) * (h->L[2] / cs / 2);
+            const int64_t per_class = (int64_t)(h->L[0] / 2) * (h->L[1] / 2) * (pz / 2);
             double passes = 0.0;
             for (int n : per_colour) passes += (double)ceil_div(n * per_class, (int64_t)S * nt) * (S == 2 ? 1.85 : 1.0);
             out.push_back({cs, nt, S, waves * per_sm * passes});
@@ -955,21 +975,34 @@ int cluster_geometry(esp_handle *h, int cs, int nt, int S)
         if (rc0) return rc0;
     }
     const int maxst = h->cl_maxst;
-    const int pz = h->L[2] / cs, n_local = h->N / cs;
-    const size_t smem = cluster_smem_bytes(n_local, h->nf, h->obs ? 3 : 1, h->cl_sbytes);
+    int pz = 0, nA = 0;
+    if (!slab_split(h->L[2], cs, pz, nA)) {
+        h->err = "no slab split of the supercell's z planes over this cluster size";
+        return ESP_EINVAL;
+    }
+    const int Lx = h->L[0], Ly = h->L[1], Lz = h->L[2], Hx = Lx / 2, Hy = Ly / 2;
+    const int nclass = 8 * h->na;
+    const int n_big = Hx * Hy * (pz / 2) * nclass;
+    const size_t smem = cluster_smem_bytes(n_big, h->nf, h->obs ? 3 : 1, h->cl_sbytes);
     CK(cluster_configure(smem, cs, nt, S));
-    const int Lx = h->L[0], Ly = h->L[1], Lz = h->L[2], Hx = Lx / 2, Hy = Ly / 2, Hzl = pz / 2;
-    const int per_class = Hx * Hy * Hzl;
+    // rank of plane z
+    std::vector<int> owner(Lz);
+    for (int q = 0; q < cs; ++q)
+        for (int z = slab_z0(pz, nA, q); z < slab_z0(pz, nA, q) + slab_planes(pz, nA, q); ++z) owner[z] = q;
     // stencil entry e of local site l on rank q: its local index, with
     // 0x80000000 | (owner rank << 24) when the owner is another rank; stored
-    // as [q][e / 4][l][e % 4] so a thread reads four entries in one 16-byte load
-    std::vector<uint32_t> tab((size_t)cs * maxst * n_local);
-    for (int q = 0; q < cs; ++q)
+    // as [q][e / 4][l][e % 4] (the ranks' blocks one after another) so a
+    // thread reads four entries in one 16-byte load
+    std::vector<uint32_t> tab((size_t)maxst * h->N);
+    for (int q = 0; q < cs; ++q) {
+        const int z0 = slab_z0(pz, nA, q), per_class = Hx * Hy * (slab_planes(pz, nA, q) / 2);
+        const int n_local = per_class * nclass;
+        const size_t base = (size_t)maxst * (size_t)(z0 / 2) * Hx * Hy * nclass;   // in entries
         for (int l = 0; l < n_local; ++l) {
             const int k = l / per_class, rem = l % per_class;
             const int hx = rem % Hx, hy = (rem / Hx) % Hy, hzl = rem / (Hx * Hy);
             const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pzb = k & 1;
-            const int x = 2 * hx + px, y = 2 * hy + py, z = q * pz + 2 * hzl + pzb;
+            const int x = 2 * hx + px, y = 2 * hy + py, z = z0 + 2 * hzl + pzb;
             const auto &lst = h->prep.stencil[at];
             for (int e = 0; e < maxst; ++e) {
                 uint32_t v = (uint32_t)l;  // padding: the site itself
@@ -978,13 +1011,15 @@ int cluster_geometry(esp_handle *h, int cs, int nt, int S)
                     const int xn = ((x + se.dx) % Lx + Lx) % Lx, yn = ((y + se.dy) % Ly + Ly) % Ly;
                     const int zn = ((z + se.dz) % Lz + Lz) % Lz;
                     const int kn = (se.b << 3) | ((xn & 1) << 2) | ((yn & 1) << 1) | (zn & 1);
-                    const int rn = zn / pz;
-                    const int ln = kn * per_class + ((((zn - rn * pz) >> 1) * Hy + (yn >> 1)) * Hx + (xn >> 1));
+                    const int rn = owner[zn];
+                    const int pcn = Hx * Hy * (slab_planes(pz, nA, rn) / 2);
+                    const int ln = kn * pcn + ((((zn - slab_z0(pz, nA, rn)) >> 1) * Hy + (yn >> 1)) * Hx + (xn >> 1));
                     v = rn == q ? (uint32_t)ln : (0x80000000u | ((uint32_t)rn << 24) | (uint32_t)ln);
                 }
-                tab[(((size_t)q * (maxst / 4) + e / 4) * n_local + l) * 4 + e % 4] = v;
+                tab[base + (((size_t)(e / 4) * n_local + l) * 4 + e % 4)] = v;
             }
         }
+    }
     CK(cudaStreamSynchronize(h->st));
     dfree(h->d_nbidx);
     CK(dalloc(&h->d_nbidx, tab.size()));
@@ -995,6 +1030,7 @@ int cluster_geometry(esp_handle *h, int cs, int nt, int S)
     h->cthreads = nt;
     h->csites = S;
     h->pz = pz;
+    h->cl_nA = nA;
     h->cluster_smem = smem;
     h->cluster_ok = true;
     h->slab_ok = false;   // slabs of this geometry are made from the arrays when needed

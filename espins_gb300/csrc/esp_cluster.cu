@@ -74,10 +74,12 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
     const int csize = (int)cluster.num_blocks();
     const int r = blockIdx.x / csize;  // replica of this cluster
     const int Hx = a.Lx >> 1, Hy = a.Ly >> 1;
-    const int Hzl = a.pz >> 1;                      // half planes per CTA
+    const int Hzl = slab_planes(a.pz, a.nA, rank) >> 1;   // half planes of this CTA
     const int per_class = Hx * Hy * Hzl;
     const int n_local = per_class * a.nclass;
-    const int z0 = rank * a.pz;
+    const int z0 = slab_z0(a.pz, a.nA, rank);
+    const size_t site0 = (size_t)(z0 >> 1) * Hx * Hy * a.nclass;   // sites of the ranks before this one
+    const FastDiv fd_pc = rank < a.nA ? a.fd_pc : a.fd_pc2;
     const unsigned long long sweep_base = a.sweep_base + (a.ctr ? a.ctr[0] : 0ull);
     const long long meas_base = a.meas_base + (a.ctr ? (long long)a.ctr[2] : 0ll);
 
@@ -112,10 +114,10 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
     }
     // this CTA's slab: one contiguous block of 3 n_local floats, or gathered
     // from the spin arrays
-    float *slab = a.slab ? a.slab + ((size_t)r * csize + rank) * 3 * n_local : nullptr;
+    float *slab = a.slab ? a.slab + ((size_t)r * a.N + site0) * 3 : nullptr;
     auto slab_global = [&](int l) -> size_t {
         int k, rem, q1, hx, hy, hzl;
-        fdivmod(l, a.fd_pc, k, rem);
+        fdivmod(l, fd_pc, k, rem);
         fdivmod(rem, a.fd_hx, q1, hx);
         fdivmod(q1, a.fd_hy, hzl, hy);
         const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
@@ -176,7 +178,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
 #pragma unroll
         for (int s = 0; s < SN; ++s) {
             int ci, rem, q1, hx, hy, hzl;
-            fdivmod(its[s], a.fd_pc, ci, rem);
+            fdivmod(its[s], fd_pc, ci, rem);
             const int k = st->class_order[c0 + ci];
             l[s] = k * per_class + rem;
             fdivmod(rem, a.fd_hx, q1, hx);
@@ -195,7 +197,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
             // 8 with zero-coupling self entries
             cnt_k = st->count[k];   // equal for the SN sites
             nb[s] = nbt + k * st->maxst;
-            tab[s] = reinterpret_cast<const uint4 *>(a.nbidx) + (size_t)rank * (st->maxst >> 2) * n_local + l[s];
+            tab[s] = reinterpret_cast<const uint4 *>(a.nbidx) + (size_t)(st->maxst >> 2) * site0 + l[s];
         }
         // a batch of NB neighbours of every site: read from this CTA's shared
         // memory when every lane of the warp finds all of them here (warps
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
                 float op = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
                 for (int l = threadIdx.x; l < n_local; l += blockDim.x) {
                     int k, rem;
-                    fdivmod(l, a.fd_pc, k, rem);
+                    fdivmod(l, fd_pc, k, rem);
                     obs_add(s3[3 * l], s3[3 * l + 1], s3[3 * l + 2], __ldg(a.obs_atom + (k >> 3)), op, qx, qy, qz);
                 }
                 v[4] = op; v[5] = qx; v[6] = qy; v[7] = qz;
@@ -595,12 +597,22 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : 2) k_sweep_cluster(const Cl
 __device__ __forceinline__ int slab_row(const SlabArgs &a, int q, int l)
 {
     int k, rem, q1, hx, hy, hzl;
-    fdivmod(l, a.fd_pc, k, rem);
+    fdivmod(l, q < a.nA ? a.fd_pc : a.fd_pc2, k, rem);
     fdivmod(rem, a.fd_hx, q1, hx);
     fdivmod(q1, a.fd_hy, hzl, hy);
     const int at = k >> 3, px = (k >> 2) & 1, py = (k >> 1) & 1, pz = k & 1;
-    const int x = 2 * hx + px, y = 2 * hy + py, z = q * a.pz + 2 * hzl + pz;
+    const int x = 2 * hx + px, y = 2 * hy + py, z = slab_z0(a.pz, a.nA, q) + 2 * hzl + pz;
     return __ldg(a.inv + ((z * a.Ly + y) * a.Lx + x) * a.na + at);
+}
+
+// Sites of rank q and the first of them in a replica's slab order.
+__device__ __forceinline__ int slab_sites(const SlabArgs &a, int q)
+{
+    return (slab_planes(a.pz, a.nA, q) >> 1) * (a.Lx >> 1) * (a.Ly >> 1) * 8 * a.na;
+}
+__device__ __forceinline__ size_t slab_site0(const SlabArgs &a, int q)
+{
+    return (size_t)(slab_z0(a.pz, a.nA, q) >> 1) * (a.Lx >> 1) * (a.Ly >> 1) * 8 * a.na;
 }
 
 // grid (n_local / 32, cs, R / 32) rounded up, blocks of 32 x 8 threads
@@ -610,17 +622,19 @@ __global__ void __launch_bounds__(256) k_to_slabs(const SlabArgs a)
     __shared__ int rows[32];
     const int l0 = blockIdx.x * 32, q = blockIdx.y, r0 = blockIdx.z * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
-    if (ty == 0) rows[tx] = l0 + tx < a.n_local ? slab_row(a, q, l0 + tx) : 0;
+    const int nl = slab_sites(a, q);
+    const size_t s0 = slab_site0(a, q);
+    if (ty == 0) rows[tx] = l0 + tx < nl ? slab_row(a, q, l0 + tx) : 0;
     __syncthreads();
     for (int j = ty; j < 32; j += 8)
-        if (l0 + j < a.n_local && r0 + tx < a.R) {
+        if (l0 + j < nl && r0 + tx < a.R) {
             const size_t g = (size_t)rows[j] * a.R + r0 + tx;
             t[0][tx][j] = a.sx[g]; t[1][tx][j] = a.sy[g]; t[2][tx][j] = a.sz[g];
         }
     __syncthreads();
     for (int j = ty; j < 32; j += 8)
-        if (r0 + j < a.R && l0 + tx < a.n_local) {
-            float *o = a.slab + (((size_t)(r0 + j) * a.cs + q) * a.n_local + l0 + tx) * 3;
+        if (r0 + j < a.R && l0 + tx < nl) {
+            float *o = a.slab + ((size_t)(r0 + j) * a.N + s0 + l0 + tx) * 3;
             o[0] = t[0][j][tx]; o[1] = t[1][j][tx]; o[2] = t[2][j][tx];
         }
 }
@@ -631,15 +645,17 @@ __global__ void __launch_bounds__(256) k_from_slabs(const SlabArgs a)
     __shared__ int rows[32];
     const int l0 = blockIdx.x * 32, q = blockIdx.y, r0 = blockIdx.z * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
-    if (ty == 0) rows[tx] = l0 + tx < a.n_local ? slab_row(a, q, l0 + tx) : 0;
+    const int nl = slab_sites(a, q);
+    const size_t s0 = slab_site0(a, q);
+    if (ty == 0) rows[tx] = l0 + tx < nl ? slab_row(a, q, l0 + tx) : 0;
     for (int j = ty; j < 32; j += 8)
-        if (r0 + j < a.R && l0 + tx < a.n_local) {
-            const float *i = a.slab + (((size_t)(r0 + j) * a.cs + q) * a.n_local + l0 + tx) * 3;
+        if (r0 + j < a.R && l0 + tx < nl) {
+            const float *i = a.slab + ((size_t)(r0 + j) * a.N + s0 + l0 + tx) * 3;
             t[0][j][tx] = i[0]; t[1][j][tx] = i[1]; t[2][j][tx] = i[2];
         }
     __syncthreads();
     for (int j = ty; j < 32; j += 8)
-        if (l0 + j < a.n_local && r0 + tx < a.R) {
+        if (l0 + j < nl && r0 + tx < a.R) {
             const size_t g = (size_t)rows[j] * a.R + r0 + tx;
             a.sx[g] = t[0][tx][j]; a.sy[g] = t[1][tx][j]; a.sz[g] = t[2][tx][j];
         }

@@ -31,6 +31,13 @@ struct ClusterStencil {
     int class_order[kMaxClasses];
 };
 
+// The z planes of a replica over the cs CTAs of its cluster: ranks
+// [0, nA) hold pz planes, the others pz - 2 (pz even; nA == cs when every
+// slab is equal), so any even Lz with Lz / 2 >= cs splits.  Local sites of a
+// rank follow those of the ranks before it in the replica's slab order.
+__host__ __device__ inline int slab_planes(int pz, int nA, int q) { return q < nA ? pz : pz - 2; }
+__host__ __device__ inline int slab_z0(int pz, int nA, int q) { return q < nA ? q * pz : nA * pz + (q - nA) * (pz - 2); }
+
 inline size_t cluster_stencil_bytes(int nclass, int maxst)
 {
     return sizeof(ClusterStencil) + (size_t)nclass * maxst * sizeof(ClusterNbr);
@@ -42,7 +49,7 @@ struct ClusterArgs {
     // [rank][entry / 4][local site][entry % 4]: the neighbour's local index,
     // | 0x80000000 | (owner rank << 24) when the owner is a peer CTA
     const uint32_t *nbidx;
-    int Lx, Ly, Lz, na, N, R, nclass, pz;  // pz: z planes per CTA (even)
+    int Lx, Ly, Lz, na, N, R, nclass, pz, nA;  // slab_planes(pz, nA, rank) z planes per CTA
     int has_b, has_d, has_si, has_f;
     // state: the slabs of every replica, [r][rank][local site][x, y, z],
     // converted from and to the handle's spin arrays around the launch; or,
@@ -72,8 +79,8 @@ struct ClusterArgs {
     // device counters [sweep, swap, measurement, unit] added to sweep_base
     // and meas_base, or null
     const unsigned long long *ctr;
-    // divisions by per-class sites and half-cell extents
-    FastDiv fd_pc, fd_hx, fd_hy;
+    // divisions by per-class sites (ranks < nA, the others) and half-cell extents
+    FastDiv fd_pc, fd_pc2, fd_hx, fd_hy;
     double rn_inv;                  // 1 / N
     uint32_t key0, key1;
     int mode;
@@ -90,14 +97,14 @@ struct ClusterArgs {
 // The handle's spin arrays (element (p, r) at p*R + r, p = inv[reference
 // site]) to and from the slab layout of the cluster path, [r][rank][l][3]
 // with l the kernel's local site order (class-major, then half-cell x, y, z
-// within the rank's pz planes): shared-memory transposes of 32 sites x 32
+// within the rank's planes): shared-memory transposes of 32 sites x 32
 // replicas, coalesced on both sides.
 struct SlabArgs {
     float *sx, *sy, *sz;
     float *slab;
     const int32_t *inv;
-    int Lx, Ly, na, R, pz, cs, n_local;
-    FastDiv fd_pc, fd_hx, fd_hy;
+    int Lx, Ly, na, R, pz, nA, cs, N, n_local;   // n_local: the largest rank's sites
+    FastDiv fd_pc, fd_pc2, fd_hx, fd_hy;
 };
 cudaError_t launch_to_slabs(const SlabArgs &a, cudaStream_t st);
 cudaError_t launch_from_slabs(const SlabArgs &a, cudaStream_t st);

@@ -26,6 +26,8 @@ def _cases():
         # 4096 sites: one CTA per replica stages its slab through the
         # contiguous buffer, two or more gather it directly
         "sc16_j1j2_dm": sc_mcin(16, [(1e-3, NN), (3e-4, NNN)], [3.0, 12.0, 40.0], dm=1e-4),
+        # 32768 sites: slabs of 12 + 10 + 10 planes on 3 CTAs, staged
+        "sc32_j1_dm": sc_mcin(32, [(1e-3, NN)], [4.0, 20.0], dm=2e-4),
         "bcc_pt": parse_mcin(lattice_mcin(BCC, 8, [(2e-3, BCC1), (5e-4, NN), (-1e-4, NNN)], tems=[10.0, 20.0, 40.0, 80.0],
                                           single_ion=-5e-5, pt=True, pt_steps_swap=5), "bcc"),
     }
@@ -101,18 +103,20 @@ def test_cluster_kernel_is_chosen_for_invariant_lattices_only():
         assert e.sweep_kernel()[0] == "ell"
 
 
-@pytest.mark.parametrize("case", ["sc_j1j2_bq_si", "bcc_pt", "sc16_j1j2_dm"])
+@pytest.mark.parametrize("case", ["sc_j1j2_bq_si", "bcc_pt", "sc16_j1j2_dm", "sc32_j1_dm"])
 def test_trajectory_does_not_depend_on_cluster_geometry(case):
     """Every (CTAs per replica, threads per CTA) geometry the GPU can run gives
     the same spins and rejected counts (same colour order and random stream);
-    only the FP32 grouping of the per-sweep sums may differ."""
+    only the FP32 grouping of the per-sweep sums may differ.  CTA counts that
+    do not divide the z plane pairs give slabs of two heights (e.g. 4 + 4 + 2
+    + 2 planes of a 12-plane lattice on 4 CTAs)."""
     inp = _cases()[case]
     h = build_hamiltonian(inp)
     rng = np.random.default_rng(8)
     v = rng.normal(size=(len(inp.tems), h.n, 3))
     s0 = v / np.linalg.norm(v, axis=2, keepdims=True)
     outs = []
-    geoms = [(cs, nt, sp) for cs in (1, 2, 4) for nt, sp in ((512, 1), (512, 2), (256, 1))]
+    geoms = [(cs, nt, sp) for cs in (1, 2, 3, 4, 5) for nt, sp in ((512, 1), (512, 2), (256, 1))]
     for cs, nt, sp in geoms:
         with _engine(h, inp.tems, "cluster") as e:
             try:
@@ -124,6 +128,8 @@ def test_trajectory_does_not_depend_on_cluster_geometry(case):
             e.sweep(20, 11, seed=5)
             outs.append(((cs, nt), e.get_spins(), e.rejected(), e.running_energy()))
     assert len(outs) >= 2, [o[0] for o in outs]
+    pairs = h.supercell[2] // 2
+    assert any(pairs % g[0] for g, *_ in outs), [o[0] for o in outs]   # an uneven split ran
     for g, s, rej, en in outs[1:]:
         assert np.array_equal(s, outs[0][1]), g
         assert np.array_equal(rej, outs[0][2]), g
