@@ -600,9 +600,10 @@ __global__ void __launch_bounds__(kTilePThreads, NB == 1 ? 2 : 1) k_sweep_tile_p
 
 // e_run / m_run / rejected of every replica from the tiles' slots, and the
 // slots cleared, in two passes with a fixed summation order (deterministic
-// for any grid).  Pass 1: block b sums tiles [32 b, 32 b + 32) of every slot
-// word, thread q of the words (4 R doubles, then R counts) walking the tiles
-// in order, so a warp reads 32 consecutive words of a tile.
+// for any grid).  Pass 1: block (b, y) sums tiles [32 b, 32 b + 32) of slot
+// words [256 y, 256 y + 256), thread q of the words (4 R doubles, then R
+// counts) walking the tiles in order, so a warp reads 32 consecutive words of
+// a tile.
 __global__ void __launch_bounds__(256) k_tile_fold_chunks(TileFoldArgs a)
 {
     const int t0 = blockIdx.x * kTileFoldChunk;
@@ -610,7 +611,8 @@ __global__ void __launch_bounds__(256) k_tile_fold_chunks(TileFoldArgs a)
     const int W = 4 * a.R;
     double *chunk = a.part + (size_t)a.ntiles * W;
     unsigned long long *chunk_rej = a.part_rej + (size_t)a.ntiles * a.R;
-    for (int q = threadIdx.x; q < W + a.R; q += blockDim.x) {
+    const int q = blockIdx.y * blockDim.x + threadIdx.x;
+    if (q < W + a.R) {
         // loads first, then the clearing stores, so the loads of a thread
         // are all in flight together
         if (q < W) {
@@ -739,7 +741,7 @@ cudaError_t launch_tile_p(const TileArgs &a, size_t smem, int num_sms, int nb, c
 
 cudaError_t launch_tile_fold(const TileFoldArgs &a, cudaStream_t st)
 {
-    k_tile_fold_chunks<<<tile_fold_chunks(a.ntiles), 256, 0, st>>>(a);
+    k_tile_fold_chunks<<<dim3(tile_fold_chunks(a.ntiles), (5 * a.R + 255) / 256), 256, 0, st>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_tile_fold_total<<<(5 * a.R + 255) / 256, 256, 0, st>>>(a);

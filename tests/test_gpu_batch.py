@@ -50,7 +50,8 @@ def test_pt_groups_take_the_host_protocol_decisions():
 
 
 def _handles(kinds):
-    """One handle per (L, lattices, pt, kernel) in kinds, begun on its schedule."""
+    """One handle per (L, lattices, pt, kernel) in kinds, begun on its schedule
+    ("tile:T,G,variant" fixes the tiled kernel's geometry)."""
     out = []
     for L, nlat, pt, kernel in kinds:
         inp = batch_lattice_mcin(L, replicas=4)
@@ -60,6 +61,9 @@ def _handles(kinds):
         e.upload(h)
         e.set_temperatures(np.tile(inp.tems, nlat))
         e.set_pt_groups(4)
+        if kernel.startswith("tile:"):
+            e.set_tile_geometry(*(int(x) for x in kernel[5:].split(",")))
+            kernel = "tile"
         e.set_sweep_kernel(kernel)
         e.init_spins("rand", seed=L)
         e.set_series(64)
@@ -69,7 +73,8 @@ def _handles(kinds):
     return out
 
 
-KINDS = [(4, 2, True, "ell"), (8, 3, True, "cluster"), (6, 1, False, "ell"), (12, 2, False, "cluster")]
+KINDS = [(4, 2, True, "ell"), (8, 3, True, "cluster"), (6, 1, False, "ell"), (12, 2, False, "cluster"),
+         (16, 2, True, "tile:4,8,2")]
 
 
 def test_batch_graph_replays_equal_separate_advances():
