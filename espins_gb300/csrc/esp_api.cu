@@ -863,11 +863,19 @@ std::vector<TileGeom> tile_candidates(const esp_handle *h)
             const double bytes = 12.0 * (b * b * b + 1.0) / std::min(1.0, G / 8.0);
             const double items = (double)(ntiles / 8) * (h->R / G);
             // pipelined persistent variants: the copies overlap the updates,
-            // within a CTA (one per SM) or across the two CTAs of an SM
+            // within a CTA (one per SM) or across the CTAs of an SM (two of
+            // 256 threads, four of 128 for groups of 4 replicas).  The replica
+            // groups of one tile go to neighbouring CTAs at about the same
+            // time, so groups of 4 do not waste half of each sector; measured
+            // on SC 128^3 x 64 they still ran 15% slower than groups of 8
+            // (more, shorter items: more box set-up and barriers per update).
             if (tile_p_supported(T, G, h->na)) {
-                if (tile_p_smem_bytes(T, G, h->na, h->tile_maxst, 1) <= 110 * 1024) {
-                    double cost = 0.45 * bytes;
-                    if (items < 8.0 * h->num_sms) cost *= 8.0 * h->num_sms / items;
+                const int per_sm = G == 4 ? 4 : 2;
+                // 228 KB per SM, 1 KB of it reserved per CTA, 96 B static per CTA
+                const size_t fits = (size_t)228 * 1024 / per_sm - 1024 - 128;
+                if (tile_p_smem_bytes(T, G, h->na, h->tile_maxst, 1) <= fits) {
+                    double cost = (G == 4 ? 0.48 : 0.45) * 12.0 * (b * b * b + 1.0);
+                    if (items < 4.0 * per_sm * h->num_sms) cost *= 4.0 * per_sm * h->num_sms / items;
                     out.push_back({T, G, 2, cost});
                 }
                 if (tile_p_smem_bytes(T, G, h->na, h->tile_maxst, 2) <= 226 * 1024) {

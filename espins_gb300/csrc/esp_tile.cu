@@ -305,6 +305,10 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 __device__ __forceinline__ int box_slot(int b) { return (b & ~7) | ((b >> 1) & 3) | ((b & 1) << 2); }
 
 constexpr int kTilePThreads = 256;
+// threads of a persistent CTA: 128 for groups of 4 replicas with one box
+// buffer (four CTAs per SM: the same warps per SM as two of 256, in items of
+// half the size, so a launch's last round idles less), else 256
+__host__ __device__ constexpr int tile_p_nt(int G, int NB) { return NB == 1 && G == 4 ? 128 : kTilePThreads; }
 constexpr int kInvPerThread = 16;   // box sites per thread for the index prefetch (<= 4096 box sites)
 
 // Couplings of one stencil entry with every value in both lanes of a float2,
@@ -319,11 +323,12 @@ struct PairNbr {
 // and the other CTA's updates cover the copy.  EG stencil entries per group
 // of neighbour loads in flight.
 template <int T, int G, int NB>
-__global__ void __launch_bounds__(kTilePThreads, NB == 1 ? 2 : 1) k_sweep_tile_p(const TileArgs a)
+__global__ void __launch_bounds__(tile_p_nt(G, NB), NB == 2 ? 1 : 2 * kTilePThreads / tile_p_nt(G, NB))
+    k_sweep_tile_p(const TileArgs a)
 {
     // SL floats per box slot: x of the G replicas, then y, then z; a thread
     // updates replicas (2 gp, 2 gp + 1) of a site
-    constexpr int NT = kTilePThreads, B = T + 2, H = T / 2, PC = H * H * H, CH = G / 4, GP = G / 2, SL = 3 * G;
+    constexpr int NT = tile_p_nt(G, NB), B = T + 2, H = T / 2, PC = H * H * H, CH = G / 4, GP = G / 2, SL = 3 * G;
     // entries per group of neighbour loads in flight: B/DM entries (EB), then
     // exchange-only ones (EG); the bounds skip the table's padding beyond them
     constexpr int EB = NB == 2 ? 8 : 2, EG = NB == 2 ? 8 : 4;
@@ -683,13 +688,13 @@ size_t tile_p_smem_bytes(int T, int G, int na, int maxst, int nb)
     const size_t B = (size_t)T + 2, nbs = B * B * B * na, nbs8 = (nbs + 7) & ~(size_t)7;
     return sizeof(ClusterStencil) + (size_t)na * maxst * sizeof(PairNbr) +
            (size_t)8 * na * maxst * sizeof(int) + nb * ((nbs + 3) & ~(size_t)3) * sizeof(int) +
-           (size_t)3 * nb * nbs8 * G * sizeof(float) + (size_t)(kTilePThreads / 32) * G * (4 * sizeof(double) + 8);
+           (size_t)3 * nb * nbs8 * G * sizeof(float) + (size_t)(tile_p_nt(G, nb) / 32) * G * (4 * sizeof(double) + 8);
 }
 
 bool tile_p_supported(int T, int G, int na)
 {
     const int B = T + 2;
-    if (B * B * B * na > kInvPerThread * kTilePThreads) return false;
+    if (B * B * B * na > kInvPerThread * tile_p_nt(G, 1)) return false;   // the smaller CTA bounds it
     return (T == 4 || T == 6 || T == 8) && (G == 4 || G == 8 || G == 16);
 }
 
@@ -698,7 +703,24 @@ template <int T, int G, int NB>
 cudaError_t launch_p(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
 {
     if (configure) return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sweep_tile_p<T, G, NB>), smem);
-    k_sweep_tile_p<T, G, NB><<<blocks, kTilePThreads, smem, st>>>(a);
+    if (blocks <= 0) {   // the persistent grid: as many CTAs as fit on the GPU at once
+        // CTAs per SM of this kernel at this shared-memory size (kept for the
+        // next launch of the same size)
+        static size_t c_smem = 0;
+        static int c_per_sm = 0;
+        if (c_per_sm == 0 || c_smem != smem) {
+            int per_sm = 0;
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_tile_p<T, G, NB>,
+                                                                          tile_p_nt(G, NB), smem);
+            if (e != cudaSuccess) return e;
+            if (per_sm < 1) return cudaErrorInvalidConfiguration;
+            c_per_sm = per_sm;
+            c_smem = smem;
+        }
+        const int items = (a.ntx / 2) * (a.nty / 2) * (a.ntz / 2) * (a.R / G), slots = c_per_sm * -blocks;
+        blocks = items < slots ? items : slots;
+    }
+    k_sweep_tile_p<T, G, NB><<<blocks, tile_p_nt(G, NB), smem, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -732,11 +754,10 @@ cudaError_t tile_p_configure(int T, int G, int nb, size_t smem)
 
 cudaError_t launch_tile_p(const TileArgs &a, size_t smem, int num_sms, int nb, cudaStream_t st)
 {
-    if (!tile_p_supported(a.T, a.G, a.na) || a.R % a.G != 0 || (nb != 1 && nb != 2)) return cudaErrorInvalidValue;
-    const int items = (a.ntx / 2) * (a.nty / 2) * (a.ntz / 2) * (a.R / a.G);
-    const int slots = nb == 1 ? 2 * num_sms : num_sms;   // persistent CTAs: one per SM, or two
-    const int blocks = items < slots ? items : slots;
-    return nb == 1 ? launch_pt<1>(a, smem, blocks, st, false) : launch_pt<2>(a, smem, blocks, st, false);
+    if (!tile_p_supported(a.T, a.G, a.na) || a.R % a.G != 0 || (nb != 1 && nb != 2) || num_sms < 1)
+        return cudaErrorInvalidValue;
+    // blocks = -SMs: the launcher sizes the persistent grid from the occupancy
+    return nb == 1 ? launch_pt<1>(a, smem, -num_sms, st, false) : launch_pt<2>(a, smem, -num_sms, st, false);
 }
 
 cudaError_t launch_tile_fold(const TileFoldArgs &a, cudaStream_t st)

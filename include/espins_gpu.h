@@ -293,8 +293,9 @@ int esp_get_cluster_geometry(const esp_handle *h, int32_t *cluster_size, int32_t
  * every supercell edge), replicas per CTA, and the variant: 0 one CTA per
  * tile; persistent CTAs (tile 4, 6 or 8; 4, 8 or 16 replicas) that copy their
  * tiles asynchronously, 1 one per SM copying the next tile while updating the
- * current one, 2 two per SM (at most 128 registers a thread) each copying,
- * then updating, while the other updates.  All give the same trajectory. */
+ * current one, 2 two per SM (four of 128 threads for 4 replicas; at most 128
+ * registers a thread) each copying, then updating, while the others update.
+ * All give the same trajectory. */
 int esp_set_tile_geometry(esp_handle *h, int32_t tile, int32_t replicas, int32_t pipelined);
 int esp_get_tile_geometry(const esp_handle *h, int32_t *tile, int32_t *replicas, int32_t *pipelined);
 /* The kernel in use (1 ELL, 2 cluster, 3 the learned-proposal sweep, 4
