@@ -104,7 +104,8 @@ __device__ __forceinline__ FieldQ lane_of(const FieldQ2 &f, int k)
 // spin n and the energy change de.
 __device__ __forceinline__ bool tile_trial(const TileArgs &a, const ClusterStencil *st, FieldQ f, int at,
                                            uint32_t orig, uint32_t r, uint32_t sw_lo, uint32_t sw_hi, float beta,
-                                           float ox, float oy, float oz, float &nx, float &ny, float &nz, float &de)
+                                           float ox, float oy, float oz, float &nx, float &ny, float &nz, float &de,
+                                           bool hb)
 {
     if (a.has_si) si_form(st->si[at], f.qxx, f.qyy, f.qzz, f.qxy, f.qxz, f.qyz);
     if (a.has_f) {
@@ -113,7 +114,7 @@ __device__ __forceinline__ bool tile_trial(const TileArgs &a, const ClusterStenc
     }
     const Philox4 xr = philox4x32_10(orig, r, sw_lo, sw_hi, a.key0, a.key1);
     trial_spin(a.mode, a.tilt, st->mag[at], ox, oy, oz, xr.x, xr.y, nx, ny, nz);
-    de = delta_energy(a.has_b || a.has_si, f.gx, f.gy, f.gz, f.qxx, f.qyy, f.qzz, f.qxy, f.qxz, f.qyz, ox, oy, oz, nx,
+    de = delta_energy(hb || a.has_si, f.gx, f.gy, f.gz, f.qxx, f.qyy, f.qzz, f.qxy, f.qxz, f.qyz, ox, oy, oz, nx,
                       ny, nz);
     return metropolis_accept(beta, de, xr.z);
 }
@@ -233,7 +234,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_sweep_tile(const TileArgs a
             }
             const int orig = (((z0 + lz) * a.Ly + (y0 + ly)) * a.Lx + (x0 + lx)) * na + at;
             float nx, ny, nz, de;
-            if (tile_trial(a, st, f, at, (uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, beta, ox, oy, oz, nx, ny, nz, de)) {
+            if (tile_trial(a, st, f, at, (uint32_t)orig, (uint32_t)r, sw_lo, sw_hi, beta, ox, oy, oz, nx, ny, nz, de,
+                           a.has_b)) {
                 sx[l] = nx; sy[l] = ny; sz[l] = nz;
                 accE += de;
                 accX += __fsub_rn(nx, ox); accY += __fsub_rn(ny, oy); accZ += __fsub_rn(nz, oz);
@@ -322,7 +324,10 @@ struct PairNbr {
 // registers a thread, twice the warps; each CTA copies its box, then updates,
 // and the other CTA's updates cover the copy.  EG stencil entries per group
 // of neighbour loads in flight.
-template <int T, int G, int NB>
+// FL: the biquadratic (bit 0) and DM (bit 1) terms as compile-time flags, or
+// 4: read from the arguments (the one-CTA-per-SM variant, kept to one
+// instantiation per shape).
+template <int T, int G, int NB, int FL>
 __global__ void __launch_bounds__(tile_p_nt(G, NB), NB == 2 ? 1 : 2 * kTilePThreads / tile_p_nt(G, NB))
     k_sweep_tile_p(const TileArgs a)
 {
@@ -333,6 +338,8 @@ __global__ void __launch_bounds__(tile_p_nt(G, NB), NB == 2 ? 1 : 2 * kTilePThre
     // exchange-only ones (EG); the bounds skip the table's padding beyond them
     constexpr int EB = NB == 2 ? 8 : 2, EG = NB == 2 ? 8 : 4;
     static_assert(NB == 1 || NB == 2, "box buffers");
+    const bool hb = FL == 4 ? a.has_b != 0 : (FL & 1) != 0;
+    const bool hd = FL == 4 ? a.has_d != 0 : (FL & 2) != 0;
     static_assert(G % 4 == 0 && 32 % GP == 0 && (T & 1) == 0, "tile shape");
     const int na = a.na, maxst = a.maxst;
     const int ngroups = a.R / G;
@@ -514,8 +521,8 @@ __global__ void __launch_bounds__(tile_p_nt(G, NB), NB == 2 ? 1 : 2 * kTilePThre
                     for (int j = 0; j < EB; ++j) {
                         const PairNbr &p = nb[e0 + j];
                         entry_exchange(f, p.nJ, tx_[j], ty_[j], tz_[j]);
-                        if (a.has_b) entry_bq(f, p.B, tx_[j], ty_[j], tz_[j]);
-                        if (a.has_d) entry_dm(f, p.Dx, p.Dy, p.Dz, p.nDx, p.nDy, p.nDz, tx_[j], ty_[j], tz_[j]);
+                        if (hb) entry_bq(f, p.B, tx_[j], ty_[j], tz_[j]);
+                        if (hd) entry_dm(f, p.Dx, p.Dy, p.Dz, p.nDx, p.nDy, p.nDz, tx_[j], ty_[j], tz_[j]);
                     }
                 }
                 for (e0 = s_nbd8[at]; e0 < nall; e0 += EG) {   // exchange only
@@ -536,7 +543,7 @@ __global__ void __launch_bounds__(tile_p_nt(G, NB), NB == 2 ? 1 : 2 * kTilePThre
                     const float sx0 = k ? ox.y : ox.x, sy0 = k ? oy.y : oy.x, sz0 = k ? oz.y : oz.x;
                     float nx, ny, nz, de;
                     if (tile_trial(a, st, lane_of(f, k), at, (uint32_t)orig, (uint32_t)(r + k), sw_lo, sw_hi,
-                                   k ? beta1 : beta0, sx0, sy0, sz0, nx, ny, nz, de)) {
+                                   k ? beta1 : beta0, sx0, sy0, sz0, nx, ny, nz, de, hb)) {
                         own[k] = nx; own[G + k] = ny; own[2 * G + k] = nz;
                         accE[k] += de;
                         accX[k] += __fsub_rn(nx, sx0); accY[k] += __fsub_rn(ny, sy0); accZ[k] += __fsub_rn(nz, sz0);
@@ -699,10 +706,10 @@ bool tile_p_supported(int T, int G, int na)
 }
 
 namespace {
-template <int T, int G, int NB>
-cudaError_t launch_p(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
+template <int T, int G, int NB, int FL>
+cudaError_t launch_pf(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
 {
-    if (configure) return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sweep_tile_p<T, G, NB>), smem);
+    if (configure) return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sweep_tile_p<T, G, NB, FL>), smem);
     if (blocks <= 0) {   // the persistent grid: as many CTAs as fit on the GPU at once
         // CTAs per SM of this kernel at this shared-memory size (kept for the
         // next launch of the same size)
@@ -710,7 +717,7 @@ cudaError_t launch_p(const TileArgs &a, size_t smem, int blocks, cudaStream_t st
         static int c_per_sm = 0;
         if (c_per_sm == 0 || c_smem != smem) {
             int per_sm = 0;
-            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_tile_p<T, G, NB>,
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_tile_p<T, G, NB, FL>,
                                                                           tile_p_nt(G, NB), smem);
             if (e != cudaSuccess) return e;
             if (per_sm < 1) return cudaErrorInvalidConfiguration;
@@ -720,8 +727,32 @@ cudaError_t launch_p(const TileArgs &a, size_t smem, int blocks, cudaStream_t st
         const int items = (a.ntx / 2) * (a.nty / 2) * (a.ntz / 2) * (a.R / G), slots = c_per_sm * -blocks;
         blocks = items < slots ? items : slots;
     }
-    k_sweep_tile_p<T, G, NB><<<blocks, tile_p_nt(G, NB), smem, st>>>(a);
+    k_sweep_tile_p<T, G, NB, FL><<<blocks, tile_p_nt(G, NB), smem, st>>>(a);
     return cudaGetLastError();
+}
+
+// the two-CTA variant with the terms as compile-time flags (configured all
+// four at once), the one-CTA variant reading them from the arguments
+template <int T, int G, int NB>
+cudaError_t launch_p(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
+{
+    if constexpr (NB == 2) {
+        return launch_pf<T, G, NB, 4>(a, smem, blocks, st, configure);
+    } else {
+        if (configure) {
+            cudaError_t e = launch_pf<T, G, NB, 0>(a, smem, blocks, st, true);
+            if (e == cudaSuccess) e = launch_pf<T, G, NB, 1>(a, smem, blocks, st, true);
+            if (e == cudaSuccess) e = launch_pf<T, G, NB, 2>(a, smem, blocks, st, true);
+            if (e == cudaSuccess) e = launch_pf<T, G, NB, 3>(a, smem, blocks, st, true);
+            return e;
+        }
+        switch ((a.has_b ? 1 : 0) | (a.has_d ? 2 : 0)) {
+        case 0: return launch_pf<T, G, NB, 0>(a, smem, blocks, st, false);
+        case 1: return launch_pf<T, G, NB, 1>(a, smem, blocks, st, false);
+        case 2: return launch_pf<T, G, NB, 2>(a, smem, blocks, st, false);
+        default: return launch_pf<T, G, NB, 3>(a, smem, blocks, st, false);
+        }
+    }
 }
 
 template <int T, int NB>
