@@ -85,6 +85,7 @@ struct esp_handle {
     bool tile_ok = false;
     int tile_T = 0, tile_G = 0, tile_nt[3] = {0, 0, 0}, ntiles = 0;
     int tile_variant = 0;           // 0 one CTA per tile; pipelined persistent: 1 one CTA per SM, 2 two
+    int tile_blocks = 0;            // persistent grid of the pipelined variants
     size_t tile_smem = 0;
     int4 *d_tile_offs = nullptr;
     ClusterNbr *d_tile_cpl = nullptr;
@@ -407,7 +408,7 @@ int tile_sweeps(esp_handle *h, int64_t n, int64_t first, const esp_sweep_opts *o
         a.sweep = (unsigned long long)(first + w - (h->capturing ? h->cap_base[0] : 0));
         for (int ph = 0; ph < 8; ++ph) {
             a.phase = ph;
-            if (h->tile_variant) CK(launch_tile_p(a, h->tile_smem, h->num_sms, 3 - h->tile_variant, h->st));
+            if (h->tile_variant) CK(launch_tile_p(a, h->tile_smem, h->tile_blocks, 3 - h->tile_variant, h->st));
             else CK(launch_tile(a, h->tile_smem, h->st));
             h->launches++;
         }
@@ -914,6 +915,14 @@ int tile_geometry(esp_handle *h, int T, int G, int variant)
         CK(dalloc(&h->d_tile_rej, slots));
         CK(cudaMemsetAsync(h->d_tile_part, 0, sizeof(double) * 4 * slots, h->st));
         CK(cudaMemsetAsync(h->d_tile_rej, 0, sizeof(unsigned long long) * slots, h->st));
+    }
+    if (variant) {
+        // as many persistent CTAs as the GPU holds at once
+        TileArgs shape{};
+        shape.T = T; shape.G = G; shape.na = h->na; shape.R = h->R;
+        shape.ntx = nt[0]; shape.nty = nt[1]; shape.ntz = nt[2];
+        shape.has_b = h->prep.has_b; shape.has_d = h->prep.has_d;
+        CK(tile_p_grid(shape, smem, h->num_sms, 3 - variant, &h->tile_blocks));
     }
     h->tile_T = T; h->tile_G = G; h->tile_variant = variant;
     for (int d = 0; d < 3; ++d) h->tile_nt[d] = nt[d];

@@ -17,6 +17,8 @@
 // G replicas of a site are contiguous (element (p, r) at p*R + r).
 #include "esp_tile.h"
 
+#include <algorithm>
+
 namespace esp {
 
 namespace {
@@ -706,27 +708,16 @@ bool tile_p_supported(int T, int G, int na)
 }
 
 namespace {
+// configure: allow the shared memory; blocks < 0: store the CTAs one SM
+// holds in *per_sm (the occupancy calculator); else launch `blocks` CTAs
 template <int T, int G, int NB, int FL>
-cudaError_t launch_pf(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
+cudaError_t launch_pf(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure,
+                      int *per_sm = nullptr)
 {
     if (configure) return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sweep_tile_p<T, G, NB, FL>), smem);
-    if (blocks <= 0) {   // the persistent grid: as many CTAs as fit on the GPU at once
-        // CTAs per SM of this kernel at this shared-memory size (kept for the
-        // next launch of the same size)
-        static size_t c_smem = 0;
-        static int c_per_sm = 0;
-        if (c_per_sm == 0 || c_smem != smem) {
-            int per_sm = 0;
-            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_tile_p<T, G, NB, FL>,
-                                                                          tile_p_nt(G, NB), smem);
-            if (e != cudaSuccess) return e;
-            if (per_sm < 1) return cudaErrorInvalidConfiguration;
-            c_per_sm = per_sm;
-            c_smem = smem;
-        }
-        const int items = (a.ntx / 2) * (a.nty / 2) * (a.ntz / 2) * (a.R / G), slots = c_per_sm * -blocks;
-        blocks = items < slots ? items : slots;
-    }
+    if (blocks < 0)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_sweep_tile_p<T, G, NB, FL>, tile_p_nt(G, NB),
+                                                             smem);
     k_sweep_tile_p<T, G, NB, FL><<<blocks, tile_p_nt(G, NB), smem, st>>>(a);
     return cudaGetLastError();
 }
@@ -734,10 +725,10 @@ cudaError_t launch_pf(const TileArgs &a, size_t smem, int blocks, cudaStream_t s
 // the two-CTA variant with the terms as compile-time flags (configured all
 // four at once), the one-CTA variant reading them from the arguments
 template <int T, int G, int NB>
-cudaError_t launch_p(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
+cudaError_t launch_p(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure, int *per_sm)
 {
     if constexpr (NB == 2) {
-        return launch_pf<T, G, NB, 4>(a, smem, blocks, st, configure);
+        return launch_pf<T, G, NB, 4>(a, smem, blocks, st, configure, per_sm);
     } else {
         if (configure) {
             cudaError_t e = launch_pf<T, G, NB, 0>(a, smem, blocks, st, true);
@@ -747,29 +738,30 @@ cudaError_t launch_p(const TileArgs &a, size_t smem, int blocks, cudaStream_t st
             return e;
         }
         switch ((a.has_b ? 1 : 0) | (a.has_d ? 2 : 0)) {
-        case 0: return launch_pf<T, G, NB, 0>(a, smem, blocks, st, false);
-        case 1: return launch_pf<T, G, NB, 1>(a, smem, blocks, st, false);
-        case 2: return launch_pf<T, G, NB, 2>(a, smem, blocks, st, false);
-        default: return launch_pf<T, G, NB, 3>(a, smem, blocks, st, false);
+        case 0: return launch_pf<T, G, NB, 0>(a, smem, blocks, st, false, per_sm);
+        case 1: return launch_pf<T, G, NB, 1>(a, smem, blocks, st, false, per_sm);
+        case 2: return launch_pf<T, G, NB, 2>(a, smem, blocks, st, false, per_sm);
+        default: return launch_pf<T, G, NB, 3>(a, smem, blocks, st, false, per_sm);
         }
     }
 }
 
 template <int T, int NB>
-cudaError_t launch_pg(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
+cudaError_t launch_pg(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure, int *per_sm)
 {
-    if (a.G == 4) return launch_p<T, 4, NB>(a, smem, blocks, st, configure);
-    if (a.G == 8) return launch_p<T, 8, NB>(a, smem, blocks, st, configure);
-    if (a.G == 16) return launch_p<T, 16, NB>(a, smem, blocks, st, configure);
+    if (a.G == 4) return launch_p<T, 4, NB>(a, smem, blocks, st, configure, per_sm);
+    if (a.G == 8) return launch_p<T, 8, NB>(a, smem, blocks, st, configure, per_sm);
+    if (a.G == 16) return launch_p<T, 16, NB>(a, smem, blocks, st, configure, per_sm);
     return cudaErrorInvalidValue;
 }
 
 template <int NB>
-cudaError_t launch_pt(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure)
+cudaError_t launch_pt(const TileArgs &a, size_t smem, int blocks, cudaStream_t st, bool configure,
+                      int *per_sm = nullptr)
 {
-    if (a.T == 4) return launch_pg<4, NB>(a, smem, blocks, st, configure);
-    if (a.T == 6) return launch_pg<6, NB>(a, smem, blocks, st, configure);
-    if (a.T == 8) return launch_pg<8, NB>(a, smem, blocks, st, configure);
+    if (a.T == 4) return launch_pg<4, NB>(a, smem, blocks, st, configure, per_sm);
+    if (a.T == 6) return launch_pg<6, NB>(a, smem, blocks, st, configure, per_sm);
+    if (a.T == 8) return launch_pg<8, NB>(a, smem, blocks, st, configure, per_sm);
     return cudaErrorInvalidValue;
 }
 }  // namespace
@@ -783,12 +775,25 @@ cudaError_t tile_p_configure(int T, int G, int nb, size_t smem)
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_tile_p(const TileArgs &a, size_t smem, int num_sms, int nb, cudaStream_t st)
+cudaError_t tile_p_grid(const TileArgs &a, size_t smem, int num_sms, int nb, int *blocks)
 {
-    if (!tile_p_supported(a.T, a.G, a.na) || a.R % a.G != 0 || (nb != 1 && nb != 2) || num_sms < 1)
+    if (!tile_p_supported(a.T, a.G, a.na) || a.R % a.G != 0 || (nb != 1 && nb != 2) || num_sms < 1 || !blocks)
         return cudaErrorInvalidValue;
-    // blocks = -SMs: the launcher sizes the persistent grid from the occupancy
-    return nb == 1 ? launch_pt<1>(a, smem, -num_sms, st, false) : launch_pt<2>(a, smem, -num_sms, st, false);
+    int per_sm = 0;
+    const cudaError_t e = nb == 1 ? launch_pt<1>(a, smem, -1, nullptr, false, &per_sm)
+                                  : launch_pt<2>(a, smem, -1, nullptr, false, &per_sm);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const long long items = (long long)(a.ntx / 2) * (a.nty / 2) * (a.ntz / 2) * (a.R / a.G);
+    *blocks = (int)std::min<long long>(items, (long long)per_sm * num_sms);
+    return cudaSuccess;
+}
+
+cudaError_t launch_tile_p(const TileArgs &a, size_t smem, int blocks, int nb, cudaStream_t st)
+{
+    if (!tile_p_supported(a.T, a.G, a.na) || a.R % a.G != 0 || (nb != 1 && nb != 2) || blocks < 1)
+        return cudaErrorInvalidValue;
+    return nb == 1 ? launch_pt<1>(a, smem, blocks, st, false) : launch_pt<2>(a, smem, blocks, st, false);
 }
 
 cudaError_t launch_tile_fold(const TileFoldArgs &a, cudaStream_t st)

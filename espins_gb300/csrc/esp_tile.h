@@ -67,6 +67,9 @@ cudaError_t launch_tile_fold(const TileFoldArgs &a, cudaStream_t st);
 size_t tile_p_smem_bytes(int T, int G, int na, int maxst, int nb);
 bool tile_p_supported(int T, int G, int na);
 cudaError_t tile_p_configure(int T, int G, int nb, size_t smem);
-cudaError_t launch_tile_p(const TileArgs &a, size_t smem, int num_sms, int nb, cudaStream_t st);
+// the persistent grid of a geometry (a's shape, T, G, R and term flags):
+// as many CTAs as the GPU holds at once, at most one per item
+cudaError_t tile_p_grid(const TileArgs &a, size_t smem, int num_sms, int nb, int *blocks);
+cudaError_t launch_tile_p(const TileArgs &a, size_t smem, int blocks, int nb, cudaStream_t st);
 
 }  // namespace esp
